@@ -1,0 +1,392 @@
+"""Benchmark of the hierarchical max-flow (HMF) solve on GB300.
+
+Workload (one step = one complete solve, initialisation + all iterations):
+256^3 float32 phantom of 4 seeded ellipsoids, 2-level tree (root -> 2
+branches -> 2 leaves each), Gaussian-NLL data terms, per-voxel smoothness
+0.2*exp(-|grad I|^2/0.01) shared by every vertex, 500 iterations,
+StepSize 0.1, CC 0.25.  Metric: voxel*label*iterations per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl ours` (default) runs libhmf_gb300.so; `--impl reference` runs the
+reference's CPU implementation of the path on the host cores (the compiled
+reference code where it was built, else the oracle's restatement of it).
+Under torchrun (N > 1) every rank solves its own volume (replicas; the path
+needs no exchange between independent volumes) and rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "ellipsoids256_tree4"
+METRIC = "HMF voxel*label*iterations/s (256^3, 2-level tree, 4 leaves, per-voxel smoothness, 500 it)"
+UNIT = "voxel*label*iter/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--iterations", type=int, default=500)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per iteration from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_%s.txt" % WORKLOAD)
+    try:
+        with open(path) as f:
+            for line in f:
+                line = line.strip()
+                if line.startswith("{"):
+                    return json.loads(line)
+    except OSError:
+        pass
+    return None
+
+
+def survey_bytes_per_iteration(w):
+    """Algorithmic bytes of one iteration, 4*V*(12*N + L + N_S + 2): every
+    non-root vertex's three flows, divergence, sink and label read and written
+    once, each data term and distinct smoothness image read once, the source
+    flow read and written."""
+    N, L, NS = w.n_nonroot, len(w.leaves), w.n_smooth_images
+    return 4.0 * w.nvox * (12 * N + L + NS + 2)
+
+
+def kernel_bytes(w):
+    """Compulsory bytes of this implementation's two kernels per iteration."""
+    N, L = w.n_nonroot, len(w.leaves)
+    kids = {v: 0 for v in range(len(w.parent))}
+    for p in w.parent:
+        if p >= 0:
+            kids[p] += 1
+    B = sum(1 for v, p in enumerate(w.parent) if p >= 0 and kids[v])
+    n_smooth_reads = sum(1 for v in w.smooth)
+    flow = 4.0 * w.nvox * (10 * N + n_smooth_reads)          # r: p3 sink label inc (+S); w: p3 div
+    tree = 4.0 * w.nvox * (N + N + (B + 1) + L + (N + 1) + N)  # r: div label sinks(B,root) D; w: sinks label
+    return flow, tree
+
+
+def cpu_reference_sample(w, seconds: float, threads: int):
+    """Reference CPU HMF on a bounded sample: the full volume for as many
+    iterations as fit in ~`seconds`, initialisation subtracted."""
+    from oracle import oracle as O
+
+    lib = None
+    try:
+        lib = O.reference_library()
+    except Exception:
+        lib = None
+    kind = "reference" if lib is not None else "port"
+
+    def run(iters):
+        t0 = time.perf_counter()
+        if kind == "reference":
+            O.solve_reference_cpu(w.dims, w.parent, w.data, w.smooth, w.alpha, iters, w.step, w.cc)
+        else:
+            O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, iters, w.step, w.cc, semantics=O.REF_CPU,
+                    threads=threads)
+        return time.perf_counter() - t0
+
+    t_init = run(0)
+    t_one = max(run(1) - t_init, 1e-6)
+    iters = max(1, min(50, int(seconds / t_one)))
+    t = max(run(iters) - t_init, 1e-6)
+    L = len(w.leaves)
+    return {"value": w.nvox * L * iters / t, "unit": UNIT, "cores": 1 if kind == "reference" else threads,
+            "kind": kind,
+            "sample": "full %dx%dx%d volume, %d of %d iterations (initialisation excluded), REF_CPU semantics"
+                      % (w.dims[0], w.dims[1], w.dims[2], iters, w.iterations),
+            "seconds": t, "iterations": iters}
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def make_workload(args, rank):
+    from robartsvtk_gb300 import synthetic
+    return synthetic.ellipsoids_tree4(seed=rank, size=args.size, iterations=args.iterations)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    w = make_workload(args, 0)
+    threads = host_threads()
+    for _ in range(max(0, args.warmup)):
+        cpu_reference_sample(w, 0.5, threads)
+    vals = []
+    last = None
+    for _ in range(max(1, args.steps)):
+        last = cpu_reference_sample(w, args.cpu_seconds / max(1, args.steps), threads)
+        vals.append(last["value"])
+    vals.sort()
+    value = vals[len(vals) // 2]
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1000.0 * w.nvox * len(w.leaves) * w.iterations / value,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "volume": list(w.dims), "vertices": len(w.parent),
+                      "leaves": len(w.leaves), "iterations": w.iterations, "semantics": "REF_CPU"},
+           "cpu_baseline": {k: last[k] for k in ("kind", "cores", "sample")} | {"value": value, "unit": UNIT},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = make_workload(args, rank)
+    L = len(w.leaves)
+    units_per_step = w.nvox * L * w.iterations
+    stream = torch.cuda.Stream()
+
+    # ---- device-resident inputs -------------------------------------------
+    d_data = {leaf: torch.from_numpy(d).cuda() for leaf, d in w.data.items()}
+    smooth_dev = {}
+    d_smooth = {}
+    for v, S in w.smooth.items():
+        key = id(S)
+        if key not in smooth_dev:
+            smooth_dev[key] = torch.from_numpy(S).cuda()
+        d_smooth[v] = smooth_dev[key]
+    solver = HMFSolver(w.dims, w.parent)
+    for leaf, t in d_data.items():
+        solver.set_data(leaf, t)
+    for v, t in d_smooth.items():
+        solver.set_smoothness(v, t)
+    for v, a in w.alpha.items():
+        solver.set_smoothness_scalar(v, a)
+    solver.set_params(w.iterations, w.step, w.cc)
+    torch.cuda.synchronize()
+
+    for _ in range(max(3, args.warmup)):
+        solver.solve(stream)
+    stream.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        solver.solve(stream)
+        launches += solver.stats()["launches"]
+    e1.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clock_info = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * units_per_step / (ms / 1000.0)
+
+    # ---- per-kernel device times (events around every launch) -------------
+    solver.set_timing(True)
+    solver.solve(stream)
+    st = solver.stats()
+    solver.set_timing(False)
+    t_flow, t_tree, t_init = st["flow_ms"], st["tree_ms"], st["init_ms"]
+
+    # ---- end to end through the public API with pinned host buffers -------
+    h_data = {leaf: torch.from_numpy(d).pin_memory() for leaf, d in w.data.items()}
+    h_smooth_obj = {}
+    h_smooth = {}
+    for v, S in w.smooth.items():
+        if id(S) not in h_smooth_obj:
+            h_smooth_obj[id(S)] = torch.from_numpy(S).pin_memory()
+        h_smooth[v] = h_smooth_obj[id(S)]
+    h_out = {leaf: torch.empty(w.dims[::-1], dtype=torch.float32).pin_memory() for leaf in w.leaves}
+    h2d = sum(t.numel() * 4 for t in h_data.values()) + sum(t.numel() * 4 for t in h_smooth_obj.values())
+    d2h = sum(t.numel() * 4 for t in h_out.values())
+
+    def e2e_step():
+        for leaf, t in h_data.items():
+            solver.set_data(leaf, t)
+        for v, t in h_smooth.items():
+            solver.set_smoothness(v, t)
+        solver.solve(stream)
+        for leaf in w.leaves:
+            solver.labels(leaf, out=h_out[leaf], stream=stream)
+
+    e2e_step()
+    if dist:
+        dist.barrier()
+    e_steps = max(2, min(args.steps, 3))
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    e2.record(stream)
+    for _ in range(e_steps):
+        e2e_step()
+    e3.record(stream)
+    stream.synchronize()
+    e2e_ms = e2.elapsed_time(e3) / e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * units_per_step / (e2e_ms / 1000.0)
+
+    # ---- roofline -----------------------------------------------------------
+    peak, peak_kind = measured_peak_hbm()
+    b_iter = survey_bytes_per_iteration(w)
+    it_ms = t_flow + t_tree
+    achieved = b_iter / (it_ms / 1000.0) / 1e9
+    flow_b, tree_b = kernel_bytes(w)
+    traffic = ncu_traffic()
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+        "traffic": traffic.get("dram_bytes_per_iteration") if traffic else None,
+        "unit_of_work": "one iteration = flow_kernel + tree_kernel launch; algorithmic bytes 4*V*(12N+L+N_S+2)"
+                        " = %.0f B" % b_iter,
+        "kernels": {
+            "flow_kernel": {"avg_ms": t_flow, "own_bytes": flow_b, "achieved_gbs": flow_b / t_flow / 1e6,
+                            "share": t_flow / it_ms},
+            "tree_kernel": {"avg_ms": t_tree, "own_bytes": tree_b, "achieved_gbs": tree_b / t_tree / 1e6,
+                            "share": t_tree / it_ms},
+            "init_kernel_ms": t_init,
+        },
+    }
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom per rank)",
+        "config": {"workload": WORKLOAD, "volume": list(w.dims), "vertices": len(w.parent), "leaves": L,
+                   "iterations": w.iterations, "step": w.step, "cc": w.cc, "semantics": "REF_CUDA",
+                   "smoothness": "per-voxel, one image shared by all vertices",
+                   "l2": "no flush: inputs + solver state %.1f GB per step >> 129 MB L2"
+                         % (solver.device_bytes() / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": launches,
+        "clocks": clock_info,
+        "roofline": roofline,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
+    if rank == 0:
+        print(json.dumps(out))
+    solver.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

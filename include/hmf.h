@@ -1,0 +1,131 @@
+/* hmf.h -- C ABI of the GB300 (sm_103a) hierarchical max-flow segmentation
+ * library, libhmf_gb300.so.
+ *
+ * This is the drop-in boundary for the RobartsVTK HMF path.  The reference
+ * reaches its GPU through free C functions on raw device buffers
+ * (ImageProcessing/vtkCudaImageAnalytics/CUDA_hierarchicalmaxflow.h:17-50),
+ * driven one full-volume pass at a time by
+ * vtkCudaHierarchicalMaxFlowSegmentation::InitializeAlgorithm/RunAlgorithm
+ * (vtkCudaHierarchicalMaxFlowSegmentation.cxx:478-716).  Here the whole solve
+ * (initialisation plus every primal-dual iteration) is one call on an opaque
+ * context, so that the iteration can be fused on the device.
+ *
+ * Conventions
+ *  - Volumes are float32, x fastest, [VZ][VY][VX] (VTK scalar layout).
+ *  - The label tree is a parent array: vertices 0..n-1, parent[v] == -1 for
+ *    the single root; the children of a vertex are taken in increasing id
+ *    order (the order vtkTree::AddChild assigns).  Leaves are the disjoint
+ *    labels; every leaf needs a data term (cost), all values >= 0.
+ *  - `where` says whether a pointer is host memory (HMF_HOST) or device
+ *    memory of the context's GPU (HMF_DEVICE).  Input pointers are borrowed,
+ *    as VTK borrows its input images: they must stay valid until the next
+ *    hmf_solve() returns.  Host inputs are copied to the device inside
+ *    hmf_solve(); device inputs are read in place.
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  All work
+ *    is ordered after the work already queued on it; calls return once the
+ *    work is queued (hmf_get_labels to host memory returns after the copy).
+ *  - Every call returns HMF_OK (0) or a negative HMF_ERR_* code; the message
+ *    is available from hmf_last_error().  No call resets the device.
+ *  - A context is not thread-safe; distinct contexts are independent.
+ */
+#ifndef HMF_GB300_H
+#define HMF_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HMF_OK 0
+#define HMF_ERR_INVALID_ARGUMENT -1
+#define HMF_ERR_TREE -2
+#define HMF_ERR_MISSING_INPUT -3
+#define HMF_ERR_CUDA -4
+#define HMF_ERR_OUT_OF_MEMORY -5
+#define HMF_ERR_STATE -6
+
+#define HMF_HOST 0
+#define HMF_DEVICE 1
+
+/* Which reference behaviour hmf_solve reproduces.
+ *  REF_CUDA: vtkCudaHierarchicalMaxFlowSegmentation (the regularised
+ *            primal-dual solver the reference runs on the GPU,
+ *            CUDA_hierarchicalmaxflow.cu:124-456).
+ *  REF_CPU:  vtkHierarchicalMaxFlowSegmentation's host code as written
+ *            (vtkMaxFlowSegmentationUtilities.cxx:29-339): its spatial flows
+ *            stay zero and branch sinks keep their initial value, so the
+ *            solve reduces to a per-voxel leaf iteration. */
+#define HMF_SEMANTICS_REF_CUDA 0
+#define HMF_SEMANTICS_REF_CPU 1
+
+typedef struct hmf_ctx hmf_ctx;
+
+/* Create a solver for one volume size and one label tree on CUDA device
+ * `device`.  Replaces the buffer planning of
+ * vtkHierarchicalMaxFlowSegmentation::RequestData (.cxx:555-905) and the GPU
+ * buffer acquisition of vtkCudaHierarchicalMaxFlowSegmentation::InitializeAlgorithm
+ * (.cxx:513-538, CUDA_GetGPUBuffers CUDA_hierarchicalmaxflow.cu:33-60).
+ * Device memory for the whole solver state is allocated here, once. */
+int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes,
+               int semantics, int device);
+int hmf_destroy(hmf_ctx* ctx);
+
+/* Data term (cost) of a leaf.  Replaces SetDataInputDataObject(idx, image)
+ * (vtkHierarchicalMaxFlowSegmentation.h:84-87). */
+int hmf_set_data(hmf_ctx* ctx, int node, const float* data, int where);
+
+/* Optional per-voxel smoothness image of a non-root vertex (NULL removes it;
+ * without an image S(x) = 1).  Replaces SetSmoothnessInputDataObject
+ * (vtkHierarchicalMaxFlowSegmentation.h:94-97).  Vertices may share one
+ * image pointer; it is then read once per voxel. */
+int hmf_set_smoothness(hmf_ctx* ctx, int node, const float* smooth, int where);
+
+/* Smoothness weight alpha >= 0 of a non-root vertex (default 1).  Replaces
+ * AddSmoothnessScalar(node, alpha) (vtkHierarchicalMaxFlowSegmentation.cxx:93-104);
+ * unlike the reference's std::map::insert, a later call replaces the value. */
+int hmf_set_smoothness_scalar(hmf_ctx* ctx, int node, double alpha);
+
+/* NumberOfIterations (clamped to [0, INT_MAX]), StepSize and CC (each clamped
+ * to [0, 1]) as vtkSetClampMacro does (vtkHierarchicalMaxFlowSegmentation.h:64-77).
+ * Defaults 100, 0.1, 0.25 (.cxx:57-59). */
+int hmf_set_params(hmf_ctx* ctx, int iterations, float step_size, float cc);
+
+/* Initialise and run all iterations.  Replaces
+ * vtkCudaHierarchicalMaxFlowSegmentation::InitializeAlgorithm + RunAlgorithm
+ * (.cxx:478-716). */
+int hmf_solve(hmf_ctx* ctx, void* stream);
+
+/* Copy the labelling of a non-root vertex (the leaves are the reference's
+ * outputs, GetOutputDataObject(idx), vtkHierarchicalMaxFlowSegmentation.cxx:337-346;
+ * branch labellings are also available) to `out` (VX*VY*VZ floats). */
+int hmf_get_labels(hmf_ctx* ctx, int node, float* out, int where, void* stream);
+
+/* Same for the sink flow of a vertex (the root's is the source flow). */
+int hmf_get_sink(hmf_ctx* ctx, int node, float* out, int where, void* stream);
+
+/* Leaf order used by the reference for its output ports (DFS pre-order,
+ * vtkHierarchicalMaxFlowSegmentation.cxx:383-398): writes up to `cap` vertex
+ * ids, returns the number of leaves (or a negative error). */
+int hmf_leaf_order(const hmf_ctx* ctx, int* out, int cap);
+
+/* Bytes of device memory the context holds. */
+size_t hmf_device_bytes(const hmf_ctx* ctx);
+
+/* Launch-level statistics of the last hmf_solve: kernels launched, and the
+ * average device time (ms) of each kernel kind measured with CUDA events on
+ * the launching stream when `timed` solves were requested through
+ * hmf_set_timing(ctx, 1).  kinds: 0 = flow (stencil), 1 = tree (per-voxel
+ * sink/label sweep), 2 = init. */
+int hmf_set_timing(hmf_ctx* ctx, int enabled);
+int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kind, int n_kinds);
+
+/* Message of the last failed call on ctx (or of the last failed hmf_create on
+ * this thread when ctx is NULL). */
+const char* hmf_last_error(const hmf_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HMF_GB300_H */

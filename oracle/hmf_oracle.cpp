@@ -1,0 +1,705 @@
+// hmf_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the oracle).
+//
+// CPU restatement of the RobartsVTK hierarchical max-flow (HMF) solver, used
+// solely as the checker for the CUDA implementation in robartsvtk_gb300/.
+// Nothing in the product links, loads or calls this file: only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm do.
+//
+// Two semantics are restated, because the reference's CPU and CUDA classes
+// compute different things (see the per-function citations):
+//
+//  * REF_CUDA  -- what vtkCudaHierarchicalMaxFlowSegmentation runs on the GPU:
+//      kernels  ImageProcessing/vtkCudaImageAnalytics/CUDA_hierarchicalmaxflow.cu:124-456
+//      launches ImageProcessing/vtkCudaImageAnalytics/vtkCudaHierarchicalMaxFlowSegmentation.cxx:106-476
+//      init     ImageProcessing/vtkCudaImageAnalytics/vtkCudaHierarchicalMaxFlowSegmentation.cxx:547-658
+//    Restated kernel by kernel (one full-volume pass each, same launch order,
+//    same FP32 operation order), templated on float / double so the same
+//    code is also the FP64 oracle.  Build with -ffp-contract=off.
+//
+//  * REF_CPU   -- what vtkHierarchicalMaxFlowSegmentation runs on the host:
+//      driver   Common/vtkRobartsCommon/vtkHierarchicalMaxFlowSegmentation.cxx:973-1259
+//      kernels  Common/vtkRobartsCommon/vtkMaxFlowSegmentationUtilities.cxx:29-339
+//    The driver below is a restatement of the recursion; the per-voxel loops
+//    come from a "Utils" policy.  PortUtils restates the reference utility
+//    loops (OpenMP over voxels, bit-identical per element).  When built with
+//    -DHMF_ORACLE_WITH_REFERENCE the same driver is linked against the
+//    reference's own compiled vtkMaxFlowSegmentationUtilities.cxx (recipe in
+//    oracle/build_oracle.py, output in oracle/_ref/), which pins the port.
+//
+// Tree convention shared with the product: vertices 0..n-1, parent[v] == -1
+// for the single root, children of a vertex in increasing id order (the order
+// vtkTree::AddChild assigns).  Leaves and branches are numbered in DFS
+// pre-order exactly as CheckInputConsistancy does
+// (vtkHierarchicalMaxFlowSegmentation.cxx:383-398).
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifdef HMF_ORACLE_WITH_REFERENCE
+// The reference's own utility loops, compiled from its source file.
+void zeroOutBuffer(float* buffer, int size);
+void setBufferToValue(float* buffer, float value, int size);
+void sumBuffer(float* bufferOut, float* bufferIn, int size);
+void copyBuffer(float* bufferOut, float* bufferIn, int size);
+void minBuffer(float* bufferOut, float* bufferIn, int size);
+void divBuffer(float* bufferOut, float* bufferIn, int size);
+void divAndStoreBuffer(float* bufferOut, float* bufferIn, float value, int size);
+void lblBuffer(float* label, float* sink, float* cap, int size);
+void constrainBuffer(float* sink, float* cap, int size);
+void updateLeafSinkFlow(float* sink, float* inc, float* div, float* label, float CC, int size);
+void updateLabel(float* sink, float* inc, float* div, float* label, float CC, int size);
+void storeSinkFlowInBuffer(float* working, float* inc, float* div, float* label, float CC, int size);
+void storeSourceFlowInBuffer(float* working, float* sink, float* div, float* label, float CC, int size);
+void ghmf_flowGradientStep(float* sink, float* inc, float* div, float* label, float StepSize, float CC, int size);
+void ghmf_applyStep(float* div, float* flowX, float* flowY, float* flowZ, int VX, int VY, int VZ, int size);
+void ghmf_computeFlowMag(float* div, float* flowX, float* flowY, float* flowZ, float* smooth, float alpha, int VX, int VY, int VZ, int size);
+void ghmf_projectOntoSet(float* div, float* flowX, float* flowY, float* flowZ, int VX, int VY, int VZ, int size);
+#endif
+
+namespace {
+
+thread_local std::string g_err;
+
+// ---------------------------------------------------------------------------
+// Tree bookkeeping (vtkHierarchicalMaxFlowSegmentation.cxx:363-505, :872-905)
+// ---------------------------------------------------------------------------
+struct Tree {
+  int n = 0;
+  int root = -1;
+  std::vector<int> parent;
+  std::vector<std::vector<int>> kids;
+  std::vector<int> preorder;    // DFS discovery order from the root
+  std::vector<int> leaf_index;  // vertex -> LeafMap value or -1
+  std::vector<int> branch_index;  // vertex -> BranchMap value or -1
+  int n_leaves = 0, n_branches = 0;
+
+  bool build(int n_nodes, const int* par) {
+    n = n_nodes;
+    if (n < 2) { g_err = "tree needs a root and at least one leaf"; return false; }
+    parent.assign(par, par + n);
+    kids.assign(n, {});
+    for (int v = 0; v < n; ++v) {
+      if (parent[v] < 0) {
+        if (root >= 0) { g_err = "tree has more than one root"; return false; }
+        root = v;
+      } else if (parent[v] >= n || parent[v] == v) {
+        g_err = "tree parent id out of range"; return false;
+      } else {
+        kids[parent[v]].push_back(v);  // increasing id order
+      }
+    }
+    if (root < 0) { g_err = "tree has no root"; return false; }
+    std::vector<int> stack{root};
+    std::vector<char> seen(n, 0);
+    while (!stack.empty()) {
+      int v = stack.back(); stack.pop_back();
+      if (seen[v]) { g_err = "tree has a cycle"; return false; }
+      seen[v] = 1;
+      preorder.push_back(v);
+      for (int k = (int)kids[v].size() - 1; k >= 0; --k) stack.push_back(kids[v][k]);
+    }
+    if ((int)preorder.size() != n) { g_err = "tree is not connected"; return false; }
+    if (kids[root].empty()) { g_err = "root has no children"; return false; }
+    leaf_index.assign(n, -1);
+    branch_index.assign(n, -1);
+    for (int v : preorder) {
+      if (kids[v].empty()) leaf_index[v] = n_leaves++;
+      else if (v != root) branch_index[v] = n_branches++;
+    }
+    return true;
+  }
+  bool leaf(int v) const { return kids[v].empty(); }
+};
+
+template <class T> inline T sat01(T x) {
+  // __saturatef: clamp to [0,1], NaN -> 0 (CUDA_hierarchicalmaxflow.cu:215)
+  if (x != x) return T(0);
+  return x < T(0) ? T(0) : (x > T(1) ? T(1) : x);
+}
+
+// ---------------------------------------------------------------------------
+// REF_CUDA restatement
+// ---------------------------------------------------------------------------
+template <class T>
+struct CudaOracle {
+  int VX, VY, VZ;
+  long V;
+  const Tree& t;
+  // per vertex state (root uses sink = source flow, work = source working)
+  std::vector<std::vector<T>> fx, fy, fz, div, sink, u, work;
+  std::vector<const float*> data, smooth;
+  std::vector<T> alpha;
+  T step, cc, icc, root_work;
+
+  CudaOracle(const Tree& tr, int vx, int vy, int vz) : VX(vx), VY(vy), VZ(vz), t(tr) {
+    V = (long)vx * vy * vz;
+  }
+
+  void alloc() {
+    int n = t.n;
+    fx.assign(n, {}); fy.assign(n, {}); fz.assign(n, {}); div.assign(n, {});
+    sink.assign(n, {}); u.assign(n, {}); work.assign(n, {});
+    for (int v = 0; v < n; ++v) {
+      sink[v].assign(V, T(0));
+      if (v != t.root) {
+        fx[v].assign(V, T(0)); fy[v].assign(V, T(0)); fz[v].assign(V, T(0));
+        div[v].assign(V, T(0)); u[v].assign(V, T(0));
+      }
+      if (!t.leaf(v)) work[v].assign(V, T(0));
+    }
+  }
+
+  // vtkCudaHierarchicalMaxFlowSegmentation.cxx:547-658 and :63-104
+  void init() {
+    std::vector<int> leaves;
+    for (int v : t.preorder) if (t.leaf(v)) leaves.push_back(v);
+    const long n = V;
+    // leafSink[i] = D[i]  (CopyBuffers)
+    for (int l : leaves) {
+      T* s = sink[l].data(); const float* d = data[l];
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) s[i] = T(d[i]);
+    }
+    // leafSink[0] = min over leaves  (kern_MinBuffers, CUDA_hierarchicalmaxflow.cu:489-499)
+    T* s0 = sink[leaves[0]].data();
+    for (size_t k = 1; k < leaves.size(); ++k) {
+      const T* sk = sink[leaves[k]].data();
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) { T a = s0[i], b = sk[i]; s0[i] = (a < b) ? a : b; }
+    }
+    // labels: [sink == D] / count  (kern_Lbl :519-529, SumBuffers, kern_DivideBuffers :584-594)
+    std::vector<T>& cnt = work[t.root];
+    std::fill(cnt.begin(), cnt.end(), T(0));
+    for (size_t k = 0; k < leaves.size(); ++k) {
+      int l = leaves[k];
+      T* sl = sink[l].data(); T* ul = u[l].data(); const float* d = data[l]; T* c = cnt.data();
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        if (k > 0) sl[i] = s0[i];
+        ul[i] = (sl[i] == T(d[i])) ? T(1) : T(0);
+        c[i] = c[i] + ul[i];
+      }
+    }
+    for (int l : leaves) {
+      T* ul = u[l].data(); const T* c = cnt.data();
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) ul[i] = ul[i] / c[i];
+    }
+    // branch sinks and the source flow = min
+    for (int v = 0; v < t.n; ++v) if (!t.leaf(v)) {
+      T* s = sink[v].data();
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) s[i] = s0[i];
+    }
+    propagate(t.root);
+  }
+
+  void propagate(int v) {  // PropogateLabels, vtkCudaHierarchicalMaxFlowSegmentation.cxx:63-104
+    if (!t.leaf(v) && v != t.root) std::fill(u[v].begin(), u[v].end(), T(0));
+    for (int k : t.kids[v]) propagate(k);
+    if (v == t.root) return;
+    int p = t.parent[v];
+    if (p == t.root) return;
+    T* up = u[p].data(); const T* uv = u[v].data();
+    const long n = V;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) up[i] = up[i] + uv[i];
+  }
+
+  // kern_CalcGradStep (CUDA_hierarchicalmaxflow.cu:233-241)
+  void grad_step(int v) {
+    const T* s = sink[v].data(); const T* c = sink[t.parent[v]].data();
+    const T* uu = u[v].data(); T* d = div[v].data();
+    const long n = V;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) d[i] = step * (((s[i] + d[i]) - c[i]) - uu[i] * icc);
+  }
+
+  // kern_DescentSpatialFlow (:254-285)
+  void descent(int v) {
+    const T* g = div[v].data(); T* px = fx[v].data(); T* py = fy[v].data(); T* pz = fz[v].data();
+    const long n = V, sxy = (long)VX * VY;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+      const int x = (int)(i % VX), y = (int)((i / VX) % VY), z = (int)(i / sxy);
+      T cur = g[i];
+      px[i] = x ? px[i] - (cur - g[i - 1]) : T(0);
+      py[i] = y ? py[i] - (cur - g[i - VX]) : T(0);
+      pz[i] = z ? pz[i] - (cur - g[i - sxy]) : T(0);
+    }
+  }
+
+  // kern_ComputeFlowMagVariSmooth / ConstSmooth (:299-380)
+  void flow_mag(int v) {
+    T* m = div[v].data(); const T* px = fx[v].data(); const T* py = fy[v].data(); const T* pz = fz[v].data();
+    const float* S = smooth[v]; const T a = alpha[v];
+    const long n = V, sxy = (long)VX * VY;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+      const int x = (int)(i % VX), y = (int)((i / VX) % VY);
+      T up = px[i] * px[i];
+      T dn = (x != VX - 1) ? px[i + 1] * px[i + 1] : T(0);
+      T F = up + dn;
+      up = py[i] * py[i];
+      dn = (y != VY - 1) ? py[i + VX] * py[i + VX] : T(0);
+      F += up + dn;
+      up = pz[i] * pz[i];
+      dn = (i + sxy < n) ? pz[i + sxy] * pz[i + sxy] : T(0);
+      F += up + dn;
+      F = std::sqrt(T(0.5) * F);
+      T sm = S ? a * T(S[i]) : a;
+      m[i] = (F > sm) ? sm / F : T(1);
+    }
+  }
+
+  // kern_Project + kern_Divergence (:401-456)
+  void project_div(int v) {
+    T* d = div[v].data(); T* px = fx[v].data(); T* py = fy[v].data(); T* pz = fz[v].data();
+    const long n = V, sxy = (long)VX * VY;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+      const int x = (int)(i % VX), y = (int)((i / VX) % VY), z = (int)(i / sxy);
+      T cur = d[i];
+      px[i] = x ? px[i] * T(0.5) * (cur + d[i - 1]) : T(0);
+      py[i] = y ? py[i] * T(0.5) * (cur + d[i - VX]) : T(0);
+      pz[i] = z ? pz[i] * T(0.5) * (cur + d[i - sxy]) : T(0);
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+      const int x = (int)(i % VX), y = (int)((i / VX) % VY);
+      T dv = px[i] + py[i] + pz[i];
+      if (x != VX - 1) dv -= px[i + 1];
+      if (y != VY - 1) dv -= py[i + VX];
+      if (i < n - sxy) dv -= pz[i + sxy];
+      d[i] = dv;
+    }
+  }
+
+  // SolveMaxFlow / UpdateLabel, vtkCudaHierarchicalMaxFlowSegmentation.cxx:106-476
+  void solve(int v) {
+    const bool is_root = (v == t.root), is_leaf = t.leaf(v), is_branch = !is_root && !is_leaf;
+    const long n = V;
+    const int nk = (int)t.kids[v].size();
+    if (!is_leaf) {
+      T init = is_branch ? T(0) : root_work;
+      std::fill(work[v].begin(), work[v].end(), init);
+    }
+    if (!is_root) { grad_step(v); descent(v); flow_mag(v); project_div(v); }
+    for (int k : t.kids[v]) solve(k);
+    if (is_branch) {
+      // kern_FindSinkPotentialAndStore (:124-132), MultiplyAndStoreBuffer (CUDA_commonKernels.cu:499)
+      T* w = work[v].data(); const T* c = sink[t.parent[v]].data(); const T* d = div[v].data();
+      const T* uu = u[v].data(); T* s = sink[v].data();
+      const T inv = T(1) / T(nk + 1);
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        w[i] = ((w[i] + c[i]) - d[i]) + uu[i] * icc;
+        s[i] = w[i] * inv;
+      }
+    }
+    if (is_root) {
+      T* w = work[v].data(); T* s = sink[v].data();
+      const T inv = T(1) / T(nk);
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) s[i] = w[i] * inv;
+    }
+    if (is_leaf) {
+      // kern_FindLeafSinkPotential (:166-174) + kern_ApplyCapacity (:187-198)
+      T* s = sink[v].data(); const T* c = sink[t.parent[v]].data(); const T* d = div[v].data();
+      const T* uu = u[v].data(); const float* D = data[v];
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        T val = (c[i] - d[i]) + uu[i] * icc;
+        T cap = T(D[i]);
+        val = (val < T(0)) ? T(0) : val;
+        val = (val > cap) ? cap : val;
+        s[i] = val;
+      }
+    }
+    for (int k = nk - 1; k >= 0; --k) {
+      // kern_UpdateLabel (:211-220)
+      int kid = t.kids[v][k];
+      const T* s = sink[kid].data(); const T* c = sink[v].data(); const T* d = div[kid].data();
+      T* uu = u[kid].data();
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) uu[i] = sat01(uu[i] + cc * ((c[i] - d[i]) - s[i]));
+    }
+    if (!is_root) {
+      // kern_FindSourcePotentialAndStore (:145-153)
+      T* w = work[t.parent[v]].data(); const T* s = sink[v].data(); const T* d = div[v].data();
+      const T* uu = u[v].data();
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < n; ++i) w[i] = ((w[i] + s[i]) + d[i]) - uu[i] * icc;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// REF_CPU: per-voxel loops of vtkMaxFlowSegmentationUtilities.cxx restated.
+// The reference reads a few floats outside some buffers (its neighbour tests
+// are inverted); here those reads are guarded and give 0, the value the
+// oracle's padded buffers hold there.  With the flows identically zero (the
+// reference multiplies them, :261-273) those terms never reach a result.
+// ---------------------------------------------------------------------------
+struct PortUtils {
+  static void zeroOut(float* b, int n) {
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) b[x] = 0.0f;
+  }
+  static void setValue(float* b, float v, int n) {
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) b[x] = v;
+  }
+  static void sum(float* o, float* i, int n) {  // :53-59
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) o[x] += i[x];
+  }
+  static void copy(float* o, float* i, int n) {  // :69-75
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) o[x] = i[x];
+  }
+  static void min(float* o, float* i, int n) {  // :77-83
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) o[x] = (o[x] > i[x]) ? i[x] : o[x];
+  }
+  static void div(float* o, float* i, int n) {  // :85-91
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) o[x] /= i[x];
+  }
+  static void divAndStore(float* o, float* i, float v, int n) {  // :93-99
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) o[x] = i[x] / v;
+  }
+  static void lbl(float* l, float* s, float* c, int n) {  // :101-107
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) l[x] = (s[x] == c[x]) ? 1.0f : 0.0f;
+  }
+  static void constrain(float* s, float* c, int n) {  // :109-115
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) s[x] = (s[x] > c[x]) ? c[x] : s[x];
+  }
+  static void leafSink(float* s, float* inc, float* d, float* l, float CC, int n) {  // :117-123
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) s[x] = inc[x] - d[x] + l[x] / CC;
+  }
+  static void label(float* s, float* inc, float* d, float* l, float CC, int n) {  // :125-131
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) l[x] += CC * (inc[x] - d[x] - s[x]);
+  }
+  static void storeSink(float* w, float* inc, float* d, float* l, float CC, int n) {  // :141-147
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) w[x] = inc[x] - d[x] + l[x] / CC;
+  }
+  static void storeSource(float* w, float* s, float* d, float* l, float CC, int n) {  // :156-162
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) w[x] += s[x] + d[x] - l[x] / CC;
+  }
+  static void gradStep(float* s, float* inc, float* d, float* l, float step, float CC, int n) {  // :253-259
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] = step * (s[x] + d[x] - inc[x] - l[x] / CC);
+  }
+  static void applyStep(float* d, float* fx, float* fy, float* fz, int VX, int VY, int VZ, int n) {  // :261-273
+    (void)VZ;
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) {
+      float cur = d[x];
+      float xa = (x % VX) ? d[x - 1] : 0.0f;
+      fx[x] *= 0.5f * (cur - xa);
+      float ya = (x / VX % VY) ? d[x - VX] : 0.0f;
+      fy[x] *= 0.5f * (cur - ya);
+      float za = (x >= VX * VY) ? d[x - VX * VY] : 0.0f;
+      fz[x] *= 0.5f * (cur - za);
+    }
+  }
+  static void flowMag(float* d, float* fx, float* fy, float* fz, float* sm, float alpha,
+                      int VX, int VY, int VZ, int n) {  // :275-307
+    (void)fy; (void)fz; (void)VZ;
+    auto at = [&](long k) -> float { return (k >= 0 && k < n) ? fx[k] : 0.0f; };
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] = fx[x] * fx[x] + fy[x] * fy[x] + fz[x] * fz[x];
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] += ((x + 1) % VX) ? 0.0f : at(x + 1) * at(x + 1);
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] += (((x + VX) / VX) % VY) ? 0.0f : at((long)x + VX) * at((long)x + VX);
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n - VX * VY; ++x) d[x] += fx[x + VX * VY] * fx[x + VX * VY];
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] = sqrtf(d[x]);
+    if (sm) {
+#pragma omp parallel for schedule(static)
+      for (int x = 0; x < n; ++x) d[x] = (d[x] > alpha * sm[x]) ? alpha * sm[x] / d[x] : 1.0f;
+    } else {
+#pragma omp parallel for schedule(static)
+      for (int x = 0; x < n; ++x) d[x] = (d[x] > alpha) ? alpha / d[x] : 1.0f;
+    }
+  }
+  static void project(float* d, float* fx, float* fy, float* fz, int VX, int VY, int VZ, int n) {  // :309-339
+    auto atz = [&](long k) -> float { return (k >= 0 && k < n) ? fz[k] : 0.0f; };
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) {
+      float cur = d[x];
+      float xa = (x % VX) ? d[x - 1] : -cur;
+      fx[x] *= 0.5f * (cur + xa);
+      float ya = (x / VX % VY) ? d[x - VX] : -cur;
+      fy[x] *= 0.5f * (cur + ya);
+      float za = (x >= VX * VY) ? d[x - VX * VY] : -cur;
+      fz[x] *= 0.5f * (cur + za);
+    }
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] = fx[x] + fy[x] + fz[x];
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] -= (x % VX) ? fx[x - 1] : 0.0f;
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] -= (x / VX % VY) ? fy[x - VX] : 0.0f;
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < n; ++x) d[x] -= (x >= VX * VY) ? atz((long)x - (long)VX * VZ) : 0.0f;
+  }
+};
+
+#ifdef HMF_ORACLE_WITH_REFERENCE
+struct RefUtils {
+  static void zeroOut(float* b, int n) { zeroOutBuffer(b, n); }
+  static void setValue(float* b, float v, int n) { setBufferToValue(b, v, n); }
+  static void sum(float* o, float* i, int n) { sumBuffer(o, i, n); }
+  static void copy(float* o, float* i, int n) { copyBuffer(o, i, n); }
+  static void min(float* o, float* i, int n) { minBuffer(o, i, n); }
+  static void div(float* o, float* i, int n) { divBuffer(o, i, n); }
+  static void divAndStore(float* o, float* i, float v, int n) { divAndStoreBuffer(o, i, v, n); }
+  static void lbl(float* l, float* s, float* c, int n) { lblBuffer(l, s, c, n); }
+  static void constrain(float* s, float* c, int n) { constrainBuffer(s, c, n); }
+  static void leafSink(float* s, float* inc, float* d, float* l, float CC, int n) { updateLeafSinkFlow(s, inc, d, l, CC, n); }
+  static void label(float* s, float* inc, float* d, float* l, float CC, int n) { updateLabel(s, inc, d, l, CC, n); }
+  static void storeSink(float* w, float* inc, float* d, float* l, float CC, int n) { storeSinkFlowInBuffer(w, inc, d, l, CC, n); }
+  static void storeSource(float* w, float* s, float* d, float* l, float CC, int n) { storeSourceFlowInBuffer(w, s, d, l, CC, n); }
+  static void gradStep(float* s, float* inc, float* d, float* l, float st, float CC, int n) { ghmf_flowGradientStep(s, inc, d, l, st, CC, n); }
+  static void applyStep(float* d, float* fx, float* fy, float* fz, int VX, int VY, int VZ, int n) { ghmf_applyStep(d, fx, fy, fz, VX, VY, VZ, n); }
+  static void flowMag(float* d, float* fx, float* fy, float* fz, float* sm, float a, int VX, int VY, int VZ, int n) { ghmf_computeFlowMag(d, fx, fy, fz, sm, a, VX, VY, VZ, n); }
+  static void project(float* d, float* fx, float* fy, float* fz, int VX, int VY, int VZ, int n) { ghmf_projectOntoSet(d, fx, fy, fz, VX, VY, VZ, n); }
+};
+#endif
+
+// Restatement of vtkHierarchicalMaxFlowSegmentation.cxx:973-1259 over a Utils policy.
+// Every buffer carries `pad` zero floats on both sides so that the reference's
+// loops, which index a little outside their buffers, stay inside memory here.
+template <class U>
+struct CpuDriver {
+  const Tree& t;
+  int VX, VY, VZ, V;
+  long pad;
+  std::vector<std::vector<float>> store;
+  std::vector<float*> fx, fy, fz, div, sink, inc, lab, work;
+  std::vector<float*> data, smooth;
+  std::vector<float> alpha;
+  float step, cc;
+
+  CpuDriver(const Tree& tr, int vx, int vy, int vz) : t(tr), VX(vx), VY(vy), VZ(vz) {
+    V = vx * vy * vz;
+    pad = (long)vx * (vy + vz + 2) + 16;
+  }
+  float* buffer() {
+    store.emplace_back((size_t)(V + 2 * pad), 0.0f);
+    return store.back().data() + pad;
+  }
+  void alloc() {
+    int n = t.n;
+    fx.assign(n, nullptr); fy = fx; fz = fx; div = fx; sink = fx; inc = fx; lab = fx; work = fx;
+    store.reserve(8 * n + 4);
+    for (int v = 0; v < n; ++v) {
+      sink[v] = buffer();
+      if (!t.leaf(v)) work[v] = buffer();
+      if (v != t.root) { fx[v] = buffer(); fy[v] = buffer(); fz[v] = buffer(); div[v] = buffer(); lab[v] = buffer(); }
+    }
+    for (int v = 0; v < n; ++v) if (v != t.root) inc[v] = sink[t.parent[v]];  // :872-905
+  }
+  void init() {  // :973-1031
+    std::vector<int> leaves;
+    for (int v : t.preorder) if (t.leaf(v)) leaves.push_back(v);
+    for (int v = 0; v < t.n; ++v) if (v != t.root && !t.leaf(v)) {
+      U::zeroOut(fx[v], V); U::zeroOut(fy[v], V); U::zeroOut(fz[v], V); U::zeroOut(div[v], V);
+    }
+    for (int l : leaves) { U::zeroOut(fx[l], V); U::zeroOut(fy[l], V); U::zeroOut(fz[l], V); U::zeroOut(div[l], V); }
+    for (int l : leaves) U::copy(sink[l], data[l], V);
+    for (size_t k = 1; k < leaves.size(); ++k) U::min(sink[leaves[0]], sink[leaves[k]], V);
+    float* src_work = work[t.root];
+    U::zeroOut(src_work, V);
+    U::lbl(lab[leaves[0]], sink[leaves[0]], data[leaves[0]], V);
+    U::sum(src_work, lab[leaves[0]], V);
+    for (size_t k = 1; k < leaves.size(); ++k) {
+      U::copy(sink[leaves[k]], sink[leaves[0]], V);
+      U::lbl(lab[leaves[k]], sink[leaves[k]], data[leaves[k]], V);
+      U::sum(src_work, lab[leaves[k]], V);
+    }
+    for (int l : leaves) U::div(lab[l], src_work, V);
+    for (int v : t.preorder) if (v != t.root && !t.leaf(v)) U::copy(sink[v], sink[leaves[0]], V);
+    U::copy(sink[t.root], sink[leaves[0]], V);
+    propagate(t.root);
+  }
+  void propagate(int v) {  // :1047-1081
+    if (!t.leaf(v)) { if (v != t.root) U::zeroOut(lab[v], V); }
+    for (int k : t.kids[v]) propagate(k);
+    if (v == t.root) return;
+    int p = t.parent[v];
+    if (p == t.root) return;
+    U::sum(lab[p], lab[v], V);
+  }
+  void solve(int v) {  // :1083-1240
+    const bool is_root = (v == t.root), is_leaf = t.leaf(v), is_branch = !is_root && !is_leaf;
+    const int nk = (int)t.kids[v].size();
+    if (!is_leaf) {
+      if (is_branch) U::zeroOut(work[v], V);
+      else U::setValue(work[v], 1.0f / cc, V);
+    }
+    if (!is_root) {
+      U::gradStep(sink[v], inc[v], div[v], lab[v], step, cc, V);
+      U::applyStep(div[v], fx[v], fy[v], fz[v], VX, VY, VZ, V);
+      U::flowMag(div[v], fx[v], fy[v], fz[v], smooth[v], alpha[v], VX, VY, VZ, V);
+      U::project(div[v], fx[v], fy[v], fz[v], VX, VY, VZ, V);
+    }
+    for (int k : t.kids[v]) solve(k);
+    if (is_branch) {
+      U::storeSink(work[v], inc[v], div[v], lab[v], cc, V);
+      // The reference passes (working, sink): the branch sink is the input and
+      // the working buffer the output (:1186-1187).
+      U::divAndStore(work[v], sink[v], (float)(nk + 1), V);
+    }
+    if (is_root) U::divAndStore(work[v], sink[v], (float)nk, V);  // same order, :1196
+    if (is_leaf) {
+      U::leafSink(sink[v], inc[v], div[v], lab[v], cc, V);
+      U::constrain(sink[v], data[v], V);
+    }
+    for (int k = nk - 1; k >= 0; --k) {
+      int kid = t.kids[v][k];
+      U::label(sink[kid], inc[kid], div[kid], lab[kid], cc, V);
+    }
+    if (!is_root) U::storeSource(work[t.parent[v]], sink[v], div[v], lab[v], cc, V);
+  }
+};
+
+struct Problem {
+  int vx, vy, vz, n_nodes;
+  const int* parent;
+  const float* const* data;
+  const float* const* smooth;
+  const double* alpha;
+  int iterations;
+  float step, cc;
+};
+
+template <class T>
+int run_cuda_semantics(const Problem& P, const Tree& t, double* u_out, double* sink_out, double* div_out) {
+  CudaOracle<T> o(t, P.vx, P.vy, P.vz);
+  o.alloc();
+  o.data.assign(t.n, nullptr); o.smooth.assign(t.n, nullptr); o.alpha.assign(t.n, T(1));
+  for (int v = 0; v < t.n; ++v) {
+    o.data[v] = P.data ? P.data[v] : nullptr;
+    o.smooth[v] = P.smooth ? P.smooth[v] : nullptr;
+    // the reference stores the scalar as float (leafSmoothnessConstants, :692)
+    o.alpha[v] = P.alpha ? T((float)P.alpha[v]) : T(1);
+  }
+  for (int v = 0; v < t.n; ++v) if (t.leaf(v) && !o.data[v]) { g_err = "missing data term for a leaf"; return -3; }
+  if (sizeof(T) == sizeof(float)) {
+    o.step = T(P.step); o.cc = T(P.cc);
+    o.icc = T(1.0f / P.cc);       // host-side 1.0f/CC (CUDA_hierarchicalmaxflow.cu:138)
+    o.root_work = T(1.0f / P.cc);  // CUDA_SetBufferToValue(…, 1.0f/CC) (.cxx:139)
+  } else {
+    o.step = T(P.step); o.cc = T(P.cc);
+    o.icc = T(1) / T(P.cc);
+    o.root_work = T(1) / T(P.cc);
+  }
+  o.init();
+  for (int it = 0; it < P.iterations; ++it) o.solve(t.root);
+  const long V = o.V;
+  for (int v = 0; v < t.n; ++v) {
+    for (long i = 0; i < V; ++i) {
+      if (u_out) u_out[(long)v * V + i] = (v == t.root) ? 0.0 : (double)o.u[v][i];
+      if (sink_out) sink_out[(long)v * V + i] = (double)o.sink[v][i];
+      if (div_out) div_out[(long)v * V + i] = (v == t.root) ? 0.0 : (double)o.div[v][i];
+    }
+  }
+  return 0;
+}
+
+template <class U>
+int run_cpu_semantics(const Problem& P, const Tree& t, double* u_out, double* sink_out, double* div_out) {
+  CpuDriver<U> d(t, P.vx, P.vy, P.vz);
+  d.alloc();
+  d.data.assign(t.n, nullptr); d.smooth.assign(t.n, nullptr); d.alpha.assign(t.n, 1.0f);
+  std::vector<std::vector<float>> copies;
+  copies.reserve(2 * t.n);
+  for (int v = 0; v < t.n; ++v) {
+    if (P.data && P.data[v]) {
+      copies.emplace_back(P.data[v], P.data[v] + d.V);
+      d.data[v] = copies.back().data();
+    }
+    if (P.smooth && P.smooth[v]) {
+      copies.emplace_back(P.smooth[v], P.smooth[v] + d.V);
+      d.smooth[v] = copies.back().data();
+    }
+    d.alpha[v] = P.alpha ? (float)P.alpha[v] : 1.0f;
+  }
+  for (int v = 0; v < t.n; ++v) if (t.leaf(v) && !d.data[v]) { g_err = "missing data term for a leaf"; return -3; }
+  d.step = P.step; d.cc = P.cc;
+  d.init();
+  for (int it = 0; it < P.iterations; ++it) d.solve(t.root);
+  const long V = d.V;
+  for (int v = 0; v < t.n; ++v) {
+    for (long i = 0; i < V; ++i) {
+      if (u_out) u_out[(long)v * V + i] = (v == t.root) ? 0.0 : (double)d.lab[v][i];
+      if (sink_out) sink_out[(long)v * V + i] = (double)d.sink[v][i];
+      if (div_out) div_out[(long)v * V + i] = (v == t.root) ? 0.0 : (double)d.div[v][i];
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// semantics: 0 = REF_CUDA, 1 = REF_CPU.  precision: 32 or 64 (REF_CUDA only).
+// Outputs (each [n_nodes * V] doubles, row v = vertex v, may be NULL):
+//   u_out labels (root row 0), sink_out sinks (root row = source flow),
+//   div_out divergence buffers (root row 0).
+// Returns 0 on success, a negative code on error (oracle_last_error()).
+#ifdef HMF_ORACLE_WITH_REFERENCE
+#define ORACLE_ENTRY oracle_ref_hmf_solve
+#else
+#define ORACLE_ENTRY oracle_hmf_solve
+#endif
+int ORACLE_ENTRY(int semantics, int precision, int threads, int vx, int vy, int vz,
+                 int n_nodes, const int* parent, const float* const* data,
+                 const float* const* smooth, const double* alpha, int iterations,
+                 float step, float cc, double* u_out, double* sink_out, double* div_out) {
+  g_err.clear();
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  if (vx <= 0 || vy <= 0 || vz <= 0) { g_err = "bad dimensions"; return -1; }
+  if ((long)vx * vy * vz > 0x7fffffffL) { g_err = "volume too large for the oracle"; return -1; }
+  Tree t;
+  if (!t.build(n_nodes, parent)) return -2;
+  Problem P{vx, vy, vz, n_nodes, parent, data, smooth, alpha, iterations, step, cc};
+#ifdef HMF_ORACLE_WITH_REFERENCE
+  if (semantics != 1) { g_err = "the reference build only restates REF_CPU"; return -4; }
+  (void)precision;
+  return run_cpu_semantics<RefUtils>(P, t, u_out, sink_out, div_out);
+#else
+  if (semantics == 1) return run_cpu_semantics<PortUtils>(P, t, u_out, sink_out, div_out);
+  if (semantics != 0) { g_err = "unknown semantics"; return -4; }
+  if (precision == 64) return run_cuda_semantics<double>(P, t, u_out, sink_out, div_out);
+  return run_cuda_semantics<float>(P, t, u_out, sink_out, div_out);
+#endif
+}
+
+const char* oracle_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"

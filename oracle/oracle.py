@@ -1,0 +1,114 @@
+"""ctypes front end of the oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py (its cpu_baseline leg and
+its reference arm) import this module, and only as the checker or as the CPU
+baseline.  The product (robartsvtk_gb300) never does.
+
+`solve()` runs hmf_oracle.cpp (REF_CUDA in FP32/FP64, or the REF_CPU port);
+`solve_reference_cpu()` runs the same REF_CPU driver linked against the
+reference's own compiled vtkMaxFlowSegmentationUtilities.cxx (only where the
+reference sources were available to build it).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+REF_CUDA = 0
+REF_CPU = 1
+
+_libs: dict[str, ctypes.CDLL] = {}
+
+
+def _load(path: str, entry: str) -> ctypes.CDLL:
+    if path in _libs:
+        return _libs[path]
+    lib = ctypes.CDLL(path)
+    fn = getattr(lib, entry)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p),
+                   ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                   ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.oracle_last_error.restype = ctypes.c_char_p
+    _libs[path] = lib
+    return lib
+
+
+def port_library() -> ctypes.CDLL:
+    return _load(build_oracle.build_port(), "oracle_hmf_solve")
+
+
+def reference_library() -> ctypes.CDLL | None:
+    path = os.path.join(build_oracle.REF_OUT, "libhmf_ref_cpu.so")
+    if not os.path.exists(path):
+        if build_oracle.build_reference_cpu() is None:
+            return None
+    try:
+        return _load(path, "oracle_ref_hmf_solve")
+    except OSError:
+        return None  # e.g. a library built for another host architecture
+
+
+def _call(lib, entry, semantics, precision, threads, dims, parent, data, smooth, alpha,
+          iterations, step, cc, want_sink, want_div):
+    vx, vy, vz = (int(d) for d in dims)
+    n = len(parent)
+    V = vx * vy * vz
+    par = (ctypes.c_int * n)(*[int(p) for p in parent])
+    keep = []
+    dptr = (ctypes.c_void_p * n)()
+    sptr = (ctypes.c_void_p * n)()
+    for v in range(n):
+        d = data.get(v) if data is not None else None
+        if d is not None:
+            a = np.ascontiguousarray(d, dtype=np.float32).reshape(-1)
+            assert a.size == V
+            keep.append(a)
+            dptr[v] = a.ctypes.data
+        s = smooth.get(v) if smooth is not None else None
+        if s is not None:
+            a = np.ascontiguousarray(s, dtype=np.float32).reshape(-1)
+            assert a.size == V
+            keep.append(a)
+            sptr[v] = a.ctypes.data
+    al = (ctypes.c_double * n)(*[float(alpha.get(v, 1.0)) if alpha else 1.0 for v in range(n)])
+    u = np.zeros((n, V), dtype=np.float64)
+    sink = np.zeros((n, V), dtype=np.float64) if want_sink else None
+    div = np.zeros((n, V), dtype=np.float64) if want_div else None
+    rc = getattr(lib, entry)(semantics, precision, threads, vx, vy, vz, n, par, dptr, sptr, al,
+                             int(iterations), float(step), float(cc), u.ctypes.data,
+                             sink.ctypes.data if sink is not None else None,
+                             div.ctypes.data if div is not None else None)
+    if rc != 0:
+        raise RuntimeError("oracle failed (%d): %s" % (rc, lib.oracle_last_error().decode()))
+    shape = (n, vz, vy, vx)
+    out = {"u": u.reshape(shape)}
+    if sink is not None:
+        out["sink"] = sink.reshape(shape)
+    if div is not None:
+        out["div"] = div.reshape(shape)
+    return out
+
+
+def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1, cc=0.25,
+          semantics=REF_CUDA, precision=32, threads=0, want_sink=False, want_div=False):
+    """Run the oracle.  `dims` = (VX, VY, VZ); `parent` = parent id per vertex
+    (-1 for the root); `data`/`smooth`/`alpha` = dicts keyed by vertex id.
+    Returns {"u": [n, VZ, VY, VX] float64 labels, optional "sink", "div"}."""
+    return _call(port_library(), "oracle_hmf_solve", semantics, precision, threads, dims, parent,
+                 data, smooth, alpha, iterations, step, cc, want_sink, want_div)
+
+
+def solve_reference_cpu(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1,
+                        cc=0.25, want_sink=False, want_div=False):
+    """REF_CPU through the reference's own compiled utility loops (single thread)."""
+    lib = reference_library()
+    if lib is None:
+        raise FileNotFoundError("reference CPU library not built (reference sources absent)")
+    return _call(lib, "oracle_ref_hmf_solve", REF_CPU, 32, 1, dims, parent, data, smooth, alpha,
+                 iterations, step, cc, want_sink, want_div)

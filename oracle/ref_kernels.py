@@ -1,0 +1,253 @@
+"""Runs the reference's own HMF CUDA kernels -- TEST INFRASTRUCTURE ONLY.
+
+oracle/build_oracle.py compiles ImageProcessing/vtkCudaImageAnalytics/CUDA_hierarchicalmaxflow.cu
+and Common/vtkCudaCommonStatic/CUDA_commonKernels.cu, unmodified, from the
+reference tree into oracle/_ref/hmf_ref_kernels.cubin.  This module loads that
+cubin through the CUDA driver API and replays the reference host code's launch
+sequence:
+    InitializeAlgorithm  vtkCudaHierarchicalMaxFlowSegmentation.cxx:547-658
+    PropogateLabels      :63-104
+    SolveMaxFlow         :106-427
+    UpdateLabel          :429-476
+with every buffer resident and padded by VX*VY floats on each side, as the
+reference allocates them (:513-538, CUDA_hierarchicalmaxflow.cu:33-60), since
+its kernels read up to one plane outside a buffer before masking.  Buffers are
+torch CUDA tensors; kernels run on torch's current stream.
+
+It is used only to generate golden vectors (tests/golden/make_golden.py) and
+to pin the REF_CUDA oracle; nothing in the product imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+CUBIN = os.path.join(build_oracle.REF_OUT, "hmf_ref_kernels.cubin")
+NUMTHREADS = 512  # vtkCudaCommon.h:23
+
+_NAMES = {
+    "zero": "_Z13ZeroOutBufferIfEvPT_i",
+    "setconst": "_Z16SetBufferToConstIfEvPT_S0_i",
+    "sum": "_Z10SumBuffersIfEvPT_S1_i",
+    "copy": "_Z11CopyBuffersIfEvPT_S1_i",
+    "mulstore": "_Z22MultiplyAndStoreBufferIfEvPT_S1_S0_i",
+    "min": "_Z15kern_MinBuffersPfS_i",
+    "lbl": "_Z8kern_LblPfS_S_i",
+    "divbuf": "_Z18kern_DivideBuffersPfS_i",
+    "sinkstore": "_Z30kern_FindSinkPotentialAndStorePfS_S_S_fi",
+    "sourcestore": "_Z32kern_FindSourcePotentialAndStorePfS_S_S_fi",
+    "leafsink": "_Z26kern_FindLeafSinkPotentialPfS_S_S_fi",
+    "capacity": "_Z18kern_ApplyCapacityPfS_i",
+    "label": "_Z16kern_UpdateLabelPfS_S_S_fi",
+    "gradstep": "_Z17kern_CalcGradStepPfS_S_S_ffi",
+    "descent": "_Z23kern_DescentSpatialFlowPfS_S_S_4int2i",
+    "magvari": "_Z29kern_ComputeFlowMagVariSmoothPfS_S_S_S_f4int2i",
+    "magconst": "_Z30kern_ComputeFlowMagConstSmoothPfS_S_S_f4int2i",
+    "project": "_Z12kern_ProjectPfS_S_S_4int2i",
+    "divergence": "_Z15kern_DivergencePfS_S_S_4int2i",
+}
+
+
+class _Int2(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_int), ("y", ctypes.c_int)]
+
+
+class _Ptr(int):
+    """A device address (kept apart from int kernel arguments)."""
+
+
+def available() -> bool:
+    return os.path.exists(CUBIN)
+
+
+class ReferenceKernels:
+    def __init__(self):
+        import torch
+
+        torch.cuda.init()
+        torch.zeros(1, device="cuda")  # make the primary context current
+        self.torch = torch
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        self.module = ctypes.c_void_p()
+        self._ck(self.cu.cuModuleLoad(ctypes.byref(self.module), CUBIN.encode()), "cuModuleLoad")
+        self.fn = {}
+        for key, name in _NAMES.items():
+            f = ctypes.c_void_p()
+            self._ck(self.cu.cuModuleGetFunction(ctypes.byref(f), self.module, name.encode()), name)
+            self.fn[key] = f
+
+    @staticmethod
+    def _ck(rc, what):
+        if rc != 0:
+            raise RuntimeError("CUDA driver call %s failed with %d" % (what, rc))
+
+    def launch(self, key, size, *args):
+        cargs = []
+        for a in args:
+            if isinstance(a, _Int2):
+                cargs.append(a)
+            elif isinstance(a, _Ptr):
+                cargs.append(ctypes.c_void_p(int(a)))
+            elif isinstance(a, float):
+                cargs.append(ctypes.c_float(a))
+            elif isinstance(a, int):
+                cargs.append(ctypes.c_int(a))
+            else:
+                raise TypeError("unsupported kernel argument %r" % (a,))
+        ptrs = (ctypes.c_void_p * len(cargs))(*[ctypes.cast(ctypes.pointer(c), ctypes.c_void_p) for c in cargs])
+        grid = (size - 1) // NUMTHREADS + 1
+        stream = ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        self._ck(self.cu.cuLaunchKernel(self.fn[key], grid, 1, 1, NUMTHREADS, 1, 1, 0, stream, ptrs, None), key)
+
+
+def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1, cc=0.25):
+    """REF_CUDA through the reference's own kernels.  Arguments as
+    oracle.oracle.solve(); returns {"u": [n, VZ, VY, VX] float32, "sink": ...}."""
+    import torch
+
+    K = ReferenceKernels()
+    vx, vy, vz = (int(d) for d in dims)
+    V = vx * vy * vz
+    pad = vx * vy + 2 * NUMTHREADS
+    n = len(parent)
+    kids = [[] for _ in range(n)]
+    root = -1
+    for v, p in enumerate(parent):
+        if p < 0:
+            root = v
+        else:
+            kids[p].append(v)
+    order = []
+    stack = [root]
+    while stack:
+        v = stack.pop()
+        order.append(v)
+        stack.extend(reversed(kids[v]))
+    leaves = [v for v in order if not kids[v]]
+    keep = []
+
+    def buf(init=None):
+        t = torch.zeros(V + 2 * pad, dtype=torch.float32, device="cuda")
+        if init is not None:
+            t[pad:pad + V] = torch.from_numpy(np.ascontiguousarray(init, dtype=np.float32).reshape(-1)).cuda()
+        keep.append(t)
+        return _Ptr(t.data_ptr() + 4 * pad)
+
+    fx, fy, fz, dv, sink, lab, work = ({} for _ in range(7))
+    for v in range(n):
+        sink[v] = buf()
+        if not kids[v]:
+            pass
+        else:
+            work[v] = buf()
+        if v != root:
+            fx[v], fy[v], fz[v], dv[v], lab[v] = buf(), buf(), buf(), buf(), buf()
+    D = {l: buf(data[l]) for l in leaves}
+    S = {}
+    for v in range(n):
+        if smooth is not None and smooth.get(v) is not None:
+            S[v] = buf(smooth[v])
+    a = {v: float(np.float32((alpha or {}).get(v, 1.0))) for v in range(n)}
+    inc = {v: sink[parent[v]] for v in range(n) if v != root}
+    dims2 = _Int2(vx, vy)
+    step = float(np.float32(step))
+    cc = float(np.float32(cc))
+    icc = float(np.float32(1.0) / np.float32(cc))
+
+    # InitializeAlgorithm (.cxx:547-658)
+    for v in range(n):
+        if v != root:
+            for b in (fx[v], fy[v], fz[v], dv[v]):
+                K.launch("zero", V, b, V)
+    for l in leaves:
+        K.launch("copy", V, sink[l], D[l], V)
+    for l in leaves[1:]:
+        K.launch("min", V, sink[leaves[0]], sink[l], V)
+    K.launch("zero", V, work[root], V)
+    K.launch("lbl", V, lab[leaves[0]], sink[leaves[0]], D[leaves[0]], V)
+    K.launch("sum", V, work[root], lab[leaves[0]], V)
+    for l in leaves[1:]:
+        K.launch("copy", V, sink[l], sink[leaves[0]], V)
+        K.launch("lbl", V, lab[l], sink[l], D[l], V)
+        K.launch("sum", V, work[root], lab[l], V)
+    for l in leaves:
+        K.launch("divbuf", V, lab[l], work[root], V)
+    for v in order:
+        if v != root and kids[v]:
+            K.launch("copy", V, sink[v], sink[leaves[0]], V)
+    K.launch("copy", V, sink[root], sink[leaves[0]], V)
+
+    def propagate(v):  # :63-104
+        if kids[v] and v != root:
+            K.launch("zero", V, lab[v], V)
+        for k in kids[v]:
+            propagate(k)
+        if v == root or parent[v] == root:
+            return
+        K.launch("sum", V, lab[parent[v]], lab[v], V)
+
+    propagate(root)
+
+    def update_label(v):  # :429-476
+        if v == root:
+            return
+        K.launch("label", V, sink[v], inc[v], dv[v], lab[v], cc, V)
+
+    def solve_node(v):  # :106-427
+        is_root, is_leaf = v == root, not kids[v]
+        is_branch = not is_root and not is_leaf
+        if not is_leaf:
+            if is_branch:
+                K.launch("zero", V, work[v], V)
+            else:
+                K.launch("setconst", V, work[v], float(np.float32(1.0) / np.float32(cc)), V)
+        if not is_root:
+            K.launch("gradstep", V, sink[v], inc[v], dv[v], lab[v], step, icc, V)
+            K.launch("descent", V, dv[v], fx[v], fy[v], fz[v], dims2, V)
+            if v in S:
+                K.launch("magvari", V, dv[v], fx[v], fy[v], fz[v], S[v], a[v], dims2, V)
+            else:
+                K.launch("magconst", V, dv[v], fx[v], fy[v], fz[v], a[v], dims2, V)
+            K.launch("project", V, dv[v], fx[v], fy[v], fz[v], dims2, V)
+            K.launch("divergence", V, dv[v], fx[v], fy[v], fz[v], dims2, V)
+        for k in kids[v]:
+            solve_node(k)
+        if is_branch:
+            K.launch("sinkstore", V, work[v], inc[v], dv[v], lab[v], icc, V)
+            K.launch("mulstore", V, work[v], sink[v], float(np.float32(1.0) / np.float32(len(kids[v]) + 1)), V)
+        if is_root:
+            K.launch("mulstore", V, work[v], sink[v], float(np.float32(1.0) / np.float32(len(kids[v]))), V)
+        if is_leaf:
+            K.launch("leafsink", V, sink[v], inc[v], dv[v], lab[v], icc, V)
+            K.launch("capacity", V, sink[v], D[v], V)
+        for k in reversed(kids[v]):
+            update_label(k)
+        if not is_root:
+            K.launch("sourcestore", V, work[parent[v]], sink[v], dv[v], lab[v], icc, V)
+
+    for _ in range(int(iterations)):
+        solve_node(root)
+    torch.cuda.synchronize()
+
+    def fetch(p):
+        return _as_tensor(keep, p, V, pad).cpu().numpy().reshape(vz, vy, vx)
+
+    u = np.zeros((n, vz, vy, vx), dtype=np.float32)
+    s = np.zeros((n, vz, vy, vx), dtype=np.float32)
+    for v in range(n):
+        s[v] = fetch(sink[v])
+        if v != root:
+            u[v] = fetch(lab[v])
+    return {"u": u, "sink": s}
+
+
+def _as_tensor(keep, ptr, V, pad):
+    for t in keep:
+        base = t.data_ptr() + 4 * pad
+        if base == ptr:
+            return t[pad:pad + V]
+    raise KeyError("unknown buffer")

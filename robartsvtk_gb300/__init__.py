@@ -1,0 +1,11 @@
+"""robartsvtk_gb300 -- GB300-native (sm_103a) hierarchical continuous max-flow
+segmentation, a drop-in for RobartsVTK's vtkHierarchicalMaxFlowSegmentation /
+vtkCudaHierarchicalMaxFlowSegmentation path.
+
+The compute is libhmf_gb300.so (CUDA kernels + C ABI, include/hmf.h); this
+package binds it and mirrors the reference's filter API.
+"""
+from .segmentation import (REF_CPU, REF_CUDA, HierarchicalMaxFlowSegmentation, HMFError,  # noqa: F401
+                           HMFSolver)
+
+__all__ = ["HMFSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]

@@ -1,0 +1,87 @@
+"""ctypes binding of the C ABI in include/hmf.h (libhmf_gb300.so).
+
+The library is the product: there is no Python or CPU fallback.  Loading
+fails loudly when the shared library is missing or cannot be built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+HMF_OK = 0
+HMF_HOST = 0
+HMF_DEVICE = 1
+HMF_SEMANTICS_REF_CUDA = 0
+HMF_SEMANTICS_REF_CPU = 1
+
+ERRORS = {
+    -1: "HMF_ERR_INVALID_ARGUMENT",
+    -2: "HMF_ERR_TREE",
+    -3: "HMF_ERR_MISSING_INPUT",
+    -4: "HMF_ERR_CUDA",
+    -5: "HMF_ERR_OUT_OF_MEMORY",
+    -6: "HMF_ERR_STATE",
+}
+
+# (name, restype, argtypes) of every symbol declared in include/hmf.h
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+SIGNATURES = [
+    ("hmf_create", _I, [ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_I), _I, _I, _I]),
+    ("hmf_destroy", _I, [_P]),
+    ("hmf_set_data", _I, [_P, _I, _P, _I]),
+    ("hmf_set_smoothness", _I, [_P, _I, _P, _I]),
+    ("hmf_set_smoothness_scalar", _I, [_P, _I, ctypes.c_double]),
+    ("hmf_set_params", _I, [_P, _I, ctypes.c_float, ctypes.c_float]),
+    ("hmf_solve", _I, [_P, _P]),
+    ("hmf_get_labels", _I, [_P, _I, _P, _I, _P]),
+    ("hmf_get_sink", _I, [_P, _I, _P, _I, _P]),
+    ("hmf_leaf_order", _I, [_P, ctypes.POINTER(_I), _I]),
+    ("hmf_device_bytes", ctypes.c_size_t, [_P]),
+    ("hmf_set_timing", _I, [_P, _I]),
+    ("hmf_get_stats", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _I]),
+    ("hmf_last_error", ctypes.c_char_p, [_P]),
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+class HMFError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "HMF_ERR"), code, message))
+        self.code = code
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libhmf_gb300.so (building it first if needed) and bind its symbols."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise FileNotFoundError("libhmf_gb300.so is not built: run robartsvtk_gb300.build.build()")
+        lib = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(rc: int, ctx=None) -> int:
+    if rc < 0:
+        msg = load().hmf_last_error(ctx)
+        raise HMFError(rc, msg.decode() if msg else "")
+    return rc

@@ -1,0 +1,697 @@
+// hmf_capi.cu -- the C ABI of include/hmf.h: solver context, device memory
+// plan, input staging and the launch sequence of one solve.
+//
+// Reference counterparts:
+//  - buffer plan      vtkHierarchicalMaxFlowSegmentation.cxx:711-905 (host) and
+//                     vtkCudaHierarchicalMaxFlowSegmentation.cxx:513-538 (device)
+//  - initialisation   vtkCudaHierarchicalMaxFlowSegmentation.cxx:478-667
+//  - iteration loop   vtkCudaHierarchicalMaxFlowSegmentation.cxx:669-716
+// The reference pages buffers between host and device when the GPU is short
+// of memory; here the whole state is resident (it fits in HBM for every
+// workload this library targets) and allocated once per context.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/hmf.h"
+#include "hmf_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr int kTX = 32, kTY = 8;
+constexpr int kTreeThreads = 256;
+
+}  // namespace
+
+struct hmf_ctx {
+  int device = 0;
+  int semantics = HMF_SEMANTICS_REF_CUDA;
+  hmf::Geometry geo{};
+  int sm_count = 0;
+
+  // tree
+  int n = 0, root = -1;
+  std::vector<int> parent;
+  std::vector<std::vector<int>> kids;
+  std::vector<int> preorder, postorder, leaves;  // leaves in DFS pre-order
+
+  // parameters (vtkHierarchicalMaxFlowSegmentation.cxx:57-59)
+  int iterations = 100;
+  float step = 0.1f;
+  float cc = 0.25f;
+  std::vector<double> alpha;
+
+  struct Input {
+    const float* ptr = nullptr;
+    int where = HMF_HOST;
+  };
+  std::vector<Input> data, smooth;
+
+  // device state
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  std::vector<float*> sink, label, div;
+  std::vector<float*> fx[2], fy[2], fz[2];
+  // input staging
+  char* staging = nullptr;
+  size_t staging_bytes = 0;
+  hmf::FlowVertex* d_flow[2] = {nullptr, nullptr};
+  hmf::TreeTable* d_tree = nullptr;
+  const float** d_smooth_list = nullptr;
+  int* d_error = nullptr;
+  int n_smooth_list = 0;
+
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_join = nullptr;
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+  cudaGraphExec_t graph_pair = nullptr;  // two iterations (both flow parities)
+  cudaGraphExec_t graph_one = nullptr;   // one iteration, parity 0
+
+  bool timing = false;
+  long long launches = 0;
+  double kind_ms[3] = {0, 0, 0};
+  long long kind_count[3] = {0, 0, 0};
+  bool solved = false;
+
+  // host copies of the device tables (kept per context: pageable-memory
+  // cudaMemcpyAsync stages them before returning)
+  std::vector<hmf::FlowVertex> h_flow;
+  hmf::TreeTable h_tree{};
+  std::vector<const float*> h_smooth_list;
+
+  std::string err;
+};
+
+namespace {
+
+int fail(hmf_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(hmf_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, e == cudaErrorMemoryAllocation ? HMF_ERR_OUT_OF_MEMORY : HMF_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int d) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+int build_tree(hmf_ctx* c, const int* par, int n) {
+  if (!par) return fail(c, HMF_ERR_TREE, "tree parent array is NULL");
+  if (n < 2) return fail(c, HMF_ERR_TREE, "the tree needs a root and at least one leaf");
+  if (n > hmf::kMaxVertices)
+    return fail(c, HMF_ERR_TREE, "trees of more than " + std::to_string(hmf::kMaxVertices) +
+                                     " vertices are not supported");
+  c->n = n;
+  c->parent.assign(par, par + n);
+  c->kids.assign(n, {});
+  c->root = -1;
+  for (int v = 0; v < n; ++v) {
+    const int p = par[v];
+    if (p < 0) {
+      if (c->root >= 0) return fail(c, HMF_ERR_TREE, "the tree has more than one root");
+      c->root = v;
+    } else if (p >= n || p == v) {
+      return fail(c, HMF_ERR_TREE, "tree parent id out of range");
+    } else {
+      c->kids[p].push_back(v);
+    }
+  }
+  if (c->root < 0) return fail(c, HMF_ERR_TREE, "the tree has no root");
+  std::vector<char> seen(n, 0);
+  std::vector<int> stack{c->root};
+  while (!stack.empty()) {
+    const int v = stack.back();
+    stack.pop_back();
+    if (seen[v]) return fail(c, HMF_ERR_TREE, "the tree has a cycle");
+    seen[v] = 1;
+    c->preorder.push_back(v);
+    for (int k = (int)c->kids[v].size() - 1; k >= 0; --k) stack.push_back(c->kids[v][k]);
+  }
+  if ((int)c->preorder.size() != n) return fail(c, HMF_ERR_TREE, "the tree is not connected");
+  for (int v : c->preorder)
+    if (c->kids[v].empty()) c->leaves.push_back(v);
+  // post-order: children (in order) before their parent
+  std::vector<std::pair<int, int>> st{{c->root, 0}};
+  while (!st.empty()) {
+    auto& top = st.back();
+    if (top.second < (int)c->kids[top.first].size()) {
+      const int kid = c->kids[top.first][top.second++];
+      st.push_back({kid, 0});
+    } else {
+      c->postorder.push_back(top.first);
+      st.pop_back();
+    }
+  }
+  return HMF_OK;
+}
+
+// Device memory plan: per non-root vertex 9 arrays (sink, label, div, two
+// sets of three flow components), the root's source flow.
+int allocate_state(hmf_ctx* c) {
+  const size_t arr = round_up((size_t)c->geo.vol * sizeof(float), 256);
+  const int nonroot = c->n - 1;
+  c->arena_bytes = arr * (size_t)(9 * nonroot + 1) + 4096;
+  CK(cudaMalloc(&c->arena, c->arena_bytes), "cudaMalloc(state)");
+  CK(cudaMemset(c->arena, 0, c->arena_bytes), "cudaMemset(state)");
+  char* p = c->arena;
+  auto take = [&]() {
+    float* r = reinterpret_cast<float*>(p);
+    p += arr;
+    return r;
+  };
+  c->sink.assign(c->n, nullptr);
+  c->label.assign(c->n, nullptr);
+  c->div.assign(c->n, nullptr);
+  for (int s = 0; s < 2; ++s) {
+    c->fx[s].assign(c->n, nullptr);
+    c->fy[s].assign(c->n, nullptr);
+    c->fz[s].assign(c->n, nullptr);
+  }
+  for (int v = 0; v < c->n; ++v) {
+    c->sink[v] = take();
+    if (v == c->root) continue;
+    c->label[v] = take();
+    c->div[v] = take();
+    for (int s = 0; s < 2; ++s) {
+      c->fx[s][v] = take();
+      c->fy[s][v] = take();
+      c->fz[s][v] = take();
+    }
+  }
+  CK(cudaMalloc(&c->d_flow[0], sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2), "cudaMalloc(tables)");
+  c->d_flow[1] = c->d_flow[0] + hmf::kMaxVertices;
+  CK(cudaMalloc(&c->d_tree, sizeof(hmf::TreeTable)), "cudaMalloc(tree table)");
+  CK(cudaMalloc(&c->d_smooth_list, sizeof(float*) * hmf::kMaxVertices), "cudaMalloc(smooth list)");
+  CK(cudaMalloc(&c->d_error, sizeof(int)), "cudaMalloc(error flag)");
+  CK(cudaMemset(c->d_error, 0, sizeof(int)), "cudaMemset(error flag)");
+  return HMF_OK;
+}
+
+// Copies (or borrows) the inputs into pitched device arrays.  Returns the
+// device pointer of each leaf's data term and each vertex's smoothness image.
+int stage_inputs(hmf_ctx* c, cudaStream_t s, std::vector<const float*>& d_data,
+                 std::vector<const float*>& d_smooth, std::vector<const float*>& distinct_smooth) {
+  const auto& G = c->geo;
+  const size_t arr = round_up((size_t)G.vol * sizeof(float), 256);
+  // which inputs need a device copy
+  std::map<std::pair<const float*, int>, int> smooth_slot;  // distinct smoothness images
+  std::vector<std::pair<const float*, int>> smooth_keys;
+  for (int v = 0; v < c->n; ++v) {
+    if (v == c->root || !c->smooth[v].ptr) continue;
+    auto key = std::make_pair(c->smooth[v].ptr, c->smooth[v].where);
+    if (!smooth_slot.count(key)) {
+      smooth_slot[key] = (int)smooth_keys.size();
+      smooth_keys.push_back(key);
+    }
+  }
+  auto borrowable = [&](const float* p, int where) {
+    return where == HMF_DEVICE && G.pitch == G.vx && (reinterpret_cast<uintptr_t>(p) % 16) == 0;
+  };
+  size_t need = 0;
+  for (int l : c->leaves)
+    if (!borrowable(c->data[l].ptr, c->data[l].where)) need += arr;
+  for (auto& k : smooth_keys)
+    if (!borrowable(k.first, k.second)) need += arr;
+  if (need > c->staging_bytes) {
+    if (c->staging) cudaFree(c->staging);
+    c->staging = nullptr;
+    c->staging_bytes = 0;
+    CK(cudaMalloc(&c->staging, need), "cudaMalloc(input staging)");
+    CK(cudaMemset(c->staging, 0, need), "cudaMemset(input staging)");
+    c->staging_bytes = need;
+  }
+  char* p = c->staging;
+  auto stage = [&](const float* src, int where, const float** out) -> int {
+    if (borrowable(src, where)) {
+      *out = src;
+      return HMF_OK;
+    }
+    float* dst = reinterpret_cast<float*>(p);
+    p += arr;
+    const cudaMemcpyKind kind = where == HMF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    CK(cudaMemcpy2DAsync(dst, (size_t)G.pitch * sizeof(float), src, (size_t)G.vx * sizeof(float),
+                         (size_t)G.vx * sizeof(float), (size_t)G.vy * G.vz, kind, s),
+       "cudaMemcpy2DAsync(input)");
+    *out = dst;
+    return HMF_OK;
+  };
+  d_data.assign(c->n, nullptr);
+  d_smooth.assign(c->n, nullptr);
+  for (int l : c->leaves) {
+    int rc = stage(c->data[l].ptr, c->data[l].where, &d_data[l]);
+    if (rc) return rc;
+  }
+  distinct_smooth.assign(smooth_keys.size(), nullptr);
+  for (size_t k = 0; k < smooth_keys.size(); ++k) {
+    int rc = stage(smooth_keys[k].first, smooth_keys[k].second, &distinct_smooth[k]);
+    if (rc) return rc;
+  }
+  for (int v = 0; v < c->n; ++v) {
+    if (v == c->root || !c->smooth[v].ptr) continue;
+    d_smooth[v] = distinct_smooth[smooth_slot[{c->smooth[v].ptr, c->smooth[v].where}]];
+  }
+  return HMF_OK;
+}
+
+int launch_flow(hmf_ctx* c, int parity, cudaStream_t s) {
+  const auto& G = c->geo;
+  hmf::FlowParams fp;
+  fp.step = c->step;
+  fp.icc = 1.0f / c->cc;
+  fp.tiles_x = (G.vx + kTX - 1) / kTX;
+  const int tiles = fp.tiles_x * ((G.vy + kTY - 1) / kTY);
+  const int nonroot = c->n - 1;
+  // enough CTAs for a few waves; split z into chunks when the xy tiling is small
+  const long long target = (long long)c->sm_count * 8;
+  int chunks = 1;
+  if ((long long)tiles * nonroot < target)
+    chunks = (int)std::min<long long>((target + (long long)tiles * nonroot - 1) / ((long long)tiles * nonroot),
+                                      std::max(1, G.vz / 8));
+  fp.zchunk = (G.vz + chunks - 1) / chunks;
+  chunks = (G.vz + fp.zchunk - 1) / fp.zchunk;
+  dim3 grid(tiles, chunks, nonroot), block(kTX, kTY);
+  hmf::flow_kernel<kTX, kTY><<<grid, block, hmf::FlowTile<kTX, kTY>::SMEM_BYTES, s>>>(c->d_flow[parity], G, fp);
+  CK(cudaGetLastError(), "flow_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
+int tree_grid(hmf_ctx* c) {
+  const long long blocks = (c->geo.vol + kTreeThreads - 1) / kTreeThreads;
+  return (int)std::min<long long>(blocks, (long long)c->sm_count * 16);
+}
+
+int launch_tree(hmf_ctx* c, cudaStream_t s) {
+  const size_t smem = 3 * (size_t)c->n * kTreeThreads * sizeof(float);
+  hmf::tree_kernel<<<tree_grid(c), kTreeThreads, smem, s>>>(c->d_tree, c->geo);
+  CK(cudaGetLastError(), "tree_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
+int record_iteration(hmf_ctx* c, int parity, cudaStream_t s) {
+  int rc = launch_flow(c, parity, s);
+  if (rc) return rc;
+  return launch_tree(c, s);
+}
+
+int capture(hmf_ctx* c, int n_iter, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  long long before = c->launches;
+  int rc = HMF_OK;
+  for (int i = 0; i < n_iter && rc == HMF_OK; ++i) rc = record_iteration(c, i & 1, c->stream);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->launches = before;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  return HMF_OK;
+}
+
+int timed(hmf_ctx* c, int kind, cudaStream_t s, int (*fn)(hmf_ctx*, cudaStream_t, int), int arg) {
+  if (!c->timing) return fn(c, s, arg);
+  CK(cudaEventRecord(c->ev_t0, s), "cudaEventRecord");
+  int rc = fn(c, s, arg);
+  if (rc) return rc;
+  CK(cudaEventRecord(c->ev_t1, s), "cudaEventRecord");
+  CK(cudaEventSynchronize(c->ev_t1), "cudaEventSynchronize");
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1), "cudaEventElapsedTime");
+  c->kind_ms[kind] += ms;
+  c->kind_count[kind] += 1;
+  return HMF_OK;
+}
+
+int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& d_data,
+                   const std::vector<const float*>& d_smooth, const std::vector<const float*>& distinct) {
+  // flow tables, one per parity
+  std::vector<hmf::FlowVertex>& fv = c->h_flow;
+  fv.assign(2 * hmf::kMaxVertices, hmf::FlowVertex{});
+  int slot = 0;
+  for (int v : c->preorder) {
+    if (v == c->root) continue;
+    for (int par = 0; par < 2; ++par) {
+      hmf::FlowVertex& f = fv[par * hmf::kMaxVertices + slot];
+      f.px_in = c->fx[par][v];
+      f.py_in = c->fy[par][v];
+      f.pz_in = c->fz[par][v];
+      f.px_out = c->fx[par ^ 1][v];
+      f.py_out = c->fy[par ^ 1][v];
+      f.pz_out = c->fz[par ^ 1][v];
+      f.sink = c->sink[v];
+      f.inc = c->sink[c->parent[v]];
+      f.label = c->label[v];
+      f.smooth = d_smooth[v];
+      f.div = c->div[v];
+      f.alpha = (float)c->alpha[v];  // stored as float, as the reference does (.cxx:692)
+    }
+    ++slot;
+  }
+  CK(cudaMemcpyAsync(c->d_flow[0], fv.data(), sizeof(hmf::FlowVertex) * fv.size(), cudaMemcpyHostToDevice, s),
+     "cudaMemcpyAsync(flow table)");
+  hmf::TreeTable& tt = c->h_tree;
+  std::memset(&tt, 0, sizeof(tt));
+  std::vector<int> entry(c->n, -1);
+  for (int i = 0; i < c->n; ++i) entry[c->postorder[i]] = i;
+  tt.n = c->n;
+  tt.n_leaves = (int)c->leaves.size();
+  tt.cc = c->cc;
+  tt.icc = 1.0f / c->cc;
+  tt.root_init = 1.0f / c->cc;
+  int kpos = 0;
+  for (int i = 0; i < c->n; ++i) {
+    const int v = c->postorder[i];
+    hmf::TreeEntry& E = tt.e[i];
+    E.sink = c->sink[v];
+    E.label = v == c->root ? nullptr : c->label[v];
+    E.div = v == c->root ? nullptr : c->div[v];
+    E.data = d_data[v];
+    E.parent = v == c->root ? -1 : entry[c->parent[v]];
+    E.first_kid = kpos;
+    E.n_kids = (int)c->kids[v].size();
+    for (int k : c->kids[v]) tt.kids[kpos++] = entry[k];
+    const int nk = E.n_kids;
+    E.inv_kids = nk == 0 ? 0.0f : (v == c->root ? 1.0f / (float)nk : 1.0f / (float)(nk + 1));
+  }
+  for (size_t j = 0; j < c->leaves.size(); ++j) tt.leaves[j] = entry[c->leaves[j]];
+  CK(cudaMemcpyAsync(c->d_tree, &tt, sizeof(tt), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(tree table)");
+  c->n_smooth_list = (int)distinct.size();
+  c->h_smooth_list = distinct;
+  if (!distinct.empty())
+    CK(cudaMemcpyAsync(c->d_smooth_list, c->h_smooth_list.data(), sizeof(float*) * distinct.size(),
+                       cudaMemcpyHostToDevice, s),
+       "cudaMemcpyAsync(smooth list)");
+  return HMF_OK;
+}
+
+int do_init(hmf_ctx* c, cudaStream_t s, int) {
+  const size_t smem = (size_t)c->n * kTreeThreads * sizeof(float);
+  hmf::init_kernel<<<tree_grid(c), kTreeThreads, smem, s>>>(c->d_tree, c->geo, c->d_smooth_list,
+                                                           c->n_smooth_list,
+                                                           c->semantics == HMF_SEMANTICS_REF_CPU,
+                                                           c->d_error);
+  CK(cudaGetLastError(), "init_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
+int do_flow(hmf_ctx* c, cudaStream_t s, int parity) { return launch_flow(c, parity, s); }
+int do_tree(hmf_ctx* c, cudaStream_t s, int) { return launch_tree(c, s); }
+int do_refcpu(hmf_ctx* c, cudaStream_t s, int) {
+  hmf::refcpu_kernel<<<tree_grid(c), kTreeThreads, 0, s>>>(c->d_tree, c->geo, c->iterations);
+  CK(cudaGetLastError(), "refcpu_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
+int configure_kernels(hmf_ctx* c) {
+  CK(cudaFuncSetAttribute(hmf::flow_kernel<kTX, kTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          hmf::FlowTile<kTX, kTY>::SMEM_BYTES),
+     "cudaFuncSetAttribute(flow_kernel)");
+  const int tree_smem = 3 * c->n * kTreeThreads * (int)sizeof(float);
+  CK(cudaFuncSetAttribute(hmf::tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_smem),
+     "cudaFuncSetAttribute(tree_kernel)");
+  CK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          c->n * kTreeThreads * (int)sizeof(float)),
+     "cudaFuncSetAttribute(init_kernel)");
+  return HMF_OK;
+}
+
+bool valid_vertex(const hmf_ctx* c, int v) { return c && v >= 0 && v < c->n; }
+
+int copy_out(hmf_ctx* c, const float* src, float* out, int where, void* stream) {
+  if (!out) return fail(c, HMF_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+  if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
+  DeviceGuard dg(c->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const auto& G = c->geo;
+  CK(cudaMemcpy2DAsync(out, (size_t)G.vx * sizeof(float), src, (size_t)G.pitch * sizeof(float),
+                       (size_t)G.vx * sizeof(float), (size_t)G.vy * G.vz,
+                       where == HMF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s),
+     "cudaMemcpy2DAsync(output)");
+  if (where == HMF_HOST) {
+    CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(output)");
+    int flag = 0;
+    CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+    if (flag)
+      return fail(c, HMF_ERR_INVALID_ARGUMENT,
+                  "Data prior and smoothness must be non-negative (the solve ran on invalid input)");
+  }
+  return HMF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
+               int device) {
+  g_create_error.clear();
+  if (!out) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (vx <= 0 || vy <= 0 || vz <= 0) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
+  if (semantics != HMF_SEMANTICS_REF_CUDA && semantics != HMF_SEMANTICS_REF_CPU)
+    return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "unknown semantics");
+  hmf_ctx* c = new hmf_ctx();
+  c->device = device;
+  c->semantics = semantics;
+  c->geo.vx = vx;
+  c->geo.vy = vy;
+  c->geo.vz = vz;
+  c->geo.pitch = (vx + 3) / 4 * 4;
+  c->geo.plane = (long long)c->geo.pitch * vy;
+  c->geo.vol = c->geo.plane * vz;
+  int rc = build_tree(c, parent, n_nodes);
+  if (rc) {
+    g_create_error = c->err;
+    delete c;
+    return rc;
+  }
+  c->alpha.assign(c->n, 1.0);
+  c->data.assign(c->n, {});
+  c->smooth.assign(c->n, {});
+  {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || device < 0 || device >= ndev) {
+      g_create_error = e != cudaSuccess ? std::string("no CUDA device: ") + cudaGetErrorString(e)
+                                        : std::string("CUDA device index out of range");
+      delete c;
+      return HMF_ERR_CUDA;
+    }
+    DeviceGuard dg(device);
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, device);
+    if (e == cudaSuccess) c->sm_count = prop.multiProcessorCount;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_t1);
+    if (e != cudaSuccess) {
+      g_create_error = std::string("CUDA setup failed: ") + cudaGetErrorString(e);
+      hmf_destroy(c);
+      return HMF_ERR_CUDA;
+    }
+    rc = allocate_state(c);
+    if (!rc) rc = configure_kernels(c);
+    if (rc) {
+      g_create_error = c->err;
+      hmf_destroy(c);
+      return rc;
+    }
+  }
+  *out = c;
+  return HMF_OK;
+}
+
+int hmf_destroy(hmf_ctx* c) {
+  if (!c) return HMF_OK;
+  DeviceGuard dg(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
+  if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
+  if (c->arena) cudaFree(c->arena);
+  if (c->staging) cudaFree(c->staging);
+  if (c->d_flow[0]) cudaFree(c->d_flow[0]);
+  if (c->d_tree) cudaFree(c->d_tree);
+  if (c->d_smooth_list) cudaFree(c->d_smooth_list);
+  if (c->d_error) cudaFree(c->d_error);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_t0) cudaEventDestroy(c->ev_t0);
+  if (c->ev_t1) cudaEventDestroy(c->ev_t1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return HMF_OK;
+}
+
+int hmf_set_data(hmf_ctx* c, int node, const float* data, int where) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
+  if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
+  if (!c->kids[node].empty())
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "data terms are only used for leaves");
+  c->data[node] = {data, where};
+  return HMF_OK;
+}
+
+int hmf_set_smoothness(hmf_ctx* c, int node, const float* smooth, int where) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
+  if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
+  if (node == c->root) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the root has no smoothness term");
+  c->smooth[node] = {smooth, where};
+  return HMF_OK;
+}
+
+int hmf_set_smoothness_scalar(hmf_ctx* c, int node, double alpha) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
+  if (!(alpha >= 0.0)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "Cannot use a negative smoothness value.");
+  c->alpha[node] = alpha;
+  return HMF_OK;
+}
+
+int hmf_set_params(hmf_ctx* c, int iterations, float step_size, float cc) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  c->iterations = std::max(0, iterations);
+  c->step = std::min(1.0f, std::max(0.0f, step_size));
+  c->cc = std::min(1.0f, std::max(0.0f, cc));
+  return HMF_OK;
+}
+
+int hmf_solve(hmf_ctx* c, void* stream) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  for (int l : c->leaves)
+    if (!c->data[l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
+  DeviceGuard dg(c->device);
+  cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
+  cudaStream_t s = c->stream;
+  c->launches = 0;
+  for (int k = 0; k < 3; ++k) c->kind_ms[k] = 0, c->kind_count[k] = 0;
+  // order after the caller's queued work
+  CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
+  CK(cudaStreamWaitEvent(s, c->ev_join, 0), "cudaStreamWaitEvent(join)");
+  CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), s), "cudaMemsetAsync(error flag)");
+  std::vector<const float*> d_data, d_smooth, distinct;
+  int rc = stage_inputs(c, s, d_data, d_smooth, distinct);
+  if (!rc) rc = prepare_tables(c, s, d_data, d_smooth, distinct);
+  if (rc) return rc;
+  // flows of parity 0 start at zero
+  const size_t bytes = (size_t)c->geo.vol * sizeof(float);
+  for (int v = 0; v < c->n; ++v) {
+    if (v == c->root) continue;
+    CK(cudaMemsetAsync(c->fx[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
+    CK(cudaMemsetAsync(c->fy[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
+    CK(cudaMemsetAsync(c->fz[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
+  }
+  rc = timed(c, 2, s, do_init, 0);
+  if (rc) return rc;
+  if (c->semantics == HMF_SEMANTICS_REF_CPU) {
+    rc = timed(c, 1, s, do_refcpu, 0);
+    if (rc) return rc;
+  } else if (c->timing) {
+    for (int it = 0; it < c->iterations; ++it) {
+      rc = timed(c, 0, s, do_flow, it & 1);
+      if (!rc) rc = timed(c, 1, s, do_tree, 0);
+      if (rc) return rc;
+    }
+  } else {
+    if (!c->graph_pair) {
+      rc = capture(c, 2, &c->graph_pair);
+      if (!rc) rc = capture(c, 1, &c->graph_one);
+      if (rc) return rc;
+    }
+    for (int it = 0; it + 1 < c->iterations; it += 2) {
+      CK(cudaGraphLaunch(c->graph_pair, s), "cudaGraphLaunch");
+      c->launches += 4;
+    }
+    if (c->iterations & 1) {
+      CK(cudaGraphLaunch(c->graph_one, s), "cudaGraphLaunch");
+      c->launches += 2;
+    }
+  }
+  // final flows live in set (iterations & 1); nothing else depends on parity
+  CK(cudaEventRecord(c->ev_join, s), "cudaEventRecord(done)");
+  CK(cudaStreamWaitEvent(user, c->ev_join, 0), "cudaStreamWaitEvent(done)");
+  c->solved = true;
+  return HMF_OK;
+}
+
+int hmf_get_labels(hmf_ctx* c, int node, float* out, int where, void* stream) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_vertex(c, node) || node == c->root)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "labels exist for non-root vertices only");
+  if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
+  return copy_out(c, c->label[node], out, where, stream);
+}
+
+int hmf_get_sink(hmf_ctx* c, int node, float* out, int where, void* stream) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
+  if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
+  return copy_out(c, c->sink[node], out, where, stream);
+}
+
+int hmf_leaf_order(const hmf_ctx* c, int* out, int cap) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  const int nl = (int)c->leaves.size();
+  for (int i = 0; i < nl && i < cap && out; ++i) out[i] = c->leaves[i];
+  return nl;
+}
+
+size_t hmf_device_bytes(const hmf_ctx* c) {
+  if (!c) return 0;
+  return c->arena_bytes + c->staging_bytes + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
+         sizeof(hmf::TreeTable);
+}
+
+int hmf_set_timing(hmf_ctx* c, int enabled) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  c->timing = enabled != 0;
+  return HMF_OK;
+}
+
+int hmf_get_stats(const hmf_ctx* c, long long* launches, double* avg_ms, int n_kinds) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (launches) *launches = c->launches;
+  for (int k = 0; k < n_kinds && k < 3 && avg_ms; ++k)
+    avg_ms[k] = c->kind_count[k] ? c->kind_ms[k] / (double)c->kind_count[k] : 0.0;
+  return HMF_OK;
+}
+
+const char* hmf_last_error(const hmf_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,291 @@
+"""Python side of the HMF drop-in.
+
+`HMFSolver` owns one C-ABI context (include/hmf.h).  `HierarchicalMaxFlowSegmentation`
+mirrors the filter surface of vtkHierarchicalMaxFlowSegmentation /
+vtkCudaHierarchicalMaxFlowSegmentation
+(Common/vtkRobartsCommon/vtkHierarchicalMaxFlowSegmentation.h:43-204) with
+numpy arrays (host) or CUDA torch tensors (device) in place of vtkImageData
+and a parent array in place of vtkTree.  Arrays are indexed [z, y, x], x
+fastest, which is VTK's scalar layout.
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+
+import numpy as np
+
+from . import _capi
+from ._capi import HMF_DEVICE, HMF_HOST, HMF_SEMANTICS_REF_CPU, HMF_SEMANTICS_REF_CUDA, HMFError, check
+
+__all__ = ["HMFSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]
+
+REF_CUDA = HMF_SEMANTICS_REF_CUDA
+REF_CPU = HMF_SEMANTICS_REF_CPU
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    handle = getattr(stream, "cuda_stream", None)
+    if handle is None:
+        raise TypeError("stream must be None, an int cudaStream_t or a torch.cuda.Stream")
+    return int(handle)
+
+
+def _array_pointer(arr, nvox: int):
+    """(pointer, where, keepalive) of a float32 contiguous volume."""
+    if isinstance(arr, np.ndarray):
+        if arr.dtype != np.float32 or not arr.flags["C_CONTIGUOUS"]:
+            raise TypeError("numpy volumes must be C-contiguous float32")
+        if arr.size != nvox:
+            raise ValueError("volume has %d voxels, expected %d" % (arr.size, nvox))
+        return arr.ctypes.data, HMF_HOST, arr
+    mod = type(arr).__module__
+    if mod.startswith("torch"):
+        import torch
+
+        if arr.dtype != torch.float32 or not arr.is_contiguous():
+            raise TypeError("torch volumes must be contiguous float32")
+        if arr.numel() != nvox:
+            raise ValueError("volume has %d voxels, expected %d" % (arr.numel(), nvox))
+        where = HMF_DEVICE if arr.is_cuda else HMF_HOST
+        return arr.data_ptr(), where, arr
+    raise TypeError("volumes must be numpy arrays or torch tensors")
+
+
+class HMFSolver:
+    """One solver context: a volume size (vx, vy, vz), a label tree given as a
+    parent array, and a semantics (REF_CUDA or REF_CPU)."""
+
+    def __init__(self, dims, parent, semantics: int = REF_CUDA, device: int = 0):
+        self._lib = _capi.load()
+        self.dims = tuple(int(d) for d in dims)
+        self.parent = [int(p) for p in parent]
+        self.nvox = self.dims[0] * self.dims[1] * self.dims[2]
+        par = (ctypes.c_int * len(self.parent))(*self.parent)
+        ctx = ctypes.c_void_p()
+        check(self._lib.hmf_create(ctypes.byref(ctx), *self.dims, par, len(self.parent), int(semantics),
+                                   int(device)))
+        self._ctx = ctx
+        self._keep: dict = {}
+        n = self._lib.hmf_leaf_order(self._ctx, None, 0)
+        buf = (ctypes.c_int * max(n, 1))()
+        self._lib.hmf_leaf_order(self._ctx, buf, n)
+        self.leaves = [buf[i] for i in range(n)]
+
+    # -- inputs ---------------------------------------------------------
+    def set_data(self, node: int, arr) -> None:
+        ptr, where, keep = _array_pointer(arr, self.nvox)
+        check(self._lib.hmf_set_data(self._ctx, int(node), ptr, where), self._ctx)
+        self._keep[("d", node)] = keep
+
+    def set_data_pointer(self, node: int, ptr: int, where: int) -> None:
+        check(self._lib.hmf_set_data(self._ctx, int(node), int(ptr), int(where)), self._ctx)
+
+    def set_smoothness(self, node: int, arr) -> None:
+        if arr is None:
+            check(self._lib.hmf_set_smoothness(self._ctx, int(node), None, HMF_HOST), self._ctx)
+            self._keep.pop(("s", node), None)
+            return
+        ptr, where, keep = _array_pointer(arr, self.nvox)
+        check(self._lib.hmf_set_smoothness(self._ctx, int(node), ptr, where), self._ctx)
+        self._keep[("s", node)] = keep
+
+    def set_smoothness_scalar(self, node: int, alpha: float) -> None:
+        check(self._lib.hmf_set_smoothness_scalar(self._ctx, int(node), float(alpha)), self._ctx)
+
+    def set_params(self, iterations: int = 100, step: float = 0.1, cc: float = 0.25) -> None:
+        check(self._lib.hmf_set_params(self._ctx, int(iterations), float(step), float(cc)), self._ctx)
+
+    def set_timing(self, enabled: bool) -> None:
+        check(self._lib.hmf_set_timing(self._ctx, 1 if enabled else 0), self._ctx)
+
+    # -- run ------------------------------------------------------------
+    def solve(self, stream=None) -> None:
+        check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
+
+    def _fetch(self, fn, node, out, stream):
+        if out is None:
+            out = np.empty((self.dims[2], self.dims[1], self.dims[0]), dtype=np.float32)
+        ptr, where, _ = _array_pointer(out, self.nvox)
+        check(fn(self._ctx, int(node), ptr, where, _stream_handle(stream)), self._ctx)
+        return out
+
+    def labels(self, node: int, out=None, stream=None):
+        """Labelling of a non-root vertex into `out` (numpy / torch), or a new
+        numpy array [VZ, VY, VX]."""
+        return self._fetch(self._lib.hmf_get_labels, node, out, stream)
+
+    def sink(self, node: int, out=None, stream=None):
+        return self._fetch(self._lib.hmf_get_sink, node, out, stream)
+
+    def stats(self):
+        launches = ctypes.c_longlong()
+        ms = (ctypes.c_double * 3)()
+        check(self._lib.hmf_get_stats(self._ctx, ctypes.byref(launches), ms, 3), self._ctx)
+        return {"launches": launches.value, "flow_ms": ms[0], "tree_ms": ms[1], "init_ms": ms[2]}
+
+    def device_bytes(self) -> int:
+        return int(self._lib.hmf_device_bytes(self._ctx))
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.hmf_destroy(self._ctx)
+            self._ctx = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class HierarchicalMaxFlowSegmentation:
+    """Filter-style API with the reference's method names.
+
+    Differences from the VTK class, all forced by the absence of VTK: the tree
+    is a parent array (SetStructure / SetHierarchy), images are arrays, and
+    GetOutputDataObject returns an array.  Errors are reported the way
+    RequestData reports them: Update() returns -1 and the message is printed
+    (vtkErrorMacro) and kept in GetLastError()."""
+
+    def __init__(self, semantics: int = REF_CUDA):
+        self.Structure = None
+        self.SmoothnessScalars: dict[int, float] = {}
+        self.NumberOfIterations = 100
+        self.CC = 0.25
+        self.StepSize = 0.1
+        self.Device = 0
+        self.Semantics = semantics
+        self._data: dict[int, object] = {}
+        self._smooth: dict[int, object] = {}
+        self._outputs: dict[int, np.ndarray] = {}
+        self._solver: HMFSolver | None = None
+        self._error = ""
+
+    # vtkSetObjectMacro(Structure, vtkTree) (.h:53-54)
+    def SetStructure(self, parent):
+        self.Structure = [int(p) for p in parent]
+
+    SetHierarchy = SetStructure
+
+    def GetStructure(self):
+        return self.Structure
+
+    # AddSmoothnessScalar (.cxx:93-104): std::map::insert keeps the first value
+    def AddSmoothnessScalar(self, node: int, alpha: float):
+        if alpha >= 0.0:
+            self.SmoothnessScalars.setdefault(int(node), float(alpha))
+        else:
+            self._report("Cannot use a negative smoothness value.")
+
+    # vtkSetClampMacro (.h:64-77)
+    def SetNumberOfIterations(self, n: int):
+        self.NumberOfIterations = max(0, min(int(n), 2**31 - 1))
+
+    def GetNumberOfIterations(self) -> int:
+        return self.NumberOfIterations
+
+    def SetCC(self, cc: float):
+        self.CC = min(1.0, max(0.0, float(cc)))
+
+    def GetCC(self) -> float:
+        return self.CC
+
+    def SetStepSize(self, s: float):
+        self.StepSize = min(1.0, max(0.0, float(s)))
+
+    def GetStepSize(self) -> float:
+        return self.StepSize
+
+    def SetDevice(self, d: int):
+        self.Device = int(d)
+
+    def GetDevice(self) -> int:
+        return self.Device
+
+    def SetDataInputDataObject(self, idx: int, image):
+        if image is None:
+            self._data.pop(int(idx), None)
+        else:
+            self._data[int(idx)] = image
+
+    def GetDataInputDataObject(self, idx: int):
+        return self._data.get(int(idx))
+
+    def SetSmoothnessInputDataObject(self, idx: int, image):
+        if image is None:
+            self._smooth.pop(int(idx), None)
+        else:
+            self._smooth[int(idx)] = image
+
+    def GetSmoothnessInputDataObject(self, idx: int):
+        return self._smooth.get(int(idx))
+
+    def GetOutputDataObject(self, idx: int):
+        return self._outputs.get(int(idx))
+
+    def GetNumberOfOutputPorts(self) -> int:
+        return len(self._solver.leaves) if self._solver else 0
+
+    def GetLastError(self) -> str:
+        return self._error
+
+    def _report(self, msg: str) -> int:
+        self._error = msg
+        print("ERROR: HierarchicalMaxFlowSegmentation: " + msg, file=sys.stderr)
+        return -1
+
+    def _shape(self, image):
+        return tuple(int(s) for s in image.shape)
+
+    # RequestData (.cxx:555-933) with CheckInputConsistancy (:363-505)
+    def Update(self, stream=None) -> int:
+        self._error = ""
+        if not self.Structure:
+            return self._report("Hierarchy must be provided.")
+        shape = None
+        for image in list(self._data.values()) + list(self._smooth.values()):
+            s = self._shape(image)
+            if len(s) != 3:
+                return self._report("Data type must be FLOAT and only have one component.")
+            if shape is None:
+                shape = s
+            elif s != shape:
+                return self._report("Inconsistant object extent.")
+        if shape is None:
+            return self._report("Missing data prior for leaf node.")
+        dims = (shape[2], shape[1], shape[0])
+        try:
+            if (self._solver is None or self._solver.dims != dims or self._solver.parent != self.Structure
+                    or getattr(self._solver, "_semantics", None) != self.Semantics):
+                if self._solver is not None:
+                    self._solver.close()
+                self._solver = HMFSolver(dims, self.Structure, self.Semantics, self.Device)
+                self._solver._semantics = self.Semantics
+            sol = self._solver
+            for leaf in sol.leaves:
+                if leaf not in self._data:
+                    return self._report("Missing data prior for leaf node.")
+                sol.set_data(leaf, self._data[leaf])
+            for v, p in enumerate(self.Structure):
+                if p < 0:
+                    continue
+                sol.set_smoothness_scalar(v, self.SmoothnessScalars.get(v, 1.0))
+                sol.set_smoothness(v, self._smooth.get(v))
+            sol.set_params(self.NumberOfIterations, self.StepSize, self.CC)
+            sol.solve(stream)
+            self._outputs = {leaf: sol.labels(leaf, stream=stream) for leaf in sol.leaves}
+        except HMFError as e:
+            return self._report(str(e))
+        return 1

@@ -1,0 +1,208 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.  GPU only.
+
+Bar: REF_CUDA labels and sinks bit-identical to the FP32 restatement of the
+reference kernels (the kernels use the same operation order, no FMA
+contraction, IEEE sqrt/division); REF_CPU bit-identical to the reference's
+compiled CPU code.  End-to-end workloads additionally state max |u - u_fp64|.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from robartsvtk_gb300 import REF_CPU, REF_CUDA, HierarchicalMaxFlowSegmentation, HMFError, HMFSolver
+from robartsvtk_gb300.synthetic import boxes_flat3, ellipsoids_tree4, random_tree_problem
+from tests.golden.cases import CASES, problem
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+LABEL_TOL = 1e-4  # per-voxel max |u_gpu - u_oracle| accepted for end-to-end workloads
+
+
+def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None):
+    import torch
+    with HMFSolver(w.dims, w.parent, semantics) as s:
+        keep = []
+        for leaf, d in w.data.items():
+            if device_inputs:
+                t = torch.from_numpy(d).cuda()
+                keep.append(t)
+                s.set_data(leaf, t)
+            else:
+                s.set_data(leaf, d)
+        for v, S in w.smooth.items():
+            if device_inputs:
+                t = torch.from_numpy(S).cuda()
+                keep.append(t)
+                s.set_smoothness(v, t)
+            else:
+                s.set_smoothness(v, S)
+        for v, a in w.alpha.items():
+            s.set_smoothness_scalar(v, a)
+        s.set_params(w.iterations if iterations is None else iterations, w.step, w.cc)
+        s.solve()
+        n = len(w.parent)
+        u = np.zeros((n,) + w.dims[::-1], np.float32)
+        sink = np.zeros_like(u)
+        for v in range(n):
+            sink[v] = s.sink(v)
+            if w.parent[v] >= 0:
+                u[v] = s.labels(v)
+        return {"u": u, "sink": sink, "stats": s.stats()}
+
+
+def oracle(w, iterations=None, **kw):
+    it = w.iterations if iterations is None else iterations
+    return O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, it, w.step, w.cc, want_sink=True, **kw)
+
+
+def assert_same(gpu, ref, what=""):
+    for k in ("u", "sink"):
+        a, b = gpu[k], ref[k].astype(np.float32)
+        diff = np.abs(a.astype(np.float64) - b.astype(np.float64))
+        assert np.array_equal(a, b), "%s %s: max |diff| %.3g at %s" % (
+            what, k, diff.max(), np.unravel_index(diff.argmax(), diff.shape))
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_ref_cuda_bitexact_golden_cases(name):
+    w = problem(name)
+    assert_same(run_gpu(w), oracle(w), name)
+
+
+@pytest.mark.parametrize("dims,parent,smooth_nodes,iters", [
+    ((5, 4, 3), [-1, 0, 0, 0], (), 7),
+    ((1, 1, 9), [-1, 0, 0], (), 12),            # single column
+    ((40, 1, 1), [-1, 0, 0], (1,), 12),         # single row
+    ((31, 17, 1), [-1, 0, 0, 0], (2,), 15),     # single plane
+    ((64, 16, 40), [-1, 0, 0, 1, 1, 2, 2], (1, 2, 3, 4, 5, 6), 9),  # z split into chunks
+    ((70, 19, 23), [-1, 0, 1, 2, 2, 1, 0], (3, 4), 11),            # partial tiles, deep tree
+    ((33, 65, 12), [-1, 0, 0, 0, 0, 0, 0, 0, 0], (), 6),           # wide root
+])
+def test_ref_cuda_bitexact_shapes(dims, parent, smooth_nodes, iters):
+    w = random_tree_problem(21, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
+    assert_same(run_gpu(w), oracle(w), str(dims))
+
+
+def test_ref_cuda_shared_smoothness_image():
+    w = random_tree_problem(22, (20, 12, 10), [-1, 0, 0, 1, 1], iterations=10)
+    S = np.random.default_rng(1).uniform(0, 1, size=(10, 12, 20)).astype(np.float32)
+    w.smooth = {v: S for v in (1, 2, 3, 4)}
+    assert_same(run_gpu(w), oracle(w))
+
+
+def test_ref_cuda_zero_iterations_is_the_initialisation():
+    w = random_tree_problem(23, (9, 8, 7), [-1, 0, 0, 1, 1], iterations=0)
+    w.data[2][0, 0, 0] = w.data[3][0, 0, 0] = w.data[4][0, 0, 0] = 0.5  # a three-way tie
+    assert_same(run_gpu(w), oracle(w))
+
+
+def test_device_inputs_equal_host_inputs():
+    w = random_tree_problem(24, (36, 10, 9), [-1, 0, 0, 1, 1], iterations=8, smooth_nodes=(1, 3))
+    a, b = run_gpu(w), run_gpu(w, device_inputs=True)
+    assert np.array_equal(a["u"], b["u"]) and np.array_equal(a["sink"], b["sink"])
+    w2 = random_tree_problem(24, (35, 10, 9), [-1, 0, 0, 1, 1], iterations=8, smooth_nodes=(1, 3))
+    assert_same(run_gpu(w2, device_inputs=True), oracle(w2), "pitched device inputs")
+
+
+def test_ref_cpu_mode_matches_reference_cpu_golden():
+    g = np.load(os.path.join(GOLDEN, "ref_cpu_golden.npz"))
+    for name in sorted(CASES):
+        w = problem(name)
+        r = run_gpu(w, semantics=REF_CPU)
+        assert np.array_equal(r["u"], g[name + "/u"]), name
+        assert np.array_equal(r["sink"], g[name + "/sink"]), name
+
+
+def test_ref_cpu_mode_matches_port_odd_shape():
+    w = random_tree_problem(25, (37, 11, 6), [-1, 0, 0, 1, 1, 1], iterations=40, smooth_nodes=(1,))
+    r = run_gpu(w, semantics=REF_CPU)
+    o = oracle(w, semantics=O.REF_CPU)
+    assert np.array_equal(r["u"], o["u"].astype(np.float32))
+
+
+def test_boxes64_flat3_end_to_end():
+    """64^3, 3 boxes, flat 3 leaves, alpha 0.1, 200 iterations."""
+    w = boxes_flat3(seed=0)
+    g = run_gpu(w)
+    o32 = oracle(w)
+    o64 = oracle(w, precision=64)
+    leaves = w.leaves
+    err = np.abs(g["u"][leaves] - o32["u"][leaves]).max()
+    err64 = np.abs(g["u"][leaves].astype(np.float64) - o64["u"][leaves]).max()
+    agree = (np.argmax(g["u"][leaves], 0) == np.argmax(o32["u"][leaves], 0)).mean()
+    print("boxes64: max|u-u32| %.3g  max|u-u64| %.3g  argmax agreement %.6f" % (err, err64, agree))
+    assert err <= LABEL_TOL and agree >= 0.999
+    assert err64 < 1e-3
+
+
+def test_ellipsoids256_tree4_full_size_first_iterations_bitexact():
+    """The 256^3 two-level workload at full size: 3 iterations against the oracle."""
+    w = ellipsoids_tree4(seed=0)
+    assert_same(run_gpu(w, iterations=3), oracle(w, iterations=3), "256^3")
+
+
+def test_ellipsoids256_tree4_full_solve_properties():
+    w = ellipsoids_tree4(seed=0)
+    a = run_gpu(w)
+    u = a["u"][w.leaves]
+    assert np.isfinite(u).all() and u.min() >= 0 and u.max() <= 1
+    assert (np.argmax(u, 0) == w.truth).mean() > 0.95
+    b = run_gpu(w)
+    assert np.array_equal(a["u"], b["u"])  # deterministic
+
+
+def test_missing_leaf_data_is_an_error():
+    with HMFSolver((4, 4, 4), [-1, 0, 0]) as s:
+        s.set_data(1, np.ones((4, 4, 4), np.float32))
+        with pytest.raises(HMFError, match="Missing data"):
+            s.solve()
+
+
+def test_negative_data_is_reported():
+    with HMFSolver((4, 4, 4), [-1, 0, 0]) as s:
+        d = np.ones((4, 4, 4), np.float32)
+        d[1, 2, 3] = -1
+        s.set_data(1, d)
+        s.set_data(2, np.ones((4, 4, 4), np.float32))
+        s.solve()
+        with pytest.raises(HMFError, match="non-negative"):
+            s.labels(1)
+
+
+def test_filter_api_end_to_end():
+    w = random_tree_problem(26, (12, 10, 8), [-1, 0, 0, 1, 1], iterations=20, smooth_nodes=(2,))
+    f = HierarchicalMaxFlowSegmentation()
+    f.SetHierarchy(w.parent)
+    for leaf, d in w.data.items():
+        f.SetDataInputDataObject(leaf, d)
+    for v, S in w.smooth.items():
+        f.SetSmoothnessInputDataObject(v, S)
+    for v, a in w.alpha.items():
+        f.AddSmoothnessScalar(v, a)
+    f.SetNumberOfIterations(w.iterations)
+    assert f.Update() == 1, f.GetLastError()
+    o = oracle(w)
+    assert f.GetNumberOfOutputPorts() == len(w.leaves)
+    for leaf in w.leaves:
+        assert np.array_equal(f.GetOutputDataObject(leaf), o["u"][leaf].astype(np.float32))
+    assert f.GetOutputDataObject(1) is None  # branch: no output port
+
+
+def test_launch_count_per_iteration():
+    w = random_tree_problem(27, (16, 16, 16), [-1, 0, 0, 0], iterations=10)
+    r = run_gpu(w)
+    assert r["stats"]["launches"] == 1 + 2 * 10  # init + (flow, tree) per iteration
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "ref_cuda_golden.npz")),
+                    reason="REF_CUDA golden vectors not generated yet")
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_against_reference_cuda_kernels_golden(name):
+    """Golden vectors produced by the reference's own CUDA kernels (compiled
+    from CUDA_hierarchicalmaxflow.cu with nvcc's default FMA contraction)."""
+    g = np.load(os.path.join(GOLDEN, "ref_cuda_golden.npz"))
+    w = problem(name)
+    r = run_gpu(w)
+    assert np.abs(r["u"] - g[name + "/u"]).max() <= LABEL_TOL

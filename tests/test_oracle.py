@@ -1,0 +1,92 @@
+"""The oracle itself: pinned against the reference's own compiled code and
+golden vectors, and checked for the invariants the reference implies.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import build_oracle
+from oracle import oracle as O
+from robartsvtk_gb300.synthetic import boxes_flat3, random_tree_problem
+from tests.golden.cases import CASES, problem
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+HAVE_REF = build_oracle.reference_available()
+
+
+def _solve(w, **kw):
+    return O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, w.iterations, w.step, w.cc, **kw)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_ref_cpu_port_matches_golden(name):
+    """REF_CPU port == outputs of the reference's compiled utilities (fixtures)."""
+    g = np.load(os.path.join(GOLDEN, "ref_cpu_golden.npz"))
+    w = problem(name)
+    res = _solve(w, semantics=O.REF_CPU, want_sink=True)
+    assert np.array_equal(res["u"].astype(np.float32), g[name + "/u"])
+    assert np.array_equal(res["sink"].astype(np.float32), g[name + "/sink"])
+
+
+@pytest.mark.skipif(not HAVE_REF, reason="reference sources not present")
+@pytest.mark.parametrize("dims,parent,smooth_nodes", [
+    ((5, 4, 3), [-1, 0, 0, 0], ()),
+    ((9, 7, 11), [-1, 0, 0, 1, 1, 1], (1, 2)),   # VZ > VY: the reference reads before its flow buffers
+    ((16, 16, 8), [-1, 0, 1, 1, 0, 4, 4], (3,)),
+])
+def test_ref_cpu_port_matches_compiled_reference(dims, parent, smooth_nodes):
+    w = random_tree_problem(7, dims, parent, iterations=33, smooth_nodes=smooth_nodes)
+    a = _solve(w, semantics=O.REF_CPU, want_sink=True, want_div=True)
+    b = O.solve_reference_cpu(w.dims, w.parent, w.data, w.smooth, w.alpha, w.iterations, w.step, w.cc,
+                              want_sink=True, want_div=True)
+    for k in ("u", "sink", "div"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_ref_cpu_flows_stay_zero():
+    """The reference CPU path multiplies zero flows (ghmf_applyStep), so every
+    divergence stays 0 and branch sinks / source keep the initial minimum."""
+    w = random_tree_problem(3, (6, 5, 4), [-1, 0, 0, 1, 1], iterations=20, smooth_nodes=(1,))
+    r = _solve(w, semantics=O.REF_CPU, want_sink=True, want_div=True)
+    assert np.all(r["div"] == 0)
+    m = np.minimum.reduce([w.data[l] for l in w.leaves])
+    assert np.array_equal(r["sink"][0], m)   # source
+    assert np.array_equal(r["sink"][1], m)   # branch
+
+
+def test_ref_cuda_fp32_close_to_fp64():
+    w = random_tree_problem(5, (11, 9, 7), [-1, 0, 0, 1, 1, 2, 2], iterations=60, smooth_nodes=(1, 4))
+    a = _solve(w, precision=32)
+    b = _solve(w, precision=64)
+    assert np.abs(a["u"] - b["u"]).max() < 1e-4
+
+
+def test_ref_cuda_labels_in_unit_interval_and_regularised():
+    w = boxes_flat3(seed=1, size=24, iterations=80)
+    r = _solve(w, want_div=True)
+    u = r["u"][1:]
+    assert u.min() >= 0.0 and u.max() <= 1.0
+    assert np.abs(r["div"][1:]).max() > 0   # spatial flows move, unlike REF_CPU
+    # the segmentation follows the phantom
+    lab = np.argmax(u, axis=0)
+    assert (lab == w.truth).mean() > 0.9
+
+
+def test_ref_cuda_threads_do_not_change_results():
+    w = random_tree_problem(9, (10, 6, 5), [-1, 0, 0, 0], iterations=15)
+    a = _solve(w, threads=1)
+    b = _solve(w, threads=4)
+    assert np.array_equal(a["u"], b["u"])
+
+
+@pytest.mark.parametrize("parent,msg", [
+    ([1, 0], "no root"),
+    ([0, -1], "out of range"),
+    ([-1, -1, 0], "more than one root"),
+    ([-1, 2, 1], "not connected"),
+    ([-1, 5], "out of range"),
+])
+def test_oracle_rejects_bad_trees(parent, msg):
+    data = {v: np.ones((2, 2, 2), np.float32) for v in range(len(parent))}
+    with pytest.raises(RuntimeError, match=msg):
+        O.solve((2, 2, 2), parent, data, iterations=1)
