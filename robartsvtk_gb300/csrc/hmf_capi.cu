@@ -586,9 +586,19 @@ int hmf_set_smoothness_scalar(hmf_ctx* c, int node, double alpha) {
 
 int hmf_set_params(hmf_ctx* c, int iterations, float step_size, float cc) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  const float step = std::min(1.0f, std::max(0.0f, step_size));
+  const float ccc = std::min(1.0f, std::max(0.0f, cc));
+  if (step != c->step || ccc != c->cc) {
+    // the captured iteration graphs hold StepSize and 1/CC as kernel arguments
+    DeviceGuard dg(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
+    if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
+    c->graph_pair = c->graph_one = nullptr;
+  }
   c->iterations = std::max(0, iterations);
-  c->step = std::min(1.0f, std::max(0.0f, step_size));
-  c->cc = std::min(1.0f, std::max(0.0f, cc));
+  c->step = step;
+  c->cc = ccc;
   return HMF_OK;
 }
 
