@@ -437,15 +437,18 @@ int do_refcpu(hmf_ctx* c, cudaStream_t s, int) {
   return HMF_OK;
 }
 
+// The dynamic shared-memory limit is a per-device property of the function,
+// shared by every context: it is always set to what the largest supported
+// tree needs, so that no context lowers it below another's requirement.
 int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::flow_kernel<kTX, kTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::FlowTile<kTX, kTY>::SMEM_BYTES),
      "cudaFuncSetAttribute(flow_kernel)");
-  const int tree_smem = 3 * c->n * kTreeThreads * (int)sizeof(float);
+  const int tree_smem = 3 * hmf::kMaxVertices * kTreeThreads * (int)sizeof(float);
   CK(cudaFuncSetAttribute(hmf::tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_smem),
      "cudaFuncSetAttribute(tree_kernel)");
   CK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          c->n * kTreeThreads * (int)sizeof(float)),
+                          hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(init_kernel)");
   return HMF_OK;
 }
