@@ -120,9 +120,43 @@ size_t hmf_device_bytes(const hmf_ctx* ctx);
 int hmf_set_timing(hmf_ctx* ctx, int enabled);
 int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kind, int n_kinds);
 
-/* Message of the last failed call on ctx (or of the last failed hmf_create on
- * this thread when ctx is NULL). */
+/* Message of the last failed call on ctx (or, when ctx is NULL, of the last
+ * failed hmf_create or hmf_solve_noalloc on this thread). */
 const char* hmf_last_error(const hmf_ctx* ctx);
+
+/* Allocation-free solve.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory while they run, such as a
+ * plugin inside an image-guidance or streaming application that reserves all
+ * GPU memory at start-up and forbids later allocations (cudaMalloc and
+ * cudaFree can synchronise the device and stall the application's other
+ * streams), or code that works inside a memory pool it does not own.
+ *
+ * It runs the same initialisation and iterations as hmf_create + hmf_solve +
+ * hmf_get_labels on the current device, but keeps all solver state in one
+ * statically sized device array of this library, HMF_NOALLOC_SCRATCH_BYTES
+ * (64 MiB), which every GPU that loads the library holds until the process
+ * exits.  It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ *  - Inputs and outputs are the caller's device buffers of VX*VY*VZ floats,
+ *    indexed by tree vertex: data[v] for every leaf, smooth[v] (or a NULL
+ *    array / NULL entry for S = 1), alpha[v] (NULL: all 1), labels[v] for
+ *    each non-root vertex whose labelling is wanted (NULL entries skipped).
+ *  - The scratch needed is 4 bytes x VX' x VY x VZ x (9 x (n_nodes - 1) + 1
+ *    + leaves + distinct smoothness images) plus about 24 KiB of tables, with
+ *    VX' = VX rounded up to a multiple of 4; a larger problem is rejected with
+ *    HMF_ERR_INVALID_ARGUMENT before anything is queued.
+ *  - The first call on a device looks up the array's device address and sets
+ *    the kernels' attributes for that device; make that first call before any
+ *    stream capture.
+ *  - Work is queued on `stream`; the call returns after it has finished
+ *    (it synchronises `stream` to report negative inputs).
+ *  - Every call shares the one array: calls whose work overlaps on the GPU
+ *    (other threads, other streams) race and corrupt each other.  Each call
+ *    clears the part of the array it uses before using it. */
+#define HMF_NOALLOC_SCRATCH_BYTES (64u << 20)
+int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
+                      const float* const* data, const float* const* smooth, const double* alpha,
+                      int iterations, float step_size, float cc, float* const* labels, void* stream);
 
 #ifdef __cplusplus
 }

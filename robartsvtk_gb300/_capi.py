@@ -44,6 +44,9 @@ SIGNATURES = [
     ("hmf_set_timing", _I, [_P, _I]),
     ("hmf_get_stats", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_last_error", ctypes.c_char_p, [_P]),
+    ("hmf_solve_noalloc", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                               ctypes.POINTER(ctypes.c_double), _I, ctypes.c_float, ctypes.c_float,
+                               ctypes.POINTER(_P), _P]),
 ]
 
 _lib = None

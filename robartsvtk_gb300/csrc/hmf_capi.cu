@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -708,3 +709,339 @@ int hmf_get_stats(const hmf_ctx* c, long long* launches, double* avg_ms, int n_k
 const char* hmf_last_error(const hmf_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// hmf_solve_noalloc: the solve above with every device buffer carved out of
+// one static array of this library instead of cudaMalloc, for callers that
+// must not allocate device memory (see include/hmf.h).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocBytes = HMF_NOALLOC_SCRATCH_BYTES;
+constexpr int kNoAllocMaxDevices = 64;
+
+// Held on every GPU that loads this library, until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of g_noalloc_scratch per device ordinal.  In host code the
+// symbol itself is only a stand-in, so the address is looked up once per
+// device, with that device current, and handed to the kernels.
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+int noalloc_fail(int code, const char* msg) {
+  g_create_error = msg;
+  return code;
+}
+
+int noalloc_cuda_fail(cudaError_t e, const char* what) {
+  g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return HMF_ERR_CUDA;
+}
+
+#define NCK(call, what)                                     \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return noalloc_cuda_fail(e_, what); \
+  } while (0)
+
+int noalloc_setup(int device, unsigned char** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return noalloc_fail(HMF_ERR_CUDA, "device ordinal beyond the supported range");
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    NCK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+    NCK(cudaFuncSetAttribute(hmf::flow_kernel<kTX, kTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             hmf::FlowTile<kTX, kTY>::SMEM_BYTES),
+        "cudaFuncSetAttribute(flow_kernel)");
+    NCK(cudaFuncSetAttribute(hmf::tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             3 * hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
+        "cudaFuncSetAttribute(tree_kernel)");
+    NCK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
+        "cudaFuncSetAttribute(init_kernel)");
+    g_noalloc_addr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_addr[device];
+  return HMF_OK;
+}
+
+// Fixed-size tree bookkeeping (no heap): children in increasing id order,
+// DFS pre-order leaves, post-order entries with the root last.
+struct NoAllocTree {
+  int n = 0, root = -1, n_leaves = 0;
+  int parent[hmf::kMaxVertices];
+  int n_kids[hmf::kMaxVertices];
+  int kids[hmf::kMaxVertices][hmf::kMaxVertices];
+  int preorder[hmf::kMaxVertices];
+  int postorder[hmf::kMaxVertices];
+  int leaves[hmf::kMaxVertices];
+};
+
+int noalloc_tree(const int* par, int n, NoAllocTree& t) {
+  if (!par || n < 2) return noalloc_fail(HMF_ERR_TREE, "the tree needs a root and at least one leaf");
+  if (n > hmf::kMaxVertices) return noalloc_fail(HMF_ERR_TREE, "the tree has too many vertices");
+  t.n = n;
+  for (int v = 0; v < n; ++v) t.n_kids[v] = 0;
+  for (int v = 0; v < n; ++v) {
+    const int p = par[v];
+    t.parent[v] = p;
+    if (p < 0) {
+      if (t.root >= 0) return noalloc_fail(HMF_ERR_TREE, "the tree has more than one root");
+      t.root = v;
+    } else if (p >= n || p == v) {
+      return noalloc_fail(HMF_ERR_TREE, "tree parent id out of range");
+    } else {
+      t.kids[p][t.n_kids[p]++] = v;
+    }
+  }
+  if (t.root < 0) return noalloc_fail(HMF_ERR_TREE, "the tree has no root");
+  int stack[hmf::kMaxVertices], top = 0, count = 0;
+  bool seen[hmf::kMaxVertices] = {};
+  stack[top++] = t.root;
+  while (top) {
+    const int v = stack[--top];
+    if (seen[v]) return noalloc_fail(HMF_ERR_TREE, "the tree has a cycle");
+    seen[v] = true;
+    t.preorder[count++] = v;
+    for (int k = t.n_kids[v] - 1; k >= 0; --k) {
+      if (top >= hmf::kMaxVertices) return noalloc_fail(HMF_ERR_TREE, "the tree has a cycle");
+      stack[top++] = t.kids[v][k];
+    }
+  }
+  if (count != n) return noalloc_fail(HMF_ERR_TREE, "the tree is not connected");
+  for (int i = 0; i < n; ++i)
+    if (t.n_kids[t.preorder[i]] == 0) t.leaves[t.n_leaves++] = t.preorder[i];
+  int vst[hmf::kMaxVertices], kst[hmf::kMaxVertices], depth = 0, m = 0;
+  vst[0] = t.root;
+  kst[0] = 0;
+  depth = 1;
+  while (depth) {
+    const int v = vst[depth - 1];
+    if (kst[depth - 1] < t.n_kids[v]) {
+      const int kid = t.kids[v][kst[depth - 1]++];
+      vst[depth] = kid;
+      kst[depth] = 0;
+      ++depth;
+    } else {
+      t.postorder[m++] = v;
+      --depth;
+    }
+  }
+  return HMF_OK;
+}
+
+}  // namespace
+
+extern "C" int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
+                                 const float* const* data, const float* const* smooth, const double* alpha,
+                                 int iterations, float step_size, float cc, float* const* labels,
+                                 void* stream) {
+  if (vx <= 0 || vy <= 0 || vz <= 0)
+    return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
+  if (semantics != HMF_SEMANTICS_REF_CUDA && semantics != HMF_SEMANTICS_REF_CPU)
+    return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "unknown semantics");
+  if (!data) return noalloc_fail(HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
+  NoAllocTree t;
+  int rc = noalloc_tree(parent, n_nodes, t);
+  if (rc) return rc;
+  for (int j = 0; j < t.n_leaves; ++j)
+    if (!data[t.leaves[j]]) return noalloc_fail(HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
+  for (int v = 0; v < t.n; ++v)
+    if (alpha && v != t.root && !(alpha[v] >= 0.0))
+      return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "Cannot use a negative smoothness value.");
+  iterations = std::max(0, iterations);
+  step_size = std::min(1.0f, std::max(0.0f, step_size));
+  cc = std::min(1.0f, std::max(0.0f, cc));
+
+  hmf::Geometry G;
+  G.vx = vx;
+  G.vy = vy;
+  G.vz = vz;
+  G.pitch = (vx + 3) / 4 * 4;
+  G.plane = (long long)G.pitch * vy;
+  G.vol = G.plane * vz;
+
+  // distinct smoothness images
+  const float* distinct[hmf::kMaxVertices];
+  int slot_of[hmf::kMaxVertices];
+  int n_distinct = 0;
+  for (int v = 0; v < t.n; ++v) {
+    slot_of[v] = -1;
+    if (v == t.root || !smooth || !smooth[v]) continue;
+    int s = 0;
+    while (s < n_distinct && distinct[s] != smooth[v]) ++s;
+    if (s == n_distinct) distinct[n_distinct++] = smooth[v];
+    slot_of[v] = s;
+  }
+
+  // scratch plan: tables, then state arrays, then pitched input copies
+  const size_t arr = round_up((size_t)G.vol * sizeof(float), 256);
+  const size_t tables = round_up(sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2, 256) +
+                        round_up(sizeof(hmf::TreeTable), 256) + round_up(sizeof(float*) * hmf::kMaxVertices, 256) +
+                        256;
+  const size_t n_arrays = (size_t)9 * (t.n - 1) + 1 + t.n_leaves + n_distinct;
+  if ((size_t)G.vol > (kNoAllocBytes / sizeof(float)) || n_arrays > kNoAllocBytes / arr ||
+      tables + n_arrays * arr > kNoAllocBytes)
+    return noalloc_fail(HMF_ERR_INVALID_ARGUMENT,
+                        "problem too large for hmf_solve_noalloc: its state exceeds the 64 MiB static scratch "
+                        "array; use hmf_create / hmf_solve");
+
+  int device = 0;
+  NCK(cudaGetDevice(&device), "cudaGetDevice");
+  unsigned char* base = nullptr;
+  rc = noalloc_setup(device, &base);
+  if (rc) return rc;
+  int sm_count = 0;
+  NCK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+
+  unsigned char* p = base;
+  auto* d_flow = reinterpret_cast<hmf::FlowVertex*>(p);
+  p += round_up(sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2, 256);
+  auto* d_tree = reinterpret_cast<hmf::TreeTable*>(p);
+  p += round_up(sizeof(hmf::TreeTable), 256);
+  auto* d_smooth_list = reinterpret_cast<const float**>(p);
+  p += round_up(sizeof(float*) * hmf::kMaxVertices, 256);
+  int* d_error = reinterpret_cast<int*>(p);
+  p += 256;
+  auto take = [&]() {
+    float* r = reinterpret_cast<float*>(p);
+    p += arr;
+    return r;
+  };
+  float* sink[hmf::kMaxVertices] = {};
+  float* label[hmf::kMaxVertices] = {};
+  float* div[hmf::kMaxVertices] = {};
+  float* fl[2][3][hmf::kMaxVertices] = {};
+  for (int v = 0; v < t.n; ++v) {
+    sink[v] = take();
+    if (v == t.root) continue;
+    label[v] = take();
+    div[v] = take();
+    for (int par = 0; par < 2; ++par)
+      for (int a = 0; a < 3; ++a) fl[par][a][v] = take();
+  }
+  const float* d_data[hmf::kMaxVertices] = {};
+  const float* d_distinct[hmf::kMaxVertices] = {};
+  for (int j = 0; j < t.n_leaves; ++j) d_data[t.leaves[j]] = take();
+  for (int k = 0; k < n_distinct; ++k) d_distinct[k] = take();
+  const size_t used = (size_t)(p - base);
+
+  // everything this call uses starts at zero
+  NCK(cudaMemsetAsync(base, 0, used, s), "cudaMemsetAsync(scratch)");
+  const size_t row = (size_t)vx * sizeof(float), prow = (size_t)G.pitch * sizeof(float);
+  for (int j = 0; j < t.n_leaves; ++j)
+    NCK(cudaMemcpy2DAsync(const_cast<float*>(d_data[t.leaves[j]]), prow, data[t.leaves[j]], row, row,
+                          (size_t)vy * vz, cudaMemcpyDeviceToDevice, s),
+        "cudaMemcpy2DAsync(data)");
+  for (int k = 0; k < n_distinct; ++k)
+    NCK(cudaMemcpy2DAsync(const_cast<float*>(d_distinct[k]), prow, distinct[k], row, row, (size_t)vy * vz,
+                          cudaMemcpyDeviceToDevice, s),
+        "cudaMemcpy2DAsync(smoothness)");
+
+  // tables, built on the host stack and staged by the (pageable) copies
+  hmf::FlowVertex fv[2 * hmf::kMaxVertices];
+  std::memset(fv, 0, sizeof(fv));
+  int slot = 0;
+  for (int i = 0; i < t.n; ++i) {
+    const int v = t.preorder[i];
+    if (v == t.root) continue;
+    for (int par = 0; par < 2; ++par) {
+      hmf::FlowVertex& f = fv[par * hmf::kMaxVertices + slot];
+      f.px_in = fl[par][0][v];
+      f.py_in = fl[par][1][v];
+      f.pz_in = fl[par][2][v];
+      f.px_out = fl[par ^ 1][0][v];
+      f.py_out = fl[par ^ 1][1][v];
+      f.pz_out = fl[par ^ 1][2][v];
+      f.sink = sink[v];
+      f.inc = sink[t.parent[v]];
+      f.label = label[v];
+      f.smooth = slot_of[v] >= 0 ? d_distinct[slot_of[v]] : nullptr;
+      f.div = div[v];
+      f.alpha = alpha ? (float)alpha[v] : 1.0f;
+    }
+    ++slot;
+  }
+  static_assert(sizeof(hmf::TreeTable) < 16384, "tree table size");
+  hmf::TreeTable tt;
+  std::memset(&tt, 0, sizeof(tt));
+  int entry[hmf::kMaxVertices];
+  for (int i = 0; i < t.n; ++i) entry[t.postorder[i]] = i;
+  tt.n = t.n;
+  tt.n_leaves = t.n_leaves;
+  tt.cc = cc;
+  tt.icc = 1.0f / cc;
+  tt.root_init = 1.0f / cc;
+  int kpos = 0;
+  for (int i = 0; i < t.n; ++i) {
+    const int v = t.postorder[i];
+    hmf::TreeEntry& E = tt.e[i];
+    E.sink = sink[v];
+    E.label = v == t.root ? nullptr : label[v];
+    E.div = v == t.root ? nullptr : div[v];
+    E.data = d_data[v];
+    E.parent = v == t.root ? -1 : entry[t.parent[v]];
+    E.first_kid = kpos;
+    E.n_kids = t.n_kids[v];
+    for (int k = 0; k < t.n_kids[v]; ++k) tt.kids[kpos++] = entry[t.kids[v][k]];
+    const int nk = E.n_kids;
+    E.inv_kids = nk == 0 ? 0.0f : (v == t.root ? 1.0f / (float)nk : 1.0f / (float)(nk + 1));
+  }
+  for (int j = 0; j < t.n_leaves; ++j) tt.leaves[j] = entry[t.leaves[j]];
+  NCK(cudaMemcpyAsync(d_flow, fv, sizeof(fv), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(flow table)");
+  NCK(cudaMemcpyAsync(d_tree, &tt, sizeof(tt), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(tree table)");
+  if (n_distinct)
+    NCK(cudaMemcpyAsync(d_smooth_list, d_distinct, sizeof(float*) * n_distinct, cudaMemcpyHostToDevice, s),
+        "cudaMemcpyAsync(smooth list)");
+
+  // initialisation and iterations, as hmf_solve queues them
+  const long long tblocks = (G.vol + kTreeThreads - 1) / kTreeThreads;
+  const int tgrid = (int)std::min<long long>(tblocks, (long long)sm_count * 16);
+  hmf::init_kernel<<<tgrid, kTreeThreads, (size_t)t.n * kTreeThreads * sizeof(float), s>>>(
+      d_tree, G, d_smooth_list, n_distinct, semantics == HMF_SEMANTICS_REF_CPU, d_error);
+  NCK(cudaGetLastError(), "init_kernel launch");
+  if (semantics == HMF_SEMANTICS_REF_CPU) {
+    hmf::refcpu_kernel<<<tgrid, kTreeThreads, 0, s>>>(d_tree, G, iterations);
+    NCK(cudaGetLastError(), "refcpu_kernel launch");
+  } else {
+    hmf::FlowParams fp;
+    fp.step = step_size;
+    fp.icc = 1.0f / cc;
+    fp.tiles_x = (vx + kTX - 1) / kTX;
+    const int tiles = fp.tiles_x * ((vy + kTY - 1) / kTY);
+    const int nonroot = t.n - 1;
+    const long long target = (long long)sm_count * 8;
+    int chunks = 1;
+    if ((long long)tiles * nonroot < target)
+      chunks = (int)std::min<long long>((target + (long long)tiles * nonroot - 1) / ((long long)tiles * nonroot),
+                                        std::max(1, vz / 8));
+    fp.zchunk = (vz + chunks - 1) / chunks;
+    chunks = (vz + fp.zchunk - 1) / fp.zchunk;
+    const dim3 fgrid(tiles, chunks, nonroot), fblock(kTX, kTY);
+    const size_t tsmem = 3 * (size_t)t.n * kTreeThreads * sizeof(float);
+    for (int it = 0; it < iterations; ++it) {
+      hmf::flow_kernel<kTX, kTY><<<fgrid, fblock, hmf::FlowTile<kTX, kTY>::SMEM_BYTES, s>>>(
+          d_flow + (it & 1) * hmf::kMaxVertices, G, fp);
+      NCK(cudaGetLastError(), "flow_kernel launch");
+      hmf::tree_kernel<<<tgrid, kTreeThreads, tsmem, s>>>(d_tree, G);
+      NCK(cudaGetLastError(), "tree_kernel launch");
+    }
+  }
+  if (labels) {
+    for (int v = 0; v < t.n; ++v) {
+      if (v == t.root || !labels[v]) continue;
+      NCK(cudaMemcpy2DAsync(labels[v], row, label[v], prow, row, (size_t)vy * vz, cudaMemcpyDeviceToDevice, s),
+          "cudaMemcpy2DAsync(labels)");
+    }
+  }
+  NCK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  int flag = 0;
+  NCK(cudaMemcpy(&flag, d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  if (flag)
+    return noalloc_fail(HMF_ERR_INVALID_ARGUMENT,
+                        "Data prior and smoothness must be non-negative (the solve ran on invalid input)");
+  return HMF_OK;
+}
