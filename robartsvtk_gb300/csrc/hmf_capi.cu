@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -21,6 +22,7 @@
 #include <vector>
 
 #include "../../include/hmf.h"
+#include "hmf_flow_tma.cuh"
 #include "hmf_kernels.cuh"
 
 namespace {
@@ -65,7 +67,10 @@ struct hmf_ctx {
   char* staging = nullptr;
   size_t staging_bytes = 0;
   hmf::FlowVertex* d_flow[2] = {nullptr, nullptr};
+  hmf::FlowVertexTMA* d_tma = nullptr;  // TMA-fed flow kernel table (both parities)
   hmf::TreeTable* d_tree = nullptr;
+  bool use_tma = true;    // flow_tma_kernel (else the shared-memory ring flow_kernel)
+  bool use_tree4 = true;  // tree4_kernel (else tree_kernel)
   const float** d_smooth_list = nullptr;
   int* d_error = nullptr;
   int n_smooth_list = 0;
@@ -85,6 +90,7 @@ struct hmf_ctx {
   // host copies of the device tables (kept per context: pageable-memory
   // cudaMemcpyAsync stages them before returning)
   std::vector<hmf::FlowVertex> h_flow;
+  std::vector<hmf::FlowVertexTMA> h_tma;
   hmf::TreeTable h_tree{};
   std::vector<const float*> h_smooth_list;
 
@@ -208,10 +214,47 @@ int allocate_state(hmf_ctx* c) {
   }
   CK(cudaMalloc(&c->d_flow[0], sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2), "cudaMalloc(tables)");
   c->d_flow[1] = c->d_flow[0] + hmf::kMaxVertices;
+  CK(cudaMalloc(&c->d_tma, sizeof(hmf::FlowVertexTMA) * hmf::kMaxVertices), "cudaMalloc(tma table)");
   CK(cudaMalloc(&c->d_tree, sizeof(hmf::TreeTable)), "cudaMalloc(tree table)");
   CK(cudaMalloc(&c->d_smooth_list, sizeof(float*) * hmf::kMaxVertices), "cudaMalloc(smooth list)");
   CK(cudaMalloc(&c->d_error, sizeof(int)), "cudaMalloc(error flag)");
   CK(cudaMemset(c->d_error, 0, sizeof(int)), "cudaMemset(error flag)");
+  return HMF_OK;
+}
+
+// cuTensorMapEncodeTiled, fetched through the runtime so that the library
+// needs no link-time dependency on the driver library.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// 3-D map of one pitched volume, box = one 36 x 32 window plane.
+int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return fail(c, HMF_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const auto& G = c->geo;
+  const cuuint64_t dims[3] = {(cuuint64_t)G.vx, (cuuint64_t)G.vy, (cuuint64_t)G.vz};
+  const cuuint64_t strides[2] = {(cuuint64_t)G.pitch * 4, (cuuint64_t)G.plane * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)hmf::kTmaBoxX, (cuuint32_t)hmf::kTmaRows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(c, HMF_ERR_CUDA, "cuTensorMapEncodeTiled failed with " + std::to_string((int)r));
   return HMF_OK;
 }
 
@@ -281,7 +324,39 @@ int stage_inputs(hmf_ctx* c, cudaStream_t s, std::vector<const float*>& d_data,
   return HMF_OK;
 }
 
+int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
+  const auto& G = c->geo;
+  hmf::FlowTmaParams fp;
+  fp.step = c->step;
+  fp.icc = 1.0f / c->cc;
+  // window outputs: at most 28 x 27, spread evenly over the volume
+  const int nx = (G.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX;
+  const int ny = (G.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY;
+  fp.out_x = (G.vx + nx - 1) / nx;
+  fp.out_y = (G.vy + ny - 1) / ny;
+  fp.tiles_x = nx;
+  fp.parity = parity;
+  fp.pad_ = 0;
+  fp.error_flag = c->d_error;
+  const int tiles = nx * ny;
+  const int nonroot = c->n - 1;
+  // two resident CTAs per SM; split z so that a launch has a few waves
+  const long long target = (long long)c->sm_count * 2 * 3;
+  int chunks = 1;
+  if ((long long)tiles * nonroot < target)
+    chunks = (int)std::min<long long>((target + (long long)tiles * nonroot - 1) / ((long long)tiles * nonroot),
+                                      std::max(1, G.vz / 16));
+  fp.zchunk = (G.vz + chunks - 1) / chunks;
+  chunks = (G.vz + fp.zchunk - 1) / fp.zchunk;
+  dim3 grid(tiles, chunks, nonroot);
+  hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(c->d_tma, G, fp);
+  CK(cudaGetLastError(), "flow_tma_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
 int launch_flow(hmf_ctx* c, int parity, cudaStream_t s) {
+  if (c->use_tma) return launch_flow_tma(c, parity, s);
   const auto& G = c->geo;
   hmf::FlowParams fp;
   fp.step = c->step;
@@ -310,6 +385,16 @@ int tree_grid(hmf_ctx* c) {
 }
 
 int launch_tree(hmf_ctx* c, cudaStream_t s) {
+  if (c->use_tree4) {
+    const size_t smem4 = 4 * (size_t)c->n * hmf::kTree4Threads * sizeof(float4);
+    const long long quads = c->geo.vol / 4;
+    const int grid = (int)std::min<long long>((quads + hmf::kTree4Threads - 1) / hmf::kTree4Threads,
+                                              (long long)c->sm_count * 32);
+    hmf::tree4_kernel<<<grid, hmf::kTree4Threads, smem4, s>>>(c->d_tree, c->geo);
+    CK(cudaGetLastError(), "tree4_kernel launch");
+    ++c->launches;
+    return HMF_OK;
+  }
   const size_t smem = 3 * (size_t)c->n * kTreeThreads * sizeof(float);
   hmf::tree_kernel<<<tree_grid(c), kTreeThreads, smem, s>>>(c->d_tree, c->geo);
   CK(cudaGetLastError(), "tree_kernel launch");
@@ -383,6 +468,35 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& 
   }
   CK(cudaMemcpyAsync(c->d_flow[0], fv.data(), sizeof(hmf::FlowVertex) * fv.size(), cudaMemcpyHostToDevice, s),
      "cudaMemcpyAsync(flow table)");
+  if (c->use_tma) {
+    std::vector<hmf::FlowVertexTMA>& tv = c->h_tma;
+    tv.assign(c->n - 1, hmf::FlowVertexTMA{});
+    int j = 0;
+    for (int v : c->preorder) {
+      if (v == c->root) continue;
+      hmf::FlowVertexTMA& f = tv[j++];
+      std::memset(&f, 0, sizeof(f));
+      int rc = HMF_OK;
+      for (int par = 0; par < 2 && !rc; ++par) {
+        rc = encode_plane_map(c, &f.flow_in[par][0], c->fx[par][v]);
+        if (!rc) rc = encode_plane_map(c, &f.flow_in[par][1], c->fy[par][v]);
+        if (!rc) rc = encode_plane_map(c, &f.flow_in[par][2], c->fz[par][v]);
+        f.flow_out[par][0] = c->fx[par ^ 1][v];
+        f.flow_out[par][1] = c->fy[par ^ 1][v];
+        f.flow_out[par][2] = c->fz[par ^ 1][v];
+      }
+      if (!rc) rc = encode_plane_map(c, &f.sink, c->sink[v]);
+      if (!rc) rc = encode_plane_map(c, &f.label, c->label[v]);
+      if (!rc) rc = encode_plane_map(c, &f.inc, c->sink[c->parent[v]]);
+      if (!rc && d_smooth[v]) rc = encode_plane_map(c, &f.smooth, d_smooth[v]);
+      if (rc) return rc;
+      f.has_smooth = d_smooth[v] != nullptr;
+      f.div = c->div[v];
+      f.alpha = (float)c->alpha[v];
+    }
+    CK(cudaMemcpyAsync(c->d_tma, tv.data(), sizeof(hmf::FlowVertexTMA) * tv.size(), cudaMemcpyHostToDevice, s),
+       "cudaMemcpyAsync(tma table)");
+  }
   hmf::TreeTable& tt = c->h_tree;
   std::memset(&tt, 0, sizeof(tt));
   std::vector<int> entry(c->n, -1);
@@ -451,6 +565,11 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(init_kernel)");
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hmf::kTmaSmemBytes),
+     "cudaFuncSetAttribute(flow_tma_kernel)");
+  CK(cudaFuncSetAttribute(hmf::tree4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          4 * hmf::kTree4MaxVertices * hmf::kTree4Threads * (int)sizeof(float4)),
+     "cudaFuncSetAttribute(tree4_kernel)");
   return HMF_OK;
 }
 
@@ -470,7 +589,8 @@ int copy_out(hmf_ctx* c, const float* src, float* out, int where, void* stream) 
     CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(output)");
     int flag = 0;
     CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
-    if (flag)
+    if (flag & 2) return fail(c, HMF_ERR_CUDA, "a TMA wait in flow_tma_kernel timed out; results are invalid");
+    if (flag & 1)
       return fail(c, HMF_ERR_INVALID_ARGUMENT,
                   "Data prior and smoothness must be non-negative (the solve ran on invalid input)");
   }
@@ -505,6 +625,12 @@ int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_n
     return rc;
   }
   c->alpha.assign(c->n, 1.0);
+  // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=scalar select the
+  // simpler kernels (same results), for comparisons.
+  if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0;
+  c->use_tree4 = c->n <= hmf::kTree4MaxVertices;
+  if (const char* e = std::getenv("HMF_TREE_KERNEL"))
+    if (std::strcmp(e, "scalar") == 0) c->use_tree4 = false;
   c->data.assign(c->n, {});
   c->smooth.assign(c->n, {});
   {
@@ -550,6 +676,7 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->arena) cudaFree(c->arena);
   if (c->staging) cudaFree(c->staging);
   if (c->d_flow[0]) cudaFree(c->d_flow[0]);
+  if (c->d_tma) cudaFree(c->d_tma);
   if (c->d_tree) cudaFree(c->d_tree);
   if (c->d_smooth_list) cudaFree(c->d_smooth_list);
   if (c->d_error) cudaFree(c->d_error);

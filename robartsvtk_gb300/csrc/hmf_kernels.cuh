@@ -327,6 +327,95 @@ __global__ void tree_kernel(const TreeTable* __restrict__ table, const Geometry 
 }
 
 // ---------------------------------------------------------------------------
+// tree4_kernel: tree_kernel on four consecutive voxels per thread (float4
+// loads and stores; rows are padded to a multiple of 4 floats, so every array
+// length is a multiple of 4).  Every load of a voxel quad is issued before the
+// sweep, and the per-vertex values (sink, divergence, label, capacity) live
+// in shared memory [n][blockDim] as float4.  Same arithmetic as tree_kernel,
+// component by component.
+// ---------------------------------------------------------------------------
+constexpr int kTree4Threads = 128;
+constexpr int kTree4MaxVertices = 24;
+
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+__global__ void __launch_bounds__(kTree4Threads) tree4_kernel(const TreeTable* __restrict__ table, const Geometry G) {
+  __shared__ TreeTable T;
+  extern __shared__ float4 v4[];
+  for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  __syncthreads();
+  const int n = T.n, nb = blockDim.x, t = threadIdx.x;
+  float4* S = v4;             // [n][nb]
+  float4* D = v4 + n * nb;    // [n][nb]
+  float4* U = v4 + 2 * n * nb;
+  float4* C = v4 + 3 * n * nb;  // capacities of leaves
+  const float icc = T.icc, cc = T.cc;
+  const int root = n - 1;
+  const long long nq = G.vol / 4;
+  for (long long q = (long long)blockIdx.x * nb + t; q < nq; q += (long long)gridDim.x * nb) {
+    const long long i = q * 4;
+#pragma unroll 4
+    for (int e = 0; e < root; ++e) {
+      const TreeEntry& E = T.e[e];
+      D[e * nb + t] = ld4(E.div + i);
+      U[e * nb + t] = ld4(E.label + i);
+      if (E.n_kids) S[e * nb + t] = ld4(E.sink + i);
+      else C[e * nb + t] = ld4(E.data + i);
+    }
+    S[root * nb + t] = ld4(T.e[root].sink + i);
+    for (int e = 0; e < n; ++e) {
+      const TreeEntry& E = T.e[e];
+      float4 r;
+      if (E.n_kids == 0) {
+        const float4 inc = S[E.parent * nb + t], d = D[e * nb + t], u = U[e * nb + t], cap = C[e * nb + t];
+        float v;
+#define HMF_LEAF(c)                          \
+  v = (inc.c - d.c) + u.c * icc;             \
+  v = (v < 0.0f) ? 0.0f : v;                 \
+  v = (v > cap.c) ? cap.c : v;               \
+  r.c = v;
+        HMF_LEAF(x) HMF_LEAF(y) HMF_LEAF(z) HMF_LEAF(w)
+#undef HMF_LEAF
+      } else {
+        const float w0 = (e == root) ? T.root_init : 0.0f;
+        float4 W = make_float4(w0, w0, w0, w0);
+        for (int j = 0; j < E.n_kids; ++j) {
+          const int c = T.kids[E.first_kid + j];
+          const float4 sc = S[c * nb + t], dc = D[c * nb + t], uc = U[c * nb + t];
+          W.x = ((W.x + sc.x) + dc.x) - uc.x * icc;
+          W.y = ((W.y + sc.y) + dc.y) - uc.y * icc;
+          W.z = ((W.z + sc.z) + dc.z) - uc.z * icc;
+          W.w = ((W.w + sc.w) + dc.w) - uc.w * icc;
+        }
+        if (e != root) {
+          const float4 inc = S[E.parent * nb + t], d = D[e * nb + t], u = U[e * nb + t];
+          W.x = ((W.x + inc.x) - d.x) + u.x * icc;
+          W.y = ((W.y + inc.y) - d.y) + u.y * icc;
+          W.z = ((W.z + inc.z) - d.z) + u.z * icc;
+          W.w = ((W.w + inc.w) - d.w) + u.w * icc;
+        }
+        r = make_float4(W.x * E.inv_kids, W.y * E.inv_kids, W.z * E.inv_kids, W.w * E.inv_kids);
+      }
+      S[e * nb + t] = r;
+    }
+    for (int e = 0; e < root; ++e) {
+      const TreeEntry& E = T.e[e];
+      const float4 inc = S[E.parent * nb + t], d = D[e * nb + t], s = S[e * nb + t], u = U[e * nb + t];
+      float4 o;
+      o.x = __saturatef(u.x + cc * ((inc.x - d.x) - s.x));
+      o.y = __saturatef(u.y + cc * ((inc.y - d.y) - s.y));
+      o.z = __saturatef(u.z + cc * ((inc.z - d.z) - s.z));
+      o.w = __saturatef(u.w + cc * ((inc.w - d.w) - s.w));
+      st4(E.label + i, o);
+      st4(E.sink + i, s);
+    }
+    st4(T.e[root].sink + i, S[root * nb + t]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // init_kernel (vtkCudaHierarchicalMaxFlowSegmentation.cxx:547-658 and
 // PropogateLabels :63-104): sinks and source = min over leaves of D; leaf
 // labels = [D == min] / count; branch labels = sums of their kids.  Also
