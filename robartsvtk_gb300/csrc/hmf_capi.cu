@@ -24,6 +24,7 @@
 #include "../../include/hmf.h"
 #include "hmf_flow_tma.cuh"
 #include "hmf_kernels.cuh"
+#include "hmf_tree_bulk.cuh"
 
 namespace {
 
@@ -70,7 +71,7 @@ struct hmf_ctx {
   hmf::FlowVertexTMA* d_tma = nullptr;  // TMA-fed flow kernel table (both parities)
   hmf::TreeTable* d_tree = nullptr;
   bool use_tma = true;    // flow_tma_kernel (else the shared-memory ring flow_kernel)
-  bool use_tree4 = true;  // tree4_kernel (else tree_kernel)
+  int tree_kind = 0;      // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
   const float** d_smooth_list = nullptr;
   int* d_error = nullptr;
   int n_smooth_list = 0;
@@ -385,7 +386,18 @@ int tree_grid(hmf_ctx* c) {
 }
 
 int launch_tree(hmf_ctx* c, cudaStream_t s) {
-  if (c->use_tree4) {
+  if (c->tree_kind == 0) {
+    const int smem = hmf::tree_bulk_smem_bytes(c->n);
+    const int vc = hmf::tree_bulk_chunk(c->n);
+    const long long chunks = (c->geo.vol + vc - 1) / vc;
+    const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
+    const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
+    hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(c->d_tree, c->geo, c->d_error);
+    CK(cudaGetLastError(), "tree_bulk_kernel launch");
+    ++c->launches;
+    return HMF_OK;
+  }
+  if (c->tree_kind == 1) {
     const size_t smem4 = 4 * (size_t)c->n * hmf::kTree4Threads * sizeof(float4);
     const long long quads = c->geo.vol / 4;
     const int grid = (int)std::min<long long>((quads + hmf::kTree4Threads - 1) / hmf::kTree4Threads,
@@ -570,6 +582,9 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::tree4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           4 * hmf::kTree4MaxVertices * hmf::kTree4Threads * (int)sizeof(float4)),
      "cudaFuncSetAttribute(tree4_kernel)");
+  CK(cudaFuncSetAttribute(hmf::tree_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          128 + hmf::kTreeBulkSmemBudget),
+     "cudaFuncSetAttribute(tree_bulk_kernel)");
   return HMF_OK;
 }
 
@@ -628,9 +643,11 @@ int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_n
   // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=scalar select the
   // simpler kernels (same results), for comparisons.
   if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0;
-  c->use_tree4 = c->n <= hmf::kTree4MaxVertices;
-  if (const char* e = std::getenv("HMF_TREE_KERNEL"))
-    if (std::strcmp(e, "scalar") == 0) c->use_tree4 = false;
+  c->tree_kind = 0;
+  if (const char* e = std::getenv("HMF_TREE_KERNEL")) {
+    if (std::strcmp(e, "quad") == 0 && c->n <= hmf::kTree4MaxVertices) c->tree_kind = 1;
+    if (std::strcmp(e, "scalar") == 0) c->tree_kind = 2;
+  }
   c->data.assign(c->n, {});
   c->smooth.assign(c->n, {});
   {

@@ -23,6 +23,7 @@
 
 #include <cuda.h>
 
+#include "hmf_async.cuh"
 #include "hmf_kernels.cuh"
 
 namespace hmf {
@@ -59,57 +60,19 @@ struct FlowTmaParams {
   int* error_flag;
 };
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-__device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* map, int x, int y, int z,
-                                               uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Wait for a completed phase for at most `limit_ns`; false on time-out (the
-// caller records the failure instead of hanging).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, uint64_t limit_ns) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  while (!mbar_try_wait(bar, parity))
-    if (global_ns() - t0 > limit_ns) return false;
-  return true;
-}
-
 constexpr uint64_t kTmaWaitLimitNs = 500000000ull;  // 0.5 s: far beyond any healthy copy
+
+// Projection multiplier of kern_ComputeFlowMag*: m = |p| > lim ? lim/|p| : 1
+// with |p| = sqrtf(h).  For lim > 1e-18 (so that lim*lim is a normal float),
+// RN(RN(lim*lim) * (1 - 2^-20)) < lim^2 (1 - 2^-21); when h is below it,
+// sqrt(h) < lim, hence RN(sqrt(h)) <= lim and the result is exactly 1 without
+// evaluating the square root or the division.  Everything else (tiny lim,
+// NaN, infinities) takes the exact path.
+__device__ __forceinline__ float projection_multiplier(float h, float lim) {
+  if (lim > 1.0e-18f && h < (lim * lim) * (1.0f - 0x1p-20f)) return 1.0f;
+  const float F = sqrtf(h);
+  return (F > lim) ? lim / F : 1.0f;
+}
 
 __global__ void __launch_bounds__(kTmaThreads, 2)
 flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, const FlowTmaParams fp) {
@@ -122,6 +85,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
   float* xm = xpy + 256;                                          // [8][32]  m(k-1), row 3
   float* xP = xm + 256;                                           // [2][8][32] P_y(k-2), row 0
   uint64_t* bars = reinterpret_cast<uint64_t*>(xP + 512);        // [3]
+  __shared__ int abort_cta;
 
   const FlowVertexTMA* V = vertices + blockIdx.z;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -138,16 +102,36 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
   const int kend = ze + 1;
   const int kload_end = min(ze + 2, G.vz - 1);
   const int par = fp.parity;
+  const float step = fp.step, icc = fp.icc;
+  // per-vertex values read once (the stores below could otherwise alias them)
   const bool has_s = V->has_smooth != 0;
   const int narr = has_s ? 7 : 6;
-  const float step = fp.step, icc = fp.icc, alpha = V->alpha;
+  const float alpha = V->alpha;
+  float* const out_x = V->flow_out[par][0];
+  float* const out_y = V->flow_out[par][1];
+  float* const out_z = V->flow_out[par][2];
+  float* const out_d = V->div;
   const bool xin = x >= 0 && x < G.vx;
-  const bool xlast = (x == G.vx - 1);
+  const bool xpos = x > 0;
+  const bool xnl = x != G.vx - 1;
+  const bool xout = lane >= 2 && lane < 2 + fp.out_x && x < G.vx;
+  // per-row constants of this thread (rows warp*4 + r of the window)
+  bool rin[4], ypos[4], ynl[4], rout[4];
+  long long rowoff[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int row = warp * 4 + r;
+    const int y = y0 - 2 + row;
+    rin[r] = xin && y >= 0 && y < G.vy;
+    ypos[r] = y > 0;
+    ynl[r] = y != G.vy - 1;
+    rout[r] = xout && row >= 2 && row < 2 + fp.out_y && y < G.vy;
+    rowoff[r] = (long long)y * G.pitch + x;
+  }
 
   // If a previous launch already timed out waiting for its copies, the whole
   // CTA returns (one read, shared by all threads), so that a broken
   // configuration fails fast instead of slowly.
-  __shared__ int abort_cta;
   if (threadIdx.x == 0) {
     abort_cta = fp.error_flag ? (*(volatile int*)fp.error_flag & 2) : 0;
     for (int s = 0; s < kTmaSlots; ++s) mbar_init(&bars[s], 1);
@@ -196,7 +180,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
     const int ko = k - 2;
     const bool doE = ko >= zs && ko < ze;                              // div(k-2), output
 
-    // ---- stage A: g(k) from the staged inputs (kern_CalcGradStep + kern_Divergence of k-1)
+    // ---- stage A: g(k) from the staged inputs (kern_CalcGradStep on the
+    // divergence kern_Divergence left, recomputed from the stored flows)
     float g[4], rx[4], ry_[4], rz[4], Scur[4];
     if (doA) {
       wait_plane(k);
@@ -204,11 +189,9 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
       if (has_next) wait_plane(k + 1);
       const float* cur = slot_of(k);
       const float* nxt = has_next ? slot_of(k + 1) : cur;
-      const bool ztop = (k == G.vz - 1);
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int row = warp * 4 + r;
-        const int y = y0 - 2 + row;
         const int i = row * kTmaBoxX + off + lane;
         const float px = cur[i], py = cur[kTmaPlane + i], pz = cur[2 * kTmaPlane + i];
         const float pxr = cur[i + 1];
@@ -217,11 +200,10 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
         const float sk = cur[3 * kTmaPlane + i], u = cur[4 * kTmaPlane + i], c = cur[5 * kTmaPlane + i];
         Scur[r] = has_s ? cur[6 * kTmaPlane + i] : 0.f;
         float d = (px + py) + pz;
-        if (!xlast) d = d - pxr;
-        if (y != G.vy - 1) d = d - pyd;
-        if (!ztop) d = d - pzn;
-        const bool in = xin && y >= 0 && y < G.vy;
-        g[r] = in ? step * (((sk + d) - c) - u * icc) : 0.f;
+        if (xnl) d = d - pxr;
+        if (ynl[r]) d = d - pyd;
+        if (has_next) d = d - pzn;
+        g[r] = rin[r] ? step * (((sk + d) - c) - u * icc) : 0.f;
         rx[r] = px;
         ry_[r] = py;
         rz[r] = pz;
@@ -238,39 +220,38 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
 
     // ---- stage B: p'(k) (kern_DescentSpatialFlow)
     float npx[4], npy[4], npz[4];
+    const float gup = warp ? xg[(warp - 1) * 32 + lane] : 0.f;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const float gxm = __shfl_up_sync(FULL, g[r], 1);
-      const float gym = r ? g[r > 0 ? r - 1 : 0] : (warp ? xg[(warp - 1) * 32 + lane] : 0.f);
-      const int y = y0 - 2 + warp * 4 + r;
-      const bool in = doA && xin && y >= 0 && y < G.vy;
-      npx[r] = (in && x > 0) ? rx[r] - (g[r] - gxm) : 0.f;
-      npy[r] = (in && y > 0) ? ry_[r] - (g[r] - gym) : 0.f;
+      const float gym = r ? g[r > 0 ? r - 1 : 0] : gup;
+      const bool in = doA && rin[r];
+      npx[r] = (in && xpos) ? rx[r] - (g[r] - gxm) : 0.f;
+      npy[r] = (in && ypos[r]) ? ry_[r] - (g[r] - gym) : 0.f;
       npz[r] = (in && k > 0) ? rz[r] - (g[r] - gprev[r]) : 0.f;
       gprev[r] = g[r];
     }
 
     // ---- stage C: m(k-1) (kern_ComputeFlowMag*)
     float m[4];
+    const float pdown = warp < 7 ? xpy[(warp + 1) * 32 + lane] : 0.f;
+    const bool znl = kc != G.vz - 1;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const float pxr = __shfl_down_sync(FULL, ppx[r], 1);
-      const float pyd = r < 3 ? ppy[r < 3 ? r + 1 : 3] : (warp < 7 ? xpy[(warp + 1) * 32 + lane] : 0.f);
-      const int y = y0 - 2 + warp * 4 + r;
+      const float pyd = r < 3 ? ppy[r < 3 ? r + 1 : 3] : pdown;
       float mv = 1.0f;
-      if (doC && xin && y >= 0 && y < G.vy) {
+      if (doC && rin[r]) {
         float up = ppx[r] * ppx[r];
-        float dn = !xlast ? pxr * pxr : 0.f;
+        float dn = xnl ? pxr * pxr : 0.f;
         float F = up + dn;
         up = ppy[r] * ppy[r];
-        dn = (y != G.vy - 1) ? pyd * pyd : 0.f;
+        dn = ynl[r] ? pyd * pyd : 0.f;
         F = F + (up + dn);
         up = ppz[r] * ppz[r];
-        dn = (kc != G.vz - 1) ? npz[r] * npz[r] : 0.f;
+        dn = znl ? npz[r] * npz[r] : 0.f;
         F = F + (up + dn);
-        F = sqrtf(0.5f * F);
-        const float lim = has_s ? alpha * Sprev[r] : alpha;
-        mv = (F > lim) ? lim / F : 1.0f;
+        mv = projection_multiplier(0.5f * F, has_s ? alpha * Sprev[r] : alpha);
       }
       m[r] = mv;
       Sprev[r] = Scur[r];
@@ -280,35 +261,36 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
 
     // ---- stage D: P(k-1) (kern_Project)
     float nPx[4], nPy[4], nPz[4];
+    const float mup = warp ? xm[(warp - 1) * 32 + lane] : 0.f;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const float mxm = __shfl_up_sync(FULL, m[r], 1);
-      const float mym = r ? m[r > 0 ? r - 1 : 0] : (warp ? xm[(warp - 1) * 32 + lane] : 0.f);
-      const int y = y0 - 2 + warp * 4 + r;
-      const bool in = doC && xin && y >= 0 && y < G.vy;
-      nPx[r] = (in && x > 0) ? (ppx[r] * 0.5f) * (m[r] + mxm) : 0.f;
-      nPy[r] = (in && y > 0) ? (ppy[r] * 0.5f) * (m[r] + mym) : 0.f;
+      const float mym = r ? m[r > 0 ? r - 1 : 0] : mup;
+      const bool in = doC && rin[r];
+      nPx[r] = (in && xpos) ? (ppx[r] * 0.5f) * (m[r] + mxm) : 0.f;
+      nPy[r] = (in && ypos[r]) ? (ppy[r] * 0.5f) * (m[r] + mym) : 0.f;
       nPz[r] = (in && kc > 0) ? (ppz[r] * 0.5f) * (m[r] + mprev[r]) : 0.f;
       if (doC) mprev[r] = m[r];
     }
 
     // ---- stage E: divergence of P(k-2) (kern_Divergence), store P(k-2) and div(k-2)
+    const float Pdown = warp < 7 ? xP[((k & 1) * 8 + warp + 1) * 32 + lane] : 0.f;
+    const bool zonl = ko != G.vz - 1;
+    const long long zoff = (long long)ko * G.plane;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const float Pxr = __shfl_down_sync(FULL, Px[r], 1);
-      const float Pyd = r < 3 ? Py[r < 3 ? r + 1 : 3] : (warp < 7 ? xP[((k & 1) * 8 + warp + 1) * 32 + lane] : 0.f);
-      const int row = warp * 4 + r;
-      const int y = y0 - 2 + row;
-      if (doE && lane >= 2 && lane < 2 + fp.out_x && row >= 2 && row < 2 + fp.out_y && x < G.vx && y < G.vy) {
+      const float Pyd = r < 3 ? Py[r < 3 ? r + 1 : 3] : Pdown;
+      if (doE && rout[r]) {
         float dv = (Px[r] + Py[r]) + Pz[r];
-        if (!xlast) dv = dv - Pxr;
-        if (y != G.vy - 1) dv = dv - Pyd;
-        if (ko != G.vz - 1) dv = dv - nPz[r];
-        const long long o = (long long)ko * G.plane + (long long)y * G.pitch + x;
-        V->flow_out[par][0][o] = Px[r];
-        V->flow_out[par][1][o] = Py[r];
-        V->flow_out[par][2][o] = Pz[r];
-        V->div[o] = dv;
+        if (xnl) dv = dv - Pxr;
+        if (ynl[r]) dv = dv - Pyd;
+        if (zonl) dv = dv - nPz[r];
+        const long long o = zoff + rowoff[r];
+        out_x[o] = Px[r];
+        out_y[o] = Py[r];
+        out_z[o] = Pz[r];
+        out_d[o] = dv;
       }
     }
 

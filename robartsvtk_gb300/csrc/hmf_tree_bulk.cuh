@@ -1,0 +1,164 @@
+// hmf_tree_bulk.cuh -- the per-voxel sink / source / label sweep of one
+// iteration (CUDA_hierarchicalmaxflow.cu:124-220 and MultiplyAndStoreBuffer,
+// launched in the order of vtkCudaHierarchicalMaxFlowSegmentation.cxx:268-426),
+// streamed through shared memory with bulk copies.
+//
+// A persistent CTA walks chunks of Vc consecutive voxels.  For every chunk it
+// brings in, with one cp.async.bulk per array, the 3(n-1)+1 arrays the sweep
+// reads -- per non-root entry its divergence, its label and either its sink
+// (branch) or its data term (leaf), plus the source flow -- into one of two
+// shared-memory stages completed by an mbarrier, so one chunk is in flight
+// while the other is swept.  Each thread sweeps four voxels (float4); new
+// sinks overwrite the staged sink / data slots in post-order (a parent's old
+// sink is read by its children before the parent replaces it), labels and
+// sinks go straight to global memory.  Same arithmetic as tree_kernel.
+#pragma once
+
+#include "hmf_async.cuh"
+#include "hmf_kernels.cuh"
+
+namespace hmf {
+
+constexpr int kTreeBulkStages = 2;
+constexpr int kTreeBulkSmemBudget = 200 * 1024;
+
+// Chunk length (voxels) for a tree of n entries: the largest power of two
+// <= 1024 whose two stages fit the shared-memory budget.
+__host__ __device__ inline int tree_bulk_chunk(int n) {
+  const int arrays = 3 * (n - 1) + 1;
+  int vc = 1024;
+  while (vc > 32 && kTreeBulkStages * arrays * vc * 4 > kTreeBulkSmemBudget) vc /= 2;
+  return vc;
+}
+
+__host__ __device__ inline int tree_bulk_smem_bytes(int n) {
+  return 128 + kTreeBulkStages * (3 * (n - 1) + 1) * tree_bulk_chunk(n) * 4;
+}
+
+__global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag) {
+  __shared__ TreeTable T;
+  __shared__ int abort_cta;
+  extern __shared__ unsigned char tb_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(tb_raw) + 127) & ~static_cast<uintptr_t>(127));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base);  // [2]
+  float* stage0 = reinterpret_cast<float*>(base + 128);
+
+  for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  if (threadIdx.x == 0) {
+    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (abort_cta) return;
+
+  const int n = T.n, root = n - 1;
+  const int arrays = 3 * (n - 1) + 1;
+  const int vc = tree_bulk_chunk(n);
+  const long long nchunks = (G.vol + vc - 1) / vc;
+  const float icc = T.icc, cc = T.cc;
+  auto stage = [&](int s) { return stage0 + (size_t)s * arrays * vc; };
+  // staged array slot of each quantity: entry e < root -> div 3e, label 3e+1,
+  // sink (branch) / data (leaf) 3e+2; the root's source flow -> 3(n-1)
+  auto sink_slot = [&](int e) { return e == root ? 3 * root : 3 * e + 2; };
+
+  auto issue = [&](long long chunk, int s) {  // thread 0 only
+    const long long v0 = chunk * vc;
+    const unsigned bytes = (unsigned)(min((long long)vc, G.vol - v0) * 4);
+    uint64_t* bar = &bars[s];
+    float* dst = stage(s);
+    mbar_expect_tx(bar, bytes * (unsigned)arrays);
+    for (int e = 0; e < root; ++e) {
+      const TreeEntry& E = T.e[e];
+      bulk_load(dst + (size_t)(3 * e) * vc, E.div + v0, bytes, bar);
+      bulk_load(dst + (size_t)(3 * e + 1) * vc, E.label + v0, bytes, bar);
+      bulk_load(dst + (size_t)(3 * e + 2) * vc, (E.n_kids ? E.sink : E.data) + v0, bytes, bar);
+    }
+    bulk_load(dst + (size_t)(3 * root) * vc, T.e[root].sink + v0, bytes, bar);
+  };
+
+  bool timed_out = false;
+  int nissued[kTreeBulkStages] = {0, 0};  // kept by thread 0
+  long long chunk = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  }
+  for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
+    const int s = j & 1;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    float* st = stage(s);
+    const long long v0 = chunk * vc;
+    const int len = (int)min((long long)vc, G.vol - v0);
+    const int q = threadIdx.x * 4;
+    if (q < len) {
+      auto at = [&](int slot) -> float4& { return *reinterpret_cast<float4*>(st + (size_t)slot * vc + q); };
+      for (int e = 0; e < n; ++e) {
+        const TreeEntry& E = T.e[e];
+        if (E.n_kids == 0) {
+          const float4 inc = at(sink_slot(E.parent)), d = at(3 * e), u = at(3 * e + 1), cap = at(3 * e + 2);
+          float4 r;
+          float v;
+#define HMF_LEAF(c)              \
+  v = (inc.c - d.c) + u.c * icc; \
+  v = (v < 0.0f) ? 0.0f : v;     \
+  v = (v > cap.c) ? cap.c : v;   \
+  r.c = v;
+          HMF_LEAF(x) HMF_LEAF(y) HMF_LEAF(z) HMF_LEAF(w)
+#undef HMF_LEAF
+          at(3 * e + 2) = r;
+        } else {
+          const float w0 = (e == root) ? T.root_init : 0.0f;
+          float4 W = make_float4(w0, w0, w0, w0);
+          for (int k = 0; k < E.n_kids; ++k) {
+            const int c = T.kids[E.first_kid + k];
+            const float4 sc = at(sink_slot(c)), dc = at(3 * c), uc = at(3 * c + 1);
+            W.x = ((W.x + sc.x) + dc.x) - uc.x * icc;
+            W.y = ((W.y + sc.y) + dc.y) - uc.y * icc;
+            W.z = ((W.z + sc.z) + dc.z) - uc.z * icc;
+            W.w = ((W.w + sc.w) + dc.w) - uc.w * icc;
+          }
+          if (e != root) {
+            const float4 inc = at(sink_slot(E.parent)), d = at(3 * e), u = at(3 * e + 1);
+            W.x = ((W.x + inc.x) - d.x) + u.x * icc;
+            W.y = ((W.y + inc.y) - d.y) + u.y * icc;
+            W.z = ((W.z + inc.z) - d.z) + u.z * icc;
+            W.w = ((W.w + inc.w) - d.w) + u.w * icc;
+          }
+          at(sink_slot(e)) = make_float4(W.x * E.inv_kids, W.y * E.inv_kids, W.z * E.inv_kids, W.w * E.inv_kids);
+        }
+      }
+      const long long i = v0 + q;
+      for (int e = 0; e < root; ++e) {
+        const TreeEntry& E = T.e[e];
+        const float4 inc = at(sink_slot(E.parent)), d = at(3 * e), sk = at(3 * e + 2), u = at(3 * e + 1);
+        float4 o;
+        o.x = __saturatef(u.x + cc * ((inc.x - d.x) - sk.x));
+        o.y = __saturatef(u.y + cc * ((inc.y - d.y) - sk.y));
+        o.z = __saturatef(u.z + cc * ((inc.z - d.z) - sk.z));
+        o.w = __saturatef(u.w + cc * ((inc.w - d.w) - sk.w));
+        *reinterpret_cast<float4*>(E.label + i) = o;
+        *reinterpret_cast<float4*>(E.sink + i) = sk;
+      }
+      *reinterpret_cast<float4*>(T.e[root].sink + i) = at(3 * root);
+    }
+    // The sweep wrote sinks into stage s with ordinary stores; order them
+    // before the bulk copy that will refill the stage (async proxy).
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();  // stage s is free again
+    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+  }
+  if (timed_out && error_flag) atomicOr(error_flag, 2);
+  if (threadIdx.x == 0) {
+    // Copies into this CTA's shared memory must have landed before it exits;
+    // after a time-out wait for the last one of each stage (bounded).
+    if (timed_out)
+      for (int s = 0; s < kTreeBulkStages; ++s)
+        if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+  }
+}
+
+}  // namespace hmf

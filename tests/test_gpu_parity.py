@@ -206,3 +206,20 @@ def test_against_reference_cuda_kernels_golden(name):
     w = problem(name)
     r = run_gpu(w)
     assert np.abs(r["u"] - g[name + "/u"]).max() <= LABEL_TOL
+
+
+@pytest.mark.parametrize("flow,tree", [("tma", "bulk"), ("ring", "bulk"), ("tma", "quad"), ("ring", "scalar")])
+def test_kernel_variants_are_bitexact(flow, tree, monkeypatch):
+    """Every flow / tree kernel variant gives the oracle's results."""
+    monkeypatch.setenv("HMF_FLOW_KERNEL", flow)
+    monkeypatch.setenv("HMF_TREE_KERNEL", tree)
+    for dims, parent in (((45, 30, 21), [-1, 0, 0, 1, 1, 2, 2]), ((29, 58, 9), [-1, 0, 0, 0])):
+        w = random_tree_problem(31, dims, parent, iterations=12, smooth_nodes=(1, 2))
+        assert_same(run_gpu(w), oracle(w), "%s/%s %s" % (flow, tree, dims))
+
+
+def test_large_tree_uses_small_chunks():
+    """A 20-vertex tree: the tree kernel's chunk shrinks to fit shared memory."""
+    parent = [-1] + [0] * 4 + [1, 1, 2, 2, 3, 3, 4, 4] + [5, 5, 6, 6, 7, 7, 8]
+    w = random_tree_problem(32, (40, 21, 13), parent, iterations=6, smooth_nodes=(3, 9))
+    assert_same(run_gpu(w), oracle(w), "20-vertex tree")
