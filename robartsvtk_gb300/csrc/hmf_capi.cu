@@ -337,7 +337,7 @@ int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
   fp.out_y = (G.vy + ny - 1) / ny;
   fp.tiles_x = nx;
   fp.parity = parity;
-  fp.pad_ = 0;
+  fp.n_vertices = c->n - 1;
   fp.error_flag = c->d_error;
   const int tiles = nx * ny;
   const int nonroot = c->n - 1;
@@ -349,7 +349,7 @@ int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
                                       std::max(1, G.vz / 16));
   fp.zchunk = (G.vz + chunks - 1) / chunks;
   chunks = (G.vz + fp.zchunk - 1) / fp.zchunk;
-  dim3 grid(tiles, chunks, nonroot);
+  dim3 grid(tiles * nonroot, chunks, 1);
   hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(c->d_tma, G, fp);
   CK(cudaGetLastError(), "flow_tma_kernel launch");
   ++c->launches;
@@ -604,7 +604,8 @@ int copy_out(hmf_ctx* c, const float* src, float* out, int where, void* stream) 
     CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(output)");
     int flag = 0;
     CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
-    if (flag & 2) return fail(c, HMF_ERR_CUDA, "a TMA wait in flow_tma_kernel timed out; results are invalid");
+    if (flag & 4) return fail(c, HMF_ERR_CUDA, "shared-memory staging area misaligned; results are invalid");
+    if (flag & 2) return fail(c, HMF_ERR_CUDA, "an asynchronous-copy wait timed out; results are invalid");
     if (flag & 1)
       return fail(c, HMF_ERR_INVALID_ARGUMENT,
                   "Data prior and smoothness must be non-negative (the solve ran on invalid input)");

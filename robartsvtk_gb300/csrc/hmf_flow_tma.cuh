@@ -13,10 +13,10 @@
 //    boundary go through shared memory.  z neighbours are carried in
 //    registers from plane to plane.
 //  * The six or seven input planes a step needs (three flow components, sink,
-//    label, parent sink, smoothness) arrive by cp.async.bulk.tensor into a
-//    three-slot shared-memory ring completed by mbarriers; plane k+2 is in
-//    flight while plane k is computed.  Every mbarrier wait is bounded: on
-//    time-out the kernel sets an error flag instead of hanging.
+//    label, parent sink, smoothness) arrive by cp.async.bulk.tensor into
+//    shared-memory rings completed by mbarriers, two planes ahead of the one
+//    being computed.  Every mbarrier wait is bounded: on time-out the kernel
+//    sets an error flag instead of hanging.
 //  * The stencil chain needs two halo columns/rows on the low side and up to
 //    two on the high side, so a window yields up to 28 x 27 outputs.
 #pragma once
@@ -31,13 +31,19 @@ namespace hmf {
 constexpr int kTmaBoxX = 36;   // box width: 16-byte aligned start plus 32 lanes plus 1
 constexpr int kTmaRows = 32;   // window rows
 constexpr int kTmaPlane = kTmaBoxX * kTmaRows;        // floats per staged array plane
-constexpr int kTmaArrays = 7;                          // px, py, pz, sink, label, inc, smooth
-constexpr int kTmaSlots = 3;
+// Two rings.  The z flow of plane k+1 is needed one step early (the divergence
+// of plane k), everything else only in its own step, so the main ring (px, py,
+// sink, label, parent sink, smoothness) has 3 slots and the pz ring 4: either
+// way two planes are in flight while one is computed.
+constexpr int kTmaMainArrays = 6;
+constexpr int kTmaMainSlots = 3;
+constexpr int kTmaPzSlots = 4;
 constexpr int kTmaMaxOutX = 28;
 constexpr int kTmaMaxOutY = 27;
 constexpr int kTmaThreads = 256;
 constexpr int kTmaSmemBytes =
-    1024 /* alignment slack */ + kTmaSlots * kTmaArrays * kTmaPlane * 4 + (3 * 256 + 2 * 256) * 4 + 64;
+                              (kTmaMainSlots * kTmaMainArrays + kTmaPzSlots) * kTmaPlane * 4 +
+                              (3 * 256 + 2 * 256) * 4 + 64;
 
 struct FlowVertexTMA {  // 64-byte aligned through its CUtensorMap members
   CUtensorMap flow_in[2][3];  // [parity][axis]: flows read in iterations of that parity
@@ -56,8 +62,13 @@ struct FlowTmaParams {
   int out_x;  // output columns per window (<= 28)
   int out_y;  // output rows per window (<= 27)
   int parity;
-  int pad_;
+  int n_vertices;  // non-root vertices (grid.x = n_vertices * tiles)
   int* error_flag;
+};
+
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
 };
 
 constexpr uint64_t kTmaWaitLimitNs = 500000000ull;  // 0.5 s: far beyond any healthy copy
@@ -68,6 +79,10 @@ constexpr uint64_t kTmaWaitLimitNs = 500000000ull;  // 0.5 s: far beyond any hea
 // sqrt(h) < lim, hence RN(sqrt(h)) <= lim and the result is exactly 1 without
 // evaluating the square root or the division.  Everything else (tiny lim,
 // NaN, infinities) takes the exact path.
+__device__ __forceinline__ bool projection_is_one(float h, float lim) {
+  return lim > 1.0e-18f && h < (lim * lim) * (1.0f - 0x1p-20f);
+}
+
 __device__ __forceinline__ float projection_multiplier(float h, float lim) {
   if (lim > 1.0e-18f && h < (lim * lim) * (1.0f - 0x1p-20f)) return 1.0f;
   const float F = sqrtf(h);
@@ -76,23 +91,30 @@ __device__ __forceinline__ float projection_multiplier(float h, float lim) {
 
 __global__ void __launch_bounds__(kTmaThreads, 2)
 flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, const FlowTmaParams fp) {
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  float* slots = reinterpret_cast<float*>(smem);                 // [3][7][32][36]
-  float* xg = slots + kTmaSlots * kTmaArrays * kTmaPlane;        // [8][32]  g(k), row 3 of each warp
+  // Pointers into the shared window are formed by pointer arithmetic only,
+  // so the compiler keeps them in the shared address space (32-bit LDS/STS).
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float* mslots = reinterpret_cast<float*>(smem_raw);            // [3][6][32][36]
+  float* zslots = mslots + kTmaMainSlots * kTmaMainArrays * kTmaPlane;  // [4][32][36]
+  float* xg = zslots + kTmaPzSlots * kTmaPlane;                   // [8][32]  g(k), row 3 of each warp
   float* xpy = xg + 256;                                          // [8][32]  p'_y(k-1), row 0
   float* xm = xpy + 256;                                          // [8][32]  m(k-1), row 3
   float* xP = xm + 256;                                           // [2][8][32] P_y(k-2), row 0
-  uint64_t* bars = reinterpret_cast<uint64_t*>(xP + 512);        // [3]
+  uint64_t* mbars = reinterpret_cast<uint64_t*>(xP + 512);       // [3]
+  uint64_t* zbars = mbars + kTmaMainSlots;                        // [4]
   __shared__ int abort_cta;
 
-  const FlowVertexTMA* V = vertices + blockIdx.z;
+  // blockIdx.x = vertex + n_vertices * tile: the vertices of one window run
+  // side by side, so a parent sink and a shared smoothness image read by
+  // several of them come from L2.
+  const int nv = fp.n_vertices;
+  const FlowVertexTMA* V = vertices + (blockIdx.x % nv);
+  const int tile = (int)(blockIdx.x / nv);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
   const int tiles_x = fp.tiles_x;
-  const int x0 = (int)(blockIdx.x % tiles_x) * fp.out_x;
-  const int y0 = (int)(blockIdx.x / tiles_x) * fp.out_y;
+  const int x0 = (tile % tiles_x) * fp.out_x;
+  const int y0 = (tile / tiles_x) * fp.out_y;
   const int xs = ((x0 + 2) / 4) * 4 - 4;  // x0 - 2 rounded down to a multiple of 4 (x0 >= 0)
   const int off = (x0 - 2) - xs;           // 0..3
   const int x = x0 - 2 + lane;
@@ -100,12 +122,13 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
   const int ze = min(zs + fp.zchunk, G.vz);
   const int kstart = max(zs - 2, 0);
   const int kend = ze + 1;
-  const int kload_end = min(ze + 2, G.vz - 1);
+  const int kmain_end = min(ze + 1, G.vz - 1);  // last plane whose g is computed
+  const int kpz_end = min(ze + 2, G.vz - 1);    // its divergence reads pz of the next plane
   const int par = fp.parity;
   const float step = fp.step, icc = fp.icc;
   // per-vertex values read once (the stores below could otherwise alias them)
   const bool has_s = V->has_smooth != 0;
-  const int narr = has_s ? 7 : 6;
+  const int narr = has_s ? 6 : 5;  // main-ring arrays
   const float alpha = V->alpha;
   float* const out_x = V->flow_out[par][0];
   float* const out_y = V->flow_out[par][1];
@@ -134,183 +157,237 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
   // configuration fails fast instead of slowly.
   if (threadIdx.x == 0) {
     abort_cta = fp.error_flag ? (*(volatile int*)fp.error_flag & 2) : 0;
-    for (int s = 0; s < kTmaSlots; ++s) mbar_init(&bars[s], 1);
+    // TMA destinations must be 128-byte aligned: refuse to run otherwise.
+    if (smem_addr(smem_raw) & 127) {
+      abort_cta = 1;
+      if (fp.error_flag) atomicOr(fp.error_flag, 4);
+    }
+    for (int s = 0; s < kTmaMainSlots; ++s) mbar_init(&mbars[s], 1);
+    for (int s = 0; s < kTmaPzSlots; ++s) mbar_init(&zbars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
   if (abort_cta) return;
 
-  auto slot_of = [&](int p) { return slots + ((p - kstart) % kTmaSlots) * (kTmaArrays * kTmaPlane); };
-  auto issue = [&](int p) {  // thread 0 only
-    uint64_t* bar = &bars[(p - kstart) % kTmaSlots];
-    float* dst = slot_of(p);
+  auto mslot = [&](int p) { return mslots + ((p - kstart) % kTmaMainSlots) * (kTmaMainArrays * kTmaPlane); };
+  auto zslot = [&](int p) { return zslots + ((p - kstart) % kTmaPzSlots) * kTmaPlane; };
+  auto issue_main = [&](int p) {  // thread 0 only
+    uint64_t* bar = &mbars[(p - kstart) % kTmaMainSlots];
+    float* dst = mslot(p);
     mbar_expect_tx(bar, (unsigned)(narr * kTmaPlane * 4));
     tma_load_plane(dst + 0 * kTmaPlane, &V->flow_in[par][0], xs, y0 - 2, p, bar);
     tma_load_plane(dst + 1 * kTmaPlane, &V->flow_in[par][1], xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 2 * kTmaPlane, &V->flow_in[par][2], xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 3 * kTmaPlane, &V->sink, xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 4 * kTmaPlane, &V->label, xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 5 * kTmaPlane, &V->inc, xs, y0 - 2, p, bar);
-    if (has_s) tma_load_plane(dst + 6 * kTmaPlane, &V->smooth, xs, y0 - 2, p, bar);
+    tma_load_plane(dst + 2 * kTmaPlane, &V->sink, xs, y0 - 2, p, bar);
+    tma_load_plane(dst + 3 * kTmaPlane, &V->label, xs, y0 - 2, p, bar);
+    tma_load_plane(dst + 4 * kTmaPlane, &V->inc, xs, y0 - 2, p, bar);
+    if (has_s) tma_load_plane(dst + 5 * kTmaPlane, &V->smooth, xs, y0 - 2, p, bar);
+  };
+  auto issue_pz = [&](int p) {  // thread 0 only
+    uint64_t* bar = &zbars[(p - kstart) % kTmaPzSlots];
+    mbar_expect_tx(bar, (unsigned)(kTmaPlane * 4));
+    tma_load_plane(zslot(p), &V->flow_in[par][2], xs, y0 - 2, p, bar);
   };
   bool timed_out = false;
-  auto wait_plane = [&](int p) {
+  auto wait_on = [&](uint64_t* bar, unsigned parity) {
     if (timed_out) return;  // results are void already; do not wait again
-    const unsigned parity = (unsigned)(((p - kstart) / kTmaSlots) & 1);
-    if (!mbar_wait_bounded(&bars[(p - kstart) % kTmaSlots], parity, kTmaWaitLimitNs)) timed_out = true;
+    if (!mbar_wait_bounded(bar, parity, kTmaWaitLimitNs)) timed_out = true;
+  };
+  auto wait_main = [&](int p) {
+    wait_on(&mbars[(p - kstart) % kTmaMainSlots], (unsigned)(((p - kstart) / kTmaMainSlots) & 1));
+  };
+  auto wait_pz = [&](int p) {
+    wait_on(&zbars[(p - kstart) % kTmaPzSlots], (unsigned)(((p - kstart) / kTmaPzSlots) & 1));
   };
 
   if (threadIdx.x == 0) {
-    if (kstart <= kload_end) issue(kstart);
-    if (kstart + 1 <= kload_end) issue(kstart + 1);
+    for (int p = kstart; p <= min(kstart + 1, kmain_end); ++p) issue_main(p);
+    for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
   }
 
-  // carries, one per row of this thread
-  float gprev[4], ppx[4], ppy[4], ppz[4], mprev[4], Px[4], Py[4], Pz[4], Sprev[4];
+  // A window whose 32 x 32 columns/rows all lie strictly inside the volume
+  // (not on its first or last column/row) needs none of the x / y boundary
+  // masks; it runs a copy of the march with those tests folded away.
+  const bool interior = x0 - 2 >= 1 && x0 + 29 <= G.vx - 2 && y0 - 2 >= 1 && y0 + 29 <= G.vy - 2;
+
+  auto march = [&](auto tag) {
+    constexpr bool INT = decltype(tag)::value;
+    // carries, one per row of this thread
+    float gprev[4], ppx[4], ppy[4], ppz[4], mprev[4], Px[4], Py[4], Pz[4], Sprev[4], pzn_c[4];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    gprev[r] = ppx[r] = ppy[r] = ppz[r] = mprev[r] = Px[r] = Py[r] = Pz[r] = Sprev[r] = 0.f;
-  }
+    for (int r = 0; r < 4; ++r) {
+      gprev[r] = ppx[r] = ppy[r] = ppz[r] = mprev[r] = Px[r] = Py[r] = Pz[r] = Sprev[r] = pzn_c[r] = 0.f;
+    }
+    bool have_pz = false;  // pzn_c holds pz of plane k (loaded in step k-1)
 
-  for (int k = kstart; k <= kend; ++k) {
-    const bool doA = k <= min(ze + 1, G.vz - 1);                     // g(k), p'(k)
-    const int kc = k - 1;
-    const bool doC = kc >= max(zs - 1, 0) && kc <= min(ze, G.vz - 1);  // m(k-1), P(k-1)
-    const int ko = k - 2;
-    const bool doE = ko >= zs && ko < ze;                              // div(k-2), output
+    for (int k = kstart; k <= kend; ++k) {
+      const bool doA = k <= kmain_end;                                   // g(k), p'(k)
+      const int kc = k - 1;
+      const bool doC = kc >= max(zs - 1, 0) && kc <= min(ze, G.vz - 1);  // m(k-1), P(k-1)
+      const int ko = k - 2;
+      const bool doE = ko >= zs && ko < ze;                              // div(k-2), output
 
-    // ---- stage A: g(k) from the staged inputs (kern_CalcGradStep on the
-    // divergence kern_Divergence left, recomputed from the stored flows)
-    float g[4], rx[4], ry_[4], rz[4], Scur[4];
-    if (doA) {
-      wait_plane(k);
-      const bool has_next = k + 1 < G.vz;
-      if (has_next) wait_plane(k + 1);
-      const float* cur = slot_of(k);
-      const float* nxt = has_next ? slot_of(k + 1) : cur;
+      // ---- stage A: g(k) from the staged inputs (kern_CalcGradStep on the
+      // divergence kern_Divergence left, recomputed from the stored flows)
+      float g[4], rx[4], ry_[4], rz[4], Scur[4];
+      if (doA) {
+        wait_main(k);
+        const bool has_next = k + 1 < G.vz;
+        if (!have_pz) wait_pz(k);
+        if (has_next) wait_pz(k + 1);
+        const float* cur = mslot(k);
+        const float* zc = zslot(k);
+        const float* zn = has_next ? zslot(k + 1) : zc;
+        float pyv[5];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) pyv[r] = cur[kTmaPlane + (warp * 4 + r) * kTmaBoxX + off + lane];
+        pyv[4] = warp < 7 ? cur[kTmaPlane + (warp * 4 + 4) * kTmaBoxX + off + lane] : 0.f;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int i = (warp * 4 + r) * kTmaBoxX + off + lane;
+          const float px = cur[i], py = pyv[r];
+          const float pz = have_pz ? pzn_c[r] : zc[i];
+          const float pxr = cur[i + 1];
+          const float pyd = pyv[r + 1];
+          const float pzn = zn[i];
+          const float sk = cur[2 * kTmaPlane + i], u = cur[3 * kTmaPlane + i], c = cur[4 * kTmaPlane + i];
+          Scur[r] = has_s ? cur[5 * kTmaPlane + i] : 0.f;
+          float d = (px + py) + pz;
+          if (INT || xnl) d = d - pxr;
+          if (INT || ynl[r]) d = d - pyd;
+          if (has_next) d = d - pzn;
+          const float gv = step * (((sk + d) - c) - u * icc);
+          g[r] = (INT || rin[r]) ? gv : 0.f;
+          rx[r] = px;
+          ry_[r] = py;
+          rz[r] = pz;
+          pzn_c[r] = pzn;
+        }
+        have_pz = has_next;
+      } else {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) g[r] = rx[r] = ry_[r] = rz[r] = Scur[r] = 0.f;
+      }
+      xg[warp * 32 + lane] = g[3];
+      xpy[warp * 32 + lane] = ppy[0];
+      xP[((k & 1) * 8 + warp) * 32 + lane] = Py[0];
+      __syncthreads();  // (1)
+      if (threadIdx.x == 0) {
+        if (k + 2 <= kmain_end) issue_main(k + 2);
+        if (k + 3 <= kpz_end) issue_pz(k + 3);
+      }
+
+      // ---- stage B: p'(k) (kern_DescentSpatialFlow)
+      float npx[4], npy[4], npz[4];
+      const float gup = warp ? xg[(warp - 1) * 32 + lane] : 0.f;
+      const bool zpos = k > 0;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const int row = warp * 4 + r;
-        const int i = row * kTmaBoxX + off + lane;
-        const float px = cur[i], py = cur[kTmaPlane + i], pz = cur[2 * kTmaPlane + i];
-        const float pxr = cur[i + 1];
-        const float pyd = row < kTmaRows - 1 ? cur[kTmaPlane + i + kTmaBoxX] : 0.f;
-        const float pzn = nxt[2 * kTmaPlane + i];
-        const float sk = cur[3 * kTmaPlane + i], u = cur[4 * kTmaPlane + i], c = cur[5 * kTmaPlane + i];
-        Scur[r] = has_s ? cur[6 * kTmaPlane + i] : 0.f;
-        float d = (px + py) + pz;
-        if (xnl) d = d - pxr;
-        if (ynl[r]) d = d - pyd;
-        if (has_next) d = d - pzn;
-        g[r] = rin[r] ? step * (((sk + d) - c) - u * icc) : 0.f;
-        rx[r] = px;
-        ry_[r] = py;
-        rz[r] = pz;
+        const float gxm = __shfl_up_sync(FULL, g[r], 1);
+        const float gym = r ? g[r > 0 ? r - 1 : 0] : gup;
+        const bool in = doA && (INT || rin[r]);
+        npx[r] = (in && (INT || xpos)) ? rx[r] - (g[r] - gxm) : 0.f;
+        npy[r] = (in && (INT || ypos[r])) ? ry_[r] - (g[r] - gym) : 0.f;
+        npz[r] = (in && zpos) ? rz[r] - (g[r] - gprev[r]) : 0.f;
+        gprev[r] = g[r];
       }
-    } else {
-#pragma unroll
-      for (int r = 0; r < 4; ++r) g[r] = rx[r] = ry_[r] = rz[r] = Scur[r] = 0.f;
-    }
-    xg[warp * 32 + lane] = g[3];
-    xpy[warp * 32 + lane] = ppy[0];
-    xP[((k & 1) * 8 + warp) * 32 + lane] = Py[0];
-    __syncthreads();  // (1)
-    if (threadIdx.x == 0 && k + 2 <= kload_end) issue(k + 2);
 
-    // ---- stage B: p'(k) (kern_DescentSpatialFlow)
-    float npx[4], npy[4], npz[4];
-    const float gup = warp ? xg[(warp - 1) * 32 + lane] : 0.f;
+      // ---- stage C: m(k-1) (kern_ComputeFlowMag*).  |p|^2 of the four rows
+      // is computed without branches so that their chains interleave; the
+      // exact square root and division run only for rows whose |p| is near or
+      // above its bound (projection_multiplier's test).
+      float m[4], h[4], lim[4];
+      bool slow[4];
+      const float pdown = warp < 7 ? xpy[(warp + 1) * 32 + lane] : 0.f;
+      const bool znl = kc != G.vz - 1;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float gxm = __shfl_up_sync(FULL, g[r], 1);
-      const float gym = r ? g[r > 0 ? r - 1 : 0] : gup;
-      const bool in = doA && rin[r];
-      npx[r] = (in && xpos) ? rx[r] - (g[r] - gxm) : 0.f;
-      npy[r] = (in && ypos[r]) ? ry_[r] - (g[r] - gym) : 0.f;
-      npz[r] = (in && k > 0) ? rz[r] - (g[r] - gprev[r]) : 0.f;
-      gprev[r] = g[r];
-    }
-
-    // ---- stage C: m(k-1) (kern_ComputeFlowMag*)
-    float m[4];
-    const float pdown = warp < 7 ? xpy[(warp + 1) * 32 + lane] : 0.f;
-    const bool znl = kc != G.vz - 1;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float pxr = __shfl_down_sync(FULL, ppx[r], 1);
-      const float pyd = r < 3 ? ppy[r < 3 ? r + 1 : 3] : pdown;
-      float mv = 1.0f;
-      if (doC && rin[r]) {
+      for (int r = 0; r < 4; ++r) {
+        const float pxr = __shfl_down_sync(FULL, ppx[r], 1);
+        const float pyd = r < 3 ? ppy[r < 3 ? r + 1 : 3] : pdown;
         float up = ppx[r] * ppx[r];
-        float dn = xnl ? pxr * pxr : 0.f;
+        float dn = (INT || xnl) ? pxr * pxr : 0.f;
         float F = up + dn;
         up = ppy[r] * ppy[r];
-        dn = ynl[r] ? pyd * pyd : 0.f;
+        dn = (INT || ynl[r]) ? pyd * pyd : 0.f;
         F = F + (up + dn);
         up = ppz[r] * ppz[r];
         dn = znl ? npz[r] * npz[r] : 0.f;
         F = F + (up + dn);
-        mv = projection_multiplier(0.5f * F, has_s ? alpha * Sprev[r] : alpha);
+        h[r] = 0.5f * F;
+        lim[r] = has_s ? alpha * Sprev[r] : alpha;
+        slow[r] = doC && (INT || rin[r]) && !projection_is_one(h[r], lim[r]);
+        m[r] = 1.0f;
+        Sprev[r] = Scur[r];
       }
-      m[r] = mv;
-      Sprev[r] = Scur[r];
-    }
-    xm[warp * 32 + lane] = m[3];
-    __syncthreads();  // (2)
-
-    // ---- stage D: P(k-1) (kern_Project)
-    float nPx[4], nPy[4], nPz[4];
-    const float mup = warp ? xm[(warp - 1) * 32 + lane] : 0.f;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float mxm = __shfl_up_sync(FULL, m[r], 1);
-      const float mym = r ? m[r > 0 ? r - 1 : 0] : mup;
-      const bool in = doC && rin[r];
-      nPx[r] = (in && xpos) ? (ppx[r] * 0.5f) * (m[r] + mxm) : 0.f;
-      nPy[r] = (in && ypos[r]) ? (ppy[r] * 0.5f) * (m[r] + mym) : 0.f;
-      nPz[r] = (in && kc > 0) ? (ppz[r] * 0.5f) * (m[r] + mprev[r]) : 0.f;
-      if (doC) mprev[r] = m[r];
-    }
+      for (int r = 0; r < 4; ++r) {
+        if (slow[r]) {
+          const float Fs = sqrtf(h[r]);
+          if (Fs > lim[r]) m[r] = lim[r] / Fs;
+        }
+      }
+      xm[warp * 32 + lane] = m[3];
+      __syncthreads();  // (2)
 
-    // ---- stage E: divergence of P(k-2) (kern_Divergence), store P(k-2) and div(k-2)
-    const float Pdown = warp < 7 ? xP[((k & 1) * 8 + warp + 1) * 32 + lane] : 0.f;
-    const bool zonl = ko != G.vz - 1;
-    const long long zoff = (long long)ko * G.plane;
+      // ---- stage D: P(k-1) (kern_Project)
+      float nPx[4], nPy[4], nPz[4];
+      const float mup = warp ? xm[(warp - 1) * 32 + lane] : 0.f;
+      const bool kcpos = kc > 0;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float Pxr = __shfl_down_sync(FULL, Px[r], 1);
-      const float Pyd = r < 3 ? Py[r < 3 ? r + 1 : 3] : Pdown;
-      if (doE && rout[r]) {
+      for (int r = 0; r < 4; ++r) {
+        const float mxm = __shfl_up_sync(FULL, m[r], 1);
+        const float mym = r ? m[r > 0 ? r - 1 : 0] : mup;
+        const bool in = doC && (INT || rin[r]);
+        nPx[r] = (in && (INT || xpos)) ? (ppx[r] * 0.5f) * (m[r] + mxm) : 0.f;
+        nPy[r] = (in && (INT || ypos[r])) ? (ppy[r] * 0.5f) * (m[r] + mym) : 0.f;
+        nPz[r] = (in && kcpos) ? (ppz[r] * 0.5f) * (m[r] + mprev[r]) : 0.f;
+        if (doC) mprev[r] = m[r];
+      }
+
+      // ---- stage E: divergence of P(k-2) (kern_Divergence), store P(k-2) and div(k-2)
+      const float Pdown = warp < 7 ? xP[((k & 1) * 8 + warp + 1) * 32 + lane] : 0.f;
+      const bool zonl = ko != G.vz - 1;
+      const long long zoff = (long long)ko * G.plane;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float Pxr = __shfl_down_sync(FULL, Px[r], 1);
+        const float Pyd = r < 3 ? Py[r < 3 ? r + 1 : 3] : Pdown;
         float dv = (Px[r] + Py[r]) + Pz[r];
-        if (xnl) dv = dv - Pxr;
-        if (ynl[r]) dv = dv - Pyd;
+        if (INT || xnl) dv = dv - Pxr;
+        if (INT || ynl[r]) dv = dv - Pyd;
         if (zonl) dv = dv - nPz[r];
-        const long long o = zoff + rowoff[r];
-        out_x[o] = Px[r];
-        out_y[o] = Py[r];
-        out_z[o] = Pz[r];
-        out_d[o] = dv;
+        if (doE && rout[r]) {
+          const long long o = zoff + rowoff[r];
+          out_x[o] = Px[r];
+          out_y[o] = Py[r];
+          out_z[o] = Pz[r];
+          out_d[o] = dv;
+        }
+      }
+
+      // ---- rotate carries
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        ppx[r] = npx[r];
+        ppy[r] = npy[r];
+        ppz[r] = npz[r];
+        Px[r] = nPx[r];
+        Py[r] = nPy[r];
+        Pz[r] = nPz[r];
       }
     }
-
-    // ---- rotate carries
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      ppx[r] = npx[r];
-      ppy[r] = npy[r];
-      ppz[r] = npz[r];
-      Px[r] = nPx[r];
-      Py[r] = nPy[r];
-      Pz[r] = nPz[r];
-    }
-  }
+  };
+  if (interior) march(BoolTag<true>{});
+  else march(BoolTag<false>{});
   if (timed_out) {
     if (fp.error_flag) atomicOr(fp.error_flag, 2);
     // Let copies still in flight into this CTA's shared memory land (bounded)
     // before the CTA exits: the last plane issued into each slot.
-    for (int p = max(kstart, kload_end - kTmaSlots + 1); p <= kload_end; ++p)
-      mbar_wait_bounded(&bars[(p - kstart) % kTmaSlots], (unsigned)(((p - kstart) / kTmaSlots) & 1),
+    for (int p = max(kstart, kmain_end - kTmaMainSlots + 1); p <= kmain_end; ++p)
+      mbar_wait_bounded(&mbars[(p - kstart) % kTmaMainSlots],
+                        (unsigned)(((p - kstart) / kTmaMainSlots) & 1), kTmaWaitLimitNs);
+    for (int p = max(kstart, kpz_end - kTmaPzSlots + 1); p <= kpz_end; ++p)
+      mbar_wait_bounded(&zbars[(p - kstart) % kTmaPzSlots], (unsigned)(((p - kstart) / kTmaPzSlots) & 1),
                         kTmaWaitLimitNs);
   }
 }

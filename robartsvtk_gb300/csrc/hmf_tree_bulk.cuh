@@ -38,16 +38,19 @@ __host__ __device__ inline int tree_bulk_smem_bytes(int n) {
 __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag) {
   __shared__ TreeTable T;
   __shared__ int abort_cta;
-  extern __shared__ unsigned char tb_raw[];
-  unsigned char* base = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(tb_raw) + 127) & ~static_cast<uintptr_t>(127));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base);  // [2]
-  float* stage0 = reinterpret_cast<float*>(base + 128);
+  extern __shared__ __align__(128) unsigned char tb_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tb_raw);  // [2]
+  float* stage0 = reinterpret_cast<float*>(tb_raw + 128);
 
   for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
   if (threadIdx.x == 0) {
     abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    // bulk-copy destinations must be 16-byte aligned: refuse to run otherwise.
+    if (smem_addr(tb_raw) & 15) {
+      abort_cta = 1;
+      if (error_flag) atomicOr(error_flag, 4);
+    }
     for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
