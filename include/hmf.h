@@ -120,6 +120,28 @@ size_t hmf_device_bytes(const hmf_ctx* ctx);
 int hmf_set_timing(hmf_ctx* ctx, int enabled);
 int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kind, int n_kinds);
 
+/* ---- Batches --------------------------------------------------------------
+ * No counterpart in the reference, which solves one volume per filter
+ * update: many volumes of different sizes that share one label tree, one set
+ * of smoothness weights and one set of parameters are solved together, every
+ * iteration in the same two kernel launches (captured in a CUDA graph), so
+ * small volumes do not leave the GPU idle.  dims holds n_volumes triples
+ * (VX, VY, VZ).  The single-volume calls above act on volume 0. */
+int hmf_create_batch(hmf_ctx** out, int n_volumes, const int* dims, const int* parent, int n_nodes,
+                     int semantics, int device);
+int hmf_num_volumes(const hmf_ctx* ctx);
+int hmf_batch_set_data(hmf_ctx* ctx, int volume, int node, const float* data, int where);
+int hmf_batch_set_smoothness(hmf_ctx* ctx, int volume, int node, const float* smooth, int where);
+int hmf_batch_get_labels(hmf_ctx* ctx, int volume, int node, float* out, int where, void* stream);
+int hmf_batch_get_sink(hmf_ctx* ctx, int volume, int node, float* out, int where, void* stream);
+
+/* Autotuner (no counterpart in the reference): times a few iterations of the
+ * flow kernel for each candidate z-chunk length (planes per CTA column) on the
+ * context's current inputs, keeps the fastest for this context and caches it
+ * for contexts of the same shape (volume sizes, tree size, device) created
+ * later in the process.  Inputs must be set; the labels are not kept. */
+int hmf_autotune(hmf_ctx* ctx, void* stream);
+
 /* Message of the last failed call on ctx (or, when ctx is NULL, of the last
  * failed hmf_create or hmf_solve_noalloc on this thread). */
 const char* hmf_last_error(const hmf_ctx* ctx);

@@ -5,7 +5,7 @@ vtkCudaHierarchicalMaxFlowSegmentation path.
 The compute is libhmf_gb300.so (CUDA kernels + C ABI, include/hmf.h); this
 package binds it and mirrors the reference's filter API.
 """
-from .segmentation import (REF_CPU, REF_CUDA, HierarchicalMaxFlowSegmentation, HMFError,  # noqa: F401
-                           HMFSolver)
+from .segmentation import (REF_CPU, REF_CUDA, HierarchicalMaxFlowSegmentation, HMFBatchSolver,  # noqa: F401
+                           HMFError, HMFSolver)
 
-__all__ = ["HMFSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]
+__all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]

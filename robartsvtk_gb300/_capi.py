@@ -44,6 +44,13 @@ SIGNATURES = [
     ("hmf_set_timing", _I, [_P, _I]),
     ("hmf_get_stats", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_last_error", ctypes.c_char_p, [_P]),
+    ("hmf_create_batch", _I, [ctypes.POINTER(_P), _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _I, _I, _I]),
+    ("hmf_num_volumes", _I, [_P]),
+    ("hmf_batch_set_data", _I, [_P, _I, _I, _P, _I]),
+    ("hmf_batch_set_smoothness", _I, [_P, _I, _I, _P, _I]),
+    ("hmf_batch_get_labels", _I, [_P, _I, _I, _P, _I, _P]),
+    ("hmf_batch_get_sink", _I, [_P, _I, _I, _P, _I, _P]),
+    ("hmf_autotune", _I, [_P, _P]),
     ("hmf_solve_noalloc", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                ctypes.POINTER(ctypes.c_double), _I, ctypes.c_float, ctypes.c_float,
                                ctypes.POINTER(_P), _P]),

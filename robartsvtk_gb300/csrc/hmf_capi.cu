@@ -9,9 +9,18 @@
 // The reference pages buffers between host and device when the GPU is short
 // of memory; here the whole state is resident (it fits in HBM for every
 // workload this library targets) and allocated once per context.
+//
+// A context holds one or more volumes (a batch) of possibly different sizes
+// that share one label tree and one set of parameters.  Every per-vertex array
+// is one allocation holding the volumes back to back, each volume a pitched
+// block; the per-voxel kernels (initialisation, tree sweep) run once over the
+// whole concatenation and the flow kernel over a table of (volume, window)
+// work items, so a batch costs the same two launches per iteration as a
+// single volume.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
@@ -38,8 +47,16 @@ constexpr int kTreeThreads = 256;
 struct hmf_ctx {
   int device = 0;
   int semantics = HMF_SEMANTICS_REF_CUDA;
-  hmf::Geometry geo{};
   int sm_count = 0;
+
+  // volumes, back to back in every per-vertex array
+  struct Volume {
+    int vx, vy, vz, pitch;
+    long long plane, vol, off;  // elements: plane, whole block, offset of the block
+  };
+  std::vector<Volume> vols;
+  long long total = 0;
+  hmf::Geometry geo{};  // per-voxel view of the concatenation (pitch 0 for batches)
 
   // tree
   int n = 0, root = -1;
@@ -57,7 +74,7 @@ struct hmf_ctx {
     const float* ptr = nullptr;
     int where = HMF_HOST;
   };
-  std::vector<Input> data, smooth;
+  std::vector<std::vector<Input>> data, smooth;  // [volume][vertex]
 
   // device state
   char* arena = nullptr;
@@ -67,11 +84,15 @@ struct hmf_ctx {
   // input staging
   char* staging = nullptr;
   size_t staging_bytes = 0;
-  hmf::FlowVertex* d_flow[2] = {nullptr, nullptr};
-  hmf::FlowVertexTMA* d_tma = nullptr;  // TMA-fed flow kernel table (both parities)
+  hmf::FlowVertex* d_flow[2] = {nullptr, nullptr};  // shared-memory ring flow kernel (one volume)
+  hmf::FlowVertexTMA* d_tma = nullptr;              // TMA flow kernel, [volume][non-root vertex]
+  hmf::FlowVolume* d_fvol = nullptr;
+  hmf::FlowItem* d_items = nullptr;
+  int n_items = 0;
+  int zchunk = 0;  // planes per window column (0: not planned yet)
   hmf::TreeTable* d_tree = nullptr;
-  bool use_tma = true;    // flow_tma_kernel (else the shared-memory ring flow_kernel)
-  int tree_kind = 0;      // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
+  bool use_tma = true;  // flow_tma_kernel (else the shared-memory ring flow_kernel)
+  int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
   const float** d_smooth_list = nullptr;
   int* d_error = nullptr;
   int n_smooth_list = 0;
@@ -92,6 +113,8 @@ struct hmf_ctx {
   // cudaMemcpyAsync stages them before returning)
   std::vector<hmf::FlowVertex> h_flow;
   std::vector<hmf::FlowVertexTMA> h_tma;
+  std::vector<hmf::FlowVolume> h_fvol;
+  std::vector<hmf::FlowItem> h_items;
   hmf::TreeTable h_tree{};
   std::vector<const float*> h_smooth_list;
 
@@ -181,10 +204,12 @@ int build_tree(hmf_ctx* c, const int* par, int n) {
 }
 
 // Device memory plan: per non-root vertex 9 arrays (sink, label, div, two
-// sets of three flow components), the root's source flow.
+// sets of three flow components), the root's source flow; every array holds
+// all volumes.
 int allocate_state(hmf_ctx* c) {
-  const size_t arr = round_up((size_t)c->geo.vol * sizeof(float), 256);
+  const size_t arr = round_up((size_t)c->total * sizeof(float), 256);
   const int nonroot = c->n - 1;
+  const int nvol = (int)c->vols.size();
   c->arena_bytes = arr * (size_t)(9 * nonroot + 1) + 4096;
   CK(cudaMalloc(&c->arena, c->arena_bytes), "cudaMalloc(state)");
   CK(cudaMemset(c->arena, 0, c->arena_bytes), "cudaMemset(state)");
@@ -215,12 +240,70 @@ int allocate_state(hmf_ctx* c) {
   }
   CK(cudaMalloc(&c->d_flow[0], sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2), "cudaMalloc(tables)");
   c->d_flow[1] = c->d_flow[0] + hmf::kMaxVertices;
-  CK(cudaMalloc(&c->d_tma, sizeof(hmf::FlowVertexTMA) * hmf::kMaxVertices), "cudaMalloc(tma table)");
+  CK(cudaMalloc(&c->d_tma, sizeof(hmf::FlowVertexTMA) * (size_t)nvol * nonroot), "cudaMalloc(tma table)");
+  CK(cudaMalloc(&c->d_fvol, sizeof(hmf::FlowVolume) * nvol), "cudaMalloc(volume table)");
   CK(cudaMalloc(&c->d_tree, sizeof(hmf::TreeTable)), "cudaMalloc(tree table)");
   CK(cudaMalloc(&c->d_smooth_list, sizeof(float*) * hmf::kMaxVertices), "cudaMalloc(smooth list)");
   CK(cudaMalloc(&c->d_error, sizeof(int)), "cudaMalloc(error flag)");
   CK(cudaMemset(c->d_error, 0, sizeof(int)), "cudaMemset(error flag)");
   return HMF_OK;
+}
+
+// Flow-kernel work plan for a given z-chunk length: windows of at most 28 x 27
+// outputs spread evenly over each volume, z split into chunks of `zchunk`
+// planes.  Items enumerate volume, then z chunk, then window, so that windows
+// that share halos run side by side.
+int plan_flow(hmf_ctx* c, int zchunk) {
+  c->h_fvol.assign(c->vols.size(), hmf::FlowVolume{});
+  c->h_items.clear();
+  for (size_t b = 0; b < c->vols.size(); ++b) {
+    const auto& V = c->vols[b];
+    hmf::FlowVolume& F = c->h_fvol[b];
+    F.G.vx = V.vx;
+    F.G.vy = V.vy;
+    F.G.vz = V.vz;
+    F.G.pitch = V.pitch;
+    F.G.plane = V.plane;
+    F.G.vol = V.vol;
+    const int nx = (V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX;
+    const int ny = (V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY;
+    F.out_x = (V.vx + nx - 1) / nx;
+    F.out_y = (V.vy + ny - 1) / ny;
+    F.tiles_x = nx;
+    F.zchunk = std::min(zchunk, V.vz);
+    const int chunks = (V.vz + F.zchunk - 1) / F.zchunk;
+    for (int zc = 0; zc < chunks; ++zc)
+      for (int t = 0; t < nx * ny; ++t) c->h_items.push_back(hmf::FlowItem{(int)b, t, zc, 0});
+  }
+  c->n_items = (int)c->h_items.size();
+  c->zchunk = zchunk;
+  if (c->d_items) cudaFree(c->d_items);
+  c->d_items = nullptr;
+  CK(cudaMalloc(&c->d_items, sizeof(hmf::FlowItem) * c->h_items.size()), "cudaMalloc(work items)");
+  CK(cudaMemcpy(c->d_items, c->h_items.data(), sizeof(hmf::FlowItem) * c->h_items.size(), cudaMemcpyHostToDevice),
+     "cudaMemcpy(work items)");
+  CK(cudaMemcpy(c->d_fvol, c->h_fvol.data(), sizeof(hmf::FlowVolume) * c->h_fvol.size(), cudaMemcpyHostToDevice),
+     "cudaMemcpy(volume table)");
+  return HMF_OK;
+}
+
+// Default z chunk: the longest power of two (>= 16 planes) that still gives
+// the launch a few waves of two CTAs per SM.
+int default_zchunk(const hmf_ctx* c) {
+  const long long target = (long long)c->sm_count * 2 * 3;
+  int maxz = 1;
+  for (const auto& V : c->vols) maxz = std::max(maxz, V.vz);
+  int z = 16;
+  while (z < maxz) z *= 2;
+  for (;; z /= 2) {
+    long long ctas = 0;
+    for (const auto& V : c->vols) {
+      const long long tiles = (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
+                              ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY);
+      ctas += tiles * ((V.vz + std::min(z, V.vz) - 1) / std::min(z, V.vz)) * (c->n - 1);
+    }
+    if (ctas >= target || z <= 16) return z;
+  }
 }
 
 // cuTensorMapEncodeTiled, fetched through the runtime so that the library
@@ -243,13 +326,12 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 3-D map of one pitched volume, box = one 36 x 32 window plane.
-int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base) {
+// 3-D map of one pitched volume block, box = one 36 x 32 window plane.
+int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return fail(c, HMF_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
-  const auto& G = c->geo;
-  const cuuint64_t dims[3] = {(cuuint64_t)G.vx, (cuuint64_t)G.vy, (cuuint64_t)G.vz};
-  const cuuint64_t strides[2] = {(cuuint64_t)G.pitch * 4, (cuuint64_t)G.plane * 4};
+  const cuuint64_t dims[3] = {(cuuint64_t)V.vx, (cuuint64_t)V.vy, (cuuint64_t)V.vz};
+  const cuuint64_t strides[2] = {(cuuint64_t)V.pitch * 4, (cuuint64_t)V.plane * 4};
   const cuuint32_t box[3] = {(cuuint32_t)hmf::kTmaBoxX, (cuuint32_t)hmf::kTmaRows, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
@@ -259,31 +341,49 @@ int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base) {
   return HMF_OK;
 }
 
-// Copies (or borrows) the inputs into pitched device arrays.  Returns the
-// device pointer of each leaf's data term and each vertex's smoothness image.
-int stage_inputs(hmf_ctx* c, cudaStream_t s, std::vector<const float*>& d_data,
-                 std::vector<const float*>& d_smooth, std::vector<const float*>& distinct_smooth) {
-  const auto& G = c->geo;
-  const size_t arr = round_up((size_t)G.vol * sizeof(float), 256);
-  // which inputs need a device copy
-  std::map<std::pair<const float*, int>, int> smooth_slot;  // distinct smoothness images
-  std::vector<std::pair<const float*, int>> smooth_keys;
+// Inputs as device arrays over the concatenation: the data term of each leaf
+// and one smoothness array per group of vertices that use the same image in
+// every volume.  A single dense, 16-byte aligned device input is used in
+// place; everything else is copied into pitched staging blocks.
+struct Staged {
+  std::vector<const float*> data;        // [vertex], leaves only
+  std::vector<const float*> smooth;      // [vertex], base of its smoothness group (or null)
+  std::vector<const float*> distinct;    // bases of the smoothness groups
+};
+
+int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out) {
+  const size_t arr = round_up((size_t)c->total * sizeof(float), 256);
+  const int nvol = (int)c->vols.size();
+  // smoothness groups: vertices whose (pointer, where) agree in every volume
+  std::map<std::vector<std::pair<const float*, int>>, int> group_of_key;
+  std::vector<std::vector<std::pair<const float*, int>>> groups;
+  std::vector<int> group(c->n, -1);
   for (int v = 0; v < c->n; ++v) {
-    if (v == c->root || !c->smooth[v].ptr) continue;
-    auto key = std::make_pair(c->smooth[v].ptr, c->smooth[v].where);
-    if (!smooth_slot.count(key)) {
-      smooth_slot[key] = (int)smooth_keys.size();
-      smooth_keys.push_back(key);
+    if (v == c->root) continue;
+    std::vector<std::pair<const float*, int>> key;
+    bool any = false;
+    for (int b = 0; b < nvol; ++b) {
+      key.push_back({c->smooth[b][v].ptr, c->smooth[b][v].ptr ? c->smooth[b][v].where : 0});
+      any = any || c->smooth[b][v].ptr;
     }
+    if (!any) continue;
+    auto it = group_of_key.find(key);
+    if (it == group_of_key.end()) {
+      it = group_of_key.emplace(key, (int)groups.size()).first;
+      groups.push_back(key);
+    }
+    group[v] = it->second;
   }
+  const bool single = nvol == 1;
+  const auto& V0 = c->vols[0];
   auto borrowable = [&](const float* p, int where) {
-    return where == HMF_DEVICE && G.pitch == G.vx && (reinterpret_cast<uintptr_t>(p) % 16) == 0;
+    return single && where == HMF_DEVICE && V0.pitch == V0.vx && (reinterpret_cast<uintptr_t>(p) % 16) == 0;
   };
   size_t need = 0;
   for (int l : c->leaves)
-    if (!borrowable(c->data[l].ptr, c->data[l].where)) need += arr;
-  for (auto& k : smooth_keys)
-    if (!borrowable(k.first, k.second)) need += arr;
+    if (!borrowable(c->data[0][l].ptr, c->data[0][l].where)) need += arr;
+  for (auto& g : groups)
+    if (!borrowable(g[0].first, g[0].second)) need += arr;
   if (need > c->staging_bytes) {
     if (c->staging) cudaFree(c->staging);
     c->staging = nullptr;
@@ -293,64 +393,54 @@ int stage_inputs(hmf_ctx* c, cudaStream_t s, std::vector<const float*>& d_data,
     c->staging_bytes = need;
   }
   char* p = c->staging;
-  auto stage = [&](const float* src, int where, const float** out) -> int {
-    if (borrowable(src, where)) {
-      *out = src;
+  // one array over the concatenation from per-volume sources (null: left as is)
+  auto stage = [&](const std::vector<std::pair<const float*, int>>& src, const float** res) -> int {
+    if (borrowable(src[0].first, src[0].second)) {
+      *res = src[0].first;
       return HMF_OK;
     }
     float* dst = reinterpret_cast<float*>(p);
     p += arr;
-    const cudaMemcpyKind kind = where == HMF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-    CK(cudaMemcpy2DAsync(dst, (size_t)G.pitch * sizeof(float), src, (size_t)G.vx * sizeof(float),
-                         (size_t)G.vx * sizeof(float), (size_t)G.vy * G.vz, kind, s),
-       "cudaMemcpy2DAsync(input)");
-    *out = dst;
+    for (int b = 0; b < nvol; ++b) {
+      if (!src[b].first) continue;
+      const auto& V = c->vols[b];
+      const cudaMemcpyKind kind = src[b].second == HMF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+      CK(cudaMemcpy2DAsync(dst + V.off, (size_t)V.pitch * sizeof(float), src[b].first, (size_t)V.vx * sizeof(float),
+                           (size_t)V.vx * sizeof(float), (size_t)V.vy * V.vz, kind, s),
+         "cudaMemcpy2DAsync(input)");
+    }
+    *res = dst;
     return HMF_OK;
   };
-  d_data.assign(c->n, nullptr);
-  d_smooth.assign(c->n, nullptr);
+  out.data.assign(c->n, nullptr);
+  out.smooth.assign(c->n, nullptr);
   for (int l : c->leaves) {
-    int rc = stage(c->data[l].ptr, c->data[l].where, &d_data[l]);
+    std::vector<std::pair<const float*, int>> src;
+    for (int b = 0; b < nvol; ++b) src.push_back({c->data[b][l].ptr, c->data[b][l].where});
+    int rc = stage(src, &out.data[l]);
     if (rc) return rc;
   }
-  distinct_smooth.assign(smooth_keys.size(), nullptr);
-  for (size_t k = 0; k < smooth_keys.size(); ++k) {
-    int rc = stage(smooth_keys[k].first, smooth_keys[k].second, &distinct_smooth[k]);
+  out.distinct.assign(groups.size(), nullptr);
+  for (size_t g = 0; g < groups.size(); ++g) {
+    int rc = stage(groups[g], &out.distinct[g]);
     if (rc) return rc;
   }
-  for (int v = 0; v < c->n; ++v) {
-    if (v == c->root || !c->smooth[v].ptr) continue;
-    d_smooth[v] = distinct_smooth[smooth_slot[{c->smooth[v].ptr, c->smooth[v].where}]];
-  }
+  for (int v = 0; v < c->n; ++v)
+    if (group[v] >= 0) out.smooth[v] = out.distinct[group[v]];
   return HMF_OK;
 }
 
 int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
-  const auto& G = c->geo;
   hmf::FlowTmaParams fp;
   fp.step = c->step;
   fp.icc = 1.0f / c->cc;
-  // window outputs: at most 28 x 27, spread evenly over the volume
-  const int nx = (G.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX;
-  const int ny = (G.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY;
-  fp.out_x = (G.vx + nx - 1) / nx;
-  fp.out_y = (G.vy + ny - 1) / ny;
-  fp.tiles_x = nx;
   fp.parity = parity;
   fp.n_vertices = c->n - 1;
+  fp.vols = c->d_fvol;
+  fp.items = c->d_items;
   fp.error_flag = c->d_error;
-  const int tiles = nx * ny;
-  const int nonroot = c->n - 1;
-  // two resident CTAs per SM; split z so that a launch has a few waves
-  const long long target = (long long)c->sm_count * 2 * 3;
-  int chunks = 1;
-  if ((long long)tiles * nonroot < target)
-    chunks = (int)std::min<long long>((target + (long long)tiles * nonroot - 1) / ((long long)tiles * nonroot),
-                                      std::max(1, G.vz / 16));
-  fp.zchunk = (G.vz + chunks - 1) / chunks;
-  chunks = (G.vz + fp.zchunk - 1) / fp.zchunk;
-  dim3 grid(tiles * nonroot, chunks, 1);
-  hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(c->d_tma, G, fp);
+  const dim3 grid((unsigned)c->n_items * (unsigned)(c->n - 1), 1, 1);
+  hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(c->d_tma, fp);
   CK(cudaGetLastError(), "flow_tma_kernel launch");
   ++c->launches;
   return HMF_OK;
@@ -358,7 +448,9 @@ int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
 
 int launch_flow(hmf_ctx* c, int parity, cudaStream_t s) {
   if (c->use_tma) return launch_flow_tma(c, parity, s);
-  const auto& G = c->geo;
+  // shared-memory ring flow kernel: single volumes only (checked at create)
+  const auto& V = c->vols[0];
+  hmf::Geometry G{V.vx, V.vy, V.vz, V.pitch, V.plane, V.vol};
   hmf::FlowParams fp;
   fp.step = c->step;
   fp.icc = 1.0f / c->cc;
@@ -439,6 +531,13 @@ int capture(hmf_ctx* c, int n_iter, cudaGraphExec_t* out) {
   return HMF_OK;
 }
 
+void drop_graphs(hmf_ctx* c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
+  if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
+  c->graph_pair = c->graph_one = nullptr;
+}
+
 int timed(hmf_ctx* c, int kind, cudaStream_t s, int (*fn)(hmf_ctx*, cudaStream_t, int), int arg) {
   if (!c->timing) return fn(c, s, arg);
   CK(cudaEventRecord(c->ev_t0, s), "cudaEventRecord");
@@ -453,9 +552,10 @@ int timed(hmf_ctx* c, int kind, cudaStream_t s, int (*fn)(hmf_ctx*, cudaStream_t
   return HMF_OK;
 }
 
-int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& d_data,
-                   const std::vector<const float*>& d_smooth, const std::vector<const float*>& distinct) {
-  // flow tables, one per parity
+int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
+  const int nvol = (int)c->vols.size();
+  const int nonroot = c->n - 1;
+  // shared-memory ring flow kernel tables (one volume), one per parity
   std::vector<hmf::FlowVertex>& fv = c->h_flow;
   fv.assign(2 * hmf::kMaxVertices, hmf::FlowVertex{});
   int slot = 0;
@@ -472,7 +572,7 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& 
       f.sink = c->sink[v];
       f.inc = c->sink[c->parent[v]];
       f.label = c->label[v];
-      f.smooth = d_smooth[v];
+      f.smooth = in.smooth[v];
       f.div = c->div[v];
       f.alpha = (float)c->alpha[v];  // stored as float, as the reference does (.cxx:692)
     }
@@ -482,29 +582,33 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& 
      "cudaMemcpyAsync(flow table)");
   if (c->use_tma) {
     std::vector<hmf::FlowVertexTMA>& tv = c->h_tma;
-    tv.assign(c->n - 1, hmf::FlowVertexTMA{});
-    int j = 0;
-    for (int v : c->preorder) {
-      if (v == c->root) continue;
-      hmf::FlowVertexTMA& f = tv[j++];
-      std::memset(&f, 0, sizeof(f));
-      int rc = HMF_OK;
-      for (int par = 0; par < 2 && !rc; ++par) {
-        rc = encode_plane_map(c, &f.flow_in[par][0], c->fx[par][v]);
-        if (!rc) rc = encode_plane_map(c, &f.flow_in[par][1], c->fy[par][v]);
-        if (!rc) rc = encode_plane_map(c, &f.flow_in[par][2], c->fz[par][v]);
-        f.flow_out[par][0] = c->fx[par ^ 1][v];
-        f.flow_out[par][1] = c->fy[par ^ 1][v];
-        f.flow_out[par][2] = c->fz[par ^ 1][v];
+    tv.assign((size_t)nvol * nonroot, hmf::FlowVertexTMA{});
+    for (int b = 0; b < nvol; ++b) {
+      const auto& V = c->vols[b];
+      int j = 0;
+      for (int v : c->preorder) {
+        if (v == c->root) continue;
+        hmf::FlowVertexTMA& f = tv[(size_t)b * nonroot + j++];
+        std::memset(&f, 0, sizeof(f));
+        int rc = HMF_OK;
+        for (int par = 0; par < 2 && !rc; ++par) {
+          rc = encode_plane_map(c, &f.flow_in[par][0], c->fx[par][v] + V.off, V);
+          if (!rc) rc = encode_plane_map(c, &f.flow_in[par][1], c->fy[par][v] + V.off, V);
+          if (!rc) rc = encode_plane_map(c, &f.flow_in[par][2], c->fz[par][v] + V.off, V);
+          f.flow_out[par][0] = c->fx[par ^ 1][v] + V.off;
+          f.flow_out[par][1] = c->fy[par ^ 1][v] + V.off;
+          f.flow_out[par][2] = c->fz[par ^ 1][v] + V.off;
+        }
+        if (!rc) rc = encode_plane_map(c, &f.sink, c->sink[v] + V.off, V);
+        if (!rc) rc = encode_plane_map(c, &f.label, c->label[v] + V.off, V);
+        if (!rc) rc = encode_plane_map(c, &f.inc, c->sink[c->parent[v]] + V.off, V);
+        const bool has_s = in.smooth[v] && c->smooth[b][v].ptr;
+        if (!rc && has_s) rc = encode_plane_map(c, &f.smooth, in.smooth[v] + V.off, V);
+        if (rc) return rc;
+        f.has_smooth = has_s;
+        f.div = c->div[v] + V.off;
+        f.alpha = (float)c->alpha[v];
       }
-      if (!rc) rc = encode_plane_map(c, &f.sink, c->sink[v]);
-      if (!rc) rc = encode_plane_map(c, &f.label, c->label[v]);
-      if (!rc) rc = encode_plane_map(c, &f.inc, c->sink[c->parent[v]]);
-      if (!rc && d_smooth[v]) rc = encode_plane_map(c, &f.smooth, d_smooth[v]);
-      if (rc) return rc;
-      f.has_smooth = d_smooth[v] != nullptr;
-      f.div = c->div[v];
-      f.alpha = (float)c->alpha[v];
     }
     CK(cudaMemcpyAsync(c->d_tma, tv.data(), sizeof(hmf::FlowVertexTMA) * tv.size(), cudaMemcpyHostToDevice, s),
        "cudaMemcpyAsync(tma table)");
@@ -525,7 +629,7 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& 
     E.sink = c->sink[v];
     E.label = v == c->root ? nullptr : c->label[v];
     E.div = v == c->root ? nullptr : c->div[v];
-    E.data = d_data[v];
+    E.data = in.data[v];
     E.parent = v == c->root ? -1 : entry[c->parent[v]];
     E.first_kid = kpos;
     E.n_kids = (int)c->kids[v].size();
@@ -535,10 +639,10 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const std::vector<const float*>& 
   }
   for (size_t j = 0; j < c->leaves.size(); ++j) tt.leaves[j] = entry[c->leaves[j]];
   CK(cudaMemcpyAsync(c->d_tree, &tt, sizeof(tt), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(tree table)");
-  c->n_smooth_list = (int)distinct.size();
-  c->h_smooth_list = distinct;
-  if (!distinct.empty())
-    CK(cudaMemcpyAsync(c->d_smooth_list, c->h_smooth_list.data(), sizeof(float*) * distinct.size(),
+  c->n_smooth_list = (int)in.distinct.size();
+  c->h_smooth_list = in.distinct;
+  if (!in.distinct.empty())
+    CK(cudaMemcpyAsync(c->d_smooth_list, c->h_smooth_list.data(), sizeof(float*) * in.distinct.size(),
                        cudaMemcpyHostToDevice, s),
        "cudaMemcpyAsync(smooth list)");
   return HMF_OK;
@@ -589,15 +693,16 @@ int configure_kernels(hmf_ctx* c) {
 }
 
 bool valid_vertex(const hmf_ctx* c, int v) { return c && v >= 0 && v < c->n; }
+bool valid_volume(const hmf_ctx* c, int b) { return c && b >= 0 && b < (int)c->vols.size(); }
 
-int copy_out(hmf_ctx* c, const float* src, float* out, int where, void* stream) {
+int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* stream) {
   if (!out) return fail(c, HMF_ERR_INVALID_ARGUMENT, "output pointer is NULL");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   DeviceGuard dg(c->device);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const auto& G = c->geo;
-  CK(cudaMemcpy2DAsync(out, (size_t)G.vx * sizeof(float), src, (size_t)G.pitch * sizeof(float),
-                       (size_t)G.vx * sizeof(float), (size_t)G.vy * G.vz,
+  const auto& V = c->vols[b];
+  CK(cudaMemcpy2DAsync(out, (size_t)V.vx * sizeof(float), src + V.off, (size_t)V.pitch * sizeof(float),
+                       (size_t)V.vx * sizeof(float), (size_t)V.vy * V.vz,
                        where == HMF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s),
      "cudaMemcpy2DAsync(output)");
   if (where == HMF_HOST) {
@@ -613,27 +718,55 @@ int copy_out(hmf_ctx* c, const float* src, float* out, int where, void* stream) 
   return HMF_OK;
 }
 
+// Process-wide cache of tuned z chunks, keyed by the work shape.
+std::mutex g_tune_mutex;
+std::map<std::string, int> g_tune_cache;
+
+std::string tune_key(const hmf_ctx* c) {
+  std::string k = std::to_string(c->sm_count) + "/" + std::to_string(c->n) + "/" + std::to_string(c->semantics);
+  for (const auto& V : c->vols) k += "/" + std::to_string(V.vx) + "x" + std::to_string(V.vy) + "x" + std::to_string(V.vz);
+  return k;
+}
+
 }  // namespace
 
 extern "C" {
 
-int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
-               int device) {
+int hmf_create_batch(hmf_ctx** out, int n_volumes, const int* dims, const int* parent, int n_nodes,
+                     int semantics, int device) {
   g_create_error.clear();
   if (!out) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
-  if (vx <= 0 || vy <= 0 || vz <= 0) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
+  if (n_volumes < 1 || !dims) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "a batch needs at least one volume");
+  for (int b = 0; b < n_volumes; ++b)
+    if (dims[3 * b] <= 0 || dims[3 * b + 1] <= 0 || dims[3 * b + 2] <= 0)
+      return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
   if (semantics != HMF_SEMANTICS_REF_CUDA && semantics != HMF_SEMANTICS_REF_CPU)
     return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "unknown semantics");
   hmf_ctx* c = new hmf_ctx();
   c->device = device;
   c->semantics = semantics;
-  c->geo.vx = vx;
-  c->geo.vy = vy;
-  c->geo.vz = vz;
-  c->geo.pitch = (vx + 3) / 4 * 4;
-  c->geo.plane = (long long)c->geo.pitch * vy;
-  c->geo.vol = c->geo.plane * vz;
+  long long off = 0;
+  for (int b = 0; b < n_volumes; ++b) {
+    hmf_ctx::Volume V;
+    V.vx = dims[3 * b];
+    V.vy = dims[3 * b + 1];
+    V.vz = dims[3 * b + 2];
+    V.pitch = (V.vx + 3) / 4 * 4;
+    V.plane = (long long)V.pitch * V.vy;
+    V.vol = V.plane * V.vz;
+    V.off = off;
+    off += V.vol;  // a multiple of 4: every block starts 16-byte aligned
+    c->vols.push_back(V);
+  }
+  c->total = off;
+  const auto& V0 = c->vols[0];
+  c->geo.vx = V0.vx;
+  c->geo.vy = V0.vy;
+  c->geo.vz = V0.vz;
+  c->geo.pitch = n_volumes == 1 ? V0.pitch : 0;
+  c->geo.plane = V0.plane;
+  c->geo.vol = c->total;
   int rc = build_tree(c, parent, n_nodes);
   if (rc) {
     g_create_error = c->err;
@@ -641,16 +774,16 @@ int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_n
     return rc;
   }
   c->alpha.assign(c->n, 1.0);
-  // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=scalar select the
-  // simpler kernels (same results), for comparisons.
-  if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0;
+  // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=quad|scalar select
+  // the simpler kernels (same results), for comparisons.
+  if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0 || n_volumes > 1;
   c->tree_kind = 0;
   if (const char* e = std::getenv("HMF_TREE_KERNEL")) {
     if (std::strcmp(e, "quad") == 0 && c->n <= hmf::kTree4MaxVertices) c->tree_kind = 1;
     if (std::strcmp(e, "scalar") == 0) c->tree_kind = 2;
   }
-  c->data.assign(c->n, {});
-  c->smooth.assign(c->n, {});
+  c->data.assign(n_volumes, std::vector<hmf_ctx::Input>(c->n));
+  c->smooth.assign(n_volumes, std::vector<hmf_ctx::Input>(c->n));
   {
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -675,6 +808,15 @@ int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_n
     }
     rc = allocate_state(c);
     if (!rc) rc = configure_kernels(c);
+    if (!rc) {
+      int z = 0;
+      {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(tune_key(c));
+        if (it != g_tune_cache.end()) z = it->second;
+      }
+      rc = plan_flow(c, z ? z : default_zchunk(c));
+    }
     if (rc) {
       g_create_error = c->err;
       hmf_destroy(c);
@@ -683,6 +825,12 @@ int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_n
   }
   *out = c;
   return HMF_OK;
+}
+
+int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
+               int device) {
+  const int dims[3] = {vx, vy, vz};
+  return hmf_create_batch(out, 1, dims, parent, n_nodes, semantics, device);
 }
 
 int hmf_destroy(hmf_ctx* c) {
@@ -695,6 +843,8 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->staging) cudaFree(c->staging);
   if (c->d_flow[0]) cudaFree(c->d_flow[0]);
   if (c->d_tma) cudaFree(c->d_tma);
+  if (c->d_fvol) cudaFree(c->d_fvol);
+  if (c->d_items) cudaFree(c->d_items);
   if (c->d_tree) cudaFree(c->d_tree);
   if (c->d_smooth_list) cudaFree(c->d_smooth_list);
   if (c->d_error) cudaFree(c->d_error);
@@ -706,23 +856,33 @@ int hmf_destroy(hmf_ctx* c) {
   return HMF_OK;
 }
 
-int hmf_set_data(hmf_ctx* c, int node, const float* data, int where) {
+int hmf_batch_set_data(hmf_ctx* c, int volume, int node, const float* data, int where) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
   if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   if (!c->kids[node].empty())
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "data terms are only used for leaves");
-  c->data[node] = {data, where};
+  c->data[volume][node] = {data, where};
+  return HMF_OK;
+}
+
+int hmf_set_data(hmf_ctx* c, int node, const float* data, int where) {
+  return hmf_batch_set_data(c, 0, node, data, where);
+}
+
+int hmf_batch_set_smoothness(hmf_ctx* c, int volume, int node, const float* smooth, int where) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
+  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
+  if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
+  if (node == c->root) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the root has no smoothness term");
+  c->smooth[volume][node] = {smooth, where};
   return HMF_OK;
 }
 
 int hmf_set_smoothness(hmf_ctx* c, int node, const float* smooth, int where) {
-  if (!c) return HMF_ERR_INVALID_ARGUMENT;
-  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
-  if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
-  if (node == c->root) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the root has no smoothness term");
-  c->smooth[node] = {smooth, where};
-  return HMF_OK;
+  return hmf_batch_set_smoothness(c, 0, node, smooth, where);
 }
 
 int hmf_set_smoothness_scalar(hmf_ctx* c, int node, double alpha) {
@@ -740,10 +900,7 @@ int hmf_set_params(hmf_ctx* c, int iterations, float step_size, float cc) {
   if (step != c->step || ccc != c->cc) {
     // the captured iteration graphs hold StepSize and 1/CC as kernel arguments
     DeviceGuard dg(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
-    if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
-    c->graph_pair = c->graph_one = nullptr;
+    drop_graphs(c);
   }
   c->iterations = std::max(0, iterations);
   c->step = step;
@@ -753,8 +910,9 @@ int hmf_set_params(hmf_ctx* c, int iterations, float step_size, float cc) {
 
 int hmf_solve(hmf_ctx* c, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
-  for (int l : c->leaves)
-    if (!c->data[l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
+  for (size_t b = 0; b < c->vols.size(); ++b)
+    for (int l : c->leaves)
+      if (!c->data[b][l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
   DeviceGuard dg(c->device);
   cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
   cudaStream_t s = c->stream;
@@ -764,12 +922,12 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
   CK(cudaStreamWaitEvent(s, c->ev_join, 0), "cudaStreamWaitEvent(join)");
   CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), s), "cudaMemsetAsync(error flag)");
-  std::vector<const float*> d_data, d_smooth, distinct;
-  int rc = stage_inputs(c, s, d_data, d_smooth, distinct);
-  if (!rc) rc = prepare_tables(c, s, d_data, d_smooth, distinct);
+  Staged staged;
+  int rc = stage_inputs(c, s, staged);
+  if (!rc) rc = prepare_tables(c, s, staged);
   if (rc) return rc;
   // flows of parity 0 start at zero
-  const size_t bytes = (size_t)c->geo.vol * sizeof(float);
+  const size_t bytes = (size_t)c->total * sizeof(float);
   for (int v = 0; v < c->n; ++v) {
     if (v == c->root) continue;
     CK(cudaMemsetAsync(c->fx[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
@@ -809,20 +967,68 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   return HMF_OK;
 }
 
-int hmf_get_labels(hmf_ctx* c, int node, float* out, int where, void* stream) {
+int hmf_autotune(hmf_ctx* c, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!c->use_tma || c->semantics != HMF_SEMANTICS_REF_CUDA) return HMF_OK;
+  const int saved_iters = c->iterations;
+  const bool saved_timing = c->timing;
+  int maxz = 1;
+  for (const auto& V : c->vols) maxz = std::max(maxz, V.vz);
+  int best_z = c->zchunk;
+  double best_ms = 1e30;
+  int rc = HMF_OK;
+  for (int z = 16; rc == HMF_OK; z *= 2) {
+    rc = plan_flow(c, std::min(z, maxz));
+    if (rc) break;
+    c->iterations = 4;
+    c->timing = true;
+    rc = hmf_solve(c, stream);
+    if (rc) break;
+    const double ms = c->kind_count[0] ? c->kind_ms[0] / (double)c->kind_count[0] : 1e30;
+    if (ms < best_ms) best_ms = ms, best_z = std::min(z, maxz);
+    if (z >= maxz) break;
+  }
+  c->iterations = saved_iters;
+  c->timing = saved_timing;
+  c->solved = false;
+  if (rc) return rc;
+  {
+    DeviceGuard dg(c->device);
+    drop_graphs(c);
+    rc = plan_flow(c, best_z);
+  }
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tune_cache[tune_key(c)] = best_z;
+  return HMF_OK;
+}
+
+int hmf_batch_get_labels(hmf_ctx* c, int volume, int node, float* out, int where, void* stream) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
   if (!valid_vertex(c, node) || node == c->root)
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "labels exist for non-root vertices only");
   if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
-  return copy_out(c, c->label[node], out, where, stream);
+  return copy_out(c, volume, c->label[node], out, where, stream);
+}
+
+int hmf_get_labels(hmf_ctx* c, int node, float* out, int where, void* stream) {
+  return hmf_batch_get_labels(c, 0, node, out, where, stream);
+}
+
+int hmf_batch_get_sink(hmf_ctx* c, int volume, int node, float* out, int where, void* stream) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
+  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
+  if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
+  return copy_out(c, volume, c->sink[node], out, where, stream);
 }
 
 int hmf_get_sink(hmf_ctx* c, int node, float* out, int where, void* stream) {
-  if (!c) return HMF_ERR_INVALID_ARGUMENT;
-  if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
-  if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
-  return copy_out(c, c->sink[node], out, where, stream);
+  return hmf_batch_get_sink(c, 0, node, out, where, stream);
 }
+
+int hmf_num_volumes(const hmf_ctx* c) { return c ? (int)c->vols.size() : HMF_ERR_INVALID_ARGUMENT; }
 
 int hmf_leaf_order(const hmf_ctx* c, int* out, int cap) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
@@ -834,7 +1040,8 @@ int hmf_leaf_order(const hmf_ctx* c, int* out, int cap) {
 size_t hmf_device_bytes(const hmf_ctx* c) {
   if (!c) return 0;
   return c->arena_bytes + c->staging_bytes + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
-         sizeof(hmf::TreeTable);
+         sizeof(hmf::FlowVertexTMA) * c->vols.size() * (c->n - 1) + sizeof(hmf::TreeTable) +
+         sizeof(hmf::FlowItem) * c->h_items.size();
 }
 
 int hmf_set_timing(hmf_ctx* c, int enabled) {

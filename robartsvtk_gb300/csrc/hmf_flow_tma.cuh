@@ -54,15 +54,31 @@ struct FlowVertexTMA {  // 64-byte aligned through its CUtensorMap members
   int has_smooth;
 };
 
+// One volume of a solve (a batch holds several of different sizes).
+struct FlowVolume {
+  Geometry G;
+  int tiles_x;  // windows across x
+  int out_x;    // output columns per window (<= 28)
+  int out_y;    // output rows per window (<= 27)
+  int zchunk;   // planes per window column
+};
+
+// One CTA's work: a window column (tile, z chunk) of one volume; the vertex is
+// blockIdx.x % n_vertices.
+struct FlowItem {
+  int vol;
+  int tile;
+  int zc;
+  int pad_;
+};
+
 struct FlowTmaParams {
   float step;
   float icc;
-  int zchunk;
-  int tiles_x;
-  int out_x;  // output columns per window (<= 28)
-  int out_y;  // output rows per window (<= 27)
   int parity;
-  int n_vertices;  // non-root vertices (grid.x = n_vertices * tiles)
+  int n_vertices;  // non-root vertices (grid.x = n_vertices * items)
+  const FlowVolume* vols;
+  const FlowItem* items;
   int* error_flag;
 };
 
@@ -90,7 +106,7 @@ __device__ __forceinline__ float projection_multiplier(float h, float lim) {
 }
 
 __global__ void __launch_bounds__(kTmaThreads, 2)
-flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, const FlowTmaParams fp) {
+flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams fp) {
   // Pointers into the shared window are formed by pointer arithmetic only,
   // so the compiler keeps them in the shared address space (32-bit LDS/STS).
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -104,22 +120,26 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
   uint64_t* zbars = mbars + kTmaMainSlots;                        // [4]
   __shared__ int abort_cta;
 
-  // blockIdx.x = vertex + n_vertices * tile: the vertices of one window run
+  // blockIdx.x = vertex + n_vertices * item: the vertices of one window run
   // side by side, so a parent sink and a shared smoothness image read by
   // several of them come from L2.
   const int nv = fp.n_vertices;
-  const FlowVertexTMA* V = vertices + (blockIdx.x % nv);
-  const int tile = (int)(blockIdx.x / nv);
+  const FlowItem item = fp.items[blockIdx.x / nv];
+  const FlowVolume FV = fp.vols[item.vol];
+  const Geometry G = FV.G;
+  const FlowVertexTMA* V = vertices + (size_t)item.vol * nv + (blockIdx.x % nv);
+  const int tile = item.tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
-  const int tiles_x = fp.tiles_x;
-  const int x0 = (tile % tiles_x) * fp.out_x;
-  const int y0 = (tile / tiles_x) * fp.out_y;
+  const int tiles_x = FV.tiles_x;
+  const int ocols = FV.out_x, orows = FV.out_y;
+  const int x0 = (tile % tiles_x) * ocols;
+  const int y0 = (tile / tiles_x) * orows;
   const int xs = ((x0 + 2) / 4) * 4 - 4;  // x0 - 2 rounded down to a multiple of 4 (x0 >= 0)
   const int off = (x0 - 2) - xs;           // 0..3
   const int x = x0 - 2 + lane;
-  const int zs = (int)blockIdx.y * fp.zchunk;
-  const int ze = min(zs + fp.zchunk, G.vz);
+  const int zs = item.zc * FV.zchunk;
+  const int ze = min(zs + FV.zchunk, G.vz);
   const int kstart = max(zs - 2, 0);
   const int kend = ze + 1;
   const int kmain_end = min(ze + 1, G.vz - 1);  // last plane whose g is computed
@@ -137,7 +157,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
   const bool xin = x >= 0 && x < G.vx;
   const bool xpos = x > 0;
   const bool xnl = x != G.vx - 1;
-  const bool xout = lane >= 2 && lane < 2 + fp.out_x && x < G.vx;
+  const bool xout = lane >= 2 && lane < 2 + ocols && x < G.vx;
   // per-row constants of this thread (rows warp*4 + r of the window)
   bool rin[4], ypos[4], ynl[4], rout[4];
   long long rowoff[4];
@@ -148,7 +168,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const Geometry G, co
     rin[r] = xin && y >= 0 && y < G.vy;
     ypos[r] = y > 0;
     ynl[r] = y != G.vy - 1;
-    rout[r] = xout && row >= 2 && row < 2 + fp.out_y && y < G.vy;
+    rout[r] = xout && row >= 2 && row < 2 + orows && y < G.vy;
     rowoff[r] = (long long)y * G.pitch + x;
   }
 

@@ -435,8 +435,10 @@ __global__ void init_kernel(const TreeTable* __restrict__ table, const Geometry 
   const int root = n - 1;
   int bad = 0;
   for (long long i = (long long)blockIdx.x * nb + t; i < G.vol; i += (long long)gridDim.x * nb) {
-    const long long row = i / G.pitch;
-    const bool inside = (i - row * G.pitch) < G.vx;
+    // pitch 0: several volumes of different pitches back to back, whose
+    // padding columns are zero (never written), so every element is checked
+    const long long row = G.pitch ? i / G.pitch : 0;
+    const bool inside = G.pitch == 0 || (i - row * G.pitch) < G.vx;
     float m = T.e[T.leaves[0]].data[i];
     for (int j = 1; j < T.n_leaves; ++j) {
       const float d = T.e[T.leaves[j]].data[i];

@@ -18,7 +18,7 @@ import numpy as np
 from . import _capi
 from ._capi import HMF_DEVICE, HMF_HOST, HMF_SEMANTICS_REF_CPU, HMF_SEMANTICS_REF_CUDA, HMFError, check
 
-__all__ = ["HMFSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]
+__all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]
 
 REF_CUDA = HMF_SEMANTICS_REF_CUDA
 REF_CPU = HMF_SEMANTICS_REF_CPU
@@ -121,6 +121,105 @@ class HMFSolver:
 
     def sink(self, node: int, out=None, stream=None):
         return self._fetch(self._lib.hmf_get_sink, node, out, stream)
+
+    def stats(self):
+        launches = ctypes.c_longlong()
+        ms = (ctypes.c_double * 3)()
+        check(self._lib.hmf_get_stats(self._ctx, ctypes.byref(launches), ms, 3), self._ctx)
+        return {"launches": launches.value, "flow_ms": ms[0], "tree_ms": ms[1], "init_ms": ms[2]}
+
+    def device_bytes(self) -> int:
+        return int(self._lib.hmf_device_bytes(self._ctx))
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.hmf_destroy(self._ctx)
+            self._ctx = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class HMFBatchSolver:
+    """Many volumes of different sizes sharing one label tree, solved together
+    (include/hmf.h, hmf_create_batch).  `dims` is a list of (VX, VY, VZ)."""
+
+    def __init__(self, dims, parent, semantics: int = REF_CUDA, device: int = 0):
+        self._lib = _capi.load()
+        self.dims = [tuple(int(d) for d in dd) for dd in dims]
+        self.parent = [int(p) for p in parent]
+        flat = (ctypes.c_int * (3 * len(self.dims)))(*[d for dd in self.dims for d in dd])
+        par = (ctypes.c_int * len(self.parent))(*self.parent)
+        ctx = ctypes.c_void_p()
+        check(self._lib.hmf_create_batch(ctypes.byref(ctx), len(self.dims), flat, par, len(self.parent),
+                                         int(semantics), int(device)))
+        self._ctx = ctx
+        self._keep: dict = {}
+        n = self._lib.hmf_leaf_order(self._ctx, None, 0)
+        buf = (ctypes.c_int * max(n, 1))()
+        self._lib.hmf_leaf_order(self._ctx, buf, n)
+        self.leaves = [buf[i] for i in range(n)]
+
+    def _nvox(self, b):
+        d = self.dims[b]
+        return d[0] * d[1] * d[2]
+
+    def set_data(self, volume: int, node: int, arr) -> None:
+        ptr, where, keep = _array_pointer(arr, self._nvox(volume))
+        check(self._lib.hmf_batch_set_data(self._ctx, int(volume), int(node), ptr, where), self._ctx)
+        self._keep[("d", volume, node)] = keep
+
+    def set_smoothness(self, volume: int, node: int, arr) -> None:
+        if arr is None:
+            check(self._lib.hmf_batch_set_smoothness(self._ctx, int(volume), int(node), None, HMF_HOST), self._ctx)
+            self._keep.pop(("s", volume, node), None)
+            return
+        ptr, where, keep = _array_pointer(arr, self._nvox(volume))
+        check(self._lib.hmf_batch_set_smoothness(self._ctx, int(volume), int(node), ptr, where), self._ctx)
+        self._keep[("s", volume, node)] = keep
+
+    def set_smoothness_scalar(self, node: int, alpha: float) -> None:
+        check(self._lib.hmf_set_smoothness_scalar(self._ctx, int(node), float(alpha)), self._ctx)
+
+    def set_params(self, iterations: int = 100, step: float = 0.1, cc: float = 0.25) -> None:
+        check(self._lib.hmf_set_params(self._ctx, int(iterations), float(step), float(cc)), self._ctx)
+
+    def set_timing(self, enabled: bool) -> None:
+        check(self._lib.hmf_set_timing(self._ctx, 1 if enabled else 0), self._ctx)
+
+    def autotune(self, stream=None) -> None:
+        check(self._lib.hmf_autotune(self._ctx, _stream_handle(stream)), self._ctx)
+
+    def solve(self, stream=None) -> None:
+        check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
+
+    def labels(self, volume: int, node: int, out=None, stream=None):
+        if out is None:
+            d = self.dims[volume]
+            out = np.empty((d[2], d[1], d[0]), dtype=np.float32)
+        ptr, where, _ = _array_pointer(out, self._nvox(volume))
+        check(self._lib.hmf_batch_get_labels(self._ctx, int(volume), int(node), ptr, where,
+                                             _stream_handle(stream)), self._ctx)
+        return out
+
+    def sink(self, volume: int, node: int, out=None, stream=None):
+        if out is None:
+            d = self.dims[volume]
+            out = np.empty((d[2], d[1], d[0]), dtype=np.float32)
+        ptr, where, _ = _array_pointer(out, self._nvox(volume))
+        check(self._lib.hmf_batch_get_sink(self._ctx, int(volume), int(node), ptr, where,
+                                           _stream_handle(stream)), self._ctx)
+        return out
 
     def stats(self):
         launches = ctypes.c_longlong()
