@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--iterations", type=int, default=500)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-sequential measurement")
+    ap.add_argument("--batch-count", type=int, default=64)
+    ap.add_argument("--batch-iterations", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
                     help="two solves (one warm, one profiled) and nothing else: the command ncu wraps")
     return ap.parse_args()
@@ -373,6 +376,8 @@ def run_ours(args):
         "clocks": clock_info,
         "roofline": roofline,
     }
+    if rank == 0 and not args.no_batched:
+        out["batched"] = bench_batched(args, stream)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
     if rank == 0:
@@ -381,6 +386,68 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def bench_batched(args, device_stream):
+    """64 volumes with axes U{48..192}, flat 3 leaves, alpha 0.15, 200
+    iterations: one batched solve (autotuned) against the same 64 volumes
+    solved one after another, each in its own context.  Inputs are resident
+    on the device; times are CUDA events on one stream."""
+    import torch
+
+    from robartsvtk_gb300 import HMFBatchSolver, HMFSolver, synthetic
+
+    ws = synthetic.batch_flat3(seed=7, count=args.batch_count, iterations=args.batch_iterations)
+    keep = []
+    dev = []
+    for w in ws:
+        d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
+        keep.extend(d.values())
+        dev.append(d)
+    L = len(ws[0].leaves)
+    units = sum(w.nvox for w in ws) * L * ws[0].iterations
+    batch = HMFBatchSolver([w.dims for w in ws], ws[0].parent)
+    for i, w in enumerate(ws):
+        for leaf, t in dev[i].items():
+            batch.set_data(i, leaf, t)
+    for v, a in ws[0].alpha.items():
+        batch.set_smoothness_scalar(v, a)
+    batch.set_params(ws[0].iterations, ws[0].step, ws[0].cc)
+    batch.autotune(device_stream)
+    singles = []
+    for i, w in enumerate(ws):
+        s = HMFSolver(w.dims, w.parent)
+        for leaf, t in dev[i].items():
+            s.set_data(leaf, t)
+        for v, a in w.alpha.items():
+            s.set_smoothness_scalar(v, a)
+        s.set_params(w.iterations, w.step, w.cc)
+        singles.append(s)
+
+    def timed(fn, reps):
+        fn()
+        device_stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(device_stream)
+        for _ in range(reps):
+            fn()
+        e1.record(device_stream)
+        device_stream.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_batch = timed(lambda: batch.solve(device_stream), 2)
+    t_seq = timed(lambda: [s.solve(device_stream) for s in singles], 1)
+    launches = batch.stats()["launches"]
+    for s in singles:
+        s.close()
+    batch.close()
+    return {"workload": "%d volumes, axes U{48..192}, flat 3 leaves, alpha 0.15, %d iterations"
+                        % (len(ws), ws[0].iterations),
+            "voxels": sum(w.nvox for w in ws),
+            "value": units / (t_batch / 1000.0), "sequential_value": units / (t_seq / 1000.0), "unit": UNIT,
+            "ms_batched": t_batch, "ms_sequential": t_seq, "speedup_vs_sequential": t_seq / t_batch,
+            "launches_per_batched_solve": launches}
 
 
 def run_profile(args):
