@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-sequential measurement")
     ap.add_argument("--batch-count", type=int, default=64)
     ap.add_argument("--batch-iterations", type=int, default=200)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
+    ap.add_argument("--adjoint-size", type=int, default=128)
+    ap.add_argument("--adjoint-iterations", type=int, default=300)
     ap.add_argument("--profile", action="store_true",
                     help="two solves (one warm, one profiled) and nothing else: the command ncu wraps")
     return ap.parse_args()
@@ -378,6 +381,8 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_batched:
         out["batched"] = bench_batched(args, stream)
+    if rank == 0 and not args.no_adjoint:
+        out["adjoint"] = bench_adjoint(args, stream)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
     if rank == 0:
@@ -448,6 +453,61 @@ def bench_batched(args, device_stream):
             "value": units / (t_batch / 1000.0), "sequential_value": units / (t_seq / 1000.0), "unit": UNIT,
             "ms_batched": t_batch, "ms_sequential": t_seq, "speedup_vs_sequential": t_seq / t_batch,
             "launches_per_batched_solve": launches}
+
+
+def bench_adjoint(args, device_stream):
+    """128^3, 4 ellipsoids, sigma 0.1, flat 4 leaves, alpha 0.1, 300
+    iterations; loss = voxelwise cross-entropy of the final labels against the
+    phantom's classes.  Times the forward solve alone and the forward +
+    adjoint (hmf_solve_adjoint) with checkpoints every 30 iterations and with
+    every state kept (automatic plan), inputs resident on the device."""
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver, synthetic
+
+    w = synthetic.ellipsoids_flat4(seed=3, size=args.adjoint_size, iterations=args.adjoint_iterations)
+    d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
+    truth = torch.from_numpy(w.truth.astype("int32")).cuda()
+    s = HMFSolver(w.dims, w.parent)
+    for leaf, t in d.items():
+        s.set_data(leaf, t)
+    for v, a in w.alpha.items():
+        s.set_smoothness_scalar(v, a)
+    s.set_params(w.iterations, w.step, w.cc)
+
+    def timed(fn, reps):
+        fn()
+        device_stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(device_stream)
+        for _ in range(reps):
+            fn()
+        e1.record(device_stream)
+        device_stream.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_fwd = timed(lambda: s.solve(device_stream), 3)
+    res = {}
+    for k in (30, 0):
+        loss = [0.0]
+
+        def run():
+            loss[0] = s.solve_adjoint(truth, checkpoint_every=k, stream=device_stream)
+
+        t = timed(run, 2)
+        plan = s.adjoint_plan()
+        res["every_state_kept" if k == 0 else "checkpoint_every_%d" % k] = {
+            "ms": t, "ratio_to_forward": t / t_fwd, "checkpoint_every": plan["checkpoint_every"],
+            "recomputed_segments": plan["recomputed_segments"], "loss": loss[0],
+            "launches": s.stats()["launches"]}
+    ga = s.alpha_gradient()
+    out = {"workload": "ellipsoids%d_flat4, %d iterations, loss = cross-entropy of final labels"
+                       % (args.adjoint_size, w.iterations),
+           "forward_ms": t_fwd, "device_bytes": s.device_bytes(),
+           "dalpha": [float(x) for x in ga[1:]], **res}
+    s.close()
+    return out
 
 
 def run_profile(args):

@@ -142,6 +142,33 @@ int hmf_batch_get_sink(hmf_ctx* ctx, int volume, int node, float* out, int where
  * later in the process.  Inputs must be set; the labels are not kept. */
 int hmf_autotune(hmf_ctx* ctx, void* stream);
 
+/* ---- Adjoint (reverse mode) -----------------------------------------------
+ * No counterpart in the reference, which only solves forward.  Solves like
+ * hmf_solve (REF_CUDA semantics, single-volume contexts) and differentiates
+ * the loss
+ *     L = -(1/V) * sum_i log(max(u_{leaf(truth_i)}(i), eps))
+ * of the final leaf labels through every iteration: truth holds one class per
+ * voxel (int32, x fastest, dense VX*VY*VZ) indexing the leaves in the order
+ * of hmf_leaf_order.  Afterwards hmf_get_data_gradient returns dL/dD for each
+ * leaf data term (per voxel, double) and hmf_get_alpha_gradient dL/dalpha for
+ * every vertex's smoothness weight; labels and sinks read as after hmf_solve.
+ * Forward states are kept in HBM every checkpoint_every iterations and the
+ * states in between recomputed segment by segment (0 = automatic: keep every
+ * state when they fit in 85% of the free device memory, else checkpoints
+ * every ceil(sqrt(iterations))).  The call returns after the backward pass
+ * (it synchronises c's stream to read the loss).  Kinks follow the forward
+ * code: saturate and the leaf capacity clamp pass gradients strictly inside
+ * their linear ranges, the projection multiplier only where |p| > alpha*S. */
+int hmf_solve_adjoint(hmf_ctx* ctx, const int* truth, int where, int checkpoint_every, double eps,
+                      double* loss, void* stream);
+int hmf_get_data_gradient(hmf_ctx* ctx, int leaf, double* out, int where, void* stream);
+/* Writes min(n, n_nodes) values (vertex id order; root and vertices without a
+ * smoothness term read 0 and their alpha respectively); returns n_nodes. */
+int hmf_get_alpha_gradient(hmf_ctx* ctx, double* out, int n);
+/* The checkpoint interval the last hmf_solve_adjoint used and how many of its
+ * segments were recomputed. */
+int hmf_get_adjoint_plan(const hmf_ctx* ctx, int* checkpoint_every, int* recomputed_segments);
+
 /* Message of the last failed call on ctx (or, when ctx is NULL, of the last
  * failed hmf_create or hmf_solve_noalloc on this thread). */
 const char* hmf_last_error(const hmf_ctx* ctx);

@@ -659,6 +659,266 @@ int run_cpu_semantics(const Problem& P, const Tree& t, double* u_out, double* si
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the REF_CUDA iteration (reverse mode), restated on the CPU.
+//
+// Loss: L = -(1/V) sum_i log(max(u_{leaf(truth(i))}(i), eps)) over the final
+// leaf labels.  Gradients: dL/dD for every leaf data term (per voxel) and
+// dL/dalpha for every non-root vertex.  Conventions at the kinks: saturate
+// passes the gradient only strictly inside (0, 1); the leaf capacity clamp
+// passes it to the sink input strictly inside (0, D) and to D when the input
+// exceeds D; the multiplier depends on |p| and alpha only when |p| > alpha*S;
+// the initial sink min(D) sends its gradient to the leaf kern_MinBuffers keeps
+// (the last one of a tie).  Forward states of every iteration are stored
+// (small problems only).
+// ---------------------------------------------------------------------------
+template <class T>
+struct AdjointRun {
+  const Tree& t;
+  CudaOracle<T>& o;
+  int VX, VY, VZ;
+  long V, sxy;
+  struct State {
+    std::vector<std::vector<T>> px, py, pz, s, u;
+  };
+  std::vector<State> states;
+
+  AdjointRun(const Tree& tr, CudaOracle<T>& ora) : t(tr), o(ora), VX(ora.VX), VY(ora.VY), VZ(ora.VZ) {
+    V = o.V;
+    sxy = (long)VX * VY;
+  }
+  State snap() const {
+    State st;
+    st.px = o.fx;
+    st.py = o.fy;
+    st.pz = o.fz;
+    st.s = o.sink;
+    st.u = o.u;
+    return st;
+  }
+  int xo(long i) const { return (int)(i % VX); }
+  int yo(long i) const { return (int)((i / VX) % VY); }
+  int zo(long i) const { return (int)(i / sxy); }
+  // kern_Divergence of flows (px, py, pz)
+  void divergence(const std::vector<T>& px, const std::vector<T>& py, const std::vector<T>& pz, std::vector<T>& d) const {
+    d.assign(V, T(0));
+    for (long i = 0; i < V; ++i) {
+      T dv = px[i] + py[i] + pz[i];
+      if (xo(i) != VX - 1) dv -= px[i + 1];
+      if (yo(i) != VY - 1) dv -= py[i + VX];
+      if (i < V - sxy) dv -= pz[i + sxy];
+      d[i] = dv;
+    }
+  }
+
+  // Backward through iteration t: (Pb, sbn, ubn) are the adjoints of state
+  // t+1 on entry and of state t on exit; Db, ab accumulate.
+  void backward_step(int it, std::vector<std::vector<T>>& Pbx, std::vector<std::vector<T>>& Pby,
+                     std::vector<std::vector<T>>& Pbz, std::vector<std::vector<T>>& sbn,
+                     std::vector<std::vector<T>>& ubn, std::vector<std::vector<double>>& Db, std::vector<double>& ab) {
+    const State& A = states[it];
+    const State& B = states[it + 1];
+    const int n = t.n, root = t.root;
+    const T icc = o.icc, cc = o.cc, tau = o.step;
+    std::vector<std::vector<T>> dnew(n), dbp(n, std::vector<T>(V, T(0)));
+    std::vector<std::vector<T>> sbo(n, std::vector<T>(V, T(0))), ubo(n, std::vector<T>(V, T(0)));
+    for (int v = 0; v < n; ++v)
+      if (v != root) divergence(B.px[v], B.py[v], B.pz[v], dnew[v]);
+    // --- phase 2 reverse: labels, then sinks in reverse post-order
+    std::vector<std::vector<T>> sbN = sbn;  // adjoint of the new sinks
+    for (int v = 0; v < n; ++v) {
+      if (v == root) continue;
+      const int p = t.parent[v];
+      for (long i = 0; i < V; ++i) {
+        const T z = A.u[v][i] + cc * ((B.s[p][i] - dnew[v][i]) - B.s[v][i]);
+        const T zb = (z > T(0) && z < T(1)) ? ubn[v][i] : T(0);
+        ubo[v][i] += zb;
+        sbN[p][i] += cc * zb;
+        dbp[v][i] -= cc * zb;
+        sbN[v][i] -= cc * zb;
+      }
+    }
+    std::vector<int> rev(t.preorder.begin(), t.preorder.end());  // parents before children
+    for (int v : rev) {
+      const auto& kids = t.kids[v];
+      if (kids.empty()) {
+        const int p = t.parent[v];
+        for (long i = 0; i < V; ++i) {
+          const T y = (A.s[p][i] - dnew[v][i]) + A.u[v][i] * icc;
+          const T cap = T(o.data[v][i]);
+          if (y < T(0)) continue;
+          if (y > cap) {
+            Db[v][i] += (double)sbN[v][i];
+            continue;
+          }
+          const T yb = sbN[v][i];
+          sbo[p][i] += yb;
+          dbp[v][i] -= yb;
+          ubo[v][i] += icc * yb;
+        }
+      } else {
+        const T inv = (v == root) ? T(1) / T((int)kids.size()) : T(1) / T((int)kids.size() + 1);
+        for (long i = 0; i < V; ++i) {
+          const T Wb = sbN[v][i] * inv;
+          if (v != root) {
+            sbo[t.parent[v]][i] += Wb;
+            dbp[v][i] -= Wb;
+            ubo[v][i] += icc * Wb;
+          }
+          for (int k : kids) {
+            sbN[k][i] += Wb;
+            dbp[k][i] += Wb;
+            ubo[k][i] -= icc * Wb;
+          }
+        }
+      }
+    }
+    // --- phase 1 reverse, vertex by vertex
+    for (int v = 0; v < n; ++v) {
+      if (v == root) continue;
+      const int p = t.parent[v];
+      std::vector<T> dold, g(V), ppx(V), ppy(V), ppz(V), Fm(V), lim(V), m(V);
+      divergence(A.px[v], A.py[v], A.pz[v], dold);
+      for (long i = 0; i < V; ++i) g[i] = tau * (((A.s[v][i] + dold[i]) - A.s[p][i]) - A.u[v][i] * icc);
+      for (long i = 0; i < V; ++i) {
+        ppx[i] = xo(i) ? A.px[v][i] - (g[i] - g[i - 1]) : T(0);
+        ppy[i] = yo(i) ? A.py[v][i] - (g[i] - g[i - VX]) : T(0);
+        ppz[i] = zo(i) ? A.pz[v][i] - (g[i] - g[i - sxy]) : T(0);
+      }
+      for (long i = 0; i < V; ++i) {
+        T up = ppx[i] * ppx[i];
+        T dn = (xo(i) != VX - 1) ? ppx[i + 1] * ppx[i + 1] : T(0);
+        T F = up + dn;
+        up = ppy[i] * ppy[i];
+        dn = (yo(i) != VY - 1) ? ppy[i + VX] * ppy[i + VX] : T(0);
+        F += up + dn;
+        up = ppz[i] * ppz[i];
+        dn = (i + sxy < V) ? ppz[i + sxy] * ppz[i + sxy] : T(0);
+        F += up + dn;
+        Fm[i] = std::sqrt(T(0.5) * F);
+        lim[i] = o.smooth[v] ? o.alpha[v] * T(o.smooth[v][i]) : o.alpha[v];
+        m[i] = (Fm[i] > lim[i]) ? lim[i] / Fm[i] : T(1);
+      }
+      // total adjoint of the new flows P: incoming plus through div'
+      std::vector<T> tx(V), ty(V), tz(V);
+      for (long i = 0; i < V; ++i) {
+        tx[i] = Pbx[v][i] + dbp[v][i] - (xo(i) ? dbp[v][i - 1] : T(0));
+        ty[i] = Pby[v][i] + dbp[v][i] - (yo(i) ? dbp[v][i - VX] : T(0));
+        tz[i] = Pbz[v][i] + dbp[v][i] - (zo(i) ? dbp[v][i - sxy] : T(0));
+      }
+      std::vector<T> F2b(V, T(0));
+      double asum = 0.0;
+      for (long i = 0; i < V; ++i) {
+        T mb = T(0);
+        if (xo(i)) mb += tx[i] * T(0.5) * ppx[i];
+        if (xo(i) != VX - 1) mb += tx[i + 1] * T(0.5) * ppx[i + 1];
+        if (yo(i)) mb += ty[i] * T(0.5) * ppy[i];
+        if (yo(i) != VY - 1) mb += ty[i + VX] * T(0.5) * ppy[i + VX];
+        if (zo(i)) mb += tz[i] * T(0.5) * ppz[i];
+        if (i + sxy < V) mb += tz[i + sxy] * T(0.5) * ppz[i + sxy];
+        if (Fm[i] > lim[i]) {
+          F2b[i] = -mb * lim[i] / (T(4) * Fm[i] * Fm[i] * Fm[i]);
+          asum += (double)(mb / Fm[i] * (o.smooth[v] ? T(o.smooth[v][i]) : T(1)));
+        }
+      }
+      ab[v] += asum;
+      std::vector<T> qx(V), qy(V), qz(V);  // adjoint of p'
+      for (long i = 0; i < V; ++i) {
+        qx[i] = xo(i) ? tx[i] * T(0.5) * (m[i] + m[i - 1]) + T(2) * ppx[i] * (F2b[i] + F2b[i - 1]) : T(0);
+        qy[i] = yo(i) ? ty[i] * T(0.5) * (m[i] + m[i - VX]) + T(2) * ppy[i] * (F2b[i] + F2b[i - VX]) : T(0);
+        qz[i] = zo(i) ? tz[i] * T(0.5) * (m[i] + m[i - sxy]) + T(2) * ppz[i] * (F2b[i] + F2b[i - sxy]) : T(0);
+      }
+      std::vector<T> dbo(V);
+      for (long i = 0; i < V; ++i) {
+        T gb = -(qx[i] + qy[i] + qz[i]);
+        if (xo(i) != VX - 1) gb += qx[i + 1];
+        if (yo(i) != VY - 1) gb += qy[i + VX];
+        if (i + sxy < V) gb += qz[i + sxy];
+        sbo[v][i] += tau * gb;
+        ubo[v][i] -= tau * icc * gb;
+        sbo[p][i] -= tau * gb;
+        dbo[i] = tau * gb;
+      }
+      for (long i = 0; i < V; ++i) {
+        Pbx[v][i] = qx[i] + dbo[i] - (xo(i) ? dbo[i - 1] : T(0));
+        Pby[v][i] = qy[i] + dbo[i] - (yo(i) ? dbo[i - VX] : T(0));
+        Pbz[v][i] = qz[i] + dbo[i] - (zo(i) ? dbo[i - sxy] : T(0));
+      }
+    }
+    sbn = sbo;
+    ubn = ubo;
+  }
+};
+
+template <class T>
+int run_adjoint(const Problem& P, const Tree& t, const int* truth, double eps, double* loss_out,
+                double* dD_out /* [n][V] */, double* dalpha_out /* [n] */, double* u_out) {
+  CudaOracle<T> o(t, P.vx, P.vy, P.vz);
+  o.alloc();
+  o.data.assign(t.n, nullptr);
+  o.smooth.assign(t.n, nullptr);
+  o.alpha.assign(t.n, T(1));
+  for (int v = 0; v < t.n; ++v) {
+    o.data[v] = P.data ? P.data[v] : nullptr;
+    o.smooth[v] = P.smooth ? P.smooth[v] : nullptr;
+    o.alpha[v] = P.alpha ? T((float)P.alpha[v]) : T(1);
+  }
+  for (int v = 0; v < t.n; ++v) if (t.leaf(v) && !o.data[v]) { g_err = "missing data term for a leaf"; return -3; }
+  if (sizeof(T) == sizeof(float)) {
+    o.step = T(P.step); o.cc = T(P.cc); o.icc = T(1.0f / P.cc); o.root_work = T(1.0f / P.cc);
+  } else {
+    o.step = T(P.step); o.cc = T(P.cc); o.icc = T(1) / T(P.cc); o.root_work = T(1) / T(P.cc);
+  }
+  o.init();
+  AdjointRun<T> A(t, o);
+  A.states.push_back(A.snap());
+  for (int it = 0; it < P.iterations; ++it) {
+    o.solve(t.root);
+    A.states.push_back(A.snap());
+  }
+  const long V = o.V;
+  std::vector<int> leaves;
+  for (int v : t.preorder) if (t.leaf(v)) leaves.push_back(v);
+  // loss and its gradient on the final leaf labels
+  const int n = t.n;
+  std::vector<std::vector<T>> Pbx(n, std::vector<T>(V, T(0))), Pby = Pbx, Pbz = Pbx, sbn = Pbx, ubn = Pbx;
+  double loss = 0.0;
+  const auto& U = A.states.back().u;
+  for (long i = 0; i < V; ++i) {
+    const int cls = truth[i];
+    if (cls < 0 || cls >= (int)leaves.size()) { g_err = "truth class out of range"; return -1; }
+    const int l = leaves[cls];
+    const T uv = U[l][i];
+    const T ue = uv > T(eps) ? uv : T(eps);
+    loss -= std::log((double)ue) / (double)V;
+    if (uv > T(eps)) ubn[l][i] = T(-1.0 / ((double)V * (double)uv));
+  }
+  std::vector<std::vector<double>> Db(n, std::vector<double>(V, 0.0));
+  std::vector<double> ab(n, 0.0);
+  for (int it = P.iterations - 1; it >= 0; --it) A.backward_step(it, Pbx, Pby, Pbz, sbn, ubn, Db, ab);
+  // initial sinks = min over leaves (kern_MinBuffers keeps the last of a tie)
+  for (long i = 0; i < V; ++i) {
+    int arg = leaves[0];
+    float mv = o.data[leaves[0]][i];
+    for (size_t k = 1; k < leaves.size(); ++k) {
+      const float d = o.data[leaves[k]][i];
+      if (!(mv < d)) { mv = d; arg = leaves[k]; }
+    }
+    double tot = 0.0;
+    for (int v = 0; v < n; ++v) tot += (double)sbn[v][i];
+    Db[arg][i] += tot;
+  }
+  if (loss_out) *loss_out = loss;
+  for (int v = 0; v < n; ++v) {
+    if (dalpha_out) dalpha_out[v] = ab[v];
+    for (long i = 0; i < V; ++i) {
+      if (dD_out) dD_out[(long)v * V + i] = Db[v][i];
+      if (u_out) u_out[(long)v * V + i] = (v == t.root) ? 0.0 : (double)U[v][i];
+    }
+  }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -699,6 +959,29 @@ int ORACLE_ENTRY(int semantics, int precision, int threads, int vx, int vy, int 
   return run_cuda_semantics<float>(P, t, u_out, sink_out, div_out);
 #endif
 }
+
+#ifndef HMF_ORACLE_WITH_REFERENCE
+// Loss and gradients of the REF_CUDA solve (see AdjointRun).  truth: class
+// per voxel = index into the DFS pre-order leaf list.  dD_out [n_nodes * V]
+// (leaf rows filled), dalpha_out [n_nodes], u_out [n_nodes * V] final labels.
+int oracle_hmf_adjoint(int precision, int threads, int vx, int vy, int vz, int n_nodes, const int* parent,
+                       const float* const* data, const float* const* smooth, const double* alpha,
+                       int iterations, float step, float cc, const int* truth, double eps,
+                       double* loss_out, double* dD_out, double* dalpha_out, double* u_out) {
+  g_err.clear();
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  if (vx <= 0 || vy <= 0 || vz <= 0) { g_err = "bad dimensions"; return -1; }
+  Tree t;
+  if (!t.build(n_nodes, parent)) return -2;
+  Problem P{vx, vy, vz, n_nodes, parent, data, smooth, alpha, iterations, step, cc};
+  if (precision == 64) return run_adjoint<double>(P, t, truth, eps, loss_out, dD_out, dalpha_out, u_out);
+  return run_adjoint<float>(P, t, truth, eps, loss_out, dD_out, dalpha_out, u_out);
+}
+#endif
 
 const char* oracle_last_error(void) { return g_err.c_str(); }
 

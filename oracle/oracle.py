@@ -112,3 +112,44 @@ def solve_reference_cpu(dims, parent, data, smooth=None, alpha=None, iterations=
         raise FileNotFoundError("reference CPU library not built (reference sources absent)")
     return _call(lib, "oracle_ref_hmf_solve", REF_CPU, 32, 1, dims, parent, data, smooth, alpha,
                  iterations, step, cc, want_sink, want_div)
+
+
+def adjoint(dims, parent, data, truth, smooth=None, alpha=None, iterations=20, step=0.1, cc=0.25, eps=1e-6,
+            precision=64, threads=0):
+    """Loss -(1/V) sum log(max(u_truth, eps)) of the REF_CUDA solve and its
+    gradients (oracle restatement of the adjoint).  truth: int32 [VZ, VY, VX]
+    class index into the DFS pre-order leaf list.  Returns
+    {"loss", "dD": [n, VZ, VY, VX], "dalpha": [n], "u": [n, VZ, VY, VX]}."""
+    lib = port_library()
+    fn = lib.oracle_hmf_adjoint
+    fn.restype = ctypes.c_int
+    vx, vy, vz = (int(d) for d in dims)
+    n = len(parent)
+    V = vx * vy * vz
+    par = (ctypes.c_int * n)(*[int(p) for p in parent])
+    keep = []
+    dptr = (ctypes.c_void_p * n)()
+    sptr = (ctypes.c_void_p * n)()
+    for v in range(n):
+        if data.get(v) is not None:
+            a = np.ascontiguousarray(data[v], dtype=np.float32).reshape(-1)
+            keep.append(a)
+            dptr[v] = a.ctypes.data
+        if smooth and smooth.get(v) is not None:
+            a = np.ascontiguousarray(smooth[v], dtype=np.float32).reshape(-1)
+            keep.append(a)
+            sptr[v] = a.ctypes.data
+    al = (ctypes.c_double * n)(*[float((alpha or {}).get(v, 1.0)) for v in range(n)])
+    tr = np.ascontiguousarray(truth, dtype=np.int32).reshape(-1)
+    loss = ctypes.c_double()
+    dD = np.zeros((n, V), np.float64)
+    da = np.zeros(n, np.float64)
+    u = np.zeros((n, V), np.float64)
+    rc = fn(int(precision), int(threads), vx, vy, vz, n, par, dptr, sptr, al, int(iterations), ctypes.c_float(step),
+            ctypes.c_float(cc), tr.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(eps), ctypes.byref(loss),
+            dD.ctypes.data_as(ctypes.c_void_p), da.ctypes.data_as(ctypes.c_void_p),
+            u.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("oracle adjoint failed (%d): %s" % (rc, lib.oracle_last_error().decode()))
+    shape = (n, vz, vy, vx)
+    return {"loss": loss.value, "dD": dD.reshape(shape), "dalpha": da, "u": u.reshape(shape)}

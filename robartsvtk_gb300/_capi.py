@@ -51,6 +51,10 @@ SIGNATURES = [
     ("hmf_batch_get_labels", _I, [_P, _I, _I, _P, _I, _P]),
     ("hmf_batch_get_sink", _I, [_P, _I, _I, _P, _I, _P]),
     ("hmf_autotune", _I, [_P, _P]),
+    ("hmf_solve_adjoint", _I, [_P, _P, _I, _I, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _P]),
+    ("hmf_get_data_gradient", _I, [_P, _I, _P, _I, _P]),
+    ("hmf_get_alpha_gradient", _I, [_P, ctypes.POINTER(ctypes.c_double), _I]),
+    ("hmf_get_adjoint_plan", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("hmf_solve_noalloc", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                ctypes.POINTER(ctypes.c_double), _I, ctypes.c_float, ctypes.c_float,
                                ctypes.POINTER(_P), _P]),

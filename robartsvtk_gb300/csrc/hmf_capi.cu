@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "../../include/hmf.h"
+#include "hmf_ctx.hpp"
 #include "hmf_flow_tma.cuh"
 #include "hmf_kernels.cuh"
 #include "hmf_tree_bulk.cuh"
@@ -44,84 +45,7 @@ constexpr int kTreeThreads = 256;
 
 }  // namespace
 
-struct hmf_ctx {
-  int device = 0;
-  int semantics = HMF_SEMANTICS_REF_CUDA;
-  int sm_count = 0;
-
-  // volumes, back to back in every per-vertex array
-  struct Volume {
-    int vx, vy, vz, pitch;
-    long long plane, vol, off;  // elements: plane, whole block, offset of the block
-  };
-  std::vector<Volume> vols;
-  long long total = 0;
-  hmf::Geometry geo{};  // per-voxel view of the concatenation (pitch 0 for batches)
-
-  // tree
-  int n = 0, root = -1;
-  std::vector<int> parent;
-  std::vector<std::vector<int>> kids;
-  std::vector<int> preorder, postorder, leaves;  // leaves in DFS pre-order
-
-  // parameters (vtkHierarchicalMaxFlowSegmentation.cxx:57-59)
-  int iterations = 100;
-  float step = 0.1f;
-  float cc = 0.25f;
-  std::vector<double> alpha;
-
-  struct Input {
-    const float* ptr = nullptr;
-    int where = HMF_HOST;
-  };
-  std::vector<std::vector<Input>> data, smooth;  // [volume][vertex]
-
-  // device state
-  char* arena = nullptr;
-  size_t arena_bytes = 0;
-  std::vector<float*> sink, label, div;
-  std::vector<float*> fx[2], fy[2], fz[2];
-  // input staging
-  char* staging = nullptr;
-  size_t staging_bytes = 0;
-  hmf::FlowVertex* d_flow[2] = {nullptr, nullptr};  // shared-memory ring flow kernel (one volume)
-  hmf::FlowVertexTMA* d_tma = nullptr;              // TMA flow kernel, [volume][non-root vertex]
-  hmf::FlowVolume* d_fvol = nullptr;
-  hmf::FlowItem* d_items = nullptr;
-  int n_items = 0;
-  int zchunk = 0;  // planes per window column (0: not planned yet)
-  hmf::TreeTable* d_tree = nullptr;
-  bool use_tma = true;  // flow_tma_kernel (else the shared-memory ring flow_kernel)
-  int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
-  const float** d_smooth_list = nullptr;
-  int* d_error = nullptr;
-  int n_smooth_list = 0;
-
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev_join = nullptr;
-  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
-  cudaGraphExec_t graph_pair = nullptr;  // two iterations (both flow parities)
-  cudaGraphExec_t graph_one = nullptr;   // one iteration, parity 0
-
-  bool timing = false;
-  long long launches = 0;
-  double kind_ms[3] = {0, 0, 0};
-  long long kind_count[3] = {0, 0, 0};
-  bool solved = false;
-
-  // host copies of the device tables (kept per context: pageable-memory
-  // cudaMemcpyAsync stages them before returning)
-  std::vector<hmf::FlowVertex> h_flow;
-  std::vector<hmf::FlowVertexTMA> h_tma;
-  std::vector<hmf::FlowVolume> h_fvol;
-  std::vector<hmf::FlowItem> h_items;
-  hmf::TreeTable h_tree{};
-  std::vector<const float*> h_smooth_list;
-
-  std::string err;
-};
-
-namespace {
+namespace hmfi {
 
 int fail(hmf_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -133,25 +57,6 @@ int cuda_fail(hmf_ctx* c, cudaError_t e, const char* what) {
   return fail(c, e == cudaErrorMemoryAllocation ? HMF_ERR_OUT_OF_MEMORY : HMF_ERR_CUDA,
               std::string(what) + ": " + cudaGetErrorString(e));
 }
-
-#define CK(call, what)                                  \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
-  } while (0)
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int d) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != d) cudaSetDevice(d);
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
-
-size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 int build_tree(hmf_ctx* c, const int* par, int n) {
   if (!par) return fail(c, HMF_ERR_TREE, "tree parent array is NULL");
@@ -345,11 +250,6 @@ int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ct
 // and one smoothness array per group of vertices that use the same image in
 // every volume.  A single dense, 16-byte aligned device input is used in
 // place; everything else is copied into pitched staging blocks.
-struct Staged {
-  std::vector<const float*> data;        // [vertex], leaves only
-  std::vector<const float*> smooth;      // [vertex], base of its smoothness group (or null)
-  std::vector<const float*> distinct;    // bases of the smoothness groups
-};
 
 int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out) {
   const size_t arr = round_up((size_t)c->total * sizeof(float), 256);
@@ -695,6 +595,18 @@ int configure_kernels(hmf_ctx* c) {
 bool valid_vertex(const hmf_ctx* c, int v) { return c && v >= 0 && v < c->n; }
 bool valid_volume(const hmf_ctx* c, int b) { return c && b >= 0 && b < (int)c->vols.size(); }
 
+int check_error_flag(hmf_ctx* c) {
+  int flag = 0;
+  CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  if (flag & 4) return fail(c, HMF_ERR_CUDA, "shared-memory staging area misaligned; results are invalid");
+  if (flag & 2) return fail(c, HMF_ERR_CUDA, "an asynchronous-copy wait timed out; results are invalid");
+  if (flag & 1)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT,
+                "Data prior and smoothness must be non-negative (the solve ran on invalid input)");
+  if (flag & 8) return fail(c, HMF_ERR_INVALID_ARGUMENT, "a ground-truth class index is not a leaf index");
+  return HMF_OK;
+}
+
 int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* stream) {
   if (!out) return fail(c, HMF_ERR_INVALID_ARGUMENT, "output pointer is NULL");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
@@ -707,13 +619,7 @@ int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* s
      "cudaMemcpy2DAsync(output)");
   if (where == HMF_HOST) {
     CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(output)");
-    int flag = 0;
-    CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
-    if (flag & 4) return fail(c, HMF_ERR_CUDA, "shared-memory staging area misaligned; results are invalid");
-    if (flag & 2) return fail(c, HMF_ERR_CUDA, "an asynchronous-copy wait timed out; results are invalid");
-    if (flag & 1)
-      return fail(c, HMF_ERR_INVALID_ARGUMENT,
-                  "Data prior and smoothness must be non-negative (the solve ran on invalid input)");
+    return check_error_flag(c);
   }
   return HMF_OK;
 }
@@ -728,7 +634,42 @@ std::string tune_key(const hmf_ctx* c) {
   return k;
 }
 
-}  // namespace
+int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged) {
+  for (size_t b = 0; b < c->vols.size(); ++b)
+    for (int l : c->leaves)
+      if (!c->data[b][l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
+  cudaStream_t s = c->stream;
+  c->launches = 0;
+  for (int k = 0; k < 3; ++k) c->kind_ms[k] = 0, c->kind_count[k] = 0;
+  c->solved = false;
+  // order after the caller's queued work
+  CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
+  CK(cudaStreamWaitEvent(s, c->ev_join, 0), "cudaStreamWaitEvent(join)");
+  CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), s), "cudaMemsetAsync(error flag)");
+  int rc = stage_inputs(c, s, staged);
+  if (!rc) rc = prepare_tables(c, s, staged);
+  if (rc) return rc;
+  // flows of parity 0 start at zero
+  const size_t bytes = (size_t)c->total * sizeof(float);
+  for (int v = 0; v < c->n; ++v) {
+    if (v == c->root) continue;
+    CK(cudaMemsetAsync(c->fx[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
+    CK(cudaMemsetAsync(c->fy[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
+    CK(cudaMemsetAsync(c->fz[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
+  }
+  return timed(c, 2, s, do_init, 0);
+}
+
+int end_solve(hmf_ctx* c, cudaStream_t user) {
+  CK(cudaEventRecord(c->ev_join, c->stream), "cudaEventRecord(done)");
+  CK(cudaStreamWaitEvent(user, c->ev_join, 0), "cudaStreamWaitEvent(done)");
+  c->solved = true;
+  return HMF_OK;
+}
+
+}  // namespace hmfi
+
+using namespace hmfi;
 
 extern "C" {
 
@@ -851,6 +792,7 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_t0) cudaEventDestroy(c->ev_t0);
   if (c->ev_t1) cudaEventDestroy(c->ev_t1);
+  adjoint_free(c);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return HMF_OK;
@@ -910,31 +852,11 @@ int hmf_set_params(hmf_ctx* c, int iterations, float step_size, float cc) {
 
 int hmf_solve(hmf_ctx* c, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
-  for (size_t b = 0; b < c->vols.size(); ++b)
-    for (int l : c->leaves)
-      if (!c->data[b][l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
   DeviceGuard dg(c->device);
   cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
   cudaStream_t s = c->stream;
-  c->launches = 0;
-  for (int k = 0; k < 3; ++k) c->kind_ms[k] = 0, c->kind_count[k] = 0;
-  // order after the caller's queued work
-  CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
-  CK(cudaStreamWaitEvent(s, c->ev_join, 0), "cudaStreamWaitEvent(join)");
-  CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), s), "cudaMemsetAsync(error flag)");
   Staged staged;
-  int rc = stage_inputs(c, s, staged);
-  if (!rc) rc = prepare_tables(c, s, staged);
-  if (rc) return rc;
-  // flows of parity 0 start at zero
-  const size_t bytes = (size_t)c->total * sizeof(float);
-  for (int v = 0; v < c->n; ++v) {
-    if (v == c->root) continue;
-    CK(cudaMemsetAsync(c->fx[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
-    CK(cudaMemsetAsync(c->fy[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
-    CK(cudaMemsetAsync(c->fz[0][v], 0, bytes, s), "cudaMemsetAsync(flows)");
-  }
-  rc = timed(c, 2, s, do_init, 0);
+  int rc = begin_solve(c, user, staged);
   if (rc) return rc;
   if (c->semantics == HMF_SEMANTICS_REF_CPU) {
     rc = timed(c, 1, s, do_refcpu, 0);
@@ -961,10 +883,7 @@ int hmf_solve(hmf_ctx* c, void* stream) {
     }
   }
   // final flows live in set (iterations & 1); nothing else depends on parity
-  CK(cudaEventRecord(c->ev_join, s), "cudaEventRecord(done)");
-  CK(cudaStreamWaitEvent(user, c->ev_join, 0), "cudaStreamWaitEvent(done)");
-  c->solved = true;
-  return HMF_OK;
+  return end_solve(c, user);
 }
 
 int hmf_autotune(hmf_ctx* c, void* stream) {
@@ -1039,7 +958,7 @@ int hmf_leaf_order(const hmf_ctx* c, int* out, int cap) {
 
 size_t hmf_device_bytes(const hmf_ctx* c) {
   if (!c) return 0;
-  return c->arena_bytes + c->staging_bytes + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
+  return c->arena_bytes + c->staging_bytes + adjoint_bytes(c) + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
          sizeof(hmf::FlowVertexTMA) * c->vols.size() * (c->n - 1) + sizeof(hmf::TreeTable) +
          sizeof(hmf::FlowItem) * c->h_items.size();
 }

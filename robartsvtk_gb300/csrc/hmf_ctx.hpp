@@ -1,0 +1,143 @@
+// hmf_ctx.hpp -- the solver context behind the opaque hmf_ctx handle of
+// include/hmf.h, and the forward-solve helpers that the translation units of
+// the library share (hmf_capi.cu defines them; hmf_adjoint.cu reuses them).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/hmf.h"
+#include "hmf_types.cuh"
+
+struct hmf_ctx {
+  int device = 0;
+  int semantics = HMF_SEMANTICS_REF_CUDA;
+  int sm_count = 0;
+
+  // volumes, back to back in every per-vertex array
+  struct Volume {
+    int vx, vy, vz, pitch;
+    long long plane, vol, off;  // elements: plane, whole block, offset of the block
+  };
+  std::vector<Volume> vols;
+  long long total = 0;
+  hmf::Geometry geo{};  // per-voxel view of the concatenation (pitch 0 for batches)
+
+  // tree
+  int n = 0, root = -1;
+  std::vector<int> parent;
+  std::vector<std::vector<int>> kids;
+  std::vector<int> preorder, postorder, leaves;  // leaves in DFS pre-order
+
+  // parameters (vtkHierarchicalMaxFlowSegmentation.cxx:57-59)
+  int iterations = 100;
+  float step = 0.1f;
+  float cc = 0.25f;
+  std::vector<double> alpha;
+
+  struct Input {
+    const float* ptr = nullptr;
+    int where = HMF_HOST;
+  };
+  std::vector<std::vector<Input>> data, smooth;  // [volume][vertex]
+
+  // device state
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  std::vector<float*> sink, label, div;
+  std::vector<float*> fx[2], fy[2], fz[2];
+  // input staging
+  char* staging = nullptr;
+  size_t staging_bytes = 0;
+  hmf::FlowVertex* d_flow[2] = {nullptr, nullptr};  // shared-memory ring flow kernel (one volume)
+  hmf::FlowVertexTMA* d_tma = nullptr;              // TMA flow kernel, [volume][non-root vertex]
+  hmf::FlowVolume* d_fvol = nullptr;
+  hmf::FlowItem* d_items = nullptr;
+  int n_items = 0;
+  int zchunk = 0;  // planes per window column (0: not planned yet)
+  hmf::TreeTable* d_tree = nullptr;
+  bool use_tma = true;  // flow_tma_kernel (else the shared-memory ring flow_kernel)
+  int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
+  const float** d_smooth_list = nullptr;
+  int* d_error = nullptr;
+  int n_smooth_list = 0;
+
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_join = nullptr;
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+  cudaGraphExec_t graph_pair = nullptr;  // two iterations (both flow parities)
+  cudaGraphExec_t graph_one = nullptr;   // one iteration, parity 0
+
+  bool timing = false;
+  long long launches = 0;
+  double kind_ms[3] = {0, 0, 0};
+  long long kind_count[3] = {0, 0, 0};
+  bool solved = false;
+
+  // host copies of the device tables (kept per context: pageable-memory
+  // cudaMemcpyAsync stages them before returning)
+  std::vector<hmf::FlowVertex> h_flow;
+  std::vector<hmf::FlowVertexTMA> h_tma;
+  std::vector<hmf::FlowVolume> h_fvol;
+  std::vector<hmf::FlowItem> h_items;
+  hmf::TreeTable h_tree{};
+  std::vector<const float*> h_smooth_list;
+
+  // reverse-mode state of hmf_solve_adjoint (hmf_adjoint.cu), created on demand
+  struct AdjointState* adj = nullptr;
+
+  std::string err;
+};
+
+namespace hmfi {
+
+int fail(hmf_ctx* c, int code, const std::string& msg);
+int cuda_fail(hmf_ctx* c, cudaError_t e, const char* what);
+
+#define CK(call, what)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int d) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Inputs as device arrays over the concatenation of the volumes.
+struct Staged {
+  std::vector<const float*> data;      // [vertex], leaves only
+  std::vector<const float*> smooth;    // [vertex], base of its smoothness group (or null)
+  std::vector<const float*> distinct;  // bases of the smoothness groups
+};
+
+// Joins the caller's stream, stages the inputs, writes the kernel tables,
+// zeroes the parity-0 flows and runs the initialisation kernel on c->stream.
+int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged);
+// Hands c->stream's work back to the caller's stream.
+int end_solve(hmf_ctx* c, cudaStream_t user);
+// One flow launch (reads flow set `parity`, writes the other) and one sweep.
+int launch_flow(hmf_ctx* c, int parity, cudaStream_t s);
+int launch_tree(hmf_ctx* c, cudaStream_t s);
+bool valid_vertex(const hmf_ctx* c, int v);
+bool valid_volume(const hmf_ctx* c, int b);
+// Error flag set by the kernels (bit 0 negative input, 1 wait time-out,
+// 2 misaligned staging, 3 label index out of range), as a status.
+int check_error_flag(hmf_ctx* c);
+
+// hmf_adjoint.cu
+void adjoint_free(hmf_ctx* c);
+size_t adjoint_bytes(const hmf_ctx* c);
+
+}  // namespace hmfi

@@ -28,60 +28,6 @@
 
 namespace hmf {
 
-constexpr int kTmaBoxX = 36;   // box width: 16-byte aligned start plus 32 lanes plus 1
-constexpr int kTmaRows = 32;   // window rows
-constexpr int kTmaPlane = kTmaBoxX * kTmaRows;        // floats per staged array plane
-// Two rings.  The z flow of plane k+1 is needed one step early (the divergence
-// of plane k), everything else only in its own step, so the main ring (px, py,
-// sink, label, parent sink, smoothness) has 3 slots and the pz ring 4: either
-// way two planes are in flight while one is computed.
-constexpr int kTmaMainArrays = 6;
-constexpr int kTmaMainSlots = 3;
-constexpr int kTmaPzSlots = 4;
-constexpr int kTmaMaxOutX = 28;
-constexpr int kTmaMaxOutY = 27;
-constexpr int kTmaThreads = 256;
-constexpr int kTmaSmemBytes =
-                              (kTmaMainSlots * kTmaMainArrays + kTmaPzSlots) * kTmaPlane * 4 +
-                              (3 * 256 + 2 * 256) * 4 + 64;
-
-struct FlowVertexTMA {  // 64-byte aligned through its CUtensorMap members
-  CUtensorMap flow_in[2][3];  // [parity][axis]: flows read in iterations of that parity
-  CUtensorMap sink, label, inc, smooth;
-  float* flow_out[2][3];      // [parity][axis]: flows written in iterations of that parity
-  float* div;
-  float alpha;
-  int has_smooth;
-};
-
-// One volume of a solve (a batch holds several of different sizes).
-struct FlowVolume {
-  Geometry G;
-  int tiles_x;  // windows across x
-  int out_x;    // output columns per window (<= 28)
-  int out_y;    // output rows per window (<= 27)
-  int zchunk;   // planes per window column
-};
-
-// One CTA's work: a window column (tile, z chunk) of one volume; the vertex is
-// blockIdx.x % n_vertices.
-struct FlowItem {
-  int vol;
-  int tile;
-  int zc;
-  int pad_;
-};
-
-struct FlowTmaParams {
-  float step;
-  float icc;
-  int parity;
-  int n_vertices;  // non-root vertices (grid.x = n_vertices * items)
-  const FlowVolume* vols;
-  const FlowItem* items;
-  int* error_flag;
-};
-
 template <bool B>
 struct BoolTag {
   static constexpr bool value = B;

@@ -21,67 +21,9 @@
 // FP32 CPU restatement of those kernels exactly.
 #pragma once
 
-#include <cuda_runtime.h>
-#include <stdint.h>
+#include "hmf_types.cuh"
 
 namespace hmf {
-
-constexpr int kMaxVertices = 64;
-
-// Per non-root vertex, one iteration parity (flows ping-pong between two sets
-// because a CTA reads flows of its neighbours' tiles).
-struct FlowVertex {
-  const float* px_in;
-  const float* py_in;
-  const float* pz_in;
-  float* px_out;
-  float* py_out;
-  float* pz_out;
-  const float* sink;    // own sink flow, previous iteration
-  const float* inc;     // parent's sink (or the source flow), previous iteration
-  const float* label;   // own label, previous iteration
-  const float* smooth;  // per-voxel smoothness or nullptr (S == 1)
-  float* div;           // out: divergence of the projected flows
-  float alpha;
-  int pad_;
-};
-
-struct Geometry {
-  int vx, vy, vz;
-  int pitch;        // floats per row (vx rounded up to a multiple of 4)
-  long long plane;  // pitch * vy
-  long long vol;    // plane * vz (elements per array, padding included)
-};
-
-struct FlowParams {
-  float step;  // StepSize
-  float icc;   // 1.0f / CC, computed in float as the reference host does
-  int zchunk;  // planes per CTA
-  int tiles_x;
-};
-
-// Post-order tree table for the per-voxel sweep; entries 0..n-1, root last.
-struct TreeEntry {
-  float* sink;          // sink flow (root: source flow)
-  float* label;         // nullptr for the root
-  const float* div;     // nullptr for the root
-  const float* data;    // leaves: data term (capacity)
-  int parent;           // entry index of the parent, -1 for the root
-  int first_kid;        // into TreeTable::kids
-  int n_kids;
-  float inv_kids;       // 1.0f / (kids + 1) for branches, 1.0f / kids for the root
-};
-
-struct TreeTable {
-  int n;
-  int n_leaves;
-  float cc;
-  float icc;
-  float root_init;  // 1.0f / CC
-  int kids[kMaxVertices];
-  int leaves[kMaxVertices];  // entry indices of the leaves in DFS pre-order
-  TreeEntry e[kMaxVertices];
-};
 
 // ---------------------------------------------------------------------------
 // flow_kernel

@@ -1,0 +1,123 @@
+// hmf_types.cuh -- plain data types and launch constants shared by the
+// kernels (hmf_kernels.cuh, hmf_flow_tma.cuh, hmf_tree_bulk.cuh) and the host
+// code of the solver context.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hmf {
+
+constexpr int kMaxVertices = 64;
+
+// Per non-root vertex, one iteration parity (flows ping-pong between two sets
+// because a CTA reads flows of its neighbours' tiles).
+struct FlowVertex {
+  const float* px_in;
+  const float* py_in;
+  const float* pz_in;
+  float* px_out;
+  float* py_out;
+  float* pz_out;
+  const float* sink;    // own sink flow, previous iteration
+  const float* inc;     // parent's sink (or the source flow), previous iteration
+  const float* label;   // own label, previous iteration
+  const float* smooth;  // per-voxel smoothness or nullptr (S == 1)
+  float* div;           // out: divergence of the projected flows
+  float alpha;
+  int pad_;
+};
+
+struct Geometry {
+  int vx, vy, vz;
+  int pitch;        // floats per row (vx rounded up to a multiple of 4)
+  long long plane;  // pitch * vy
+  long long vol;    // plane * vz (elements per array, padding included)
+};
+
+struct FlowParams {
+  float step;  // StepSize
+  float icc;   // 1.0f / CC, computed in float as the reference host does
+  int zchunk;  // planes per CTA
+  int tiles_x;
+};
+
+// Post-order tree table for the per-voxel sweep; entries 0..n-1, root last.
+struct TreeEntry {
+  float* sink;          // sink flow (root: source flow)
+  float* label;         // nullptr for the root
+  const float* div;     // nullptr for the root
+  const float* data;    // leaves: data term (capacity)
+  int parent;           // entry index of the parent, -1 for the root
+  int first_kid;        // into TreeTable::kids
+  int n_kids;
+  float inv_kids;       // 1.0f / (kids + 1) for branches, 1.0f / kids for the root
+};
+
+struct TreeTable {
+  int n;
+  int n_leaves;
+  float cc;
+  float icc;
+  float root_init;  // 1.0f / CC
+  int kids[kMaxVertices];
+  int leaves[kMaxVertices];  // entry indices of the leaves in DFS pre-order
+  TreeEntry e[kMaxVertices];
+};
+
+constexpr int kTmaBoxX = 36;   // box width: 16-byte aligned start plus 32 lanes plus 1
+constexpr int kTmaRows = 32;   // window rows
+constexpr int kTmaPlane = kTmaBoxX * kTmaRows;        // floats per staged array plane
+// Two rings.  The z flow of plane k+1 is needed one step early (the divergence
+// of plane k), everything else only in its own step, so the main ring (px, py,
+// sink, label, parent sink, smoothness) has 3 slots and the pz ring 4: either
+// way two planes are in flight while one is computed.
+constexpr int kTmaMainArrays = 6;
+constexpr int kTmaMainSlots = 3;
+constexpr int kTmaPzSlots = 4;
+constexpr int kTmaMaxOutX = 28;
+constexpr int kTmaMaxOutY = 27;
+constexpr int kTmaThreads = 256;
+constexpr int kTmaSmemBytes =
+                              (kTmaMainSlots * kTmaMainArrays + kTmaPzSlots) * kTmaPlane * 4 +
+                              (3 * 256 + 2 * 256) * 4 + 64;
+
+struct FlowVertexTMA {  // 64-byte aligned through its CUtensorMap members
+  CUtensorMap flow_in[2][3];  // [parity][axis]: flows read in iterations of that parity
+  CUtensorMap sink, label, inc, smooth;
+  float* flow_out[2][3];      // [parity][axis]: flows written in iterations of that parity
+  float* div;
+  float alpha;
+  int has_smooth;
+};
+
+// One volume of a solve (a batch holds several of different sizes).
+struct FlowVolume {
+  Geometry G;
+  int tiles_x;  // windows across x
+  int out_x;    // output columns per window (<= 28)
+  int out_y;    // output rows per window (<= 27)
+  int zchunk;   // planes per window column
+};
+
+// One CTA's work: a window column (tile, z chunk) of one volume; the vertex is
+// blockIdx.x % n_vertices.
+struct FlowItem {
+  int vol;
+  int tile;
+  int zc;
+  int pad_;
+};
+
+struct FlowTmaParams {
+  float step;
+  float icc;
+  int parity;
+  int n_vertices;  // non-root vertices (grid.x = n_vertices * items)
+  const FlowVolume* vols;
+  const FlowItem* items;
+  int* error_flag;
+};
+
+}  // namespace hmf

@@ -122,6 +122,60 @@ class HMFSolver:
     def sink(self, node: int, out=None, stream=None):
         return self._fetch(self._lib.hmf_get_sink, node, out, stream)
 
+    # -- adjoint ----------------------------------------------------------
+    def solve_adjoint(self, truth, checkpoint_every: int = 0, eps: float = 1e-6, stream=None) -> float:
+        """Solve, then differentiate L = -(1/V) sum log(max(u_truth, eps)) of
+        the final leaf labels.  truth: int32 [VZ, VY, VX] indices into
+        `self.leaves` (numpy, or a torch tensor on the host or the device).
+        Returns L; gradients via data_gradient() / alpha_gradient()."""
+        if isinstance(truth, np.ndarray):
+            if truth.dtype != np.int32 or not truth.flags["C_CONTIGUOUS"] or truth.size != self.nvox:
+                raise TypeError("truth must be a C-contiguous int32 array of the volume's size")
+            ptr, where, keep = truth.ctypes.data, HMF_HOST, truth
+        else:
+            import torch
+
+            if truth.dtype != torch.int32 or not truth.is_contiguous() or truth.numel() != self.nvox:
+                raise TypeError("truth must be a contiguous int32 tensor of the volume's size")
+            ptr, where, keep = truth.data_ptr(), HMF_DEVICE if truth.is_cuda else HMF_HOST, truth
+        loss = ctypes.c_double()
+        check(self._lib.hmf_solve_adjoint(self._ctx, ptr, where, int(checkpoint_every), float(eps),
+                                          ctypes.byref(loss), _stream_handle(stream)), self._ctx)
+        del keep
+        return loss.value
+
+    def data_gradient(self, leaf: int, out=None, stream=None):
+        """dL/dD of a leaf's data term, float64 [VZ, VY, VX] (numpy, or a
+        float64 torch tensor given as `out`)."""
+        if out is None:
+            out = np.empty((self.dims[2], self.dims[1], self.dims[0]), dtype=np.float64)
+            ptr, where = out.ctypes.data, HMF_HOST
+        elif isinstance(out, np.ndarray):
+            if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != self.nvox:
+                raise TypeError("out must be a C-contiguous float64 array of the volume's size")
+            ptr, where = out.ctypes.data, HMF_HOST
+        else:
+            import torch
+
+            if out.dtype != torch.float64 or not out.is_contiguous() or out.numel() != self.nvox:
+                raise TypeError("out must be a contiguous float64 tensor of the volume's size")
+            ptr, where = out.data_ptr(), HMF_DEVICE if out.is_cuda else HMF_HOST
+        check(self._lib.hmf_get_data_gradient(self._ctx, int(leaf), ptr, where, _stream_handle(stream)), self._ctx)
+        return out
+
+    def alpha_gradient(self) -> np.ndarray:
+        """dL/dalpha per vertex id (the root reads 0)."""
+        buf = (ctypes.c_double * len(self.parent))()
+        rc = self._lib.hmf_get_alpha_gradient(self._ctx, buf, len(self.parent))
+        check(min(rc, 0), self._ctx)
+        return np.array(buf[:], dtype=np.float64)
+
+    def adjoint_plan(self) -> dict:
+        k = ctypes.c_int()
+        r = ctypes.c_int()
+        check(self._lib.hmf_get_adjoint_plan(self._ctx, ctypes.byref(k), ctypes.byref(r)), self._ctx)
+        return {"checkpoint_every": k.value, "recomputed_segments": r.value}
+
     def stats(self):
         launches = ctypes.c_longlong()
         ms = (ctypes.c_double * 3)()
