@@ -1,24 +1,33 @@
 // hmf_adjoint.cu -- hmf_solve_adjoint and the gradient getters of
 // include/hmf.h (no counterpart in the reference, which only solves forward).
 //
-// Forward: the solver's own kernels (flow_tma_kernel / tree_bulk_kernel),
-// one iteration at a time, with the state (flows, sinks, labels) copied into
-// a checkpoint slot every k iterations.  Backward: segment by segment from
-// the last, the segment's states are recomputed from its checkpoint with the
-// same forward kernels (bit-identical to the first pass) and kept in segment
-// slots, then the backward steps of hmf_adjoint.cuh run from the last
-// iteration of the segment to its first.  With k >= iterations (the default
-// when HBM holds every state) nothing is recomputed: the forward pass keeps
-// all states.  Memory: (ceil(T/k) + k + 1) state slots of 5(n-1)+1 arrays
-// each, plus 8n + 11 float arrays and one double array per leaf.
+// Forward: the solver's own kernels (flow_tma_kernel, tree_bulk_kernel) run
+// over per-iteration tables that read the state of iteration t from its slot
+// and write the state of t+1 into the next slot, so keeping a state costs no
+// copy.  States at multiples of k go to checkpoint slots C_m; the others go
+// to segment slots S_1..S_k (state a+j of the segment starting at a in S_j).
+// Backward: segment by segment from the last, the segment's inner states are
+// recomputed into S_j with the same tables (bit-identical to the first pass),
+// then one backward step per iteration runs from the segment's last
+// iteration to its first: adj_sweep_reg_kernel (trees of up to 8 vertices;
+// adj_tree_kernel beyond) reverses the sink/label sweep of all vertices, and
+// adj_flow_tma_kernel reverses the flow step of every vertex
+// (HMF_ADJOINT_KERNEL=chain selects adj_tree_kernel and the unfused
+// per-vertex kernels of hmf_adjoint.cuh instead; same results).  With k >= iterations (the default
+// when HBM holds every state) nothing is recomputed.  Memory:
+// (ceil(T/k) + k) slots of 6(n-1)+1 arrays, plus 13n+11 float arrays and one
+// double array per leaf.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
 #include "hmf_adjoint.cuh"
+#include "hmf_adjoint_flow.cuh"
+#include "hmf_adjoint_sweep.cuh"
 #include "hmf_ctx.hpp"
 
 using namespace hmfi;
@@ -32,25 +41,40 @@ constexpr int kAdjTemps = 11;  // g, ppx, ppy, ppz, m, Fm, F2b, qx, qy, qz, dbo
 
 struct AdjointState {
   int k = 0, iterations = 0;
-  int A = 0;           // arrays per state slot
-  long long arr = 0;   // floats per array (multiple of 64)
+  int A = 0;          // arrays per state slot
+  long long arr = 0;  // floats per array (multiple of 64)
   int n_ckpt = 0, n_seg = 0;
-  bool has_fin = false;
   char* arena = nullptr;
   size_t bytes = 0;
-  float* ckpt = nullptr;  // n_ckpt slots: states 0, k, 2k, ...
-  float* seg = nullptr;   // n_seg slots: states a+1 .. b of the segment [a, b)
-  float* fin = nullptr;   // the final state, restored after a recomputing backward pass
-  float* sb[2] = {nullptr, nullptr};  // [v*arr] sink adjoints (ping-pong)
-  float* ub[2] = {nullptr, nullptr};  // [v*arr] label adjoints
+  float* slots = nullptr;             // C_0..C_{n_ckpt-1}, S_1..S_k
+  float* sb[2] = {nullptr, nullptr};  // [v*arr] sweep part of the sinks' adjoint (ping-pong)
+  float* ub[2] = {nullptr, nullptr};  // [v*arr] sweep part of the labels' adjoint
+  float* gb = nullptr;                // [v*arr] adjoint of g of the flow reverse
   float* dbp = nullptr;               // [v*arr]
-  float* Pb = nullptr;                // [(3v+axis)*arr]
+  float* Pb = nullptr;                // [((parity*n + v)*3 + axis)*arr], two sets
+  int pb_par = 0;                     // the set holding the current adjoint of the flows
   float* tmp = nullptr;               // kAdjTemps arrays
   double* Db = nullptr;               // [leaf index * arr]
   int* truth = nullptr;               // dense class indices
   double* scal = nullptr;             // [0] loss, [1 + v] alpha gradient
-  const float** d_ctx = nullptr;      // [parity * A + j] solver array j
+  const float** d_ctx = nullptr;      // solver arrays in slot order (null: not copied)
   hmf::AdjTree* d_tree = nullptr;
+  // per-transition forward tables: iteration t reads slot src(t), writes dst(t)
+  hmf::FlowVertexTMA* d_tflow = nullptr;  // [t][n-1]
+  hmf::TreeTable* d_ttree = nullptr;      // [t]
+  int table_cap = 0;
+  std::vector<hmf::FlowVertexTMA> h_tflow;
+  std::vector<hmf::TreeTable> h_ttree;
+  // reverse flow kernel: tables per state slot, its own window plan
+  hmf::AdjFlowVertex* d_aflow = nullptr;  // [slot][n-1]
+  int aflow_cap = 0;
+  std::vector<hmf::AdjFlowVertex> h_aflow;
+  hmf::FlowVolume* d_avol = nullptr;
+  hmf::FlowItem* d_aitems = nullptr;
+  int n_aitems = 0, aitems_cap = 0;
+  hmf::FlowVolume h_avol{};
+  std::vector<hmf::FlowItem> h_aitems;
+  bool chain = false;  // unfused per-vertex reverse kernels and the scalar sweep reverse
   bool done = false;
   double loss = 0.0;
   std::vector<double> alpha_grad;
@@ -62,13 +86,30 @@ namespace {
 
 // state-slot array index of the sink of vertex v (non-root j-th in id order)
 int slot_base(const hmf_ctx* c, int v) {
-  if (v == c->root) return 5 * (c->n - 1);
+  if (v == c->root) return hmf::kAdjPerVertex * (c->n - 1);
   int j = 0;
   for (int u = 0; u < v; ++u) j += u != c->root;
-  return 5 * j;
+  return hmf::kAdjPerVertex * j;
 }
 
-float* slot_ptr(const AdjointState* S, float* base, int slot) { return base + (size_t)slot * S->A * S->arr; }
+float* slot_ptr(const AdjointState* S, int slot) { return S->slots + (size_t)slot * S->A * S->arr; }
+float* slot_array(const AdjointState* S, int slot, int index) {
+  return slot_ptr(S, slot) + (size_t)index * S->arr;
+}
+
+// slot ids: C_m = m, S_j = n_ckpt + j - 1 (j >= 1)
+int ckpt_id(const AdjointState* S, int m) { return m; }
+int seg_id(const AdjointState* S, int j) { return S->n_ckpt + j - 1; }
+// the slots iteration t reads and writes
+int src_slot(const AdjointState* S, int t) {
+  const int a = (t / S->k) * S->k;
+  return t == a ? ckpt_id(S, a / S->k) : seg_id(S, t - a);
+}
+int dst_slot(const AdjointState* S, int t) {
+  const int a = (t / S->k) * S->k;
+  if ((t + 1) % S->k == 0 && t + 1 < S->iterations) return ckpt_id(S, (t + 1) / S->k);
+  return seg_id(S, t + 1 - a);
+}
 
 int grid_for(const hmf_ctx* c, long long n) {
   return (int)std::max<long long>(1, std::min<long long>((n + kAdjThreads - 1) / kAdjThreads, (long long)c->sm_count * 16));
@@ -77,25 +118,23 @@ int grid_for(const hmf_ctx* c, long long n) {
 int plan(hmf_ctx* c, int T, int k_req) {
   AdjointState* S = c->adj;
   const long long arr = (long long)round_up((size_t)c->total, 64);
-  const int A = 5 * (c->n - 1) + 1;
+  const int A = hmf::kAdjPerVertex * (c->n - 1) + 1;
   const size_t slot_bytes = (size_t)A * arr * sizeof(float);
   const int L = (int)c->leaves.size();
-  const size_t fixed = ((size_t)(8 * c->n + kAdjTemps) * arr) * sizeof(float) + (size_t)L * arr * sizeof(double) +
+  const size_t fixed = ((size_t)(13 * c->n + kAdjTemps) * arr) * sizeof(float) + (size_t)L * arr * sizeof(double) +
                        (size_t)arr * sizeof(int) + 4096;
   int k = k_req;
   if (k <= 0) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
-    const size_t held = S->bytes;  // reusable
-    const double budget = 0.85 * (double)(free_b + held);
+    const double budget = 0.85 * (double)(free_b + S->bytes);  // the held arena is reusable
     k = (double)(T + 1) * slot_bytes + fixed <= budget ? std::max(T, 1)
                                                        : std::max(1, (int)std::ceil(std::sqrt((double)T)));
   }
   k = std::max(1, std::min(k, std::max(T, 1)));
   const int n_ckpt = std::max(1, (T + k - 1) / k);
   const int n_seg = k;
-  const bool has_fin = n_ckpt > 1;
-  const size_t need = (size_t)(n_ckpt + n_seg + (has_fin ? 1 : 0)) * slot_bytes + fixed;
+  const size_t need = (size_t)(n_ckpt + n_seg) * slot_bytes + fixed;
   if (need > S->bytes) {
     if (S->arena) cudaFree(S->arena);
     S->arena = nullptr;
@@ -110,61 +149,219 @@ int plan(hmf_ctx* c, int T, int k_req) {
   S->arr = arr;
   S->n_ckpt = n_ckpt;
   S->n_seg = n_seg;
-  S->has_fin = has_fin;
   char* p = S->arena;
   auto takef = [&](size_t arrays) {
     float* r = reinterpret_cast<float*>(p);
     p += arrays * arr * sizeof(float);
     return r;
   };
-  S->ckpt = takef((size_t)n_ckpt * A);
-  S->seg = takef((size_t)n_seg * A);
-  S->fin = has_fin ? takef(A) : nullptr;
+  S->slots = takef((size_t)(n_ckpt + n_seg) * A);
   for (int q = 0; q < 2; ++q) S->sb[q] = takef(c->n);
   for (int q = 0; q < 2; ++q) S->ub[q] = takef(c->n);
+  S->gb = takef(c->n);
   S->dbp = takef(c->n);
-  S->Pb = takef(3 * (size_t)c->n);
+  S->Pb = takef(6 * (size_t)c->n);
   S->tmp = takef(kAdjTemps);
   S->Db = reinterpret_cast<double*>(p);
   p += (size_t)L * arr * sizeof(double);
   S->truth = reinterpret_cast<int*>(p);
+  if (T > S->table_cap) {
+    if (S->d_tflow) cudaFree(S->d_tflow);
+    if (S->d_ttree) cudaFree(S->d_ttree);
+    S->d_tflow = nullptr;
+    S->d_ttree = nullptr;
+    S->table_cap = 0;
+    CK(cudaMalloc(&S->d_tflow, sizeof(hmf::FlowVertexTMA) * (size_t)T * (c->n - 1)), "cudaMalloc(adjoint flow tables)");
+    CK(cudaMalloc(&S->d_ttree, sizeof(hmf::TreeTable) * (size_t)T), "cudaMalloc(adjoint tree tables)");
+    S->table_cap = T;
+  }
+  const int n_slots = n_ckpt + n_seg;
+  if (n_slots > S->aflow_cap) {
+    if (S->d_aflow) cudaFree(S->d_aflow);
+    S->d_aflow = nullptr;
+    S->aflow_cap = 0;
+    CK(cudaMalloc(&S->d_aflow, sizeof(hmf::AdjFlowVertex) * (size_t)n_slots * (c->n - 1)),
+       "cudaMalloc(adjoint reverse tables)");
+    S->aflow_cap = n_slots;
+  }
   return HMF_OK;
 }
 
-int copy_state(hmf_ctx* c, float* slot, int parity, bool to_slot, cudaStream_t s) {
+float* pb_array(const AdjointState* S, const hmf_ctx* c, int parity, int v, int axis) {
+  return S->Pb + ((size_t)(parity * c->n + v) * 3 + axis) * S->arr;
+}
+
+// Windows of at most 27 x 27 outputs spread evenly over the volume; z chunk:
+// the longest power of two (16 .. 64) that still gives two waves of one CTA
+// per SM.
+int plan_reverse(hmf_ctx* c, cudaStream_t s) {
+  AdjointState* S = c->adj;
+  const auto& V = c->vols[0];
+  hmf::FlowVolume& F = S->h_avol;
+  F.G = c->geo;
+  const int nx = (V.vx + hmf::kAfMaxOut - 1) / hmf::kAfMaxOut;
+  const int ny = (V.vy + hmf::kAfMaxOut - 1) / hmf::kAfMaxOut;
+  F.out_x = (V.vx + nx - 1) / nx;
+  F.out_y = (V.vy + ny - 1) / ny;
+  F.tiles_x = nx;
+  int z = 64;
+  while (z > 16 && (long long)nx * ny * ((V.vz + z - 1) / z) * (c->n - 1) < 2LL * c->sm_count) z /= 2;
+  F.zchunk = std::min(z, V.vz);
+  const int chunks = (V.vz + F.zchunk - 1) / F.zchunk;
+  S->h_aitems.clear();
+  for (int zc = 0; zc < chunks; ++zc)
+    for (int t = 0; t < nx * ny; ++t) S->h_aitems.push_back(hmf::FlowItem{0, t, zc, 0});
+  S->n_aitems = (int)S->h_aitems.size();
+  if (!S->d_avol) CK(cudaMalloc(&S->d_avol, sizeof(hmf::FlowVolume)), "cudaMalloc(reverse volume table)");
+  if (S->n_aitems > S->aitems_cap) {
+    if (S->d_aitems) cudaFree(S->d_aitems);
+    S->d_aitems = nullptr;
+    S->aitems_cap = 0;
+    CK(cudaMalloc(&S->d_aitems, sizeof(hmf::FlowItem) * S->n_aitems), "cudaMalloc(reverse work items)");
+    S->aitems_cap = S->n_aitems;
+  }
+  CK(cudaMemcpyAsync(S->d_avol, &F, sizeof(F), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(reverse volume table)");
+  CK(cudaMemcpyAsync(S->d_aitems, S->h_aitems.data(), sizeof(hmf::FlowItem) * S->n_aitems, cudaMemcpyHostToDevice,
+                     s),
+     "cudaMemcpyAsync(reverse work items)");
+  return HMF_OK;
+}
+
+// Reverse-kernel tables, one per state slot (the state before the iteration).
+int build_reverse_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
+  AdjointState* S = c->adj;
+  const int nv = c->n - 1, n_slots = S->n_ckpt + S->n_seg;
+  const auto& V = c->vols[0];
+  const int rows = hmf::kAfBoxY;
+  S->h_aflow.assign((size_t)n_slots * nv, hmf::AdjFlowVertex{});
+  for (int sl = 0; sl < n_slots; ++sl) {
+    int j = 0;
+    for (int v = 0; v < c->n; ++v) {
+      if (v == c->root) continue;
+      hmf::AdjFlowVertex& f = S->h_aflow[(size_t)sl * nv + j++];
+      std::memset(&f, 0, sizeof(f));
+      const int base = slot_base(c, v), pbase = slot_base(c, c->parent[v]);
+      int rc = encode_plane_map(c, &f.px, slot_array(S, sl, base + hmf::kAdjPx), V, rows);
+      if (!rc) rc = encode_plane_map(c, &f.py, slot_array(S, sl, base + hmf::kAdjPy), V, rows);
+      if (!rc) rc = encode_plane_map(c, &f.pz, slot_array(S, sl, base + hmf::kAdjPz), V, rows);
+      if (!rc) rc = encode_plane_map(c, &f.s, slot_array(S, sl, base + hmf::kAdjSink), V, rows);
+      if (!rc) rc = encode_plane_map(c, &f.c, slot_array(S, sl, pbase + hmf::kAdjSink), V, rows);
+      if (!rc) rc = encode_plane_map(c, &f.u, slot_array(S, sl, base + hmf::kAdjLabel), V, rows);
+      const bool has_s = staged.smooth[v] && c->smooth[0][v].ptr;
+      if (!rc && has_s) rc = encode_plane_map(c, &f.smooth, staged.smooth[v], V, rows);
+      for (int par = 0; par < 2 && !rc; ++par)
+        for (int ax = 0; ax < 3 && !rc; ++ax) {
+          rc = encode_plane_map(c, &f.pb[par][ax], pb_array(S, c, par, v, ax), V, rows);
+          f.pb_out[par][ax] = pb_array(S, c, par ^ 1, v, ax);
+        }
+      if (!rc) rc = encode_plane_map(c, &f.dbp, S->dbp + (size_t)v * S->arr, V, rows);
+      if (rc) return rc;
+      f.has_smooth = has_s;
+      f.gb = S->gb + (size_t)v * S->arr;
+      f.alpha_grad = S->scal + 1 + v;
+      f.alpha = (float)c->alpha[v];  // stored as float, as the reference does (.cxx:692)
+    }
+  }
+  CK(cudaMemcpyAsync(S->d_aflow, S->h_aflow.data(), sizeof(hmf::AdjFlowVertex) * S->h_aflow.size(),
+                     cudaMemcpyHostToDevice, s),
+     "cudaMemcpyAsync(adjoint reverse tables)");
+  return HMF_OK;
+}
+
+int copy_state(hmf_ctx* c, float* slot, bool to_slot, cudaStream_t s) {
   const AdjointState* S = c->adj;
   const dim3 grid((unsigned)std::min<long long>((S->arr / 4 + kAdjThreads - 1) / kAdjThreads, 1024), (unsigned)S->A);
-  hmf::adj_state_copy_kernel<<<grid, kAdjThreads, 0, s>>>(S->d_ctx + (size_t)parity * S->A, slot, S->arr,
-                                                          to_slot ? 1 : 0);
+  hmf::adj_state_copy_kernel<<<grid, kAdjThreads, 0, s>>>(S->d_ctx, slot, S->arr, to_slot ? 1 : 0);
   CK(cudaGetLastError(), "adj_state_copy_kernel launch");
   ++c->launches;
   return HMF_OK;
 }
 
-int forward_iteration(hmf_ctx* c, int parity, cudaStream_t s) {
-  int rc = launch_flow(c, parity, s);
-  if (!rc) rc = launch_tree(c, s);
+// Tables of iteration t: the flow kernel reads the flows, sinks and labels of
+// slot src(t) and writes the flows and divergence of slot dst(t); the sweep
+// reads slot src(t)'s sinks and labels and dst(t)'s divergence and writes
+// dst(t)'s sinks and labels.
+int build_transition_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
+  AdjointState* S = c->adj;
+  const int T = S->iterations, nv = c->n - 1;
+  const auto& V = c->vols[0];
+  S->h_tflow.assign((size_t)T * nv, hmf::FlowVertexTMA{});
+  S->h_ttree.assign((size_t)T, hmf::TreeTable{});
+  std::vector<int> entry(c->n, -1);
+  for (int i = 0; i < c->n; ++i) entry[c->postorder[i]] = i;
+  for (int t = 0; t < T; ++t) {
+    const int a = src_slot(S, t), b = dst_slot(S, t);
+    int j = 0;
+    for (int v : c->preorder) {
+      if (v == c->root) continue;
+      hmf::FlowVertexTMA& f = S->h_tflow[(size_t)t * nv + j++];
+      std::memset(&f, 0, sizeof(f));
+      const int base = slot_base(c, v), pbase = slot_base(c, c->parent[v]);
+      int rc = HMF_OK;
+      for (int ax = 0; ax < 3 && !rc; ++ax) {
+        rc = encode_plane_map(c, &f.flow_in[0][ax], slot_array(S, a, base + hmf::kAdjPx + ax), V);
+        f.flow_in[1][ax] = f.flow_in[0][ax];
+        f.flow_out[0][ax] = f.flow_out[1][ax] = slot_array(S, b, base + hmf::kAdjPx + ax);
+      }
+      if (!rc) rc = encode_plane_map(c, &f.sink, slot_array(S, a, base + hmf::kAdjSink), V);
+      if (!rc) rc = encode_plane_map(c, &f.label, slot_array(S, a, base + hmf::kAdjLabel), V);
+      if (!rc) rc = encode_plane_map(c, &f.inc, slot_array(S, a, pbase + hmf::kAdjSink), V);
+      const bool has_s = staged.smooth[v] && c->smooth[0][v].ptr;
+      if (!rc && has_s) rc = encode_plane_map(c, &f.smooth, staged.smooth[v], V);
+      if (rc) return rc;
+      f.has_smooth = has_s;
+      f.div = slot_array(S, b, base + hmf::kAdjDiv);
+      f.alpha = (float)c->alpha[v];  // stored as float, as the reference does (.cxx:692)
+    }
+    hmf::TreeTable& tt = S->h_ttree[t];
+    tt = c->h_tree;  // the solver's own table: tree, constants, data terms
+    for (int i = 0; i < c->n; ++i) {
+      const int v = c->postorder[i];
+      hmf::TreeEntry& E = tt.e[i];
+      const int base = slot_base(c, v);
+      E.sink = slot_array(S, a, base + hmf::kAdjSink);
+      E.sink_out = slot_array(S, b, base + hmf::kAdjSink);
+      if (v == c->root) continue;
+      E.label = slot_array(S, a, base + hmf::kAdjLabel);
+      E.label_out = slot_array(S, b, base + hmf::kAdjLabel);
+      E.div = slot_array(S, b, base + hmf::kAdjDiv);
+    }
+  }
+  if (T > 0) {
+    CK(cudaMemcpyAsync(S->d_tflow, S->h_tflow.data(), sizeof(hmf::FlowVertexTMA) * S->h_tflow.size(),
+                       cudaMemcpyHostToDevice, s),
+       "cudaMemcpyAsync(adjoint flow tables)");
+    CK(cudaMemcpyAsync(S->d_ttree, S->h_ttree.data(), sizeof(hmf::TreeTable) * S->h_ttree.size(),
+                       cudaMemcpyHostToDevice, s),
+       "cudaMemcpyAsync(adjoint tree tables)");
+  }
+  return HMF_OK;
+}
+
+int forward_iteration(hmf_ctx* c, int t, cudaStream_t s) {
+  AdjointState* S = c->adj;
+  int rc = launch_flow_tma_with(c, S->d_tflow + (size_t)t * (c->n - 1), 0, s);
+  if (!rc) rc = launch_tree_bulk_with(c, S->d_ttree + t, s);
   return rc;
 }
 
 int prepare_adjoint_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
   AdjointState* S = c->adj;
   const int n = c->n;
-  // solver arrays in slot order, per flow parity
-  S->h_ctx.assign(2 * (size_t)S->A, nullptr);
-  for (int par = 0; par < 2; ++par) {
-    const float** t = S->h_ctx.data() + (size_t)par * S->A;
-    for (int v = 0; v < n; ++v) {
-      const int b = slot_base(c, v);
-      t[b + hmf::kAdjSink] = c->sink[v];
-      if (v == c->root) continue;
-      t[b + hmf::kAdjLabel] = c->label[v];
-      t[b + hmf::kAdjPx] = c->fx[par][v];
-      t[b + hmf::kAdjPy] = c->fy[par][v];
-      t[b + hmf::kAdjPz] = c->fz[par][v];
-    }
+  // solver arrays in slot order (flows of set 0, where a solve starts); the
+  // divergence is not copied (a slot-0 divergence is never read)
+  S->h_ctx.assign((size_t)S->A, nullptr);
+  for (int v = 0; v < n; ++v) {
+    const int b = slot_base(c, v);
+    S->h_ctx[b + hmf::kAdjSink] = c->sink[v];
+    if (v == c->root) continue;
+    S->h_ctx[b + hmf::kAdjLabel] = c->label[v];
+    S->h_ctx[b + hmf::kAdjPx] = c->fx[0][v];
+    S->h_ctx[b + hmf::kAdjPy] = c->fy[0][v];
+    S->h_ctx[b + hmf::kAdjPz] = c->fz[0][v];
   }
-  if (!S->d_ctx) CK(cudaMalloc(&S->d_ctx, sizeof(float*) * 2 * (5 * hmf::kMaxVertices + 1)), "cudaMalloc(adjoint tables)");
+  if (!S->d_ctx)
+    CK(cudaMalloc(&S->d_ctx, sizeof(float*) * (hmf::kAdjPerVertex * hmf::kMaxVertices + 1)), "cudaMalloc(adjoint tables)");
   if (!S->d_tree) CK(cudaMalloc(&S->d_tree, sizeof(hmf::AdjTree)), "cudaMalloc(adjoint tree)");
   CK(cudaMemcpyAsync(S->d_ctx, S->h_ctx.data(), sizeof(float*) * S->h_ctx.size(), cudaMemcpyHostToDevice, s),
      "cudaMemcpyAsync(adjoint tables)");
@@ -174,6 +371,7 @@ int prepare_adjoint_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
   T.root = c->root;
   T.cc = c->cc;
   T.icc = 1.0f / c->cc;
+  T.step = c->step;
   int kpos = 0;
   for (int v = 0; v < n; ++v) {
     T.parent[v] = c->parent[v];
@@ -185,33 +383,77 @@ int prepare_adjoint_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
     T.sbase[v] = slot_base(c, v);
     T.data[v] = staged.data[v];
   }
+  // flow part of each sink adjoint, in the order the vertices' flow steps
+  // are reversed (id order): own (+) and children's (-) contributions
+  int q = 0;
+  for (int w = 0; w < n; ++w) {
+    T.comb_first[w] = q;
+    for (int v = 0; v < n; ++v) {
+      if (v == c->root) continue;
+      if (v == w) T.comb_v[q] = v, T.comb_sign[q++] = 1;
+      if (c->parent[v] == w) T.comb_v[q] = v, T.comb_sign[q++] = -1;
+    }
+  }
+  T.comb_first[n] = q;
   for (int k = 0; k < n; ++k) T.preorder[k] = c->preorder[k];
   for (size_t j = 0; j < c->leaves.size(); ++j) T.Db[c->leaves[j]] = S->Db + j * S->arr;
   CK(cudaMemcpyAsync(S->d_tree, &T, sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(adjoint tree)");
   return HMF_OK;
 }
 
-int backward_step(hmf_ctx* c, const Staged& staged, const float* stA, const float* stB, int cur, cudaStream_t s) {
+int backward_step(hmf_ctx* c, const Staged& staged, int slotA, int slotB, int cur, cudaStream_t s) {
   AdjointState* S = c->adj;
   const long long arr = S->arr;
   const int n = c->n;
   const hmf::Geometry G = c->geo;
+  const float* stA = slot_ptr(S, slotA);
   hmf::AdjSweep W;
   W.stA = stA;
-  W.stB = stB;
+  W.stB = slot_ptr(S, slotB);
   W.arr = arr;
   W.sbn = S->sb[cur];
   W.ubn = S->ub[cur];
+  W.gbn = S->gb;
   W.sbo = S->sb[cur ^ 1];
   W.ubo = S->ub[cur ^ 1];
   W.dbp = S->dbp;
-  {
+  if (S->chain || n > hmf::kSwMaxN) {
     const long long blocks = (G.vol + hmf::kAdjTreeThreads - 1) / hmf::kAdjTreeThreads;
     const int grid = (int)std::min<long long>(blocks, (long long)c->sm_count * 8);
     const size_t smem = 5 * (size_t)n * hmf::kAdjTreeThreads * sizeof(float);
     hmf::adj_tree_kernel<<<grid, hmf::kAdjTreeThreads, smem, s>>>(S->d_tree, G, W);
     CK(cudaGetLastError(), "adj_tree_kernel launch");
+  } else {
+    const long long blocks = (G.vol + hmf::kSwThreads - 1) / hmf::kSwThreads;
+    const int grid = (int)std::min<long long>(blocks, (long long)c->sm_count * 8);
+    switch (n) {
+#define HMF_SWEEP_CASE(N)                                                                  \
+  case N:                                                                                  \
+    hmf::adj_sweep_reg_kernel<N><<<grid, hmf::kSwThreads, 0, s>>>(S->d_tree, G, W); \
+    break;
+      HMF_SWEEP_CASE(2) HMF_SWEEP_CASE(3) HMF_SWEEP_CASE(4) HMF_SWEEP_CASE(5)
+      HMF_SWEEP_CASE(6) HMF_SWEEP_CASE(7) HMF_SWEEP_CASE(8)
+#undef HMF_SWEEP_CASE
+    }
+    CK(cudaGetLastError(), "adj_sweep_reg_kernel launch");
+  }
+  ++c->launches;
+  if (!S->chain) {
+    hmf::AdjFlowParams fp;
+    fp.step = c->step;
+    fp.icc = 1.0f / c->cc;
+    fp.parity = S->pb_par;
+    fp.n_vertices = n - 1;
+    fp.vols = S->d_avol;
+    fp.items = S->d_aitems;
+    fp.error_flag = c->d_error;
+    const dim3 grid((unsigned)S->n_aitems * (unsigned)(n - 1));
+    hmf::adj_flow_tma_kernel<<<grid, hmf::kAfThreads, hmf::kAfSmemBytes, s>>>(
+        S->d_aflow + (size_t)slotA * (n - 1), fp);
+    CK(cudaGetLastError(), "adj_flow_tma_kernel launch");
     ++c->launches;
+    S->pb_par ^= 1;
+    return HMF_OK;
   }
   hmf::AdjParams P;
   P.G = G;
@@ -243,13 +485,11 @@ int backward_step(hmf_ctx* c, const Staged& staged, const float* stA, const floa
     V.qy = t + 8 * arr;
     V.qz = t + 9 * arr;
     V.dbo = t + 10 * arr;
-    V.Pbx = S->Pb + (size_t)(3 * v + 0) * arr;
-    V.Pby = S->Pb + (size_t)(3 * v + 1) * arr;
-    V.Pbz = S->Pb + (size_t)(3 * v + 2) * arr;
+    V.Pbx = pb_array(S, c, S->pb_par, v, 0);
+    V.Pby = pb_array(S, c, S->pb_par, v, 1);
+    V.Pbz = pb_array(S, c, S->pb_par, v, 2);
     V.dbp = S->dbp + (size_t)v * arr;
-    V.sbo = S->sb[cur ^ 1] + (size_t)v * arr;
-    V.sbo_par = S->sb[cur ^ 1] + (size_t)c->parent[v] * arr;
-    V.ubo = S->ub[cur ^ 1] + (size_t)v * arr;
+    V.gb = S->gb + (size_t)v * arr;
     V.alpha_grad = S->scal + 1 + v;
     hmf::adj_grad_kernel<<<grid, kAdjThreads, 0, s>>>(V, P);
     hmf::adj_flow_kernel<<<grid, kAdjThreads, 0, s>>>(V, P);
@@ -273,12 +513,22 @@ void adjoint_free(hmf_ctx* c) {
   if (S->arena) cudaFree(S->arena);
   if (S->d_ctx) cudaFree(S->d_ctx);
   if (S->d_tree) cudaFree(S->d_tree);
+  if (S->d_tflow) cudaFree(S->d_tflow);
+  if (S->d_ttree) cudaFree(S->d_ttree);
+  if (S->d_aflow) cudaFree(S->d_aflow);
+  if (S->d_avol) cudaFree(S->d_avol);
+  if (S->d_aitems) cudaFree(S->d_aitems);
   if (S->scal) cudaFree(S->scal);
   delete S;
   c->adj = nullptr;
 }
 
-size_t adjoint_bytes(const hmf_ctx* c) { return c && c->adj ? c->adj->bytes : 0; }
+size_t adjoint_bytes(const hmf_ctx* c) {
+  if (!c || !c->adj) return 0;
+  const AdjointState* S = c->adj;
+  return S->bytes + (size_t)S->table_cap * ((c->n - 1) * sizeof(hmf::FlowVertexTMA) + sizeof(hmf::TreeTable)) +
+         (size_t)S->aflow_cap * (c->n - 1) * sizeof(hmf::AdjFlowVertex);
+}
 
 }  // namespace hmfi
 
@@ -307,11 +557,21 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
   CK(cudaFuncSetAttribute(hmf::adj_tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           5 * hmf::kMaxVertices * hmf::kAdjTreeThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(adj_tree_kernel)");
+  CK(cudaFuncSetAttribute(hmf::adj_flow_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hmf::kAfSmemBytes),
+     "cudaFuncSetAttribute(adj_flow_tma_kernel)");
+
+  {
+    const char* e = std::getenv("HMF_ADJOINT_KERNEL");
+    S->chain = e && std::strcmp(e, "chain") == 0;
+  }
   int rc = plan(c, T, checkpoint_every);
   if (rc) return rc;
   Staged staged;
-  rc = begin_solve(c, user, staged);
+  rc = begin_solve(c, user, staged);  // stages the inputs and runs the initialisation
   if (!rc) rc = prepare_adjoint_tables(c, staged, s);
+  if (!rc) rc = build_transition_tables(c, staged, s);
+  if (!rc) rc = plan_reverse(c, s);
+  if (!rc && !S->chain) rc = build_reverse_tables(c, staged, s);
   if (rc) return rc;
   const long long arr = S->arr;
   const auto& V0 = c->vols[0];
@@ -319,20 +579,22 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
   CK(cudaMemcpyAsync(S->truth, truth, dense * sizeof(int),
                      where == HMF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s),
      "cudaMemcpyAsync(truth)");
-  // zero the adjoints and the accumulators (sb, ub, dbp and Pb are contiguous)
-  CK(cudaMemsetAsync(S->sb[0], 0, (size_t)8 * n * arr * sizeof(float), s), "cudaMemsetAsync(adjoints)");
+  // zero the adjoints (sb, ub, gb, dbp and both Pb sets are contiguous) and accumulators
+  CK(cudaMemsetAsync(S->sb[0], 0, (size_t)13 * n * arr * sizeof(float), s), "cudaMemsetAsync(adjoints)");
+  S->pb_par = 0;
   CK(cudaMemsetAsync(S->Db, 0, c->leaves.size() * arr * sizeof(double), s), "cudaMemsetAsync(gradients)");
   CK(cudaMemsetAsync(S->scal, 0, sizeof(double) * (1 + hmf::kMaxVertices), s), "cudaMemsetAsync(scalars)");
 
-  // ---- forward pass with checkpoints; the last segment keeps every state
+  // ---- forward pass: the initial state into C_0, then every iteration
+  // writes its successor's slot
   const int k = S->k;
   const int a_last = T > 0 ? ((T - 1) / k) * k : 0;
-  rc = copy_state(c, slot_ptr(S, S->ckpt, 0), 0, true, s);
-  for (int it = 0; it < T && !rc; ++it) {
-    if (it > 0 && it % k == 0) rc = copy_state(c, slot_ptr(S, S->ckpt, it / k), it & 1, true, s);
-    if (!rc) rc = forward_iteration(c, it & 1, s);
-    if (!rc && it + 1 > a_last) rc = copy_state(c, slot_ptr(S, S->seg, it - a_last), (it + 1) & 1, true, s);
-  }
+  rc = copy_state(c, slot_ptr(S, ckpt_id(S, 0)), true, s);
+  for (int t = 0; t < T && !rc; ++t) rc = forward_iteration(c, t, s);
+  if (rc) return rc;
+  const int final_slot = T > 0 ? dst_slot(S, T - 1) : ckpt_id(S, 0);
+  // the final sinks and labels into the solver's arrays (hmf_get_labels / _sink)
+  rc = copy_state(c, slot_ptr(S, final_slot), false, s);
   if (rc) return rc;
   // ---- loss on the final labels; it seeds the label adjoints of the leaves
   {
@@ -340,7 +602,7 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
     std::memset(&Lo, 0, sizeof(Lo));
     Lo.n_leaves = (int)c->leaves.size();
     for (int j = 0; j < Lo.n_leaves; ++j) {
-      Lo.u[j] = c->label[c->leaves[j]];
+      Lo.u[j] = slot_array(S, final_slot, slot_base(c, c->leaves[j]) + hmf::kAdjLabel);
       Lo.ub[j] = S->ub[0] + (size_t)c->leaves[j] * arr;
     }
     Lo.n_voxels = (double)dense;
@@ -349,22 +611,14 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
     CK(cudaGetLastError(), "adj_loss_kernel launch");
     ++c->launches;
   }
-  if (S->has_fin) rc = copy_state(c, S->fin, T & 1, true, s);
   // ---- backward, segment by segment
   int cur = 0;
   for (int a = a_last; a >= 0 && T > 0 && !rc; a -= k) {
     const int b = std::min(a + k, T);
-    if (a != a_last) {
-      rc = copy_state(c, slot_ptr(S, S->ckpt, a / k), 0, false, s);
-      for (int j = 1; j <= b - a && !rc; ++j) {
-        rc = forward_iteration(c, (j - 1) & 1, s);
-        if (!rc) rc = copy_state(c, slot_ptr(S, S->seg, j - 1), j & 1, true, s);
-      }
-    }
-    for (int it = b - 1; it >= a && !rc; --it) {
-      const float* stA = it == a ? slot_ptr(S, S->ckpt, a / k) : slot_ptr(S, S->seg, it - a - 1);
-      const float* stB = slot_ptr(S, S->seg, it - a);
-      rc = backward_step(c, staged, stA, stB, cur, s);
+    if (a != a_last)
+      for (int t = a; t + 2 <= b && !rc; ++t) rc = forward_iteration(c, t, s);  // states a+1 .. b-1
+    for (int t = b - 1; t >= a && !rc; --t) {
+      rc = backward_step(c, staged, src_slot(S, t), dst_slot(S, t), cur, s);
       cur ^= 1;
     }
   }
@@ -379,14 +633,13 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
       I.Db[j] = S->Db + (size_t)j * arr;
     }
     I.sb = S->sb[cur];
+    I.gb = S->gb;
     I.arr = arr;
     I.n = n;
-    hmf::adj_init_kernel<<<grid_for(c, c->geo.vol), kAdjThreads, 0, s>>>(I, c->geo);
+    hmf::adj_init_kernel<<<grid_for(c, c->geo.vol), kAdjThreads, 0, s>>>(S->d_tree, I, c->geo);
     CK(cudaGetLastError(), "adj_init_kernel launch");
     ++c->launches;
   }
-  if (S->has_fin) rc = copy_state(c, S->fin, T & 1, false, s);
-  if (rc) return rc;
   std::vector<double> scal(1 + hmf::kMaxVertices, 0.0);
   CK(cudaMemcpyAsync(scal.data(), S->scal, sizeof(double) * scal.size(), cudaMemcpyDeviceToHost, s),
      "cudaMemcpyAsync(adjoint scalars)");

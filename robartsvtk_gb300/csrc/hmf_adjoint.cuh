@@ -21,17 +21,24 @@
 // the alpha gradient (a sum over voxels, reduced in double) depends on the
 // summation order.
 //
-// Forward states are addressed as "state slots": A = 5(n-1)+1 arrays of
-// `arr` floats each; non-root vertex j (in id order, root skipped) owns
-// arrays 5j+0 sink, +1 label, +2 px, +3 py, +4 pz; the root's sink is array
-// 5(n-1).
+// Forward states live in "state slots": A = 6(n-1)+1 arrays of `arr` floats
+// each; non-root vertex j (in id order, root skipped) owns arrays 6j+0 sink,
+// +1 label, +2 px, +3 py, +4 pz, +5 divergence of those flows; the root's sink
+// (the source flow) is array 6(n-1).  The forward kernels write every
+// iteration's state into its slot directly.
+//
+// The adjoint of a state's sinks and labels is the sum of a sweep part
+// (adj_tree_kernel of the later iteration) and a flow part (-/+ step * gb of
+// the later iteration's flow reverse, gb = adjoint of its gradient-step
+// values); the sum is formed where it is consumed, in the order the oracle
+// accumulates it (sweep part first, then vertex by vertex in id order).
 #pragma once
 
 #include "hmf_types.cuh"
 
 namespace hmf {
 
-enum { kAdjSink = 0, kAdjLabel = 1, kAdjPx = 2, kAdjPy = 3, kAdjPz = 4 };
+enum { kAdjSink = 0, kAdjLabel = 1, kAdjPx = 2, kAdjPy = 3, kAdjPz = 4, kAdjDiv = 5, kAdjPerVertex = 6 };
 constexpr int kAdjTreeThreads = 128;
 
 __device__ __forceinline__ bool adj_coords(const Geometry& G, long long i, int& x, int& y, int& z) {
@@ -54,17 +61,23 @@ __device__ __forceinline__ float adj_div(const float* px, const float* py, const
 
 // ---------------------------------------------------------------------------
 // Copies between the solver's state arrays and a state slot: blockIdx.y =
-// array j; ctx[j] = the solver's array j; slot + j*arr = the slot's.
+// array j; ctx[j] = the solver's array j (null: none -- zero-filled in the
+// slot, skipped the other way); slot + j*arr = the slot's.
 // ---------------------------------------------------------------------------
 __global__ void adj_state_copy_kernel(const float* const* __restrict__ ctx, float* slot, long long arr, int to_slot) {
   const int j = blockIdx.y;
   float4* a = reinterpret_cast<float4*>(const_cast<float*>(ctx[j]));
   float4* b = reinterpret_cast<float4*>(slot + (long long)j * arr);
+  const long long n4 = arr / 4;
+  const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, di = (long long)gridDim.x * blockDim.x;
+  if (!a) {
+    if (to_slot)
+      for (long long i = i0; i < n4; i += di) b[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
   const float4* src = to_slot ? a : b;
   float4* dst = to_slot ? b : a;
-  const long long n4 = arr / 4;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x)
-    dst[i] = src[i];
+  for (long long i = i0; i < n4; i += di) dst[i] = src[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -120,6 +133,8 @@ __global__ void adj_loss_kernel(const AdjLoss L, const int* __restrict__ truth, 
 struct AdjTree {
   int n, root;
   float cc, icc;
+  float step;  // StepSize (tau)
+  int pad_;
   int parent[kMaxVertices];
   int first_kid[kMaxVertices];
   int n_kids[kMaxVertices];
@@ -127,18 +142,36 @@ struct AdjTree {
   int kids[kMaxVertices];
   int preorder[kMaxVertices];
   int sbase[kMaxVertices];  // state-slot array index of the vertex's sink
+  // flow part of vertex w's sink adjoint: entries comb_first[w] ..
+  // comb_first[w+1]-1, vertex id order; +1: += step*gb(v) (v == w), -1:
+  // -= step*gb(v) (v a child of w)
+  int comb_first[kMaxVertices + 1];
+  int comb_v[2 * kMaxVertices];
+  int comb_sign[2 * kMaxVertices];
   const float* data[kMaxVertices];
   double* Db[kMaxVertices];
 };
+
+// Adjoint of vertex w's sink in a state: sweep part plus flow part.
+__device__ __forceinline__ float adj_sink_adjoint(const AdjTree& T, int w, const float* sweep, const float* gb,
+                                                  long long arr, long long i) {
+  float acc = sweep[w * arr + i];
+  for (int q = T.comb_first[w]; q < T.comb_first[w + 1]; ++q) {
+    const float d = T.step * gb[T.comb_v[q] * arr + i];
+    acc = T.comb_sign[q] > 0 ? acc + d : acc - d;
+  }
+  return acc;
+}
 
 struct AdjSweep {
   const float* stA;  // state slot before the iteration
   const float* stB;  // state slot after it
   long long arr;     // floats per array
-  const float* sbn;  // [v*arr] adjoint of the new sinks
-  const float* ubn;  // [v*arr] adjoint of the new labels
-  float* sbo;        // [v*arr] out: adjoint of the old sinks (sweep part)
-  float* ubo;        // [v*arr] out: adjoint of the old labels (sweep part)
+  const float* sbn;  // [v*arr] sweep part of the new sinks' adjoint
+  const float* ubn;  // [v*arr] sweep part of the new labels' adjoint
+  const float* gbn;  // [v*arr] gb of the later iteration's flow reverse (zero for the last)
+  float* sbo;        // [v*arr] out: sweep part of the old sinks' adjoint
+  float* ubo;        // [v*arr] out: sweep part of the old labels' adjoint
   float* dbp;        // [v*arr] out: adjoint of the new divergence
 };
 
@@ -155,20 +188,17 @@ __global__ void __launch_bounds__(kAdjTreeThreads) adj_tree_kernel(const AdjTree
   float* SBO = av + 2 * n * nb;
   float* UBO = av + 3 * n * nb;
   float* DBP = av + 4 * n * nb;
-  const float cc = T.cc, icc = T.icc;
+  const float cc = T.cc, icc = T.icc, step_icc = T.step * T.icc;
   const long long arr = S.arr;
   for (long long i = (long long)blockIdx.x * nb + t; i < G.vol; i += (long long)gridDim.x * nb) {
     int x, y, z;
     if (!adj_coords(G, i, x, y, z)) continue;
     for (int v = 0; v < n; ++v) {
-      SBN[v * nb + t] = S.sbn[v * arr + i];
+      SBN[v * nb + t] = adj_sink_adjoint(T, v, S.sbn, S.gbn, arr, i);
       SBO[v * nb + t] = 0.0f;
       UBO[v * nb + t] = 0.0f;
       DBP[v * nb + t] = 0.0f;
-      if (v != root) {
-        const float* B = S.stB + (long long)T.sbase[v] * arr;
-        DN[v * nb + t] = adj_div(B + kAdjPx * arr, B + kAdjPy * arr, B + kAdjPz * arr, G, i, x, y, z);
-      }
+      if (v != root) DN[v * nb + t] = S.stB[((long long)T.sbase[v] + kAdjDiv) * arr + i];
     }
     // labels: u' = sat(u + cc*((s'_parent - d') - s'))
     for (int v = 0; v < n; ++v) {
@@ -178,7 +208,8 @@ __global__ void __launch_bounds__(kAdjTreeThreads) adj_tree_kernel(const AdjTree
       const float sp = S.stB[(long long)T.sbase[p] * arr + i];
       const float sv = S.stB[(long long)T.sbase[v] * arr + i];
       const float zv = uo + cc * ((sp - DN[v * nb + t]) - sv);
-      const float zb = (zv > 0.0f && zv < 1.0f) ? S.ubn[v * arr + i] : 0.0f;
+      const float ub = S.ubn[v * arr + i] - step_icc * S.gbn[v * arr + i];
+      const float zb = (zv > 0.0f && zv < 1.0f) ? ub : 0.0f;
       UBO[v * nb + t] += zb;
       SBN[p * nb + t] += cc * zb;
       DBP[v * nb + t] -= cc * zb;
@@ -260,9 +291,7 @@ struct AdjVertex {
   float* qy;
   float* qz;
   float* dbo;        // of the old divergence
-  float* sbo;        // of the own old sink (accumulated)
-  float* sbo_par;    // of the parent's old sink (accumulated)
-  float* ubo;        // of the own old label (accumulated)
+  float* gb;         // out: of the gradient-step values g
   double* alpha_grad;
 };
 
@@ -374,7 +403,9 @@ __global__ void adj_descent_kernel(const AdjVertex V, const AdjParams P) {
   }
 }
 
-// adjoint of g -> own old sink, parent's old sink, old label, old divergence
+// adjoint of g (it reaches the own and parent's old sinks and the old label
+// through adj_sink_adjoint / the label adjoint of the next sweep reverse) and
+// of the old divergence
 __global__ void adj_gsum_kernel(const AdjVertex V, const AdjParams P) {
   const Geometry& G = P.G;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < G.vol; i += (long long)gridDim.x * blockDim.x) {
@@ -384,9 +415,7 @@ __global__ void adj_gsum_kernel(const AdjVertex V, const AdjParams P) {
     if (x != G.vx - 1) gb += V.qx[i + 1];
     if (y != G.vy - 1) gb += V.qy[i + G.pitch];
     if (z != G.vz - 1) gb += V.qz[i + G.plane];
-    V.sbo[i] += P.step * gb;
-    V.ubo[i] -= P.step * P.icc * gb;
-    V.sbo_par[i] -= P.step * gb;
+    V.gb[i] = gb;
     V.dbo[i] = P.step * gb;
   }
 }
@@ -410,14 +439,19 @@ __global__ void adj_oldflow_kernel(const AdjVertex V, const AdjParams P) {
 // ---------------------------------------------------------------------------
 struct AdjInit {
   const float* data[kMaxVertices];  // leaves, in leaf order
-  double* Db[kMaxVertices];
-  const float* sb;                  // [v*arr] adjoint of the initial sinks
+  double* Db[kMaxVertices];         // leaves, in leaf order
+  const float* sb;                  // [v*arr] sweep part of the initial sinks' adjoint
+  const float* gb;                  // [v*arr] gb of iteration 0's flow reverse
   long long arr;
   int n_leaves;
   int n;
 };
 
-__global__ void adj_init_kernel(const AdjInit A, const Geometry G) {
+__global__ void adj_init_kernel(const AdjTree* __restrict__ table, const AdjInit A, const Geometry G) {
+  __shared__ AdjTree T;
+  for (int i = threadIdx.x; i < (int)(sizeof(AdjTree) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  __syncthreads();
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < G.vol; i += (long long)gridDim.x * blockDim.x) {
     int x, y, z;
     if (!adj_coords(G, i, x, y, z)) continue;
@@ -431,7 +465,7 @@ __global__ void adj_init_kernel(const AdjInit A, const Geometry G) {
       }
     }
     double tot = 0.0;
-    for (int v = 0; v < A.n; ++v) tot += (double)A.sb[v * A.arr + i];
+    for (int v = 0; v < A.n; ++v) tot += (double)adj_sink_adjoint(T, v, A.sb, A.gb, A.arr, i);
     A.Db[arg][i] += tot;
   }
 }

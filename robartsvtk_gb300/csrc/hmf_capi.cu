@@ -231,13 +231,14 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 3-D map of one pitched volume block, box = one 36 x 32 window plane.
-int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V) {
+// 3-D map of one pitched volume block, box = one window plane of 36 columns
+// and `rows` rows.
+int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V, int rows) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return fail(c, HMF_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
   const cuuint64_t dims[3] = {(cuuint64_t)V.vx, (cuuint64_t)V.vy, (cuuint64_t)V.vz};
   const cuuint64_t strides[2] = {(cuuint64_t)V.pitch * 4, (cuuint64_t)V.plane * 4};
-  const cuuint32_t box[3] = {(cuuint32_t)hmf::kTmaBoxX, (cuuint32_t)hmf::kTmaRows, 1};
+  const cuuint32_t box[3] = {(cuuint32_t)hmf::kTmaBoxX, (cuuint32_t)rows, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -330,7 +331,9 @@ int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out) {
   return HMF_OK;
 }
 
-int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
+int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) { return launch_flow_tma_with(c, c->d_tma, parity, s); }
+
+int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s) {
   hmf::FlowTmaParams fp;
   fp.step = c->step;
   fp.icc = 1.0f / c->cc;
@@ -340,7 +343,7 @@ int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) {
   fp.items = c->d_items;
   fp.error_flag = c->d_error;
   const dim3 grid((unsigned)c->n_items * (unsigned)(c->n - 1), 1, 1);
-  hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(c->d_tma, fp);
+  hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(table, fp);
   CK(cudaGetLastError(), "flow_tma_kernel launch");
   ++c->launches;
   return HMF_OK;
@@ -377,18 +380,20 @@ int tree_grid(hmf_ctx* c) {
   return (int)std::min<long long>(blocks, (long long)c->sm_count * 16);
 }
 
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s) {
+  const int smem = hmf::tree_bulk_smem_bytes(c->n);
+  const int vc = hmf::tree_bulk_chunk(c->n);
+  const long long chunks = (c->geo.vol + vc - 1) / vc;
+  const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
+  const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
+  hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);
+  CK(cudaGetLastError(), "tree_bulk_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
 int launch_tree(hmf_ctx* c, cudaStream_t s) {
-  if (c->tree_kind == 0) {
-    const int smem = hmf::tree_bulk_smem_bytes(c->n);
-    const int vc = hmf::tree_bulk_chunk(c->n);
-    const long long chunks = (c->geo.vol + vc - 1) / vc;
-    const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
-    const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
-    hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(c->d_tree, c->geo, c->d_error);
-    CK(cudaGetLastError(), "tree_bulk_kernel launch");
-    ++c->launches;
-    return HMF_OK;
-  }
+  if (c->tree_kind == 0) return launch_tree_bulk_with(c, c->d_tree, s);
   if (c->tree_kind == 1) {
     const size_t smem4 = 4 * (size_t)c->n * hmf::kTree4Threads * sizeof(float4);
     const long long quads = c->geo.vol / 4;
@@ -526,8 +531,8 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
   for (int i = 0; i < c->n; ++i) {
     const int v = c->postorder[i];
     hmf::TreeEntry& E = tt.e[i];
-    E.sink = c->sink[v];
-    E.label = v == c->root ? nullptr : c->label[v];
+    E.sink = E.sink_out = c->sink[v];
+    E.label = E.label_out = v == c->root ? nullptr : c->label[v];
     E.div = v == c->root ? nullptr : c->div[v];
     E.data = in.data[v];
     E.parent = v == c->root ? -1 : entry[c->parent[v]];
@@ -1250,8 +1255,8 @@ extern "C" int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int 
   for (int i = 0; i < t.n; ++i) {
     const int v = t.postorder[i];
     hmf::TreeEntry& E = tt.e[i];
-    E.sink = sink[v];
-    E.label = v == t.root ? nullptr : label[v];
+    E.sink = E.sink_out = sink[v];
+    E.label = E.label_out = v == t.root ? nullptr : label[v];
     E.div = v == t.root ? nullptr : div[v];
     E.data = d_data[v];
     E.parent = v == t.root ? -1 : entry[t.parent[v]];

@@ -130,6 +130,12 @@ int end_solve(hmf_ctx* c, cudaStream_t user);
 // One flow launch (reads flow set `parity`, writes the other) and one sweep.
 int launch_flow(hmf_ctx* c, int parity, cudaStream_t s);
 int launch_tree(hmf_ctx* c, cudaStream_t s);
+// The TMA flow kernel and the bulk sweep over caller-built tables.
+int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s);
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s);
+// Tensor map of one pitched volume block; box = kTmaBoxX columns x `rows` rows.
+int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V,
+                     int rows = hmf::kTmaRows);
 bool valid_vertex(const hmf_ctx* c, int v);
 bool valid_volume(const hmf_ctx* c, int b);
 // Error flag set by the kernels (bit 0 negative input, 1 wait time-out,

@@ -28,13 +28,6 @@
 
 namespace hmf {
 
-template <bool B>
-struct BoolTag {
-  static constexpr bool value = B;
-};
-
-constexpr uint64_t kTmaWaitLimitNs = 500000000ull;  // 0.5 s: far beyond any healthy copy
-
 // Projection multiplier of kern_ComputeFlowMag*: m = |p| > lim ? lim/|p| : 1
 // with |p| = sqrtf(h).  For lim > 1e-18 (so that lim*lim is a normal float),
 // RN(RN(lim*lim) * (1 - 2^-20)) < lim^2 (1 - 2^-21); when h is below it,

@@ -261,10 +261,10 @@ __global__ void tree_kernel(const TreeTable* __restrict__ table, const Geometry 
     for (int e = 0; e < root; ++e) {
       const TreeEntry& E = T.e[e];
       const float u = U[e * nb + t] + cc * ((S[E.parent * nb + t] - D[e * nb + t]) - S[e * nb + t]);
-      E.label[i] = __saturatef(u);
-      E.sink[i] = S[e * nb + t];
+      E.label_out[i] = __saturatef(u);
+      E.sink_out[i] = S[e * nb + t];
     }
-    T.e[root].sink[i] = S[root * nb + t];
+    T.e[root].sink_out[i] = S[root * nb + t];
   }
 }
 
@@ -350,10 +350,10 @@ __global__ void __launch_bounds__(kTree4Threads) tree4_kernel(const TreeTable* _
       o.y = __saturatef(u.y + cc * ((inc.y - d.y) - s.y));
       o.z = __saturatef(u.z + cc * ((inc.z - d.z) - s.z));
       o.w = __saturatef(u.w + cc * ((inc.w - d.w) - s.w));
-      st4(E.label + i, o);
-      st4(E.sink + i, s);
+      st4(E.label_out + i, o);
+      st4(E.sink_out + i, s);
     }
-    st4(T.e[root].sink + i, S[root * nb + t]);
+    st4(T.e[root].sink_out + i, S[root * nb + t]);
   }
 }
 

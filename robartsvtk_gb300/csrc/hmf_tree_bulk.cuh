@@ -11,7 +11,9 @@
 // while the other is swept.  Each thread sweeps four voxels (float4); new
 // sinks overwrite the staged sink / data slots in post-order (a parent's old
 // sink is read by its children before the parent replaces it), labels and
-// sinks go straight to global memory.  Same arithmetic as tree_kernel.
+// sinks go straight to global memory (sink_out / label_out: in place in a
+// solve, the next state slot in the adjoint's forward pass).  Same arithmetic
+// as tree_kernel.
 #pragma once
 
 #include "hmf_async.cuh"
@@ -143,10 +145,10 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
         o.y = __saturatef(u.y + cc * ((inc.y - d.y) - sk.y));
         o.z = __saturatef(u.z + cc * ((inc.z - d.z) - sk.z));
         o.w = __saturatef(u.w + cc * ((inc.w - d.w) - sk.w));
-        *reinterpret_cast<float4*>(E.label + i) = o;
-        *reinterpret_cast<float4*>(E.sink + i) = sk;
+        *reinterpret_cast<float4*>(E.label_out + i) = o;
+        *reinterpret_cast<float4*>(E.sink_out + i) = sk;
       }
-      *reinterpret_cast<float4*>(T.e[root].sink + i) = at(3 * root);
+      *reinterpret_cast<float4*>(T.e[root].sink_out + i) = at(3 * root);
     }
     // The sweep wrote sinks into stage s with ordinary stores; order them
     // before the bulk copy that will refill the stage (async proxy).

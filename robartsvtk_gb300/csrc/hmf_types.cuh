@@ -45,8 +45,10 @@ struct FlowParams {
 
 // Post-order tree table for the per-voxel sweep; entries 0..n-1, root last.
 struct TreeEntry {
-  float* sink;          // sink flow (root: source flow)
-  float* label;         // nullptr for the root
+  float* sink;          // sink flow (root: source flow), read
+  float* label;         // nullptr for the root, read
+  float* sink_out;      // where the sweep writes the new sink (== sink in a solve)
+  float* label_out;     // where it writes the new label (== label in a solve)
   const float* div;     // nullptr for the root
   const float* data;    // leaves: data term (capacity)
   int parent;           // entry index of the parent, -1 for the root
@@ -119,5 +121,15 @@ struct FlowTmaParams {
   const FlowItem* items;
   int* error_flag;
 };
+
+// Compile-time flag passed to generic lambdas (kernel specialisations).
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
+
+// Bound of every mbarrier wait of the copy pipelines; a wait that runs out
+// sets the error flag instead of hanging.
+constexpr uint64_t kTmaWaitLimitNs = 500000000ull;  // 0.5 s: far beyond any healthy copy
 
 }  // namespace hmf

@@ -59,17 +59,28 @@ def assert_matches(g, o, w, what=""):
     np.testing.assert_allclose(g["dalpha"], o["dalpha"], rtol=1e-9, atol=1e-15 * max(1.0, np.abs(o["dalpha"]).max()))
 
 
-@pytest.mark.parametrize("dims", [(9, 8, 7), (37, 29, 21), (61, 45, 37)])
-def test_adjoint_matches_oracle(dims):
+@pytest.fixture(params=["fused", "chain"])
+def reverse_kernel(request, monkeypatch):
+    """The fused reverse flow kernel (default) and the unfused per-vertex chain."""
+    if request.param == "chain":
+        monkeypatch.setenv("HMF_ADJOINT_KERNEL", "chain")
+    else:
+        monkeypatch.delenv("HMF_ADJOINT_KERNEL", raising=False)
+    return request.param
+
+
+@pytest.mark.parametrize("dims", [(9, 8, 7), (37, 29, 21), (61, 45, 37), (28, 27, 1), (1, 7, 11), (55, 1, 9),
+                                  (5, 4, 3), (64, 50, 40)])
+def test_adjoint_matches_oracle(dims, reverse_kernel):
     w, truth = problem(7, dims)
     g = run_gpu(w, truth)
     o = run_oracle(w, truth)
-    assert_matches(g, o, w, str(dims))
+    assert_matches(g, o, w, "%s %s" % (dims, reverse_kernel))
     assert g["plan"]["recomputed_segments"] == 0  # everything fits: no recomputation
 
 
 @pytest.mark.parametrize("k", [1, 3, 5])
-def test_adjoint_checkpointing_recomputes_exactly(k):
+def test_adjoint_checkpointing_recomputes_exactly(k, reverse_kernel):
     w, truth = problem(11, (33, 20, 17), iterations=13)
     o = run_oracle(w, truth)
     g = run_gpu(w, truth, checkpoint_every=k)
@@ -81,12 +92,12 @@ def test_adjoint_checkpointing_recomputes_exactly(k):
         assert np.array_equal(u, f["u"][v].astype(np.float32)), v
 
 
-def test_adjoint_flat_tree_without_smoothness_images():
+def test_adjoint_flat_tree_without_smoothness_images(reverse_kernel):
     w, truth = problem(21, (40, 24, 18), parent=[-1, 0, 0, 0, 0], iterations=10, smooth_nodes=())
     assert_matches(run_gpu(w, truth), run_oracle(w, truth), w, "flat4")
 
 
-def test_adjoint_deep_tree():
+def test_adjoint_deep_tree(reverse_kernel):
     parent = [-1, 0, 0, 1, 1, 2, 2, 3, 3]
     w, truth = problem(31, (23, 19, 13), parent=parent, iterations=9, smooth_nodes=(1, 4, 6))
     assert_matches(run_gpu(w, truth), run_oracle(w, truth), w, "deep")
