@@ -9,7 +9,7 @@
 // Backward: segment by segment from the last, the segment's inner states are
 // recomputed into S_j with the same tables (bit-identical to the first pass),
 // then one backward step per iteration runs from the segment's last
-// iteration to its first: adj_sweep_reg_kernel (trees of up to 8 vertices;
+// iteration to its first: adj_sweep_kernel (trees of up to 8 vertices;
 // adj_tree_kernel beyond) reverses the sink/label sweep of all vertices, and
 // adj_flow_tma_kernel reverses the flow step of every vertex
 // (HMF_ADJOINT_KERNEL=chain selects adj_tree_kernel and the unfused
@@ -424,18 +424,25 @@ int backward_step(hmf_ctx* c, const Staged& staged, int slotA, int slotB, int cu
     hmf::adj_tree_kernel<<<grid, hmf::kAdjTreeThreads, smem, s>>>(S->d_tree, G, W);
     CK(cudaGetLastError(), "adj_tree_kernel launch");
   } else {
-    const long long blocks = (G.vol + hmf::kSwThreads - 1) / hmf::kSwThreads;
-    const int grid = (int)std::min<long long>(blocks, (long long)c->sm_count * 8);
-    switch (n) {
-#define HMF_SWEEP_CASE(N)                                                                  \
-  case N:                                                                                  \
-    hmf::adj_sweep_reg_kernel<N><<<grid, hmf::kSwThreads, 0, s>>>(S->d_tree, G, W); \
+    const int smem = hmf::adj_sweep_smem_bytes(n);
+    const long long chunks = (G.vol + hmf::kSwVc - 1) / hmf::kSwVc;
+    const int per_sm = std::max(1, (227 * 1024) / (smem + (int)sizeof(hmf::AdjTree) + 1024));
+    const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
+    bool pre = true;  // vertex ids in pre-order: the sink pass runs in id order
+    for (int k = 0; k < n; ++k) pre = pre && c->preorder[k] == k;
+    switch (n * 2 + (pre ? 1 : 0)) {
+#define HMF_SWEEP_CASE(N)                                                                                  \
+  case 2 * N:                                                                                              \
+    hmf::adj_sweep_kernel<N, false><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);           \
+    break;                                                                                                 \
+  case 2 * N + 1:                                                                                          \
+    hmf::adj_sweep_kernel<N, true><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);            \
     break;
       HMF_SWEEP_CASE(2) HMF_SWEEP_CASE(3) HMF_SWEEP_CASE(4) HMF_SWEEP_CASE(5)
       HMF_SWEEP_CASE(6) HMF_SWEEP_CASE(7) HMF_SWEEP_CASE(8)
 #undef HMF_SWEEP_CASE
     }
-    CK(cudaGetLastError(), "adj_sweep_reg_kernel launch");
+    CK(cudaGetLastError(), "adj_sweep_kernel launch");
   }
   ++c->launches;
   if (!S->chain) {
@@ -560,6 +567,16 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
   CK(cudaFuncSetAttribute(hmf::adj_flow_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hmf::kAfSmemBytes),
      "cudaFuncSetAttribute(adj_flow_tma_kernel)");
 
+#define HMF_SWEEP_ATTR(N)                                                                                  \
+  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                          hmf::adj_sweep_smem_bytes(N)),                                                     \
+     "cudaFuncSetAttribute(adj_sweep_kernel)");                                                              \
+  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                          hmf::adj_sweep_smem_bytes(N)),                                                     \
+     "cudaFuncSetAttribute(adj_sweep_kernel)");
+  HMF_SWEEP_ATTR(2) HMF_SWEEP_ATTR(3) HMF_SWEEP_ATTR(4) HMF_SWEEP_ATTR(5)
+  HMF_SWEEP_ATTR(6) HMF_SWEEP_ATTR(7) HMF_SWEEP_ATTR(8)
+#undef HMF_SWEEP_ATTR
   {
     const char* e = std::getenv("HMF_ADJOINT_KERNEL");
     S->chain = e && std::strcmp(e, "chain") == 0;

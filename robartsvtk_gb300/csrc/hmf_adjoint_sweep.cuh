@@ -1,27 +1,36 @@
 // hmf_adjoint_sweep.cuh -- reverse of the per-voxel sink / label sweep for
-// trees of N <= 8 vertices with every per-vertex quantity in registers (the
-// register form of adj_tree_kernel in hmf_adjoint.cuh; same FP32 operations
-// in the same order).
+// trees of N <= 8 vertices (the staged, register-resident form of
+// adj_tree_kernel in hmf_adjoint.cuh; same FP32 operations in the same
+// order).
 //
-// One thread per voxel of the pitched layout (padding columns included: their
-// values are finite and never read back).  All inputs of the voxel are
-// independent coalesced loads issued before any arithmetic: the sweep parts
-// of the later state's sink and label adjoints, the later flow reverse's gb,
-// the sinks and labels before the iteration, the sinks and divergences after
-// it, the data terms and the leaves' accumulated data-term gradients (so the
-// double-precision accumulation is not a dependent read-modify-write at the
-// end).  Per-vertex arrays are indexed only by unrolled
-// compile-time indices; a runtime vertex (a parent, a child, the pre-order
-// position) is reached through predicated selects, which keeps them in
-// registers.
+// A persistent CTA walks chunks of 256 consecutive voxels of the pitched
+// layout (padding columns included: their values are finite and never read
+// back).  For every chunk thread 0 issues one cp.async.bulk per input array
+// -- per vertex the sweep parts of the later state's sink and label
+// adjoints, the later flow reverse's gb, the sink and label before the
+// iteration, the sink and divergence after it, the data term and the
+// accumulated data-term gradient (double) -- into one of two shared-memory
+// stages, so the next chunk streams in while this one is reversed.  Stage
+// slots sit at fixed [quantity][vertex] positions (absent quantities are not
+// copied and not read), so every shared-memory offset is a compile-time
+// constant; one thread reverses one voxel with all per-vertex values in
+// registers.  When the vertex ids are in pre-order (PRE), the sink pass runs
+// in compile-time vertex order; otherwise runtime vertices (parents,
+// children, pre-order positions) are reached through predicated selects.
 #pragma once
 
 #include "hmf_adjoint.cuh"
+#include "hmf_async.cuh"
 
 namespace hmf {
 
-constexpr int kSwThreads = 128;
+constexpr int kSwVc = 256;     // voxels per chunk = threads per CTA
 constexpr int kSwMaxN = 8;
+constexpr int kSwKinds = 10;   // float slots per vertex: 8 quantities + one double (2 floats)
+
+enum { kSwSBN = 0, kSwUB, kSwGB, kSwAS, kSwAU, kSwBS, kSwBD, kSwD, kSwDB };  // kSwDB: double, 2 slots
+
+__host__ __device__ constexpr int adj_sweep_smem_bytes(int N) { return 128 + 2 * kSwKinds * N * kSwVc * 4; }
 
 template <int N>
 __device__ __forceinline__ float sw_sel(const float (&a)[N], int v) {
@@ -39,120 +48,223 @@ __device__ __forceinline__ void sw_add(float (&a)[N], int v, float x) {
     if (w == v) a[w] = a[w] + x;
 }
 
-template <int N>
-__device__ __forceinline__ void sw_addd(double (&a)[N], bool (&hit)[N], int v, float x) {
-#pragma unroll
-  for (int w = 0; w < N; ++w)
-    if (w == v) {
-      a[w] += (double)x;
-      hit[w] = true;
-    }
-}
-
-template <int N>
-__global__ void __launch_bounds__(kSwThreads) adj_sweep_reg_kernel(const AdjTree* __restrict__ table, const Geometry G,
-                                                                   const AdjSweep S) {
+template <int N, bool PRE>
+__global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restrict__ table, const Geometry G,
+                                                          const AdjSweep S, int* __restrict__ error_flag) {
   __shared__ AdjTree T;
+  __shared__ int abort_cta;
+  extern __shared__ __align__(128) unsigned char sw_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sw_raw);  // [2]
+  float* stage0 = reinterpret_cast<float*>(sw_raw + 128);
+  constexpr int kStage = kSwKinds * N * kSwVc;  // floats per stage
+
   for (int i = threadIdx.x; i < (int)(sizeof(AdjTree) / 4); i += blockDim.x)
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  if (threadIdx.x == 0) {
+    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    if (smem_addr(sw_raw) & 15) {  // bulk-copy destinations must be 16-byte aligned
+      abort_cta = 1;
+      if (error_flag) atomicOr(error_flag, 4);
+    }
+    for (int s = 0; s < 2; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   __syncthreads();
+  if (abort_cta) return;
+
   const int root = T.root;
   const float cc = T.cc, icc = T.icc, step = T.step, step_icc = T.step * T.icc;
   const long long arr = S.arr;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < G.vol;
-       i += (long long)gridDim.x * blockDim.x) {
-    float SBN[N], UB[N], GB[N], AS[N], AU[N], BS[N], BD[N], D[N];
-    double DB[N];  // data-term gradients of the leaves, read with the inputs
-    bool hit[N];
-#pragma unroll
+  const long long nchunks = (G.vol + kSwVc - 1) / kSwVc;
+
+  auto issue = [&](long long chunk, int s) {  // thread 0 only
+    const long long v0 = chunk * kSwVc;
+    const unsigned len = (unsigned)min((long long)kSwVc, G.vol - v0);
+    uint64_t* bar = &bars[s];
+    float* dst = stage0 + (size_t)s * kStage;
+    unsigned total = 0;  // expected bytes first (the copies complete against it)
+    for (int v = 0; v < N; ++v) {
+      const bool nr = v != root, leaf = T.n_kids[v] == 0;
+      total += len * 4 * (3 + (nr ? 4 : 0)) + (leaf ? len * 8 : 0);
+    }
+    mbar_expect_tx(bar, total);
+    auto ld = [&](int kind, int v, const float* src) {
+      bulk_load(dst + (size_t)(kind * N + v) * kSwVc, src + v0, len * 4, bar);
+    };
     for (int v = 0; v < N; ++v) {
       const long long b = T.sbase[v];
-      SBN[v] = S.sbn[v * arr + i];
-      BS[v] = S.stB[b * arr + i];
-      AS[v] = T.n_kids[v] ? S.stA[b * arr + i] : 0.f;   // read by leaf children
-      D[v] = T.n_kids[v] ? 0.f : T.data[v][i];
-      DB[v] = T.n_kids[v] ? 0.0 : T.Db[v][i];
-      hit[v] = false;
-      const bool nr = v != root;
-      UB[v] = nr ? S.ubn[v * arr + i] : 0.f;
-      GB[v] = nr ? S.gbn[v * arr + i] : 0.f;
-      AU[v] = nr ? S.stA[(b + kAdjLabel) * arr + i] : 0.f;
-      BD[v] = nr ? S.stB[(b + kAdjDiv) * arr + i] : 0.f;
+      const bool nr = v != root, leaf = T.n_kids[v] == 0;
+      ld(kSwSBN, v, S.sbn + v * arr);
+      ld(kSwBS, v, S.stB + b * arr);
+      if (leaf) ld(kSwD, v, T.data[v]);
+      else ld(kSwAS, v, S.stA + b * arr);
+      if (nr) {
+        ld(kSwUB, v, S.ubn + v * arr);
+        ld(kSwGB, v, S.gbn + v * arr);
+        ld(kSwAU, v, S.stA + (b + kAdjLabel) * arr);
+        ld(kSwBD, v, S.stB + (b + kAdjDiv) * arr);
+      }
+      if (leaf) bulk_load(dst + (size_t)(kSwDB * N + 2 * v) * kSwVc, T.Db[v] + v0, len * 8, bar);
     }
-    // full adjoints of the later state: sinks (sweep part, then the flow
-    // part vertex by vertex in id order: own +step*gb, children's -step*gb)
-    // and labels (sweep part - step*icc*gb)
+  };
+
+  bool timed_out = false;
+  int nissued[2] = {0, 0};
+  long long chunk = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  }
+  for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
+    const int s = j & 1;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    const float* st = stage0 + (size_t)s * kStage;
+    const long long v0 = chunk * kSwVc;
+    const int len = (int)min((long long)kSwVc, G.vol - v0);
+    const int q = threadIdx.x;
+    if (q < len) {
+      auto at = [&](int kind, int v) { return st[(kind * N + v) * kSwVc + q]; };
+      float SBN[N], UB[N], GB[N], AS[N], AU[N], BS[N], BD[N], D[N];
+      double DB[N];
+      bool hit[N];
 #pragma unroll
-    for (int w = 0; w < N; ++w) {
-      float a = SBN[w];
+      for (int v = 0; v < N; ++v) {
+        const bool nr = v != root, leaf = T.n_kids[v] == 0;
+        SBN[v] = at(kSwSBN, v);
+        BS[v] = at(kSwBS, v);
+        AS[v] = leaf ? 0.f : at(kSwAS, v);
+        D[v] = leaf ? at(kSwD, v) : 0.f;
+        DB[v] = leaf ? reinterpret_cast<const double*>(st + (kSwDB * N + 2 * v) * kSwVc)[q] : 0.0;
+        UB[v] = nr ? at(kSwUB, v) : 0.f;
+        GB[v] = nr ? at(kSwGB, v) : 0.f;
+        AU[v] = nr ? at(kSwAU, v) : 0.f;
+        BD[v] = nr ? at(kSwBD, v) : 0.f;
+        hit[v] = false;
+      }
+      // full adjoints of the later state: sinks (sweep part, then the flow
+      // part vertex by vertex in id order: own +step*gb, children's -step*gb)
+      // and labels (sweep part - step*icc*gb)
+#pragma unroll
+      for (int w = 0; w < N; ++w) {
+        float a = SBN[w];
+#pragma unroll
+        for (int v = 0; v < N; ++v) {
+          if (v == root) continue;
+          const float d = step * GB[v];
+          if (v == w) a = a + d;
+          else if (T.parent[v] == w) a = a - d;
+        }
+        SBN[w] = a;
+        UB[w] = UB[w] - step_icc * GB[w];
+      }
+      float SBO[N], UBO[N], DBP[N];
+#pragma unroll
+      for (int v = 0; v < N; ++v) SBO[v] = UBO[v] = DBP[v] = 0.f;
+      // labels: u' = sat(u + cc*((s'_parent - d') - s')), vertex id order
 #pragma unroll
       for (int v = 0; v < N; ++v) {
         if (v == root) continue;
-        const float d = step * GB[v];
-        if (v == w) a = a + d;
-        else if (T.parent[v] == w) a = a - d;
-      }
-      SBN[w] = a;
-      UB[w] = UB[w] - step_icc * GB[w];
-    }
-    float SBO[N], UBO[N], DBP[N];
-#pragma unroll
-    for (int v = 0; v < N; ++v) SBO[v] = UBO[v] = DBP[v] = 0.f;
-    // labels: u' = sat(u + cc*((s'_parent - d') - s')), vertex id order
-#pragma unroll
-    for (int v = 0; v < N; ++v) {
-      if (v == root) continue;
-      const int p = T.parent[v];
-      const float zv = AU[v] + cc * ((sw_sel(BS, p) - BD[v]) - BS[v]);
-      const float zb = (zv > 0.0f && zv < 1.0f) ? UB[v] : 0.0f;
-      UBO[v] = UBO[v] + zb;
-      sw_add(SBN, p, cc * zb);
-      DBP[v] = DBP[v] - cc * zb;
-      SBN[v] = SBN[v] - cc * zb;
-    }
-    // sinks, parents before children (pre-order)
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const int v = T.preorder[k];
-      const float sbn = sw_sel(SBN, v);
-      if (T.n_kids[v] == 0) {
         const int p = T.parent[v];
-        const float yv = (sw_sel(AS, p) - sw_sel(BD, v)) + sw_sel(AU, v) * icc;
-        if (yv < 0.0f) continue;
-        if (yv > sw_sel(D, v)) {
-          sw_addd(DB, hit, v, sbn);
-          continue;
-        }
-        sw_add(SBO, p, sbn);
-        sw_add(DBP, v, -sbn);
-        sw_add(UBO, v, icc * sbn);
-      } else {
-        const float Wb = sbn * T.inv_kids[v];
-        if (v != root) {
-          sw_add(SBO, T.parent[v], Wb);
-          sw_add(DBP, v, -Wb);
-          sw_add(UBO, v, icc * Wb);
-        }
-        const float iW = icc * Wb;
+        const float zv = AU[v] + cc * ((sw_sel(BS, p) - BD[v]) - BS[v]);
+        const float zb = (zv > 0.0f && zv < 1.0f) ? UB[v] : 0.0f;
+        UBO[v] = UBO[v] + zb;
+        sw_add(SBN, p, cc * zb);
+        DBP[v] = DBP[v] - cc * zb;
+        SBN[v] = SBN[v] - cc * zb;
+      }
+      // sinks, parents before children (pre-order)
 #pragma unroll
-        for (int w = 0; w < N; ++w)
-          if (T.parent[w] == v) {
-            SBN[w] = SBN[w] + Wb;
-            DBP[w] = DBP[w] + Wb;
-            UBO[w] = UBO[w] - iW;
+      for (int k = 0; k < N; ++k) {
+        if (PRE) {
+          const int v = k;  // ids are in pre-order
+          if (T.n_kids[v] == 0) {
+            const int p = T.parent[v];
+            const float yv = (sw_sel(AS, p) - BD[v]) + AU[v] * icc;
+            if (yv < 0.0f) continue;
+            if (yv > D[v]) {
+              DB[v] += (double)SBN[v];
+              hit[v] = true;
+              continue;
+            }
+            const float yb = SBN[v];
+            sw_add(SBO, p, yb);
+            DBP[v] = DBP[v] - yb;
+            UBO[v] = UBO[v] + icc * yb;
+          } else {
+            const float Wb = SBN[v] * T.inv_kids[v];
+            if (v != root) {
+              sw_add(SBO, T.parent[v], Wb);
+              DBP[v] = DBP[v] - Wb;
+              UBO[v] = UBO[v] + icc * Wb;
+            }
+            const float iW = icc * Wb;
+#pragma unroll
+            for (int w = v + 1; w < N; ++w)  // children follow their parent in pre-order
+              if (T.parent[w] == v) {
+                SBN[w] = SBN[w] + Wb;
+                DBP[w] = DBP[w] + Wb;
+                UBO[w] = UBO[w] - iW;
+              }
           }
-      }
-    }
+        } else {
+          const int v = T.preorder[k];
+          const float sbn = sw_sel(SBN, v);
+          if (T.n_kids[v] == 0) {
+            const int p = T.parent[v];
+            const float yv = (sw_sel(AS, p) - sw_sel(BD, v)) + sw_sel(AU, v) * icc;
+            if (yv < 0.0f) continue;
+            if (yv > sw_sel(D, v)) {
 #pragma unroll
-    for (int v = 0; v < N; ++v) {
-      S.sbo[v * arr + i] = SBO[v];
-      if (v != root) {
-        S.ubo[v * arr + i] = UBO[v];
-        S.dbp[v * arr + i] = DBP[v];
+              for (int w = 0; w < N; ++w)
+                if (w == v) {
+                  DB[w] += (double)sbn;
+                  hit[w] = true;
+                }
+              continue;
+            }
+            sw_add(SBO, p, sbn);
+            sw_add(DBP, v, -sbn);
+            sw_add(UBO, v, icc * sbn);
+          } else {
+            const float Wb = sbn * T.inv_kids[v];
+            if (v != root) {
+              sw_add(SBO, T.parent[v], Wb);
+              sw_add(DBP, v, -Wb);
+              sw_add(UBO, v, icc * Wb);
+            }
+            const float iW = icc * Wb;
+#pragma unroll
+            for (int w = 0; w < N; ++w)
+              if (T.parent[w] == v) {
+                SBN[w] = SBN[w] + Wb;
+                DBP[w] = DBP[w] + Wb;
+                UBO[w] = UBO[w] - iW;
+              }
+          }
+        }
       }
-      if (hit[v]) T.Db[v][i] = DB[v];
+      const long long i = v0 + q;
+#pragma unroll
+      for (int v = 0; v < N; ++v) {
+        S.sbo[v * arr + i] = SBO[v];
+        if (v != root) {
+          S.ubo[v * arr + i] = UBO[v];
+          S.dbp[v * arr + i] = DBP[v];
+        }
+        if (hit[v]) T.Db[v][i] = DB[v];
+      }
     }
+    // order this chunk's generic reads of stage s before the bulk copy that
+    // refills it (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
+  if (timed_out && error_flag) atomicOr(error_flag, 2);
+  if (threadIdx.x == 0 && timed_out)
+    for (int s = 0; s < 2; ++s)
+      if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
 }
 
 }  // namespace hmf

@@ -97,6 +97,12 @@ def test_adjoint_flat_tree_without_smoothness_images(reverse_kernel):
     assert_matches(run_gpu(w, truth), run_oracle(w, truth), w, "flat4")
 
 
+def test_adjoint_two_level_tree_in_preorder(reverse_kernel):
+    """Vertex ids in pre-order (the sweep reverse's compile-time order)."""
+    w, truth = problem(71, (45, 31, 26), parent=[-1, 0, 1, 1, 0, 4, 4], iterations=9, smooth_nodes=(1, 2, 5))
+    assert_matches(run_gpu(w, truth), run_oracle(w, truth), w, "tree4")
+
+
 def test_adjoint_deep_tree(reverse_kernel):
     parent = [-1, 0, 0, 1, 1, 2, 2, 3, 3]
     w, truth = problem(31, (23, 19, 13), parent=parent, iterations=9, smooth_nodes=(1, 4, 6))
