@@ -9,9 +9,10 @@
 //   g -> p' -> (|p|, m, adjoint of m -> F2b) -> q -> gb -> old-flow adjoint
 // reaches three voxels to the low side and two to the high side, so a CTA
 // owns a 32 x 32 (x, y) window with up to 27 x 27 outputs and marches along
-// z: thread (lane, row) = column x0-3+lane, row y0-3+row; x neighbours move
-// by warp shuffles, y neighbours through small exchange planes in shared
-// memory, z neighbours stay in registers.  Per plane k the CTA computes g,
+// z: lane = column x0-3+lane, warp w holds rows 2w and 2w+1 (y0-3+row) in
+// registers; x neighbours move by warp shuffles, y neighbours across a warp
+// boundary through small exchange rows in shared memory, z neighbours stay
+// in registers.  Per plane k the CTA computes g,
 // p' and the total new-flow adjoint t on plane k, m / F2b and q on k-1, gb on
 // k-2 and the old-flow adjoints on k-3 (two __syncthreads per plane).  Input
 // planes arrive by cp.async.bulk.tensor into mbarrier rings two planes ahead;
@@ -32,8 +33,10 @@ constexpr int kAfPlane = 1216;              // floats per staged plane (36 x 33 
 constexpr int kAfMainArrays = 10;           // px, py, s, c, u, Pbx, Pby, Pbz, dbp, S
 constexpr int kAfMainSlots = 3;
 constexpr int kAfPzSlots = 4;
-constexpr int kAfThreads = 1024;            // 32 rows x 32 lanes
-constexpr int kAfX = 34 * 32;               // exchange plane: rows -1 .. 32
+constexpr int kAfR = 2;                     // rows per thread
+constexpr int kAfWarps = 32 / kAfR;
+constexpr int kAfThreads = 32 * kAfWarps;   // 512
+constexpr int kAfX = (kAfWarps + 2) * 32;   // exchange row per warp, plus zero rows for warps -1 and 16
 constexpr int kAfXPlanes = 11;              // g, p'y[2], ty[2], m, F2b, qy[2], dbo[2]
 constexpr int kAfMaxOut = 27;
 constexpr int kAfSmemBytes =
@@ -64,32 +67,35 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   extern __shared__ __align__(1024) unsigned char af_raw[];
   float* mslots = reinterpret_cast<float*>(af_raw);                      // [3][10][1216]
   float* zslots = mslots + kAfMainSlots * kAfMainArrays * kAfPlane;      // [4][1216]
-  float* xp = zslots + kAfPzSlots * kAfPlane;                            // [11][34][32]
+  float* xp = zslots + kAfPzSlots * kAfPlane;                            // [11][18][32]
   uint64_t* mbars = reinterpret_cast<uint64_t*>(xp + kAfXPlanes * kAfX); // [3]
   uint64_t* zbars = mbars + kAfMainSlots;                                // [4]
-  float* XG = xp;
-  float* XPPY = xp + 1 * kAfX;  // [2]
-  float* XTY = xp + 3 * kAfX;   // [2]
-  float* XM = xp + 5 * kAfX;
-  float* XF = xp + 6 * kAfX;
-  float* XQY = xp + 7 * kAfX;   // [2]
-  float* XD = xp + 9 * kAfX;    // [2]
+  // exchange rows: *_L = the last row of each warp (read by the next warp as
+  // its y-1 neighbour), *_F = the first row (read by the previous warp as y+1)
+  float* XG_L = xp;
+  float* XPPY_F = xp + 1 * kAfX;  // [2] by plane parity
+  float* XTY_F = xp + 3 * kAfX;   // [2]
+  float* XM_L = xp + 5 * kAfX;
+  float* XF_L = xp + 6 * kAfX;
+  float* XQY_F = xp + 7 * kAfX;   // [2]
+  float* XD_L = xp + 9 * kAfX;    // [2]
   __shared__ int abort_cta;
-  __shared__ double red[32];
+  __shared__ int stop;
+  __shared__ double red[kAfWarps];
 
   const int nv = fp.n_vertices;
   const FlowItem item = fp.items[blockIdx.x / nv];
   const FlowVolume FV = fp.vols[item.vol];
   const Geometry G = FV.G;
   const AdjFlowVertex* V = vertices + (size_t)item.vol * nv + (blockIdx.x % nv);
-  const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
   const int ocols = FV.out_x, orows = FV.out_y;
   const int x0 = (item.tile % FV.tiles_x) * ocols;
   const int y0 = (item.tile / FV.tiles_x) * orows;
   const int xs = ((x0 + 1) / 4) * 4 - 4;  // x0 - 3 rounded down to a multiple of 4 (x0 >= 0)
   const int off = (x0 - 3) - xs;           // 0..3
-  const int x = x0 - 3 + lane, y = y0 - 3 + row;
+  const int x = x0 - 3 + lane;
   const int zs = item.zc * FV.zchunk;
   const int ze = min(zs + FV.zchunk, G.vz);
   const int kstart = max(zs - 3, 0);
@@ -105,12 +111,23 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   float* const oy = V->pb_out[par][1];
   float* const oz = V->pb_out[par][2];
   float* const ogb = V->gb;
-  const bool in = x >= 0 && x < G.vx && y >= 0 && y < G.vy;
-  const bool xpos = x > 0, xnl = x != G.vx - 1, ypos = y > 0, ynl = y != G.vy - 1;
-  const bool own = in && lane >= 3 && lane < 3 + ocols && row >= 3 && row < 3 + orows;
-  const long long rowoff = (long long)y * G.pitch + x;
-  const int si = row * kAfBoxX + off + lane;  // this thread's element in a staged plane
-  const int xi = (row + 1) * 32 + lane;       // ... in an exchange plane
+  const bool xin = x >= 0 && x < G.vx, xpos = x > 0, xnl = x != G.vx - 1;
+  const bool xown = xin && lane >= 3 && lane < 3 + ocols;
+  bool rin[kAfR], ypos[kAfR], ynl[kAfR], rown[kAfR];
+  long long rowoff[kAfR];
+  int si[kAfR];
+#pragma unroll
+  for (int j = 0; j < kAfR; ++j) {
+    const int row = warp * kAfR + j;
+    const int y = y0 - 3 + row;
+    rin[j] = xin && y >= 0 && y < G.vy;
+    ypos[j] = y > 0;
+    ynl[j] = y != G.vy - 1;
+    rown[j] = rin[j] && xown && row >= 3 && row < 3 + orows;
+    rowoff[j] = (long long)y * G.pitch + x;
+    si[j] = row * kAfBoxX + off + lane;  // element in a staged plane
+  }
+  const int xw = (warp + 1) * 32 + lane;  // this warp's entry in an exchange row
 
   if (threadIdx.x == 0) {
     abort_cta = fp.error_flag ? (*(volatile int*)fp.error_flag & 2) : 0;
@@ -122,8 +139,9 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     for (int s = 0; s < kAfPzSlots; ++s) mbar_init(&zbars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    stop = 0;
   }
-  // exchange planes: rows -1 and 32 are read as zeros (never written)
+  // exchange rows of warps -1 and 16 are read as zeros (never written)
   for (int i = threadIdx.x; i < kAfXPlanes * kAfX; i += kAfThreads) xp[i] = 0.f;
   __syncthreads();
   if (abort_cta) return;
@@ -155,7 +173,6 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   // barrier that precedes the reads (the barrier extends its acquire to every
   // thread).  A wait that runs out raises `stop`, read by all after the
   // barrier: the CTA leaves the march, drains its copies and reports.
-  __shared__ int stop;
   auto wait0 = [&](uint64_t* bar, unsigned parity) {  // thread 0 only
     if (stop) return;
     if (!mbar_wait_bounded(bar, parity, kTmaWaitLimitNs)) stop = 1;
@@ -167,7 +184,6 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     wait0(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1));
   };
   if (threadIdx.x == 0) {
-    stop = 0;
     for (int p = kstart; p <= min(kstart + 1, kA_end); ++p) issue_main(p);
     for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
     wait_main0(kstart);
@@ -184,21 +200,27 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
 
   auto march = [&](auto tag) {
     constexpr bool INT = decltype(tag)::value;
-    const bool vin = INT || in, vxpos = INT || xpos, vxnl = INT || xnl, vypos = INT || ypos, vynl = INT || ynl;
-    // carries (this thread's column)
-    float gprev = 0.f, dbp_prev = 0.f;                                                          // plane k-1
-    float ppx_c = 0.f, ppy_c = 0.f, ppz_c = 0.f, tx_c = 0.f, ty_c = 0.f, tz_c = 0.f, S_c = 0.f;  // plane k-1
-    float m_prev = 1.f, f_prev = 0.f;                                                          // plane k-2
-    float qx_e = 0.f, qy_e = 0.f, qz_e = 0.f;                                                  // q of plane k-2
-    float qx_f = 0.f, qy_f = 0.f, qz_f = 0.f;                                                  // q of plane k-3
-    float dbo_f = 0.f, dbo_ff = 0.f;                                                           // dbo of k-3, k-4
-    float pzn_c = 0.f;
+    const bool vxpos = INT || xpos, vxnl = INT || xnl;
+    // carries, one per row of this thread
+    float gprev[kAfR], dbp_prev[kAfR];                                        // plane k-1
+    float ppx_c[kAfR], ppy_c[kAfR], ppz_c[kAfR], tx_c[kAfR], ty_c[kAfR], tz_c[kAfR], S_c[kAfR];  // k-1
+    float m_prev[kAfR], f_prev[kAfR];                                         // plane k-2
+    float qx_e[kAfR], qy_e[kAfR], qz_e[kAfR];                                 // q of plane k-2
+    float qx_f[kAfR], qy_f[kAfR], qz_f[kAfR];                                 // q of plane k-3
+    float dbo_f[kAfR], dbo_ff[kAfR];                                          // dbo of planes k-3, k-4
+    float pzn_c[kAfR];
+#pragma unroll
+    for (int j = 0; j < kAfR; ++j) {
+      gprev[j] = dbp_prev[j] = ppx_c[j] = ppy_c[j] = ppz_c[j] = tx_c[j] = ty_c[j] = tz_c[j] = S_c[j] = 0.f;
+      m_prev[j] = 1.f;
+      f_prev[j] = qx_e[j] = qy_e[j] = qz_e[j] = qx_f[j] = qy_f[j] = qz_f[j] = dbo_f[j] = dbo_ff[j] = pzn_c[j] = 0.f;
+    }
     bool have_pz = false;
     const float* cur = mslot(kstart);
     const float* zc = zslot(kstart);
-    int msi = 0, zsi = 0;  // ring positions of plane k
-    long long go = (long long)(kstart - 2) * G.plane + rowoff;      // gb output at plane k-2
-    long long fo = (long long)(kstart - 3) * G.plane + rowoff;      // old-flow output at plane k-3
+    int msi = 0, zsi = 0;                           // ring positions of plane k
+    long long go = (long long)(kstart - 2) * G.plane;  // plane offset of gb outputs (plane k-2)
+    long long fo = (long long)(kstart - 3) * G.plane;  // ... of old-flow outputs (plane k-3)
 
     for (int k = kstart; k <= kend; ++k) {
       const bool doA = k <= kA_end;
@@ -208,39 +230,46 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       const bool doE = ko >= kstart && ko <= ze - 1;
       const int kf = k - 3;
       const bool doF = kf >= zs && kf < ze;
-      const int kb = k & 1;  // exchange-plane parity of plane k
+      const int kb = k & 1;  // exchange-row parity of plane k
 
       // ---- stage A: g(k) (kern_CalcGradStep on the recomputed divergence)
-      float g = 0.f, px = 0.f, py = 0.f, pz = 0.f, Pbx = 0.f, Pby = 0.f, Pbz = 0.f, dbp = 0.f, dbpl = 0.f,
-            dbpu = 0.f, Sk = 0.f;
+      float g[kAfR], px[kAfR], py[kAfR], pz[kAfR], Pbx[kAfR], Pby[kAfR], Pbz[kAfR], dbp[kAfR], dbpl[kAfR],
+          dbpu[kAfR], Sk[kAfR];
+#pragma unroll
+      for (int j = 0; j < kAfR; ++j)
+        g[j] = px[j] = py[j] = pz[j] = Pbx[j] = Pby[j] = Pbz[j] = dbp[j] = dbpl[j] = dbpu[j] = Sk[j] = 0.f;
       if (doA) {
         const bool has_next = k + 1 < G.vz;
         const int znext = zsi + 1 == kAfPzSlots ? 0 : zsi + 1;
         const float* zn = zslots + znext * kAfPlane;
-        px = cur[si];
-        py = cur[kAfPlane + si];
-        pz = have_pz ? pzn_c : zc[si];
-        const float pxr = cur[si + 1];
-        const float pyd = cur[kAfPlane + si + kAfBoxX];
-        const float pzn = has_next ? zn[si] : 0.f;
-        const float sk = cur[2 * kAfPlane + si], c = cur[3 * kAfPlane + si], u = cur[4 * kAfPlane + si];
-        Pbx = cur[5 * kAfPlane + si];
-        Pby = cur[6 * kAfPlane + si];
-        Pbz = cur[7 * kAfPlane + si];
-        dbp = cur[8 * kAfPlane + si];
-        dbpl = (off + lane) > 0 ? cur[8 * kAfPlane + si - 1] : 0.f;
-        dbpu = row > 0 ? cur[8 * kAfPlane + si - kAfBoxX] : 0.f;
-        Sk = has_s ? cur[9 * kAfPlane + si] : 0.f;
-        float d = (px + py) + pz;
-        if (vxnl) d = d - pxr;
-        if (vynl) d = d - pyd;
-        if (has_next) d = d - pzn;
-        const float gv = step * (((sk + d) - c) - u * icc);
-        g = vin ? gv : 0.f;
-        pzn_c = pzn;
+#pragma unroll
+        for (int j = 0; j < kAfR; ++j) {
+          const int e = si[j];
+          px[j] = cur[e];
+          py[j] = cur[kAfPlane + e];
+          pz[j] = have_pz ? pzn_c[j] : zc[e];
+          const float pxr = cur[e + 1];
+          const float pyd = cur[kAfPlane + e + kAfBoxX];
+          const float pzn = has_next ? zn[e] : 0.f;
+          const float sk = cur[2 * kAfPlane + e], c = cur[3 * kAfPlane + e], u = cur[4 * kAfPlane + e];
+          Pbx[j] = cur[5 * kAfPlane + e];
+          Pby[j] = cur[6 * kAfPlane + e];
+          Pbz[j] = cur[7 * kAfPlane + e];
+          dbp[j] = cur[8 * kAfPlane + e];
+          dbpl[j] = (off + lane) > 0 ? cur[8 * kAfPlane + e - 1] : 0.f;
+          dbpu[j] = (warp * kAfR + j) > 0 ? cur[8 * kAfPlane + e - kAfBoxX] : 0.f;
+          Sk[j] = has_s ? cur[9 * kAfPlane + e] : 0.f;
+          float d = (px[j] + py[j]) + pz[j];
+          if (vxnl) d = d - pxr;
+          if (INT || ynl[j]) d = d - pyd;
+          if (has_next) d = d - pzn;
+          const float gv = step * (((sk + d) - c) - u * icc);
+          g[j] = (INT || rin[j]) ? gv : 0.f;
+          pzn_c[j] = pzn;
+        }
         have_pz = has_next;
       }
-      XG[xi] = g;
+      XG_L[xw] = g[kAfR - 1];
       __syncthreads();  // (1)
       if (threadIdx.x == 0) {
         if (k + 2 <= kA_end) issue_main(k + 2);
@@ -249,64 +278,76 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow) and the total adjoint t(k)
       // of the new flows (incoming plus through the new divergence)
-      float ppx_n = 0.f, ppy_n = 0.f, ppz_n = 0.f, tx_n = 0.f, ty_n = 0.f, tz_n = 0.f;
+      float ppx_n[kAfR], ppy_n[kAfR], ppz_n[kAfR], tx_n[kAfR], ty_n[kAfR], tz_n[kAfR];
       {
-        const float gxm = __shfl_up_sync(FULL, g, 1);
-        const float gym = XG[xi - 32];
-        if (doA && vin) {
-          ppx_n = vxpos ? px - (g - gxm) : 0.f;
-          ppy_n = vypos ? py - (g - gym) : 0.f;
-          ppz_n = k > 0 ? pz - (g - gprev) : 0.f;
-          tx_n = (Pbx + dbp) - (vxpos ? dbpl : 0.f);
-          ty_n = (Pby + dbp) - (vypos ? dbpu : 0.f);
-          tz_n = (Pbz + dbp) - (k > 0 ? dbp_prev : 0.f);
+        const float gup = XG_L[xw - 32];
+#pragma unroll
+        for (int j = 0; j < kAfR; ++j) {
+          const float gxm = __shfl_up_sync(FULL, g[j], 1);
+          const float gym = j ? g[j > 0 ? j - 1 : 0] : gup;
+          const bool vin = doA && (INT || rin[j]);
+          const bool vyp = INT || ypos[j];
+          ppx_n[j] = (vin && vxpos) ? px[j] - (g[j] - gxm) : 0.f;
+          ppy_n[j] = (vin && vyp) ? py[j] - (g[j] - gym) : 0.f;
+          ppz_n[j] = (vin && k > 0) ? pz[j] - (g[j] - gprev[j]) : 0.f;
+          tx_n[j] = vin ? (Pbx[j] + dbp[j]) - (vxpos ? dbpl[j] : 0.f) : 0.f;
+          ty_n[j] = vin ? (Pby[j] + dbp[j]) - (vyp ? dbpu[j] : 0.f) : 0.f;
+          tz_n[j] = vin ? (Pbz[j] + dbp[j]) - (k > 0 ? dbp_prev[j] : 0.f) : 0.f;
+          if (doA) {
+            gprev[j] = g[j];
+            dbp_prev[j] = dbp[j];
+          }
         }
-        if (doA) {
-          gprev = g;
-          dbp_prev = dbp;
-        }
-        XPPY[kb * kAfX + xi] = ppy_n;
-        XTY[kb * kAfX + xi] = ty_n;
+        XPPY_F[kb * kAfX + xw] = ppy_n[0];
+        XTY_F[kb * kAfX + xw] = ty_n[0];
       }
 
       // ---- stage C: |p|, m(k-1) and the adjoint of the multiplier -> F2b(k-1)
-      float m = 1.f, f2b = 0.f;
+      float m[kAfR], f2b[kAfR];
       {
-        const float pxr = __shfl_down_sync(FULL, ppx_c, 1);
-        const float txr = __shfl_down_sync(FULL, tx_c, 1);
-        const float pyd = XPPY[(kb ^ 1) * kAfX + xi + 32];
-        const float tyd = XTY[(kb ^ 1) * kAfX + xi + 32];
-        if (doC && vin) {
-          const bool znl = kc != G.vz - 1;
-          float up = ppx_c * ppx_c;
-          float dn = vxnl ? pxr * pxr : 0.f;
-          float F = up + dn;
-          up = ppy_c * ppy_c;
-          dn = vynl ? pyd * pyd : 0.f;
-          F = F + (up + dn);
-          up = ppz_c * ppz_c;
-          dn = znl ? ppz_n * ppz_n : 0.f;
-          F = F + (up + dn);
-          const float h = 0.5f * F;
-          const float lim = has_s ? alpha * S_c : alpha;
-          if (!(lim > 1.0e-18f && h < (lim * lim) * (1.0f - 0x1p-20f))) {  // else |p| <= lim exactly: m = 1
-            const float Fm = sqrtf(h);
-            if (Fm > lim) {
-              float mb = 0.f;
-              if (vxpos) mb = mb + (tx_c * 0.5f) * ppx_c;
-              if (vxnl) mb = mb + (txr * 0.5f) * pxr;
-              if (vypos) mb = mb + (ty_c * 0.5f) * ppy_c;
-              if (vynl) mb = mb + (tyd * 0.5f) * pyd;
-              if (kc > 0) mb = mb + (tz_c * 0.5f) * ppz_c;
-              if (znl) mb = mb + (tz_n * 0.5f) * ppz_n;
-              m = lim / Fm;
-              f2b = -mb * lim / (4.0f * Fm * Fm * Fm);
-              if (own && kc >= zs && kc < ze) asum += (double)(mb / Fm * (has_s ? S_c : 1.0f));
+        const float pdown = XPPY_F[(kb ^ 1) * kAfX + xw + 32];
+        const float tdown = XTY_F[(kb ^ 1) * kAfX + xw + 32];
+        const bool znl = kc != G.vz - 1;
+#pragma unroll
+        for (int j = 0; j < kAfR; ++j) {
+          const float pxr = __shfl_down_sync(FULL, ppx_c[j], 1);
+          const float txr = __shfl_down_sync(FULL, tx_c[j], 1);
+          const float pyd = j < kAfR - 1 ? ppy_c[j < kAfR - 1 ? j + 1 : j] : pdown;
+          const float tyd = j < kAfR - 1 ? ty_c[j < kAfR - 1 ? j + 1 : j] : tdown;
+          m[j] = 1.f;
+          f2b[j] = 0.f;
+          if (doC && (INT || rin[j])) {
+            const bool vyp = INT || ypos[j], vyn = INT || ynl[j];
+            float up = ppx_c[j] * ppx_c[j];
+            float dn = vxnl ? pxr * pxr : 0.f;
+            float F = up + dn;
+            up = ppy_c[j] * ppy_c[j];
+            dn = vyn ? pyd * pyd : 0.f;
+            F = F + (up + dn);
+            up = ppz_c[j] * ppz_c[j];
+            dn = znl ? ppz_n[j] * ppz_n[j] : 0.f;
+            F = F + (up + dn);
+            const float h = 0.5f * F;
+            const float lim = has_s ? alpha * S_c[j] : alpha;
+            if (!(lim > 1.0e-18f && h < (lim * lim) * (1.0f - 0x1p-20f))) {  // else |p| <= lim exactly: m = 1
+              const float Fm = sqrtf(h);
+              if (Fm > lim) {
+                float mb = 0.f;
+                if (vxpos) mb = mb + (tx_c[j] * 0.5f) * ppx_c[j];
+                if (vxnl) mb = mb + (txr * 0.5f) * pxr;
+                if (vyp) mb = mb + (ty_c[j] * 0.5f) * ppy_c[j];
+                if (vyn) mb = mb + (tyd * 0.5f) * pyd;
+                if (kc > 0) mb = mb + (tz_c[j] * 0.5f) * ppz_c[j];
+                if (znl) mb = mb + (tz_n[j] * 0.5f) * ppz_n[j];
+                m[j] = lim / Fm;
+                f2b[j] = -mb * lim / (4.0f * Fm * Fm * Fm);
+                if (rown[j] && kc >= zs && kc < ze) asum += (double)(mb / Fm * (has_s ? S_c[j] : 1.0f));
+              }
             }
           }
         }
-        XM[xi] = m;
-        XF[xi] = f2b;
+        XM_L[xw] = m[kAfR - 1];
+        XF_L[xw] = f2b[kAfR - 1];
       }
       if (threadIdx.x == 0) {  // the planes the next step's stage A reads
         if (k + 1 <= kA_end) wait_main0(k + 1);
@@ -316,67 +357,85 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       if (stop) break;
 
       // ---- stage D: q(k-1), the adjoint of p'
-      float qx_n = 0.f, qy_n = 0.f, qz_n = 0.f;
+      float qx_n[kAfR], qy_n[kAfR], qz_n[kAfR];
       {
-        const float mxm = __shfl_up_sync(FULL, m, 1);
-        const float fxm = __shfl_up_sync(FULL, f2b, 1);
-        const float mym = XM[xi - 32];
-        const float fym = XF[xi - 32];
-        if (doC && vin) {
-          qx_n = vxpos ? (tx_c * 0.5f) * (m + mxm) + (2.0f * ppx_c) * (f2b + fxm) : 0.f;
-          qy_n = vypos ? (ty_c * 0.5f) * (m + mym) + (2.0f * ppy_c) * (f2b + fym) : 0.f;
-          qz_n = kc > 0 ? (tz_c * 0.5f) * (m + m_prev) + (2.0f * ppz_c) * (f2b + f_prev) : 0.f;
+        const float mup = XM_L[xw - 32], fup = XF_L[xw - 32];
+#pragma unroll
+        for (int j = 0; j < kAfR; ++j) {
+          const float mxm = __shfl_up_sync(FULL, m[j], 1);
+          const float fxm = __shfl_up_sync(FULL, f2b[j], 1);
+          const float mym = j ? m[j > 0 ? j - 1 : 0] : mup;
+          const float fym = j ? f2b[j > 0 ? j - 1 : 0] : fup;
+          qx_n[j] = qy_n[j] = qz_n[j] = 0.f;
+          if (doC && (INT || rin[j])) {
+            qx_n[j] = vxpos ? (tx_c[j] * 0.5f) * (m[j] + mxm) + (2.0f * ppx_c[j]) * (f2b[j] + fxm) : 0.f;
+            qy_n[j] = (INT || ypos[j]) ? (ty_c[j] * 0.5f) * (m[j] + mym) + (2.0f * ppy_c[j]) * (f2b[j] + fym) : 0.f;
+            qz_n[j] = kc > 0 ? (tz_c[j] * 0.5f) * (m[j] + m_prev[j]) + (2.0f * ppz_c[j]) * (f2b[j] + f_prev[j]) : 0.f;
+          }
+          if (doC) {
+            m_prev[j] = m[j];
+            f_prev[j] = f2b[j];
+          }
         }
-        if (doC) {
-          m_prev = m;
-          f_prev = f2b;
-        }
-        XQY[(kb ^ 1) * kAfX + xi] = qy_n;  // plane k-1
+        XQY_F[(kb ^ 1) * kAfX + xw] = qy_n[0];  // plane k-1
       }
 
       // ---- stage E: gb(k-2), the adjoint of g, and dbo = step * gb
-      float dbo = 0.f;
+      float dbo[kAfR];
       {
-        const float qxr = __shfl_down_sync(FULL, qx_e, 1);
-        const float qyd = XQY[kb * kAfX + xi + 32];  // plane k-2
-        if (doE && vin) {
-          float gb = -((qx_e + qy_e) + qz_e);
-          if (vxnl) gb = gb + qxr;
-          if (vynl) gb = gb + qyd;
-          if (ko != G.vz - 1) gb = gb + qz_n;
-          dbo = step * gb;
-          if (own && ko >= zs) ogb[go] = gb;
+        const float qdown = XQY_F[kb * kAfX + xw + 32];  // plane k-2
+#pragma unroll
+        for (int j = 0; j < kAfR; ++j) {
+          const float qxr = __shfl_down_sync(FULL, qx_e[j], 1);
+          const float qyd = j < kAfR - 1 ? qy_e[j < kAfR - 1 ? j + 1 : j] : qdown;
+          dbo[j] = 0.f;
+          if (doE && (INT || rin[j])) {
+            float gb = -((qx_e[j] + qy_e[j]) + qz_e[j]);
+            if (vxnl) gb = gb + qxr;
+            if (INT || ynl[j]) gb = gb + qyd;
+            if (ko != G.vz - 1) gb = gb + qz_n[j];
+            dbo[j] = step * gb;
+            if (rown[j] && ko >= zs) ogb[go + rowoff[j]] = gb;
+          }
         }
-        XD[kb * kAfX + xi] = dbo;  // plane k-2
+        XD_L[kb * kAfX + xw] = dbo[kAfR - 1];  // plane k-2
       }
 
       // ---- stage F: adjoint of the old flows at k-3
       {
-        const float dxl = __shfl_up_sync(FULL, dbo_f, 1);
-        const float dyu = XD[(kb ^ 1) * kAfX + xi - 32];  // plane k-3
-        if (doF && own) {
-          ox[fo] = (qx_f + dbo_f) - (vxpos ? dxl : 0.f);
-          oy[fo] = (qy_f + dbo_f) - (vypos ? dyu : 0.f);
-          oz[fo] = (qz_f + dbo_f) - (kf > 0 ? dbo_ff : 0.f);
+        const float dup = XD_L[(kb ^ 1) * kAfX + xw - 32];  // plane k-3
+#pragma unroll
+        for (int j = 0; j < kAfR; ++j) {
+          const float dxl = __shfl_up_sync(FULL, dbo_f[j], 1);
+          const float dyu = j ? dbo_f[j > 0 ? j - 1 : 0] : dup;
+          if (doF && rown[j]) {
+            const long long o = fo + rowoff[j];
+            ox[o] = (qx_f[j] + dbo_f[j]) - (vxpos ? dxl : 0.f);
+            oy[o] = (qy_f[j] + dbo_f[j]) - ((INT || ypos[j]) ? dyu : 0.f);
+            oz[o] = (qz_f[j] + dbo_f[j]) - (kf > 0 ? dbo_ff[j] : 0.f);
+          }
         }
       }
 
       // ---- rotate carries and ring positions
-      ppx_c = ppx_n;
-      ppy_c = ppy_n;
-      ppz_c = ppz_n;
-      tx_c = tx_n;
-      ty_c = ty_n;
-      tz_c = tz_n;
-      S_c = Sk;
-      qx_f = qx_e;
-      qy_f = qy_e;
-      qz_f = qz_e;
-      qx_e = qx_n;
-      qy_e = qy_n;
-      qz_e = qz_n;
-      dbo_ff = dbo_f;
-      dbo_f = dbo;
+#pragma unroll
+      for (int j = 0; j < kAfR; ++j) {
+        ppx_c[j] = ppx_n[j];
+        ppy_c[j] = ppy_n[j];
+        ppz_c[j] = ppz_n[j];
+        tx_c[j] = tx_n[j];
+        ty_c[j] = ty_n[j];
+        tz_c[j] = tz_n[j];
+        S_c[j] = Sk[j];
+        qx_f[j] = qx_e[j];
+        qy_f[j] = qy_e[j];
+        qz_f[j] = qz_e[j];
+        qx_e[j] = qx_n[j];
+        qy_e[j] = qy_n[j];
+        qz_e[j] = qz_n[j];
+        dbo_ff[j] = dbo_f[j];
+        dbo_f[j] = dbo[j];
+      }
       msi = msi + 1 == kAfMainSlots ? 0 : msi + 1;
       zsi = zsi + 1 == kAfPzSlots ? 0 : zsi + 1;
       cur = mslots + msi * (kAfMainArrays * kAfPlane);
@@ -391,27 +450,23 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
 
   // alpha gradient: block sum, one atomic per CTA
   for (int o = 16; o > 0; o >>= 1) asum += __shfl_down_sync(FULL, asum, o);
-  if (lane == 0) red[row] = asum;
+  if (lane == 0) red[warp] = asum;
   __syncthreads();
-  if (row == 0) {
-    double v = red[lane];
+  if (warp == 0) {
+    double v = lane < kAfWarps ? red[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
     if (lane == 0 && v != 0.0) atomicAdd(V->alpha_grad, v);
   }
-  if (timed_out) {
+  if (timed_out && threadIdx.x == 0) {
     if (fp.error_flag) atomicOr(fp.error_flag, 2);
-  }
-  if (threadIdx.x == 0) {
     // copies still in flight into this CTA's shared memory must land before it
-    // exits: after a time-out wait (bounded) for the last plane of each slot
-    if (timed_out) {
-      for (int p = max(kstart, kA_end - kAfMainSlots + 1); p <= kA_end; ++p)
-        mbar_wait_bounded(&mbars[(p - kstart) % kAfMainSlots], (unsigned)(((p - kstart) / kAfMainSlots) & 1),
-                          kTmaWaitLimitNs);
-      for (int p = max(kstart, kpz_end - kAfPzSlots + 1); p <= kpz_end; ++p)
-        mbar_wait_bounded(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1),
-                          kTmaWaitLimitNs);
-    }
+    // exits: wait (bounded) for the last plane of each slot
+    for (int p = max(kstart, kA_end - kAfMainSlots + 1); p <= kA_end; ++p)
+      mbar_wait_bounded(&mbars[(p - kstart) % kAfMainSlots], (unsigned)(((p - kstart) / kAfMainSlots) & 1),
+                        kTmaWaitLimitNs);
+    for (int p = max(kstart, kpz_end - kAfPzSlots + 1); p <= kpz_end; ++p)
+      mbar_wait_bounded(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1),
+                        kTmaWaitLimitNs);
   }
 }
 
