@@ -169,6 +169,41 @@ int hmf_get_alpha_gradient(hmf_ctx* ctx, double* out, int n);
  * segments were recomputed. */
 int hmf_get_adjoint_plan(const hmf_ctx* ctx, int* checkpoint_every, int* recomputed_segments);
 
+/* ---- Vote and energy (the steps after a solve) ----------------------------
+ * hmf_vote replaces CUDA_CIV_COMPUTE (CUDA_imagevote.h, the vtkCudaImageVote
+ * filter) for float inputs and int labels: out[i] = values[k] of the input k
+ * with the largest value at voxel i (values NULL: k).  semantics
+ * HMF_SEMANTICS_REF_CUDA follows vtkCudaImageVote (running maximum from
+ * input 0, an input takes over when value >= maximum: the last of a tie
+ * wins, CUDA_imagevote.cu:30-46), HMF_SEMANTICS_REF_CPU follows vtkImageVote
+ * (the first maximum wins, vtkImageVote.cxx:285-306).  `where` applies to
+ * the inputs and the output alike; errors read with hmf_last_error(NULL).
+ * hmf_get_vote / hmf_batch_get_vote vote over a context's final leaf labels
+ * (leaves in hmf_leaf_order, ids = vertex ids; the context's semantics picks
+ * the tie rule); the output is dense VX*VY*VZ. */
+int hmf_vote(int n_inputs, const float* const* inputs, const int* values, long long n_voxels, int semantics,
+             int* out, int where, void* stream);
+int hmf_get_vote(hmf_ctx* ctx, int* out, int where, void* stream);
+int hmf_batch_get_vote(hmf_ctx* ctx, int volume, int* out, int where, void* stream);
+
+/* Energy decomposition of a labelling; replaces the CUDA_GHMFD_* launchers
+ * (CUDA_hierarchicalmaxflowdecomp.h) behind
+ * vtkCudaHierarchicalMaxFlowDecomposition::GetF0 / GetF
+ * (vtkCudaHierarchicalMaxFlowDecomposition.h).  f0 = sum over leaves and
+ * voxels of D*u; f[v] (per vertex id, root 0) = sum over voxels of
+ * S_v * 0.5*sqrt(|grad u_v|^2) with clamped central differences, S_v = 1
+ * without a smoothness image, a branch's labelling being the sum of its
+ * children's.  Per-voxel terms in FP32 as the reference forms them, sums in
+ * FP64.  data, labels: per vertex id (leaves needed); smooth may be NULL.
+ * Synchronous.  hmf_get_energy / hmf_batch_get_energy evaluate a context's
+ * final labels with its own inputs (which must still be valid); they return
+ * n_nodes. */
+int hmf_decomposition_energy(int vx, int vy, int vz, const int* parent, int n_nodes, const float* const* data,
+                             const float* const* labels, const float* const* smooth, int where, double* f0,
+                             double* f, void* stream);
+int hmf_get_energy(hmf_ctx* ctx, double* f0, double* f, int n);
+int hmf_batch_get_energy(hmf_ctx* ctx, int volume, double* f0, double* f, int n);
+
 /* Message of the last failed call on ctx (or, when ctx is NULL, of the last
  * failed hmf_create or hmf_solve_noalloc on this thread). */
 const char* hmf_last_error(const hmf_ctx* ctx);

@@ -102,7 +102,8 @@ def build_reference_cubin(force: bool = False) -> str | None:
     d2 = os.path.join(REFERENCE_ROOT, "Common/vtkCudaCommonStatic")
     d3 = os.path.join(REFERENCE_ROOT, "Common/vtkCudaCommon")
     out = os.path.join(REF_OUT, "hmf_ref_kernels.cubin")
-    srcs = [unit, os.path.join(d1, "CUDA_hierarchicalmaxflow.cu"), os.path.join(d2, "CUDA_commonKernels.cu")]
+    srcs = [unit, os.path.join(d1, "CUDA_hierarchicalmaxflow.cu"), os.path.join(d2, "CUDA_commonKernels.cu"),
+            os.path.join(d1, "CUDA_hierarchicalmaxflowdecomp.cu"), os.path.join(d1, "CUDA_imagevote.cu")]
     if force or not _newer(out, srcs):
         # `saturate` was a legacy CUDA helper that CUDA 13 no longer ships.
         _run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",

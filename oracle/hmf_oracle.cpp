@@ -961,6 +961,114 @@ int ORACLE_ENTRY(int semantics, int precision, int threads, int vx, int vy, int 
 }
 
 #ifndef HMF_ORACLE_WITH_REFERENCE
+// Label vote over n_inputs float images of n voxels (the step after the
+// solve that turns label probabilities into one label per voxel).
+// semantics 0 = vtkCudaImageVote: the running maximum starts at input 0 and
+// each input k in port order replaces it when value >= maximum
+// (CUDA_imagevote.cu:30-46, launched per input :249-256), so the last of a
+// tie wins.  semantics 1 = vtkImageVote (CPU, vtkImageVote.cxx:285-306): the
+// first input, then any strictly greater one, wins; no input -> 0.
+int oracle_vote(int semantics, int n_inputs, const float* const* inputs, const int* values, long long n, int* out) {
+  g_err.clear();
+  if (n_inputs < 1) { g_err = "the vote needs at least one input"; return -1; }
+  for (long long i = 0; i < n; ++i) {
+    if (semantics == 0) {
+      float mx = inputs[0][i];
+      int id = values[0];
+      for (int k = 0; k < n_inputs; ++k) {
+        const float v = inputs[k][i];
+        if (v >= mx) { id = values[k]; mx = v; }
+      }
+      out[i] = id;
+    } else {
+      int id = -1;
+      float mx = 0.0f;
+      for (int k = 0; k < n_inputs; ++k)
+        if (id == -1 || inputs[k][i] > mx) { id = values[k]; mx = inputs[k][i]; }
+      out[i] = id == -1 ? 0 : id;
+    }
+  }
+  return 0;
+}
+
+// Energy decomposition of a labelling (vtkCudaHierarchicalMaxFlowDecomposition,
+// .cxx:640-806, kernels CUDA_hierarchicalmaxflowdecomp.cu:19-279).
+//   f0   = sum over leaves and voxels of D_l * u_l            (:670, :40-86)
+//   f[v] = sum over voxels of S_v * g_v for every non-root vertex, where
+//          g = 0.5f * sqrtf(((0 + dX^2) + dY^2) + dZ^2) with central
+//          differences clamped at the volume border (:19-38) and S_v = 1
+//          without a smoothness image; a branch's labelling is the sum of its
+//          children's, added in child order (:750-806).
+// Per-voxel terms in FP32 as the reference kernels form them; the sums over
+// voxels in FP64 (the reference reduces in FP32).  terms_out (optional,
+// [n][V]): the per-voxel terms S_v*g_v.
+int oracle_energy(int vx, int vy, int vz, int n_nodes, const int* parent, const float* const* data,
+                  const float* const* labels, const float* const* smooth, double* f0_out, double* f_out,
+                  float* terms_out) {
+  g_err.clear();
+  if (vx <= 0 || vy <= 0 || vz <= 0) { g_err = "bad dimensions"; return -1; }
+  Tree t;
+  if (!t.build(n_nodes, parent)) return -2;
+  const long V = (long)vx * vy * vz;
+  for (int v = 0; v < n_nodes; ++v)
+    if (t.leaf(v) && (!data || !data[v] || !labels || !labels[v])) { g_err = "missing leaf data or label"; return -3; }
+  // labellings of every non-root vertex: leaves as given, branches summed
+  std::vector<std::vector<float>> u(n_nodes);
+  std::vector<int> post;
+  {
+    std::vector<std::pair<int, int>> st{{t.root, 0}};
+    while (!st.empty()) {
+      auto& top = st.back();
+      if (top.second < (int)t.kids[top.first].size()) {
+        const int k = t.kids[top.first][top.second++];
+        st.push_back({k, 0});
+      } else {
+        post.push_back(top.first);
+        st.pop_back();
+      }
+    }
+  }
+  for (int v : post) {
+    if (v == t.root) continue;
+    if (t.leaf(v)) {
+      u[v].assign(labels[v], labels[v] + V);
+    } else {
+      u[v].assign(V, 0.0f);
+      for (int k : t.kids[v])
+        for (long i = 0; i < V; ++i) u[v][i] = u[v][i] + u[k][i];
+    }
+  }
+  double f0 = 0.0;
+  for (int v : t.preorder)
+    if (t.leaf(v))
+      for (long i = 0; i < V; ++i) f0 += (double)(data[v][i] * u[v][i]);
+  const long sxy = (long)vx * vy;
+  for (int v = 0; v < n_nodes; ++v) {
+    double fv = 0.0;
+    if (v != t.root) {
+      const std::vector<float>& b = u[v];
+      for (long i = 0; i < V; ++i) {
+        const int x = (int)(i % vx), y = (int)((i / vx) % vy), z = (int)(i / sxy);
+        const float cur = b[i];
+        float g2 = 0.0f;
+        const float xh = x == vx - 1 ? cur : b[i + 1], xl = x == 0 ? cur : b[i - 1];
+        g2 += (xh - xl) * (xh - xl);
+        const float yh = y == vy - 1 ? cur : b[i + vx], yl = y == 0 ? cur : b[i - vx];
+        g2 += (yh - yl) * (yh - yl);
+        const float zh = z == vz - 1 ? cur : b[i + sxy], zl = z == 0 ? cur : b[i - sxy];
+        g2 += (zh - zl) * (zh - zl);
+        float term = 0.5f * std::sqrt(g2);
+        if (smooth && smooth[v]) term = smooth[v][i] * term;
+        if (terms_out) terms_out[(long)v * V + i] = term;
+        fv += (double)term;
+      }
+    }
+    if (f_out) f_out[v] = fv;
+  }
+  if (f0_out) *f0_out = f0;
+  return 0;
+}
+
 // Loss and gradients of the REF_CUDA solve (see AdjointRun).  truth: class
 // per voxel = index into the DFS pre-order leaf list.  dD_out [n_nodes * V]
 // (leaf rows filled), dalpha_out [n_nodes], u_out [n_nodes * V] final labels.

@@ -153,3 +153,55 @@ def adjoint(dims, parent, data, truth, smooth=None, alpha=None, iterations=20, s
         raise RuntimeError("oracle adjoint failed (%d): %s" % (rc, lib.oracle_last_error().decode()))
     shape = (n, vz, vy, vx)
     return {"loss": loss.value, "dD": dD.reshape(shape), "dalpha": da, "u": u.reshape(shape)}
+
+
+def vote(inputs, values=None, semantics=REF_CUDA):
+    """Label vote over float images (oracle restatement): returns int32 ids,
+    values[k] for the winning input k (default: k)."""
+    lib = port_library()
+    fn = lib.oracle_vote
+    fn.restype = ctypes.c_int
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in inputs]
+    shape = arrs[0].shape
+    n = arrs[0].size
+    ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    vals = np.ascontiguousarray(values if values is not None else np.arange(len(arrs)), dtype=np.int32)
+    out = np.zeros(n, np.int32)
+    rc = fn(int(semantics), len(arrs), ptrs, vals.ctypes.data_as(ctypes.c_void_p), ctypes.c_longlong(n),
+            out.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("oracle vote failed (%d): %s" % (rc, lib.oracle_last_error().decode()))
+    return out.reshape(shape)
+
+
+def energy(dims, parent, data, labels, smooth=None, want_terms=False):
+    """Energy decomposition of leaf labellings (oracle restatement):
+    {"f0": float, "f": [n] per vertex, optional "terms": [n, VZ, VY, VX]}."""
+    lib = port_library()
+    fn = lib.oracle_energy
+    fn.restype = ctypes.c_int
+    vx, vy, vz = (int(d) for d in dims)
+    n = len(parent)
+    V = vx * vy * vz
+    par = (ctypes.c_int * n)(*[int(p) for p in parent])
+    keep = []
+    dp = (ctypes.c_void_p * n)()
+    lp = (ctypes.c_void_p * n)()
+    sp = (ctypes.c_void_p * n)()
+    for v in range(n):
+        for src, dst in ((data, dp), (labels, lp), (smooth, sp)):
+            if src is not None and src.get(v) is not None:
+                a = np.ascontiguousarray(src[v], dtype=np.float32).reshape(-1)
+                keep.append(a)
+                dst[v] = a.ctypes.data
+    f0 = ctypes.c_double()
+    f = np.zeros(n, np.float64)
+    terms = np.zeros((n, V), np.float32) if want_terms else None
+    rc = fn(vx, vy, vz, n, par, dp, lp, sp, ctypes.byref(f0), f.ctypes.data_as(ctypes.c_void_p),
+            terms.ctypes.data_as(ctypes.c_void_p) if terms is not None else None)
+    if rc != 0:
+        raise RuntimeError("oracle energy failed (%d): %s" % (rc, lib.oracle_last_error().decode()))
+    out = {"f0": f0.value, "f": f}
+    if terms is not None:
+        out["terms"] = terms.reshape((n, vz, vy, vx))
+    return out

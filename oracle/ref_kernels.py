@@ -14,8 +14,10 @@ reference allocates them (:513-538, CUDA_hierarchicalmaxflow.cu:33-60), since
 its kernels read up to one plane outside a buffer before masking.  Buffers are
 torch CUDA tensors; kernels run on torch's current stream.
 
+It also runs the reference's vote kernel (CUDA_imagevote.cu) and the
+gradient kernel of its energy decomposition (CUDA_hierarchicalmaxflowdecomp.cu).
 It is used only to generate golden vectors (tests/golden/make_golden.py) and
-to pin the REF_CUDA oracle; nothing in the product imports it.
+to pin the oracle; nothing in the product imports it.
 """
 from __future__ import annotations
 
@@ -49,11 +51,20 @@ _NAMES = {
     "magconst": "_Z30kern_ComputeFlowMagConstSmoothPfS_S_S_f4int2i",
     "project": "_Z12kern_ProjectPfS_S_S_4int2i",
     "divergence": "_Z15kern_DivergencePfS_S_S_4int2i",
+    # vote (CUDA_imagevote.cu:30, instantiated for float inputs / int labels)
+    "civ": "_Z23CUDA_CIV_kernMinWithMapIfiEvPT_S1_PT0_S2_i",
+    # energy decomposition (CUDA_hierarchicalmaxflowdecomp.cu:19)
+    "ghmfd_grad": "_Z25kern_GHMFD_GradientBufferPfS_4int3i",
+    "mul": "_Z15MultiplyBuffersIfEvPT_S1_i",
 }
 
 
 class _Int2(ctypes.Structure):
     _fields_ = [("x", ctypes.c_int), ("y", ctypes.c_int)]
+
+
+class _Int3(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_int), ("y", ctypes.c_int), ("z", ctypes.c_int)]
 
 
 class _Ptr(int):
@@ -88,7 +99,7 @@ class ReferenceKernels:
     def launch(self, key, size, *args):
         cargs = []
         for a in args:
-            if isinstance(a, _Int2):
+            if isinstance(a, (_Int2, _Int3)):
                 cargs.append(a)
             elif isinstance(a, _Ptr):
                 cargs.append(ctypes.c_void_p(int(a)))
@@ -251,3 +262,57 @@ def _as_tensor(keep, ptr, V, pad):
         if base == ptr:
             return t[pad:pad + V]
     raise KeyError("unknown buffer")
+
+
+def _padded(keep, V, pad, init=None, dtype=None):
+    import torch
+
+    t = torch.zeros(V + 2 * pad, dtype=dtype or torch.float32, device="cuda")
+    if init is not None:
+        t[pad:pad + V] = torch.from_numpy(np.ascontiguousarray(init).reshape(-1)).cuda()
+    keep.append(t)
+    return t, _Ptr(t.data_ptr() + t.element_size() * pad)
+
+
+def vote(inputs, values):
+    """The reference CUDA vote (CUDA_CIV_COMPUTE, CUDA_imagevote.cu:230-268):
+    maximum buffer = input 0, then kern_MinWithMap per input in order (its
+    kernels read before their bounds check, so buffers are padded).
+    Returns int32 labels shaped like the inputs."""
+    import torch
+
+    K = ReferenceKernels()
+    shape = np.asarray(inputs[0]).shape
+    V = int(np.prod(shape))
+    pad = 2 * NUMTHREADS
+    keep = []
+    _, pmx = _padded(keep, V, pad, np.asarray(inputs[0], dtype=np.float32))
+    out, pout = _padded(keep, V, pad, dtype=torch.int32)
+    for k, a in enumerate(inputs):
+        _, pin = _padded(keep, V, pad, np.asarray(a, dtype=np.float32))
+        K.launch("civ", V, pin, pmx, pout, int(values[k]), V)
+    torch.cuda.synchronize()
+    return out[pad:pad + V].cpu().numpy().reshape(shape)
+
+
+def gradient_terms(label, dims, smooth=None):
+    """kern_GHMFD_GradientBuffer of one labelling, times a smoothness image
+    by MultiplyBuffers when given, as CUDA_GHMFD_*ForLabel form the per-voxel
+    terms (CUDA_hierarchicalmaxflowdecomp.cu:19-38, :88-139).  float32
+    [VZ, VY, VX]."""
+    import torch
+
+    K = ReferenceKernels()
+    vx, vy, vz = (int(d) for d in dims)
+    V = vx * vy * vz
+    pad = vx * vy + 2 * NUMTHREADS
+    keep = []
+    _, plab = _padded(keep, V, pad, np.asarray(label, dtype=np.float32))
+    g, pg = _padded(keep, V, pad)
+    K.launch("ghmfd_grad", V, plab, pg, _Int3(vx, vy, vz), V)
+    if smooth is not None:
+        sm, psm = _padded(keep, V, pad, np.asarray(smooth, dtype=np.float32))
+        K.launch("mul", V, psm, pg, V)
+        g = sm
+    torch.cuda.synchronize()
+    return g[pad:pad + V].cpu().numpy().reshape(vz, vy, vx)

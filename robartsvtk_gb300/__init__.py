@@ -6,6 +6,7 @@ The compute is libhmf_gb300.so (CUDA kernels + C ABI, include/hmf.h); this
 package binds it and mirrors the reference's filter API.
 """
 from .segmentation import (REF_CPU, REF_CUDA, HierarchicalMaxFlowSegmentation, HMFBatchSolver,  # noqa: F401
-                           HMFError, HMFSolver)
+                           HMFError, HMFSolver, decomposition_energy, vote)
 
-__all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]
+__all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError",
+           "vote", "decomposition_energy"]

@@ -55,6 +55,14 @@ SIGNATURES = [
     ("hmf_get_data_gradient", _I, [_P, _I, _P, _I, _P]),
     ("hmf_get_alpha_gradient", _I, [_P, ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_get_adjoint_plan", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("hmf_vote", _I, [_I, ctypes.POINTER(_P), ctypes.POINTER(_I), ctypes.c_longlong, _I, _P, _I, _P]),
+    ("hmf_get_vote", _I, [_P, _P, _I, _P]),
+    ("hmf_batch_get_vote", _I, [_P, _I, _P, _I, _P]),
+    ("hmf_decomposition_energy", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                      ctypes.POINTER(_P), _I, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double), _P]),
+    ("hmf_get_energy", _I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
+    ("hmf_batch_get_energy", _I, [_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_solve_noalloc", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                ctypes.POINTER(ctypes.c_double), _I, ctypes.c_float, ctypes.c_float,
                                ctypes.POINTER(_P), _P]),

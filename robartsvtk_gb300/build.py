@@ -1,6 +1,6 @@
 """Builds libhmf_gb300.so in-tree (robartsvtk_gb300/_build/) for sm_103a.
 
-Three translation units (the solver, its adjoint, the C++ facade), compiled
+Four translation units (the solver, its adjoint, the vote and energy, the C++ facade), compiled
 in parallel with nvcc and linked into one shared library that exports the C
 ABI of include/hmf.h and the C++ facade of csrc/hmf_segmentation.hpp.  The
 kernel units are compiled with -fmad=false so the FP32 arithmetic follows the
@@ -25,6 +25,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompi
 UNITS = {
     "hmf_capi.o": ("hmf_capi.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     "hmf_adjoint.o": ("hmf_adjoint.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
+    "hmf_post.o": ("hmf_post.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     "hmf_segmentation.o": ("hmf_segmentation.cpp", ["-x", "cu"]),
 }
 

@@ -654,6 +654,8 @@ int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged) {
   int rc = stage_inputs(c, s, staged);
   if (!rc) rc = prepare_tables(c, s, staged);
   if (rc) return rc;
+  c->st_data = staged.data;
+  c->st_smooth = staged.smooth;
   // flows of parity 0 start at zero
   const size_t bytes = (size_t)c->total * sizeof(float);
   for (int v = 0; v < c->n; ++v) {

@@ -85,6 +85,9 @@ struct hmf_ctx {
   hmf::TreeTable h_tree{};
   std::vector<const float*> h_smooth_list;
 
+  // the staged inputs of the last solve (per vertex; for hmf_get_energy)
+  std::vector<const float*> st_data, st_smooth;
+
   // reverse-mode state of hmf_solve_adjoint (hmf_adjoint.cu), created on demand
   struct AdjointState* adj = nullptr;
 

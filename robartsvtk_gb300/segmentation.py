@@ -18,7 +18,8 @@ import numpy as np
 from . import _capi
 from ._capi import HMF_DEVICE, HMF_HOST, HMF_SEMANTICS_REF_CPU, HMF_SEMANTICS_REF_CUDA, HMFError, check
 
-__all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError"]
+__all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError",
+           "vote", "decomposition_energy"]
 
 REF_CUDA = HMF_SEMANTICS_REF_CUDA
 REF_CPU = HMF_SEMANTICS_REF_CPU
@@ -121,6 +122,19 @@ class HMFSolver:
 
     def sink(self, node: int, out=None, stream=None):
         return self._fetch(self._lib.hmf_get_sink, node, out, stream)
+
+    # -- vote and energy --------------------------------------------------
+    def vote(self, out=None, stream=None):
+        """Label per voxel: the leaf (vertex id) with the largest final label,
+        ties as the context's semantics (REF_CUDA: last leaf, REF_CPU: first).
+        int32 [VZ, VY, VX] numpy array, or into `out` (numpy or torch int32)."""
+        return _fetch_vote(lambda ptr, where, s: self._lib.hmf_get_vote(self._ctx, ptr, where, s),
+                           self.dims, out, stream, self._ctx)
+
+    def energy(self):
+        """Energy decomposition of the final labels: (f0, f) with f per vertex id."""
+        return _fetch_energy(lambda f0, f, n: self._lib.hmf_get_energy(self._ctx, f0, f, n), len(self.parent),
+                             self._ctx)
 
     # -- adjoint ----------------------------------------------------------
     def solve_adjoint(self, truth, checkpoint_every: int = 0, eps: float = 1e-6, stream=None) -> float:
@@ -275,6 +289,18 @@ class HMFBatchSolver:
                                            _stream_handle(stream)), self._ctx)
         return out
 
+    def vote(self, volume: int, out=None, stream=None):
+        """Label per voxel of one volume (see HMFSolver.vote)."""
+        b = int(volume)
+        return _fetch_vote(lambda ptr, where, s: self._lib.hmf_batch_get_vote(self._ctx, b, ptr, where, s),
+                           self.dims[b], out, stream, self._ctx)
+
+    def energy(self, volume: int):
+        """Energy decomposition of one volume's final labels: (f0, f)."""
+        b = int(volume)
+        return _fetch_energy(lambda f0, f, n: self._lib.hmf_batch_get_energy(self._ctx, b, f0, f, n),
+                             len(self.parent), self._ctx)
+
     def stats(self):
         launches = ctypes.c_longlong()
         ms = (ctypes.c_double * 3)()
@@ -301,6 +327,97 @@ class HMFBatchSolver:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def _fetch_vote(call, dims, out, stream, ctx):
+    nvox = dims[0] * dims[1] * dims[2]
+    if out is None:
+        out = np.empty((dims[2], dims[1], dims[0]), dtype=np.int32)
+    if isinstance(out, np.ndarray):
+        if out.dtype != np.int32 or not out.flags["C_CONTIGUOUS"] or out.size != nvox:
+            raise TypeError("out must be a C-contiguous int32 array of the volume's size")
+        ptr, where = out.ctypes.data, HMF_HOST
+    else:
+        import torch
+
+        if out.dtype != torch.int32 or not out.is_contiguous() or out.numel() != nvox:
+            raise TypeError("out must be a contiguous int32 tensor of the volume's size")
+        ptr, where = out.data_ptr(), HMF_DEVICE if out.is_cuda else HMF_HOST
+    check(call(ptr, where, _stream_handle(stream)), ctx)
+    return out
+
+
+def _fetch_energy(call, n, ctx):
+    f0 = ctypes.c_double()
+    f = (ctypes.c_double * n)()
+    check(call(ctypes.byref(f0), f, n), ctx)
+    return f0.value, np.array(f[:], dtype=np.float64)
+
+
+def vote(inputs, values=None, semantics: int = REF_CUDA, out=None, stream=None):
+    """Label vote over equally sized float32 images (numpy on the host or
+    torch tensors on the device): out[i] = values[k] of the input with the
+    largest value (values default: 0..n-1).  Replaces vtkCudaImageVote
+    (REF_CUDA ties: last wins) / vtkImageVote (REF_CPU: first wins)."""
+    lib = _capi.load()
+    n = len(inputs)
+    if n == 0:  # the library reports the error
+        check(lib.hmf_vote(0, None, None, 0, int(semantics), None, HMF_HOST, None))
+    nvox = int(np.prod(inputs[0].shape))
+    keep = []
+    ptrs = (ctypes.c_void_p * n)()
+    where = None
+    for k, a in enumerate(inputs):
+        p, w, kp = _array_pointer(a, nvox)
+        if where is None:
+            where = w
+        elif w != where:
+            raise ValueError("vote inputs must all be on the host or all on the device")
+        ptrs[k] = p
+        keep.append(kp)
+    vals = np.ascontiguousarray(values if values is not None else np.arange(n), dtype=np.int32)
+    if out is None:
+        if where == HMF_DEVICE:
+            import torch
+
+            out = torch.empty(tuple(inputs[0].shape), dtype=torch.int32, device=inputs[0].device)
+        else:
+            out = np.empty(tuple(inputs[0].shape), dtype=np.int32)
+    optr = out.data_ptr() if where == HMF_DEVICE else out.ctypes.data
+    check(lib.hmf_vote(n, ptrs, vals.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), nvox, int(semantics), optr,
+                       where, _stream_handle(stream)))
+    return out
+
+
+def decomposition_energy(dims, parent, data, labels, smooth=None, stream=None):
+    """Energy decomposition of leaf labellings (dicts by vertex id; numpy on
+    the host or CUDA tensors): (f0, f per vertex id).  Replaces
+    vtkCudaHierarchicalMaxFlowDecomposition's GetF0 / GetF."""
+    lib = _capi.load()
+    dims = tuple(int(d) for d in dims)
+    nvox = dims[0] * dims[1] * dims[2]
+    n = len(parent)
+    par = (ctypes.c_int * n)(*[int(p) for p in parent])
+    keep = []
+    arrays = {}
+    where = None
+    for name, src in (("d", data), ("l", labels), ("s", smooth or {})):
+        arr = (ctypes.c_void_p * n)()
+        for v, a in src.items():
+            p, w, kp = _array_pointer(a, nvox)
+            if where is None:
+                where = w
+            elif w != where:
+                raise ValueError("energy inputs must all be on the host or all on the device")
+            arr[int(v)] = p
+            keep.append(kp)
+        arrays[name] = arr
+    f0 = ctypes.c_double()
+    f = (ctypes.c_double * n)()
+    check(lib.hmf_decomposition_energy(dims[0], dims[1], dims[2], par, n, arrays["d"], arrays["l"], arrays["s"],
+                                       where if where is not None else HMF_HOST, ctypes.byref(f0), f,
+                                       _stream_handle(stream)))
+    return f0.value, np.array(f[:], dtype=np.float64)
 
 
 class HierarchicalMaxFlowSegmentation:

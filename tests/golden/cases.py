@@ -16,3 +16,25 @@ CASES = {
 def problem(name):
     seed, dims, parent, iters, smooth_nodes = CASES[name]
     return random_tree_problem(seed, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
+
+# vote and energy-decomposition cases: name -> (seed, (VX, VY, VZ), vote inputs)
+POST_CASES = {
+    "post_9x7x5": (21, (9, 7, 5), 4),
+    "post_1x13x4": (22, (1, 13, 4), 3),
+    "post_31x2x3": (23, (31, 2, 3), 5),
+}
+
+
+def post_problem(name):
+    """Vote inputs quantised to a few levels (so that ties occur), their ids,
+    one labelling and one smoothness image."""
+    import numpy as np
+
+    seed, dims, n_in = POST_CASES[name]
+    rng = np.random.default_rng(seed)
+    shape = dims[::-1]
+    inputs = [(rng.integers(0, 4, size=shape) / 4.0).astype(np.float32) for _ in range(n_in)]
+    values = [int(v) for v in rng.permutation(10)[:n_in]]
+    label = rng.random(shape).astype(np.float32)
+    smooth = rng.random(shape).astype(np.float32)
+    return {"dims": dims, "inputs": inputs, "values": values, "label": label, "smooth": smooth}

@@ -9,6 +9,11 @@
       (oracle/_ref/hmf_ref_kernels.cubin, built from CUDA_hierarchicalmaxflow.cu
       and CUDA_commonKernels.cu), replaying the launch order of
       vtkCudaHierarchicalMaxFlowSegmentation.cxx:106-658.
+  python -m tests.golden.make_golden --ref-post OUT.npz   (on a GPU)
+      the reference's vote kernel (CUDA_imagevote.cu) over seeded images with
+      ties, and the per-voxel terms of its energy decomposition
+      (CUDA_hierarchicalmaxflowdecomp.cu) of seeded labellings, with and
+      without a smoothness image (POST_CASES in tests/golden/cases.py).
 """
 import os
 import sys
@@ -48,9 +53,28 @@ def ref_cuda(path):
     np.savez_compressed(path, **out)
 
 
+def ref_post(path):
+    from oracle import ref_kernels
+    from tests.golden.cases import POST_CASES, post_problem
+    out = {}
+    for name in POST_CASES:
+        p = post_problem(name)
+        out[name + "/vote_inputs"] = np.stack(p["inputs"])
+        out[name + "/vote_values"] = np.asarray(p["values"], np.int32)
+        out[name + "/vote"] = ref_kernels.vote(p["inputs"], p["values"])
+        out[name + "/label"] = p["label"]
+        out[name + "/smooth"] = p["smooth"]
+        out[name + "/grad"] = ref_kernels.gradient_terms(p["label"], p["dims"])
+        out[name + "/grad_smooth"] = ref_kernels.gradient_terms(p["label"], p["dims"], p["smooth"])
+    np.savez_compressed(path, **out)
+
+
 if __name__ == "__main__":
     if "--ref-cpu" in sys.argv:
         ref_cpu(os.path.join(HERE, "ref_cpu_golden.npz"))
     if "--ref-cuda" in sys.argv:
         i = sys.argv.index("--ref-cuda")
         ref_cuda(sys.argv[i + 1] if i + 1 < len(sys.argv) else os.path.join(HERE, "ref_cuda_golden.npz"))
+    if "--ref-post" in sys.argv:
+        i = sys.argv.index("--ref-post")
+        ref_post(sys.argv[i + 1] if i + 1 < len(sys.argv) else os.path.join(HERE, "ref_post_golden.npz"))
