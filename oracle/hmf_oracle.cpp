@@ -995,7 +995,8 @@ int oracle_vote(int semantics, int n_inputs, const float* const* inputs, const i
 // .cxx:640-806, kernels CUDA_hierarchicalmaxflowdecomp.cu:19-279).
 //   f0   = sum over leaves and voxels of D_l * u_l            (:670, :40-86)
 //   f[v] = sum over voxels of S_v * g_v for every non-root vertex, where
-//          g = 0.5f * sqrtf(((0 + dX^2) + dY^2) + dZ^2) with central
+//          g = 0.5f * sqrtf(fma(dZ, dZ, fma(dY, dY, fma(dX, dX, 0)))) (the
+//          reference kernel as nvcc contracts it) with central
 //          differences clamped at the volume border (:19-38) and S_v = 1
 //          without a smoothness image; a branch's labelling is the sum of its
 //          children's, added in child order (:750-806).
@@ -1050,13 +1051,15 @@ int oracle_energy(int vx, int vy, int vz, int n_nodes, const int* parent, const 
       for (long i = 0; i < V; ++i) {
         const int x = (int)(i % vx), y = (int)((i / vx) % vy), z = (int)(i / sxy);
         const float cur = b[i];
+        // the reference kernel is compiled with multiply-add contraction:
+        // each `g += d*d` is one fused multiply-add
         float g2 = 0.0f;
         const float xh = x == vx - 1 ? cur : b[i + 1], xl = x == 0 ? cur : b[i - 1];
-        g2 += (xh - xl) * (xh - xl);
+        g2 = std::fma(xh - xl, xh - xl, g2);
         const float yh = y == vy - 1 ? cur : b[i + vx], yl = y == 0 ? cur : b[i - vx];
-        g2 += (yh - yl) * (yh - yl);
+        g2 = std::fma(yh - yl, yh - yl, g2);
         const float zh = z == vz - 1 ? cur : b[i + sxy], zl = z == 0 ? cur : b[i - sxy];
-        g2 += (zh - zl) * (zh - zl);
+        g2 = std::fma(zh - zl, zh - zl, g2);
         float term = 0.5f * std::sqrt(g2);
         if (smooth && smooth[v]) term = smooth[v][i] * term;
         if (terms_out) terms_out[(long)v * V + i] = term;

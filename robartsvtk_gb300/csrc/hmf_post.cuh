@@ -12,7 +12,8 @@
 //  energy_kernel  f0 = sum of D_l * u_l over leaves and voxels; per non-root
 //                 vertex f_v = sum of S_v * 0.5*sqrt(|grad u_v|^2) with the
 //                 clamped central differences of kern_GHMFD_GradientBuffer
-//                 (CUDA_hierarchicalmaxflowdecomp.cu:19-38), a branch's
+//                 (CUDA_hierarchicalmaxflowdecomp.cu:19-38; its `g += d*d`
+//                 compiled to fused multiply-adds), a branch's
 //                 labelling being the sum of its children's in child order
 //                 (vtkCudaHierarchicalMaxFlowDecomposition.cxx:750-806).  One
 //                 pass over all vertices per voxel (the reference makes one
@@ -123,10 +124,12 @@ __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable*
           for (int p = 0; p < 7; ++p) u7[e][p] = u7[e][p] + u7[c][p];
         }
       }
-      float g2 = 0.0f;
-      g2 += (u7[e][1] - u7[e][2]) * (u7[e][1] - u7[e][2]);
-      g2 += (u7[e][3] - u7[e][4]) * (u7[e][3] - u7[e][4]);
-      g2 += (u7[e][5] - u7[e][6]) * (u7[e][5] - u7[e][6]);
+      // kern_GHMFD_GradientBuffer as compiled (multiply-add contraction):
+      // g += d*d is one fused multiply-add per axis
+      const float dx = u7[e][1] - u7[e][2], dy = u7[e][3] - u7[e][4], dz = u7[e][5] - u7[e][6];
+      float g2 = __fmaf_rn(dx, dx, 0.0f);
+      g2 = __fmaf_rn(dy, dy, g2);
+      g2 = __fmaf_rn(dz, dz, g2);
       float term = 0.5f * sqrtf(g2);
       if (T.smooth[e]) term = __ldg(T.smooth[e] + i) * term;
       acc[1 + e] += (double)term;
