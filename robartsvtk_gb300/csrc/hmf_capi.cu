@@ -800,6 +800,7 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->ev_t0) cudaEventDestroy(c->ev_t0);
   if (c->ev_t1) cudaEventDestroy(c->ev_t1);
   adjoint_free(c);
+  if (c->d_post) cudaFree(c->d_post);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return HMF_OK;

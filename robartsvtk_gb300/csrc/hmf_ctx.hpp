@@ -87,6 +87,7 @@ struct hmf_ctx {
 
   // the staged inputs of the last solve (per vertex; for hmf_get_energy)
   std::vector<const float*> st_data, st_smooth;
+  char* d_post = nullptr;  // hmf_get_energy's table and sums (hmf_post.cu), made on first use
 
   // reverse-mode state of hmf_solve_adjoint (hmf_adjoint.cu), created on demand
   struct AdjointState* adj = nullptr;

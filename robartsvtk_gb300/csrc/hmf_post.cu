@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -40,36 +41,59 @@ struct Scratch {
 };
 
 int launch_vote(hmf_ctx* c, const hmf::VoteInputs& in, const hmf::Geometry& G, int* out, cudaStream_t s) {
-  const long long dense = (long long)G.vx * G.vy * G.vz;
-  hmf::vote_kernel<<<grid_for(dense), hmf::kPostThreads, 0, s>>>(in, G, out);
-  CK(cudaGetLastError(), "vote_kernel launch");
+  bool quads = G.pitch % 4 == 0;
+  for (int k = 0; k < in.n; ++k) quads = quads && (reinterpret_cast<uintptr_t>(in.in[k]) % 16) == 0;
+  if (quads) {
+    const long long nq = (long long)G.vy * G.vz * (G.pitch / 4);
+    hmf::vote4_kernel<<<grid_for(nq), hmf::kPostThreads, 0, s>>>(in, G, out);
+    CK(cudaGetLastError(), "vote4_kernel launch");
+  } else {
+    const long long dense = (long long)G.vx * G.vy * G.vz;
+    hmf::vote_kernel<<<grid_for(dense), hmf::kPostThreads, 0, s>>>(in, G, out);
+    CK(cudaGetLastError(), "vote_kernel launch");
+  }
   return HMF_OK;
 }
 
+constexpr size_t kEnergyTableBytes = (sizeof(hmf::EnergyTable) + 255) / 256 * 256;
+constexpr size_t kEnergyBuffer = kEnergyTableBytes + sizeof(double) * (1 + hmf::kMaxVertices);
+
 // Energy of leaf labellings over a tree; arrays pitched per G.  Synchronous.
+// `buffer` (kEnergyBuffer bytes of device memory) holds the table and the
+// sums; null: allocated for this call.
 int launch_energy(hmf_ctx* c, const hmf::EnergyTable& tab, const hmf::Geometry& G, double* f0, double* f,
-                  int n_nodes, cudaStream_t s) {
-  hmf::EnergyTable* d_tab = nullptr;
-  double* d_sums = nullptr;
-  CK(cudaMalloc(&d_tab, sizeof(tab)), "cudaMalloc(energy table)");
-  cudaError_t e = cudaMalloc(&d_sums, sizeof(double) * (1 + hmf::kMaxVertices));
-  if (e != cudaSuccess) {
-    cudaFree(d_tab);
-    return cuda_fail(c, e, "cudaMalloc(energy sums)");
+                  int n_nodes, cudaStream_t s, char* buffer) {
+  char* own = nullptr;
+  if (!buffer) {
+    CK(cudaMalloc(&own, kEnergyBuffer), "cudaMalloc(energy buffer)");
+    buffer = own;
   }
+  hmf::EnergyTable* d_tab = reinterpret_cast<hmf::EnergyTable*>(buffer);
+  double* d_sums = reinterpret_cast<double*>(buffer + kEnergyTableBytes);
   std::vector<double> sums(1 + hmf::kMaxVertices, 0.0);
-  e = cudaMemcpyAsync(d_tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaMemcpyAsync(d_tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_sums, 0, sizeof(double) * sums.size(), s);
   if (e == cudaSuccess) {
-    const long long dense = (long long)G.vx * G.vy * G.vz;
-    hmf::energy_kernel<<<grid_for(dense), hmf::kPostThreads, 0, s>>>(d_tab, G, d_sums);
+    int dev = 0, sms = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::max(1, std::min(G.vy * G.vz, sms * 16));  // one row per block step
+    switch (tab.n) {
+#define HMF_ENERGY_CASE(N)                                                         \
+  case N:                                                                          \
+    hmf::energy_reg_kernel<N><<<grid, hmf::kPostThreads, 0, s>>>(d_tab, G, d_sums); \
+    break;
+      HMF_ENERGY_CASE(1) HMF_ENERGY_CASE(2) HMF_ENERGY_CASE(3) HMF_ENERGY_CASE(4)
+      HMF_ENERGY_CASE(5) HMF_ENERGY_CASE(6) HMF_ENERGY_CASE(7) HMF_ENERGY_CASE(8)
+#undef HMF_ENERGY_CASE
+      default:
+        hmf::energy_kernel<<<grid, hmf::kPostThreads, 0, s>>>(d_tab, G, d_sums);
+    }
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(sums.data(), d_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(d_tab);
-  cudaFree(d_sums);
+  if (own) cudaFree(own);
   if (e != cudaSuccess) return cuda_fail(c, e, "energy_kernel");
   if (f0) *f0 = sums[0];
   for (int v = 0; v < n_nodes && f; ++v) f[v] = sums[1 + v];
@@ -122,6 +146,7 @@ int energy_tree(hmf_ctx* c, const int* parent, int n_nodes, hmf::EnergyTable& ta
     if (v == root) continue;
     const int i = entry[v];
     tab.vertex[i] = v;
+    tab.parent_entry[i] = parent[v] == root ? -1 : entry[parent[v]];
     tab.first_kid[i] = kp;
     tab.n_kids[i] = (int)kids[v].size();
     for (int k : kids[v]) tab.kids[kp++] = entry[k];
@@ -206,7 +231,7 @@ int hmf_decomposition_energy(int vx, int vy, int vz, const int* parent, int n_no
     if (smooth && smooth[v] && (rc = bring(smooth[v], &tab.smooth[e]))) return rc;
   }
   hmf::Geometry G{vx, vy, vz, vx, (long long)vx * vy, (long long)V};
-  return launch_energy(c, tab, G, f0, f, n_nodes, s);
+  return launch_energy(c, tab, G, f0, f, n_nodes, s, nullptr);
 }
 
 int hmf_batch_get_vote(hmf_ctx* c, int volume, int* out, int where, void* stream) {
@@ -272,7 +297,8 @@ int hmf_batch_get_energy(hmf_ctx* c, int volume, double* f0, double* f, int n) {
   }
   hmf::Geometry G{V.vx, V.vy, V.vz, V.pitch, V.plane, V.vol};
   std::vector<double> fv(c->n, 0.0);
-  rc = launch_energy(c, tab, G, f0, fv.data(), c->n, c->stream);
+  if (!c->d_post) CK(cudaMalloc(&c->d_post, kEnergyBuffer), "cudaMalloc(energy buffer)");
+  rc = launch_energy(c, tab, G, f0, fv.data(), c->n, c->stream, c->d_post);
   if (rc) return rc;
   for (int v = 0; v < n && v < c->n && f; ++v) f[v] = fv[v];
   return c->n;

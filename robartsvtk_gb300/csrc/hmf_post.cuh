@@ -8,20 +8,24 @@
 //                 launched per input :249-256: the last of a tie wins),
 //                 semantics 1 follows vtkImageVote (first input, then any
 //                 strictly greater one: vtkImageVote.cxx:285-306).  One pass:
-//                 every input read once, one int written.
+//                 every input read once, one int written.  vote4_kernel is
+//                 the same four voxels at a time for 16-byte aligned rows.
 //  energy_kernel  f0 = sum of D_l * u_l over leaves and voxels; per non-root
 //                 vertex f_v = sum of S_v * 0.5*sqrt(|grad u_v|^2) with the
 //                 clamped central differences of kern_GHMFD_GradientBuffer
 //                 (CUDA_hierarchicalmaxflowdecomp.cu:19-38; its `g += d*d`
-//                 compiled to fused multiply-adds), a branch's
-//                 labelling being the sum of its children's in child order
+//                 compiled to fused multiply-adds), a branch's labelling
+//                 being the sum of its children's in child order
 //                 (vtkCudaHierarchicalMaxFlowDecomposition.cxx:750-806).  One
 //                 pass over all vertices per voxel (the reference makes one
 //                 gradient, one multiply and one reduction pass per vertex);
 //                 per-voxel terms in FP32 in the reference's operation order,
 //                 sums in FP64 (the reference reduces in FP32).
+//                 energy_reg_kernel<N> is the same with every per-vertex
+//                 value in registers, for trees of N <= 8 non-root vertices.
 // Arrays are pitched rows (`pitch` floats per row, dense when pitch == vx);
-// outputs of the vote are dense.
+// outputs of the vote are dense.  The energy kernels walk rows (one row per
+// block step, threads across x), so no voxel index is divided.
 #pragma once
 
 #include "hmf_types.cuh"
@@ -70,6 +74,53 @@ __global__ void __launch_bounds__(kPostThreads) vote_kernel(const VoteInputs V, 
   }
 }
 
+// The vote over pitched rows four voxels at a time: requires pitch % 4 == 0
+// and 16-byte aligned inputs (every solver array is).  Quad q covers pitched
+// elements 4q..4q+3 of one row; outputs only where x < vx.
+__global__ void __launch_bounds__(kPostThreads) vote4_kernel(const VoteInputs V, const Geometry G, int* __restrict__ out) {
+  const long long rows = (long long)G.vy * G.vz;
+  const int qpr = G.pitch >> 2;  // quads per row
+  const long long nq = rows * qpr;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x) {
+    const long long r = q / qpr;
+    const int x = (int)(q - r * qpr) * 4;
+    const long long i = r * G.pitch + x;
+    float4 mx = __ldg(reinterpret_cast<const float4*>(V.in[0] + i));
+    int id0, id1, id2, id3;
+    id0 = id1 = id2 = id3 = V.values[0];  // input 0 always takes the first turn
+    if (V.semantics == 0) {
+      for (int k = 1; k < V.n; ++k) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(V.in[k] + i));
+        const int val = V.values[k];
+        if (v.x >= mx.x) id0 = val, mx.x = v.x;
+        if (v.y >= mx.y) id1 = val, mx.y = v.y;
+        if (v.z >= mx.z) id2 = val, mx.z = v.z;
+        if (v.w >= mx.w) id3 = val, mx.w = v.w;
+      }
+    } else {
+      // "no winner yet" stays true while the winning id is -1 (vtkImageVote's marker)
+      bool none0 = id0 == -1, none1 = none0, none2 = none0, none3 = none0;
+      for (int k = 1; k < V.n; ++k) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(V.in[k] + i));
+        const int val = V.values[k];
+        if (none0 || v.x > mx.x) id0 = val, mx.x = v.x, none0 = val == -1;
+        if (none1 || v.y > mx.y) id1 = val, mx.y = v.y, none1 = val == -1;
+        if (none2 || v.z > mx.z) id2 = val, mx.z = v.z, none2 = val == -1;
+        if (none3 || v.w > mx.w) id3 = val, mx.w = v.w, none3 = val == -1;
+      }
+      if (id0 == -1) id0 = 0;
+      if (id1 == -1) id1 = 0;
+      if (id2 == -1) id2 = 0;
+      if (id3 == -1) id3 = 0;
+    }
+    int* o = out + r * G.vx + x;
+    if (x < G.vx) o[0] = id0;
+    if (x + 1 < G.vx) o[1] = id1;
+    if (x + 2 < G.vx) o[2] = id2;
+    if (x + 3 < G.vx) o[3] = id3;
+  }
+}
+
 // Tree in post-order for the energy: entry e's children precede it.
 struct EnergyTable {
   int n;  // entries (the root excluded)
@@ -78,10 +129,49 @@ struct EnergyTable {
   int n_kids[kMaxVertices];
   int kids[kMaxVertices];             // entry indices, child order
   int vertex[kMaxVertices];           // vertex id of each entry
+  int parent_entry[kMaxVertices];     // entry index of the parent (-1: the root)
   const float* label[kMaxVertices];   // leaves: labelling
   const float* data[kMaxVertices];    // leaves: data term
   const float* smooth[kMaxVertices];  // smoothness image or null (S = 1)
 };
+
+// kern_GHMFD_GradientBuffer's term from the labelling at the voxel's six
+// neighbours (+x, -x, +y, -y, +z, -z in u[1..6]), as compiled: g += d*d is
+// one fused multiply-add per axis.
+__device__ __forceinline__ float energy_grad_term(const float* u) {
+  const float dx = u[1] - u[2], dy = u[3] - u[4], dz = u[5] - u[6];
+  float g2 = __fmaf_rn(dx, dx, 0.0f);
+  g2 = __fmaf_rn(dy, dy, g2);
+  g2 = __fmaf_rn(dz, dz, g2);
+  return 0.5f * sqrtf(g2);
+}
+
+// Neighbour offsets of voxel (x, y, z) in pitched memory; at the border the
+// neighbour is the voxel itself.
+__device__ __forceinline__ void energy_offsets(const Geometry& G, int x, int y, int z, long long (&o)[7]) {
+  o[0] = 0;
+  o[1] = x == G.vx - 1 ? 0 : 1;
+  o[2] = x == 0 ? 0 : -1;
+  o[3] = y == G.vy - 1 ? 0 : (long long)G.pitch;
+  o[4] = y == 0 ? 0 : -(long long)G.pitch;
+  o[5] = z == G.vz - 1 ? 0 : G.plane;
+  o[6] = z == 0 ? 0 : -G.plane;
+}
+
+// Block sum of one quantity v into sums[e == 0 ? 0 : 1 + vertex of entry e-1]
+// (one atomic per block).  Every thread of the block calls it.
+__device__ __forceinline__ void energy_reduce_one(const EnergyTable& T, double v, int e, double* sums, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double t = lane < kPostThreads / 32 ? red[lane] : 0.0;
+    for (int s = 16; s > 0; s >>= 1) t += __shfl_down_sync(0xffffffffu, t, s);
+    if (lane == 0 && t != 0.0) atomicAdd(&sums[e == 0 ? 0 : 1 + T.vertex[e - 1]], t);
+  }
+  __syncthreads();
+}
 
 __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable* __restrict__ table, const Geometry G,
                                                               double* __restrict__ sums /* [0] f0, [1+vertex] f */) {
@@ -93,62 +183,85 @@ __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable*
   const int n = T.n;
   double acc[kMaxVertices + 1];  // [0] f0, [1+e] entry e
   for (int e = 0; e <= n; ++e) acc[e] = 0.0;
-  float u7[kMaxVertices][7];  // labelling at the voxel and its six neighbours (clamped)
-  const long long dense = (long long)G.vx * G.vy * G.vz;
-  for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < dense;
-       d += (long long)gridDim.x * blockDim.x) {
-    const long long r = d / G.vx;
-    const int x = (int)(d - r * G.vx);
-    const int y = (int)(r % G.vy), z = (int)(r / G.vy);
-    const long long i = r * G.pitch + x;
-    // neighbour offsets: +x, -x, +y, -y, +z, -z; at the border the voxel itself
-    const long long o[7] = {0,
-                            x == G.vx - 1 ? 0 : 1,
-                            x == 0 ? 0 : -1,
-                            y == G.vy - 1 ? 0 : (long long)G.pitch,
-                            y == 0 ? 0 : -(long long)G.pitch,
-                            z == G.vz - 1 ? 0 : G.plane,
-                            z == 0 ? 0 : -G.plane};
-    for (int e = 0; e < n; ++e) {
-      if (T.n_kids[e] == 0) {
-        const float* L = T.label[e];
+  float u7[kMaxVertices][7];  // labelling at the voxel and its six neighbours
+  const int rows = G.vy * G.vz;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int z = r / G.vy, y = r - z * G.vy;
+    for (int x = threadIdx.x; x < G.vx; x += blockDim.x) {
+      const long long i = (long long)r * G.pitch + x;
+      long long o[7];
+      energy_offsets(G, x, y, z, o);
+      for (int e = 0; e < n; ++e) {
+        if (T.n_kids[e] == 0) {
+          const float* L = T.label[e];
 #pragma unroll
-        for (int p = 0; p < 7; ++p) u7[e][p] = __ldg(L + i + o[p]);
-        acc[0] += (double)(__ldg(T.data[e] + i) * u7[e][0]);
-      } else {
+          for (int p = 0; p < 7; ++p) u7[e][p] = __ldg(L + i + o[p]);
+          acc[0] += (double)(__ldg(T.data[e] + i) * u7[e][0]);
+        } else {
 #pragma unroll
-        for (int p = 0; p < 7; ++p) u7[e][p] = 0.0f;
-        for (int k = 0; k < T.n_kids[e]; ++k) {
-          const int c = T.kids[T.first_kid[e] + k];
+          for (int p = 0; p < 7; ++p) u7[e][p] = 0.0f;
+          for (int k = 0; k < T.n_kids[e]; ++k) {
+            const int c = T.kids[T.first_kid[e] + k];
 #pragma unroll
-          for (int p = 0; p < 7; ++p) u7[e][p] = u7[e][p] + u7[c][p];
+            for (int p = 0; p < 7; ++p) u7[e][p] = u7[e][p] + u7[c][p];
+          }
         }
+        float term = energy_grad_term(u7[e]);
+        if (T.smooth[e]) term = __ldg(T.smooth[e] + i) * term;
+        acc[1 + e] += (double)term;
       }
-      // kern_GHMFD_GradientBuffer as compiled (multiply-add contraction):
-      // g += d*d is one fused multiply-add per axis
-      const float dx = u7[e][1] - u7[e][2], dy = u7[e][3] - u7[e][4], dz = u7[e][5] - u7[e][6];
-      float g2 = __fmaf_rn(dx, dx, 0.0f);
-      g2 = __fmaf_rn(dy, dy, g2);
-      g2 = __fmaf_rn(dz, dz, g2);
-      float term = 0.5f * sqrtf(g2);
-      if (T.smooth[e]) term = __ldg(T.smooth[e] + i) * term;
-      acc[1 + e] += (double)term;
     }
   }
-  // block sums, one atomic per quantity per block
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int e = 0; e <= n; ++e) {
-    double v = acc[e];
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-      double t = lane < kPostThreads / 32 ? red[lane] : 0.0;
-      for (int s = 16; s > 0; s >>= 1) t += __shfl_down_sync(0xffffffffu, t, s);
-      if (lane == 0 && t != 0.0) atomicAdd(&sums[e == 0 ? 0 : 1 + T.vertex[e - 1]], t);
+  for (int e = 0; e <= n; ++e) energy_reduce_one(T, acc[e], e, sums, red);
+}
+
+// The energy for trees of N non-root vertices (N <= 8), every per-vertex
+// value in registers.  Entries are in post-order, so a branch's children are
+// the earlier entries whose parent it is, met in child order.
+template <int N>
+__global__ void __launch_bounds__(kPostThreads) energy_reg_kernel(const EnergyTable* __restrict__ table,
+                                                                  const Geometry G, double* __restrict__ sums) {
+  __shared__ EnergyTable T;
+  __shared__ double red[kPostThreads / 32];
+  for (int i = threadIdx.x; i < (int)(sizeof(EnergyTable) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  __syncthreads();
+  double acc[N + 1];
+#pragma unroll
+  for (int e = 0; e <= N; ++e) acc[e] = 0.0;
+  const int rows = G.vy * G.vz;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int z = r / G.vy, y = r - z * G.vy;
+    for (int x = threadIdx.x; x < G.vx; x += blockDim.x) {
+      const long long i = (long long)r * G.pitch + x;
+      long long o[7];
+      energy_offsets(G, x, y, z, o);
+      float u7[N][7];
+#pragma unroll
+      for (int e = 0; e < N; ++e) {
+        if (T.n_kids[e] == 0) {
+          const float* L = T.label[e];
+#pragma unroll
+          for (int p = 0; p < 7; ++p) u7[e][p] = __ldg(L + i + o[p]);
+          acc[0] += (double)(__ldg(T.data[e] + i) * u7[e][0]);
+        } else {
+#pragma unroll
+          for (int p = 0; p < 7; ++p) u7[e][p] = 0.0f;
+#pragma unroll
+          for (int k = 0; k < e; ++k)
+            if (T.parent_entry[k] == e) {
+#pragma unroll
+              for (int p = 0; p < 7; ++p) u7[e][p] = u7[e][p] + u7[k][p];
+            }
+        }
+        float term = energy_grad_term(u7[e]);
+        if (T.smooth[e]) term = __ldg(T.smooth[e] + i) * term;
+        acc[1 + e] += (double)term;
+      }
     }
-    __syncthreads();
   }
+#pragma unroll
+  for (int e = 0; e <= N; ++e) energy_reduce_one(T, acc[e], e, sums, red);
 }
 
 }  // namespace hmf

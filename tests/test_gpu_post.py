@@ -105,6 +105,27 @@ def test_energy_standalone_matches_oracle():
     np.testing.assert_allclose(fd, o["f"], rtol=1e-11, atol=0)
 
 
+def test_energy_large_tree_and_dense_quads():
+    """Eleven non-root vertices (past the register-resident kernels' eight) and
+    rows a multiple of four wide (the four-voxel vote)."""
+    rng = np.random.default_rng(17)
+    parent = [-1, 0, 0, 1, 1, 1, 2, 2, 3, 3, 6, 6]
+    dims = (16, 9, 7)
+    shape = dims[::-1]
+    leaves = [v for v in range(1, len(parent)) if v not in parent]
+    lab = {l: rng.random(shape).astype(np.float32) for l in leaves}
+    dat = {l: rng.random(shape).astype(np.float32) for l in leaves}
+    sm = {4: rng.random(shape).astype(np.float32), 6: rng.random(shape).astype(np.float32)}
+    o = O.energy(dims, parent, dat, lab, sm)
+    f0, f = decomposition_energy(dims, parent, dat, lab, sm)
+    assert abs(f0 - o["f0"]) <= 1e-11 * abs(o["f0"])
+    np.testing.assert_allclose(f, o["f"], rtol=1e-11, atol=0)
+    ins = tie_images(3, shape, 6)
+    vals = [11, 3, 8, 1, 5, 2]
+    for semantics in (REF_CUDA, REF_CPU):
+        assert np.array_equal(vote(ins, vals, semantics=semantics), O.vote(ins, vals, semantics=semantics))
+
+
 def test_context_energy_matches_oracle():
     w = random_tree_problem(9, (31, 22, 15), PARENT, iterations=15, smooth_nodes=(1, 4, 5))
     o = O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, w.iterations, w.step, w.cc)
