@@ -430,7 +430,7 @@ def bench_post(w, solver, device_stream):
     for name, t, b in (("vote", t_vote, b_vote), ("energy", t_energy, b_energy)):
         gbs = b / t / 1e6
         res[name] = {"ms": t, "bytes": b, "achieved_gbs": gbs, "frac": gbs / peak}
-    res["energy"]["note"] = "includes the table upload and the 8-byte-per-vertex sums read back"
+    res["energy"]["note"] = "one call: the sums zeroed, one kernel, the 8-byte-per-vertex sums read back, a stream sync"
     return res
 
 

@@ -71,24 +71,45 @@ int launch_energy(hmf_ctx* c, const hmf::EnergyTable& tab, const hmf::Geometry& 
   hmf::EnergyTable* d_tab = reinterpret_cast<hmf::EnergyTable*>(buffer);
   double* d_sums = reinterpret_cast<double*>(buffer + kEnergyTableBytes);
   std::vector<double> sums(1 + hmf::kMaxVertices, 0.0);
-  cudaError_t e = cudaMemcpyAsync(d_tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_sums, 0, sizeof(double) * sums.size(), s);
-  if (e == cudaSuccess) {
-    int dev = 0, sms = 148;
+  // persistent grid: as many blocks as are resident at once, each walking rows
+  auto grid_of = [&](auto kernel) {
+    int dev = 0, sms = 148, per = 1;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = std::max(1, std::min(G.vy * G.vz, sms * 16));  // one row per block step
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, hmf::kPostThreads, 0) != cudaSuccess || per < 1)
+      per = 1;
+    return std::max(1, std::min(G.vy * G.vz, sms * per));
+  };
+  cudaError_t e = cudaMemsetAsync(d_sums, 0, sizeof(double) * sums.size(), s);
+  if (e == cudaSuccess && tab.n <= hmf::kEnergyRegMax && G.plane <= INT32_MAX) {
+    hmf::EnergyRegParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.sum_index[0] = 0;
+    for (int k = 0; k < tab.n; ++k) {
+      P.label[k] = tab.label[k];
+      P.data[k] = tab.data[k];
+      P.smooth[k] = tab.smooth[k];
+      if (tab.n_kids[k] == 0) P.leaf_mask |= 1u << k;
+      if (tab.parent_entry[k] >= 0) P.kids[tab.parent_entry[k]] |= 1u << k;
+      P.sum_index[1 + k] = 1 + tab.vertex[k];
+    }
+    auto launch = [&](auto kernel) { kernel<<<grid_of(kernel), hmf::kPostThreads, 0, s>>>(P, G, d_sums); };
     switch (tab.n) {
-#define HMF_ENERGY_CASE(N)                                                         \
-  case N:                                                                          \
-    hmf::energy_reg_kernel<N><<<grid, hmf::kPostThreads, 0, s>>>(d_tab, G, d_sums); \
-    break;
-      HMF_ENERGY_CASE(1) HMF_ENERGY_CASE(2) HMF_ENERGY_CASE(3) HMF_ENERGY_CASE(4)
-      HMF_ENERGY_CASE(5) HMF_ENERGY_CASE(6) HMF_ENERGY_CASE(7) HMF_ENERGY_CASE(8)
-#undef HMF_ENERGY_CASE
-      default:
-        hmf::energy_kernel<<<grid, hmf::kPostThreads, 0, s>>>(d_tab, G, d_sums);
+      case 1: launch(hmf::energy_reg_kernel<1>); break;
+      case 2: launch(hmf::energy_reg_kernel<2>); break;
+      case 3: launch(hmf::energy_reg_kernel<3>); break;
+      case 4: launch(hmf::energy_reg_kernel<4>); break;
+      case 5: launch(hmf::energy_reg_kernel<5>); break;
+      case 6: launch(hmf::energy_reg_kernel<6>); break;
+      case 7: launch(hmf::energy_reg_kernel<7>); break;
+      default: launch(hmf::energy_reg_kernel<8>); break;
     }
     e = cudaGetLastError();
+  } else if (e == cudaSuccess) {
+    e = cudaMemcpyAsync(d_tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      hmf::energy_kernel<<<grid_of(hmf::energy_kernel), hmf::kPostThreads, 0, s>>>(d_tab, G, d_sums);
+      e = cudaGetLastError();
+    }
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(sums.data(), d_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, s);

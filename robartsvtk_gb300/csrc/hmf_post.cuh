@@ -21,11 +21,14 @@
 //                 gradient, one multiply and one reduction pass per vertex);
 //                 per-voxel terms in FP32 in the reference's operation order,
 //                 sums in FP64 (the reference reduces in FP32).
-//                 energy_reg_kernel<N> is the same with every per-vertex
-//                 value in registers, for trees of N <= 8 non-root vertices.
+//                 energy_reg_kernel<N> is the same for trees of N <= 8
+//                 non-root vertices: the tree in kernel parameters (bit
+//                 masks: no table reads per voxel), every per-vertex value
+//                 in registers, one warp per row at a time.
 // Arrays are pitched rows (`pitch` floats per row, dense when pitch == vx);
-// outputs of the vote are dense.  The energy kernels walk rows (one row per
-// block step, threads across x), so no voxel index is divided.
+// outputs of the vote are dense.  The energy kernels walk rows, so no voxel
+// index is divided; per-thread sums are float-float (FP32 pipes), merged in
+// FP64 per warp.
 #pragma once
 
 #include "hmf_types.cuh"
@@ -158,19 +161,50 @@ __device__ __forceinline__ void energy_offsets(const Geometry& G, int x, int y, 
   o[6] = z == 0 ? 0 : -G.plane;
 }
 
-// Block sum of one quantity v into sums[e == 0 ? 0 : 1 + vertex of entry e-1]
-// (one atomic per block).  Every thread of the block calls it.
-__device__ __forceinline__ void energy_reduce_one(const EnergyTable& T, double v, int e, double* sums, double* red) {
+// Float-float running sum (hi + lo): each term is added with Knuth's
+// TwoSum, its rounding error collected in lo.  FP32 instructions only (the
+// FP64 rate of this part is a small fraction of FP32's); relative error about
+// n * 2^-48 after n terms of one sign, against 2^-24 for a plain float sum.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void ff_add(FF& a, float t) {
+  const float s = a.hi + t;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (t - bb);
+  a.hi = s;
+  a.lo += err;
+}
+
+__device__ __forceinline__ FF ff_merge(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b.hi - bb);
+  return {s, (a.lo + b.lo) + err};
+}
+
+// Block sum of one quantity into *dst (float-float across the warp, double
+// across warps, one atomic per block).  Every thread of the block calls it.
+__device__ __forceinline__ void energy_reduce_to(FF v, double* dst, double* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
-  if (lane == 0) red[warp] = v;
+  for (int s = 16; s > 0; s >>= 1) {
+    const FF o = {__shfl_down_sync(0xffffffffu, v.hi, s), __shfl_down_sync(0xffffffffu, v.lo, s)};
+    v = ff_merge(v, o);
+  }
+  if (lane == 0) red[warp] = (double)v.hi + (double)v.lo;
   __syncthreads();
   if (warp == 0) {
     double t = lane < kPostThreads / 32 ? red[lane] : 0.0;
-    for (int s = 16; s > 0; s >>= 1) t += __shfl_down_sync(0xffffffffu, t, s);
-    if (lane == 0 && t != 0.0) atomicAdd(&sums[e == 0 ? 0 : 1 + T.vertex[e - 1]], t);
+    for (int s = kPostThreads / 64; s > 0; s >>= 1) t += __shfl_down_sync(0xffffffffu, t, s);
+    if (lane == 0 && t != 0.0) atomicAdd(dst, t);
   }
   __syncthreads();
+}
+
+// sums[0] = f0, sums[1 + vertex of entry e-1] = f of that vertex.
+__device__ __forceinline__ void energy_reduce_one(const EnergyTable& T, FF v, int e, double* sums, double* red) {
+  energy_reduce_to(v, &sums[e == 0 ? 0 : 1 + T.vertex[e - 1]], red);
 }
 
 __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable* __restrict__ table, const Geometry G,
@@ -181,8 +215,8 @@ __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable*
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
   __syncthreads();
   const int n = T.n;
-  double acc[kMaxVertices + 1];  // [0] f0, [1+e] entry e
-  for (int e = 0; e <= n; ++e) acc[e] = 0.0;
+  FF acc[kMaxVertices + 1];  // [0] f0, [1+e] entry e
+  for (int e = 0; e <= n; ++e) acc[e] = {0.0f, 0.0f};
   float u7[kMaxVertices][7];  // labelling at the voxel and its six neighbours
   const int rows = G.vy * G.vz;
   for (int r = blockIdx.x; r < rows; r += gridDim.x) {
@@ -196,7 +230,7 @@ __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable*
           const float* L = T.label[e];
 #pragma unroll
           for (int p = 0; p < 7; ++p) u7[e][p] = __ldg(L + i + o[p]);
-          acc[0] += (double)(__ldg(T.data[e] + i) * u7[e][0]);
+          ff_add(acc[0], __ldg(T.data[e] + i) * u7[e][0]);
         } else {
 #pragma unroll
           for (int p = 0; p < 7; ++p) u7[e][p] = 0.0f;
@@ -208,60 +242,80 @@ __global__ void __launch_bounds__(kPostThreads) energy_kernel(const EnergyTable*
         }
         float term = energy_grad_term(u7[e]);
         if (T.smooth[e]) term = __ldg(T.smooth[e] + i) * term;
-        acc[1 + e] += (double)term;
+        ff_add(acc[1 + e], term);
       }
     }
   }
   for (int e = 0; e <= n; ++e) energy_reduce_one(T, acc[e], e, sums, red);
 }
 
-// The energy for trees of N non-root vertices (N <= 8), every per-vertex
-// value in registers.  Entries are in post-order, so a branch's children are
-// the earlier entries whose parent it is, met in child order.
+// The tree of energy_reg_kernel: entries in post-order (a branch's children
+// are earlier entries, in child order).
+constexpr int kEnergyRegMax = 8;
+struct EnergyRegParams {
+  const float* label[kEnergyRegMax];   // leaves: labelling
+  const float* data[kEnergyRegMax];    // leaves: data term
+  const float* smooth[kEnergyRegMax];  // smoothness image or null (S = 1)
+  unsigned kids[kEnergyRegMax];        // bit k: entry k is a child of entry e
+  int sum_index[kEnergyRegMax + 1];    // quantity q (0: f0, 1+e: entry e) -> index into sums
+  unsigned leaf_mask;                  // bit e: entry e is a leaf
+};
+
+// The energy for trees of N non-root vertices (N <= 8).  Each warp takes a
+// row (y, z) at a time, lanes across x; the y and z neighbour offsets are set
+// once per row (`plane` below 2^31 floats).
 template <int N>
-__global__ void __launch_bounds__(kPostThreads) energy_reg_kernel(const EnergyTable* __restrict__ table,
+__global__ void __launch_bounds__(kPostThreads, 3) energy_reg_kernel(const __grid_constant__ EnergyRegParams P,
                                                                   const Geometry G, double* __restrict__ sums) {
-  __shared__ EnergyTable T;
   __shared__ double red[kPostThreads / 32];
-  for (int i = threadIdx.x; i < (int)(sizeof(EnergyTable) / 4); i += blockDim.x)
-    reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
-  __syncthreads();
-  double acc[N + 1];
+  FF acc[N + 1];
 #pragma unroll
-  for (int e = 0; e <= N; ++e) acc[e] = 0.0;
+  for (int q = 0; q <= N; ++q) acc[q] = {0.0f, 0.0f};
+  const int lane = threadIdx.x & 31;
+  const int n_warps = gridDim.x * (kPostThreads / 32);
   const int rows = G.vy * G.vz;
-  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+  for (int r = blockIdx.x * (kPostThreads / 32) + (threadIdx.x >> 5); r < rows; r += n_warps) {
     const int z = r / G.vy, y = r - z * G.vy;
-    for (int x = threadIdx.x; x < G.vx; x += blockDim.x) {
-      const long long i = (long long)r * G.pitch + x;
-      long long o[7];
-      energy_offsets(G, x, y, z, o);
+    const long long row = (long long)r * G.pitch;
+    const int dyp = y == G.vy - 1 ? 0 : G.pitch;
+    const int dym = y == 0 ? 0 : -G.pitch;
+    const int dzp = z == G.vz - 1 ? 0 : (int)G.plane;
+    const int dzm = z == 0 ? 0 : -(int)G.plane;
+    for (int x = lane; x < G.vx; x += 32) {
+      const long long i = row + x;
+      const int xp = x == G.vx - 1 ? 0 : 1;
+      const int xm = x == 0 ? 0 : -1;
       float u7[N][7];
 #pragma unroll
       for (int e = 0; e < N; ++e) {
-        if (T.n_kids[e] == 0) {
-          const float* L = T.label[e];
-#pragma unroll
-          for (int p = 0; p < 7; ++p) u7[e][p] = __ldg(L + i + o[p]);
-          acc[0] += (double)(__ldg(T.data[e] + i) * u7[e][0]);
+        if (P.leaf_mask >> e & 1u) {
+          const float* c = P.label[e] + i;
+          u7[e][0] = __ldg(c);
+          u7[e][1] = __ldg(c + xp);
+          u7[e][2] = __ldg(c + xm);
+          u7[e][3] = __ldg(c + dyp);
+          u7[e][4] = __ldg(c + dym);
+          u7[e][5] = __ldg(c + dzp);
+          u7[e][6] = __ldg(c + dzm);
+          ff_add(acc[0], __ldg(P.data[e] + i) * u7[e][0]);
         } else {
 #pragma unroll
           for (int p = 0; p < 7; ++p) u7[e][p] = 0.0f;
 #pragma unroll
           for (int k = 0; k < e; ++k)
-            if (T.parent_entry[k] == e) {
+            if (P.kids[e] >> k & 1u) {
 #pragma unroll
               for (int p = 0; p < 7; ++p) u7[e][p] = u7[e][p] + u7[k][p];
             }
         }
         float term = energy_grad_term(u7[e]);
-        if (T.smooth[e]) term = __ldg(T.smooth[e] + i) * term;
-        acc[1 + e] += (double)term;
+        if (P.smooth[e]) term = __ldg(P.smooth[e] + i) * term;
+        ff_add(acc[1 + e], term);
       }
     }
   }
 #pragma unroll
-  for (int e = 0; e <= N; ++e) energy_reduce_one(T, acc[e], e, sums, red);
+  for (int q = 0; q <= N; ++q) energy_reduce_to(acc[q], sums + P.sum_index[q], red);
 }
 
 }  // namespace hmf
