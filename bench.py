@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--adjoint-iterations", type=int, default=300)
     ap.add_argument("--profile", action="store_true",
                     help="two solves (one warm, one profiled) and nothing else: the command ncu wraps")
+    ap.add_argument("--profile-post", action="store_true",
+                    help="one solve, then two votes and two energy evaluations of its labels: the command ncu wraps")
     return ap.parse_args()
 
 
@@ -580,10 +582,44 @@ def run_profile(args):
     return 0
 
 
+def run_profile_post(args):
+    """One solve of the benchmark workload (--size, --iterations), then two
+    votes into a device buffer and two energy decompositions of its labels."""
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver
+
+    w = make_workload(args, 0)
+    solver = HMFSolver(w.dims, w.parent)
+    keep = {}
+    for leaf, d in w.data.items():
+        keep[("d", leaf)] = torch.from_numpy(d).cuda()
+        solver.set_data(leaf, keep[("d", leaf)])
+    for v, S in w.smooth.items():
+        if ("s", id(S)) not in keep:
+            keep[("s", id(S))] = torch.from_numpy(S).cuda()
+        solver.set_smoothness(v, keep[("s", id(S))])
+    for v, a in w.alpha.items():
+        solver.set_smoothness_scalar(v, a)
+    solver.set_params(w.iterations, w.step, w.cc)
+    solver.solve()
+    out = torch.empty(w.dims[::-1], dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        solver.vote(out=out)
+    torch.cuda.synchronize()
+    energies = [solver.energy() for _ in range(2)]
+    print(json.dumps({"profile_post": WORKLOAD, "volume": list(w.dims), "iterations": w.iterations,
+                      "f0": energies[-1][0]}))
+    solver.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.profile:
         return run_profile(args)
+    if args.profile_post:
+        return run_profile_post(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

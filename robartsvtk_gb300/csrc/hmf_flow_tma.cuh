@@ -169,6 +169,10 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   // masks; it runs a copy of the march with those tests folded away.
   const bool interior = x0 - 2 >= 1 && x0 + 29 <= G.vx - 2 && y0 - 2 >= 1 && y0 + 29 <= G.vy - 2;
 
+  // The z-march.  Steps k in [zs + 2, min(ze + 1, vz - 2)] are steady: every
+  // stage runs and no z boundary is near, so the step is compiled a second
+  // time (ST) with those tests folded away; the few steps before and after
+  // run the general form.
   auto march = [&](auto tag) {
     constexpr bool INT = decltype(tag)::value;
     // carries, one per row of this thread
@@ -179,20 +183,22 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     }
     bool have_pz = false;  // pzn_c holds pz of plane k (loaded in step k-1)
 
-    for (int k = kstart; k <= kend; ++k) {
-      const bool doA = k <= kmain_end;                                   // g(k), p'(k)
+    auto zstep = [&](const int k, auto stag) {
+      constexpr bool ST = decltype(stag)::value;
+      const bool doA = ST || k <= kmain_end;                                   // g(k), p'(k)
       const int kc = k - 1;
-      const bool doC = kc >= max(zs - 1, 0) && kc <= min(ze, G.vz - 1);  // m(k-1), P(k-1)
+      const bool doC = ST || (kc >= max(zs - 1, 0) && kc <= min(ze, G.vz - 1));  // m(k-1), P(k-1)
       const int ko = k - 2;
-      const bool doE = ko >= zs && ko < ze;                              // div(k-2), output
+      const bool doE = ST || (ko >= zs && ko < ze);                              // div(k-2), output
 
       // ---- stage A: g(k) from the staged inputs (kern_CalcGradStep on the
       // divergence kern_Divergence left, recomputed from the stored flows)
       float g[4], rx[4], ry_[4], rz[4], Scur[4];
       if (doA) {
         wait_main(k);
-        const bool has_next = k + 1 < G.vz;
-        if (!have_pz) wait_pz(k);
+        const bool has_next = ST || k + 1 < G.vz;
+        const bool pz_held = ST || have_pz;
+        if (!pz_held) wait_pz(k);
         if (has_next) wait_pz(k + 1);
         const float* cur = mslot(k);
         const float* zc = zslot(k);
@@ -205,7 +211,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         for (int r = 0; r < 4; ++r) {
           const int i = (warp * 4 + r) * kTmaBoxX + off + lane;
           const float px = cur[i], py = pyv[r];
-          const float pz = have_pz ? pzn_c[r] : zc[i];
+          const float pz = pz_held ? pzn_c[r] : zc[i];
           const float pxr = cur[i + 1];
           const float pyd = pyv[r + 1];
           const float pzn = zn[i];
@@ -239,7 +245,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow)
       float npx[4], npy[4], npz[4];
       const float gup = warp ? xg[(warp - 1) * 32 + lane] : 0.f;
-      const bool zpos = k > 0;
+      const bool zpos = ST || k > 0;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const float gxm = __shfl_up_sync(FULL, g[r], 1);
@@ -253,12 +259,12 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
 
       // ---- stage C: m(k-1) (kern_ComputeFlowMag*).  |p|^2 of the four rows
       // is computed without branches so that their chains interleave; the
-      // exact square root and division run only for rows whose |p| is near or
-      // above its bound (projection_multiplier's test).
+      // exact square root and division run only where a row's |p| is near or
+      // above its bound (projection_multiplier's test), behind one warp vote.
       float m[4], h[4], lim[4];
       bool slow[4];
       const float pdown = warp < 7 ? xpy[(warp + 1) * 32 + lane] : 0.f;
-      const bool znl = kc != G.vz - 1;
+      const bool znl = ST || kc != G.vz - 1;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const float pxr = __shfl_down_sync(FULL, ppx[r], 1);
@@ -278,11 +284,13 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         m[r] = 1.0f;
         Sprev[r] = Scur[r];
       }
+      if (__any_sync(FULL, slow[0] || slow[1] || slow[2] || slow[3])) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        if (slow[r]) {
-          const float Fs = sqrtf(h[r]);
-          if (Fs > lim[r]) m[r] = lim[r] / Fs;
+        for (int r = 0; r < 4; ++r) {
+          if (slow[r]) {
+            const float Fs = sqrtf(h[r]);
+            if (Fs > lim[r]) m[r] = lim[r] / Fs;
+          }
         }
       }
       xm[warp * 32 + lane] = m[3];
@@ -291,7 +299,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       // ---- stage D: P(k-1) (kern_Project)
       float nPx[4], nPy[4], nPz[4];
       const float mup = warp ? xm[(warp - 1) * 32 + lane] : 0.f;
-      const bool kcpos = kc > 0;
+      const bool kcpos = ST || kc > 0;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const float mxm = __shfl_up_sync(FULL, m[r], 1);
@@ -305,7 +313,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
 
       // ---- stage E: divergence of P(k-2) (kern_Divergence), store P(k-2) and div(k-2)
       const float Pdown = warp < 7 ? xP[((k & 1) * 8 + warp + 1) * 32 + lane] : 0.f;
-      const bool zonl = ko != G.vz - 1;
+      const bool zonl = ST || ko != G.vz - 1;
       const long long zoff = (long long)ko * G.plane;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
@@ -334,7 +342,13 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         Py[r] = nPy[r];
         Pz[r] = nPz[r];
       }
-    }
+    };
+
+    const int k_lo = zs + 2, k_hi = min(ze + 1, G.vz - 2);
+    int k = kstart;
+    for (; k <= kend && k < k_lo; ++k) zstep(k, BoolTag<false>{});
+    for (; k <= k_hi; ++k) zstep(k, BoolTag<true>{});
+    for (; k <= kend; ++k) zstep(k, BoolTag<false>{});
   };
   if (interior) march(BoolTag<true>{});
   else march(BoolTag<false>{});
