@@ -121,7 +121,9 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       abort_cta = 1;
       if (fp.error_flag) atomicOr(fp.error_flag, 4);
     }
-    for (int s = 0; s < kTmaMainSlots; ++s) mbar_init(&mbars[s], 1);
+    // one arrival per main-ring array: each array's copy is issued (with its
+    // own expect_tx) by the lane 0 of its own warp
+    for (int s = 0; s < kTmaMainSlots; ++s) mbar_init(&mbars[s], (unsigned)narr);
     for (int s = 0; s < kTmaPzSlots; ++s) mbar_init(&zbars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -131,18 +133,17 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
 
   auto mslot = [&](int p) { return mslots + ((p - kstart) % kTmaMainSlots) * (kTmaMainArrays * kTmaPlane); };
   auto zslot = [&](int p) { return zslots + ((p - kstart) % kTmaPzSlots) * kTmaPlane; };
-  auto issue_main = [&](int p) {  // thread 0 only
+  // Array a of plane p into the main ring (a: 0, 1 flows x, y; 2 sink;
+  // 3 label; 4 parent sink; 5 smoothness -- the order of FlowVertexTMA's
+  // maps).  One thread per array.
+  auto main_map = [&](int a) -> const CUtensorMap* { return a < 2 ? &V->flow_in[par][a] : &V->sink + (a - 2); };
+  auto issue_main_array = [&](int p, int a, const CUtensorMap* map) {
     uint64_t* bar = &mbars[(p - kstart) % kTmaMainSlots];
-    float* dst = mslot(p);
-    mbar_expect_tx(bar, (unsigned)(narr * kTmaPlane * 4));
-    tma_load_plane(dst + 0 * kTmaPlane, &V->flow_in[par][0], xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 1 * kTmaPlane, &V->flow_in[par][1], xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 2 * kTmaPlane, &V->sink, xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 3 * kTmaPlane, &V->label, xs, y0 - 2, p, bar);
-    tma_load_plane(dst + 4 * kTmaPlane, &V->inc, xs, y0 - 2, p, bar);
-    if (has_s) tma_load_plane(dst + 5 * kTmaPlane, &V->smooth, xs, y0 - 2, p, bar);
+    mbar_expect_tx(bar, (unsigned)(kTmaPlane * 4));
+    tma_load_plane(mslot(p) + a * kTmaPlane, map, xs, y0 - 2, p, bar);
   };
-  auto issue_pz = [&](int p) {  // thread 0 only
+  const CUtensorMap* const warp_map = main_map(warp < narr ? warp : 0);  // this warp's array in the loop
+  auto issue_pz = [&](int p) {  // one thread
     uint64_t* bar = &zbars[(p - kstart) % kTmaPzSlots];
     mbar_expect_tx(bar, (unsigned)(kTmaPlane * 4));
     tma_load_plane(zslot(p), &V->flow_in[par][2], xs, y0 - 2, p, bar);
@@ -160,7 +161,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   };
 
   if (threadIdx.x == 0) {
-    for (int p = kstart; p <= min(kstart + 1, kmain_end); ++p) issue_main(p);
+    for (int p = kstart; p <= min(kstart + 1, kmain_end); ++p)
+      for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
     for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
   }
 
@@ -237,9 +239,10 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       xpy[warp * 32 + lane] = ppy[0];
       xP[((k & 1) * 8 + warp) * 32 + lane] = Py[0];
       __syncthreads();  // (1)
-      if (threadIdx.x == 0) {
-        if (k + 2 <= kmain_end) issue_main(k + 2);
-        if (k + 3 <= kpz_end) issue_pz(k + 3);
+      // the copies two planes ahead, spread over the warps' first lanes
+      if (lane == 0) {
+        if (warp < narr && k + 2 <= kmain_end) issue_main_array(k + 2, warp, warp_map);
+        if (warp == 7 && k + 3 <= kpz_end) issue_pz(k + 3);
       }
 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow)
