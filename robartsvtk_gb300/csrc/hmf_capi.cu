@@ -386,7 +386,16 @@ int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t 
   const long long chunks = (c->geo.vol + vc - 1) / vc;
   const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
   const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
-  hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);
+  switch (c->n) {
+#define HMF_TREE_N(N)                                                                 \
+  case N:                                                                             \
+    hmf::tree_bulk_n_kernel<N><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error); \
+    break;
+    HMF_TREE_N(2) HMF_TREE_N(3) HMF_TREE_N(4) HMF_TREE_N(5) HMF_TREE_N(6) HMF_TREE_N(7) HMF_TREE_N(8)
+#undef HMF_TREE_N
+    default:
+      hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);
+  }
   CK(cudaGetLastError(), "tree_bulk_kernel launch");
   ++c->launches;
   return HMF_OK;
@@ -594,6 +603,13 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::tree_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           128 + hmf::kTreeBulkSmemBudget),
      "cudaFuncSetAttribute(tree_bulk_kernel)");
+#define HMF_TREE_N_ATTR(N)                                                                    \
+  CK(cudaFuncSetAttribute(hmf::tree_bulk_n_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                          hmf::tree_bulk_smem_bytes(N)),                                      \
+     "cudaFuncSetAttribute(tree_bulk_n_kernel)");
+  HMF_TREE_N_ATTR(2) HMF_TREE_N_ATTR(3) HMF_TREE_N_ATTR(4) HMF_TREE_N_ATTR(5) HMF_TREE_N_ATTR(6)
+  HMF_TREE_N_ATTR(7) HMF_TREE_N_ATTR(8)
+#undef HMF_TREE_N_ATTR
   return HMF_OK;
 }
 

@@ -26,14 +26,14 @@ constexpr int kTreeBulkSmemBudget = 200 * 1024;
 
 // Chunk length (voxels) for a tree of n entries: the largest power of two
 // <= 1024 whose two stages fit the shared-memory budget.
-__host__ __device__ inline int tree_bulk_chunk(int n) {
+__host__ __device__ constexpr int tree_bulk_chunk(int n) {
   const int arrays = 3 * (n - 1) + 1;
   int vc = 1024;
   while (vc > 32 && kTreeBulkStages * arrays * vc * 4 > kTreeBulkSmemBudget) vc /= 2;
   return vc;
 }
 
-__host__ __device__ inline int tree_bulk_smem_bytes(int n) {
+__host__ __device__ constexpr int tree_bulk_smem_bytes(int n) {
   return 128 + kTreeBulkStages * (3 * (n - 1) + 1) * tree_bulk_chunk(n) * 4;
 }
 
@@ -164,6 +164,154 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
       for (int s = 0; s < kTreeBulkStages; ++s)
         if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
   }
+}
+
+// The same sweep for trees of N <= 8 entries (the root last, entries in
+// post-order).  The tree's shape is read once per CTA into registers -- per
+// entry the staged offset of its parent's sink, a bit mask of its children,
+// 1/(kids+1) and the output pointers -- and the chunk length is a
+// compile-time constant, so every staged array is an immediate offset from
+// one shared-memory base and the per-voxel code reads no table.
+template <int N>
+__global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
+    tree_bulk_n_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag) {
+  constexpr int R = N - 1;  // the root entry
+  constexpr int A = 3 * R + 1;
+  constexpr int VC = tree_bulk_chunk(N);
+  constexpr int Q = VC / 4;  // float4 per staged array
+  __shared__ TreeTable T;
+  __shared__ int abort_cta;
+  extern __shared__ __align__(128) unsigned char tb_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tb_raw);  // [2]
+  float4* stage0 = reinterpret_cast<float4*>(tb_raw + 128);
+
+  for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  if (threadIdx.x == 0) {
+    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    if (smem_addr(tb_raw) & 15) {
+      abort_cta = 1;
+      if (error_flag) atomicOr(error_flag, 4);
+    }
+    for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (abort_cta) return;
+
+  // staged slot of entry e's sink (root: the source flow) / divergence / label
+  auto ss = [](int e) { return e == R ? 3 * R : 3 * e + 2; };
+  unsigned leaf_mask = 0, kmask[N];
+  int poff[N];
+  float inv[N];
+  float* lout[N];
+  float* sout[N];
+#pragma unroll
+  for (int e = 0; e < N; ++e) {
+    const TreeEntry& E = T.e[e];
+    if (e != R && E.n_kids == 0) leaf_mask |= 1u << e;
+    poff[e] = e == R ? 0 : (E.parent == R ? 3 * R : 3 * E.parent + 2) * Q;
+    inv[e] = E.inv_kids;
+    lout[e] = E.label_out;
+    sout[e] = E.sink_out;
+    kmask[e] = 0;
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+      if (T.e[k].parent == e) kmask[e] |= 1u << k;
+  }
+  const float icc = T.icc, cc = T.cc, w0r = T.root_init;
+  const long long nchunks = (G.vol + VC - 1) / VC;
+
+  auto issue = [&](long long chunk, int s) {  // thread 0 only
+    const long long v0 = chunk * VC;
+    const unsigned bytes = (unsigned)(min((long long)VC, G.vol - v0) * 4);
+    uint64_t* bar = &bars[s];
+    float* dst = reinterpret_cast<float*>(stage0 + s * A * Q);
+    mbar_expect_tx(bar, bytes * (unsigned)A);
+    for (int e = 0; e < R; ++e) {
+      const TreeEntry& E = T.e[e];
+      bulk_load(dst + (3 * e) * VC, E.div + v0, bytes, bar);
+      bulk_load(dst + (3 * e + 1) * VC, E.label + v0, bytes, bar);
+      bulk_load(dst + (3 * e + 2) * VC, (E.n_kids ? E.sink : E.data) + v0, bytes, bar);
+    }
+    bulk_load(dst + (3 * R) * VC, T.e[R].sink + v0, bytes, bar);
+  };
+
+  bool timed_out = false;
+  int nissued[kTreeBulkStages] = {0, 0};  // kept by thread 0
+  long long chunk = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  }
+  for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
+    const int s = j & 1;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    const long long v0 = chunk * VC;
+    const int len = (int)min((long long)VC, G.vol - v0);
+    if ((int)threadIdx.x * 4 < len) {
+      float4* b = stage0 + s * A * Q + threadIdx.x;  // this thread's four voxels of staged array 0
+      // ---- sinks in post-order (a parent's old sink is read before it is replaced)
+#pragma unroll
+      for (int e = 0; e < N; ++e) {
+        if (e != R && (leaf_mask >> e & 1u)) {
+          const float4 inc = b[poff[e]], d = b[(3 * e) * Q], u = b[(3 * e + 1) * Q], cap = b[(3 * e + 2) * Q];
+          float4 r;
+          float v;
+#define HMF_LEAF(c)              \
+  v = (inc.c - d.c) + u.c * icc; \
+  v = (v < 0.0f) ? 0.0f : v;     \
+  v = (v > cap.c) ? cap.c : v;   \
+  r.c = v;
+          HMF_LEAF(x) HMF_LEAF(y) HMF_LEAF(z) HMF_LEAF(w)
+#undef HMF_LEAF
+          b[(3 * e + 2) * Q] = r;
+        } else {
+          const float w0 = e == R ? w0r : 0.0f;
+          float4 W = make_float4(w0, w0, w0, w0);
+#pragma unroll
+          for (int k = 0; k < e; ++k)
+            if (kmask[e] >> k & 1u) {
+              const float4 sc = b[ss(k) * Q], dc = b[(3 * k) * Q], uc = b[(3 * k + 1) * Q];
+              W.x = ((W.x + sc.x) + dc.x) - uc.x * icc;
+              W.y = ((W.y + sc.y) + dc.y) - uc.y * icc;
+              W.z = ((W.z + sc.z) + dc.z) - uc.z * icc;
+              W.w = ((W.w + sc.w) + dc.w) - uc.w * icc;
+            }
+          if (e != R) {
+            const float4 inc = b[poff[e]], d = b[(3 * e) * Q], u = b[(3 * e + 1) * Q];
+            W.x = ((W.x + inc.x) - d.x) + u.x * icc;
+            W.y = ((W.y + inc.y) - d.y) + u.y * icc;
+            W.z = ((W.z + inc.z) - d.z) + u.z * icc;
+            W.w = ((W.w + inc.w) - d.w) + u.w * icc;
+          }
+          b[ss(e) * Q] = make_float4(W.x * inv[e], W.y * inv[e], W.z * inv[e], W.w * inv[e]);
+        }
+      }
+      // ---- labels, then every new sink and label to global memory
+      const long long i = v0 + threadIdx.x * 4;
+#pragma unroll
+      for (int e = 0; e < R; ++e) {
+        const float4 inc = b[poff[e]], d = b[(3 * e) * Q], sk = b[(3 * e + 2) * Q], u = b[(3 * e + 1) * Q];
+        float4 o;
+        o.x = __saturatef(u.x + cc * ((inc.x - d.x) - sk.x));
+        o.y = __saturatef(u.y + cc * ((inc.y - d.y) - sk.y));
+        o.z = __saturatef(u.z + cc * ((inc.z - d.z) - sk.z));
+        o.w = __saturatef(u.w + cc * ((inc.w - d.w) - sk.w));
+        *reinterpret_cast<float4*>(lout[e] + i) = o;
+        *reinterpret_cast<float4*>(sout[e] + i) = sk;
+      }
+      *reinterpret_cast<float4*>(sout[R] + i) = b[(3 * R) * Q];
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();  // stage s is free again
+    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+  }
+  if (timed_out && error_flag) atomicOr(error_flag, 2);
+  if (threadIdx.x == 0 && timed_out)
+    for (int s = 0; s < kTreeBulkStages; ++s)
+      if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
 }
 
 }  // namespace hmf
