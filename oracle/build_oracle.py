@@ -1,8 +1,9 @@
 """Build recipe for the oracle (test infrastructure only).
 
 Outputs (all git-ignored):
-  oracle/_build/liboracle.so   -- the CPU restatement in hmf_oracle.cpp
-                                  (REF_CUDA in FP32/FP64 and the REF_CPU port).
+  oracle/_build/liboracle.so   -- the CPU restatements in hmf_oracle.cpp
+                                  (REF_CUDA in FP32/FP64 and the REF_CPU port)
+                                  and dag_oracle.cpp (the DAG solver).
   oracle/_ref/libhmf_ref_cpu.so -- only where the reference sources exist:
                                   the same REF_CPU driver linked against the
                                   reference's own, unmodified
@@ -51,10 +52,10 @@ def _newer(target: str, sources: list[str]) -> bool:
 
 def build_port(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "hmf_oracle.cpp")
+    srcs = [os.path.join(HERE, "hmf_oracle.cpp"), os.path.join(HERE, "dag_oracle.cpp")]
     out = os.path.join(BUILD, "liboracle.so")
-    if force or not _newer(out, [src]):
-        _run(["g++", *CXXFLAGS, src, "-o", out + ".tmp"])
+    if force or not _newer(out, srcs):
+        _run(["g++", *CXXFLAGS, *srcs, "-o", out + ".tmp"])
         os.replace(out + ".tmp", out)
     return out
 

@@ -205,3 +205,67 @@ def energy(dims, parent, data, labels, smooth=None, want_terms=False):
     if terms is not None:
         out["terms"] = terms.reshape((n, vz, vy, vx))
     return out
+
+
+def _dag_edges(edges, weights):
+    ep = np.ascontiguousarray([int(p) for p, _ in edges], dtype=np.int32)
+    ec = np.ascontiguousarray([int(c) for _, c in edges], dtype=np.int32)
+    ew = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    return ep, ec, ew
+
+
+def dag_solve(dims, n_nodes, edges, data, weights=None, smooth=None, alpha=None, iterations=100, step=0.1,
+              cc=0.25, precision=32, threads=0):
+    """The DAG max-flow solver as vtkCudaDirectedAcyclicGraphMaxFlowSegmentation
+    runs it, in the fixed task order of dag_oracle.cpp.  `edges` = [(parent,
+    child), ...] in edge order, `weights` per edge or None; `data`/`smooth`/
+    `alpha` dicts keyed by vertex id (a vertex missing from `alpha` has alpha
+    0).  Returns {"u", "sink", "inc"}: [n, VZ, VY, VX] float64."""
+    lib = port_library()
+    fn = lib.oracle_dag_solve
+    fn.restype = ctypes.c_int
+    lib.oracle_dag_last_error.restype = ctypes.c_char_p
+    vx, vy, vz = (int(d) for d in dims)
+    n = int(n_nodes)
+    V = vx * vy * vz
+    ep, ec, ew = _dag_edges(edges, weights)
+    keep = []
+    dptr = (ctypes.c_void_p * n)()
+    sptr = (ctypes.c_void_p * n)()
+    for v in range(n):
+        if data.get(v) is not None:
+            a = np.ascontiguousarray(data[v], dtype=np.float32).reshape(-1)
+            keep.append(a)
+            dptr[v] = a.ctypes.data
+        if smooth and smooth.get(v) is not None:
+            a = np.ascontiguousarray(smooth[v], dtype=np.float32).reshape(-1)
+            keep.append(a)
+            sptr[v] = a.ctypes.data
+    al = (ctypes.c_double * n)(*[float((alpha or {}).get(v, float("nan"))) for v in range(n)])
+    u = np.zeros((n, V), np.float64)
+    sink = np.zeros((n, V), np.float64)
+    inc = np.zeros((n, V), np.float64)
+    rc = fn(int(precision), int(threads), vx, vy, vz, n, len(ep), ep.ctypes.data_as(ctypes.c_void_p),
+            ec.ctypes.data_as(ctypes.c_void_p), ew.ctypes.data_as(ctypes.c_void_p) if ew is not None else None,
+            dptr, sptr, al, int(iterations), ctypes.c_float(step), ctypes.c_float(cc),
+            u.ctypes.data_as(ctypes.c_void_p), sink.ctypes.data_as(ctypes.c_void_p),
+            inc.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("oracle DAG solve failed (%d): %s" % (rc, lib.oracle_dag_last_error().decode()))
+    shape = (n, vz, vy, vx)
+    return {"u": u.reshape(shape), "sink": sink.reshape(shape), "inc": inc.reshape(shape)}
+
+
+def dag_forward(n_nodes, edges, weights=None):
+    """The rooted DAG's forward-iterator vertex order (leaves in it = output order)."""
+    lib = port_library()
+    fn = lib.oracle_dag_forward
+    fn.restype = ctypes.c_int
+    lib.oracle_dag_last_error.restype = ctypes.c_char_p
+    ep, ec, ew = _dag_edges(edges, weights)
+    out = np.zeros(int(n_nodes), np.int32)
+    rc = fn(int(n_nodes), len(ep), ep.ctypes.data_as(ctypes.c_void_p), ec.ctypes.data_as(ctypes.c_void_p),
+            ew.ctypes.data_as(ctypes.c_void_p) if ew is not None else None, out.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("oracle DAG graph rejected (%d): %s" % (rc, lib.oracle_dag_last_error().decode()))
+    return [int(v) for v in out]

@@ -14,8 +14,10 @@ reference allocates them (:513-538, CUDA_hierarchicalmaxflow.cu:33-60), since
 its kernels read up to one plane outside a buffer before masking.  Buffers are
 torch CUDA tensors; kernels run on torch's current stream.
 
-It also runs the reference's vote kernel (CUDA_imagevote.cu) and the
-gradient kernel of its energy decomposition (CUDA_hierarchicalmaxflowdecomp.cu).
+It also runs the reference's vote kernel (CUDA_imagevote.cu), the
+gradient kernel of its energy decomposition (CUDA_hierarchicalmaxflowdecomp.cu),
+and the DAG solver's tasks (vtkCudaMaxFlowSegmentationTask.cxx:309-492) in the
+fixed order that oracle/dag_oracle.cpp restates.
 It is used only to generate golden vectors (tests/golden/make_golden.py) and
 to pin the oracle; nothing in the product imports it.
 """
@@ -56,6 +58,12 @@ _NAMES = {
     # energy decomposition (CUDA_hierarchicalmaxflowdecomp.cu:19)
     "ghmfd_grad": "_Z25kern_GHMFD_GradientBufferPfS_4int3i",
     "mul": "_Z15MultiplyBuffersIfEvPT_S1_i",
+    # DAG solver tasks (CUDA_hierarchicalmaxflow.cu:610-664, CUDA_commonKernels.cu:96, :419)
+    "resetsink": "_Z20kern_ResetSinkBufferPfS_S_S_ffi",
+    "pushup": "_Z22kern_PushUpSourceFlowsPfS_S_S_S_ffi",
+    "copy2": "_Z17kern_Copy2BuffersPfS_S_i",
+    "translate": "_Z15TranslateBufferIfEvPT_S0_S0_i",
+    "sumscaled": "_Z16SumScaledBuffersIfEvPT_S1_S0_i",
 }
 
 
@@ -316,3 +324,178 @@ def gradient_terms(label, dims, smooth=None):
         g = sm
     torch.cuda.synchronize()
     return g[pad:pad + V].cpu().numpy().reshape(vz, vy, vx)
+
+
+class DagGraph:
+    """The rooted DAG bookkeeping of oracle/dag_oracle.cpp (levels, forward
+    iterator order, weighted parent and child counts) in float32 as the
+    reference computes it (vtkDirectedAcyclicGraphMaxFlowSegmentation.cxx:906-995,
+    vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:343-692)."""
+
+    def __init__(self, n_nodes, edges, weights=None):
+        f32 = np.float32
+        self.n = n = int(n_nodes)
+        self.ep = [int(p) for p, _ in edges]
+        self.ec = [int(c) for _, c in edges]
+        self.weighted = weights is not None
+        self.ew = [f32(w) for w in weights] if weights is not None else [f32(1.0)] * len(edges)
+        self.in_e = [[] for _ in range(n)]
+        self.out_e = [[] for _ in range(n)]
+        for e, (p, c) in enumerate(zip(self.ep, self.ec)):
+            self.out_e[p].append(e)
+            self.in_e[c].append(e)
+        self.root = [v for v in range(n) if not self.in_e[v]][0]
+        indeg = [len(self.in_e[v]) for v in range(n)]
+        self.level = [0] * n
+        topo = [self.root]
+        for v in topo:
+            for e in self.out_e[v]:
+                k = self.ec[e]
+                self.level[k] = max(self.level[k], self.level[v] + 1)
+                indeg[k] -= 1
+                if indeg[k] == 0:
+                    topo.append(k)
+        seen = {self.root}
+        self.forward = [self.root]
+        for v in self.forward:
+            for e in self.out_e[v]:
+                k = self.ec[e]
+                if self.level[k] == self.level[v] + 1 and k not in seen:
+                    seen.add(k)
+                    self.forward.append(k)
+        self.n_parents = [f32(0.0)] * n
+        for v in range(n):
+            acc = f32(0.0)
+            for e in self.in_e[v]:
+                acc = f32(acc + (self.ew[e] if self.weighted else f32(1.0)))
+            self.n_parents[v] = acc
+        self.wkids = [f32(0.0)] * n
+        for v in range(n):
+            acc = f32(0.0)
+            for e in self.out_e[v]:
+                t = f32((float(self.ew[e]) if self.weighted else 1.0) / float(self.n_parents[self.ec[e]]))
+                acc = f32(acc + f32(t * t))
+            self.wkids[v] = acc
+
+    def leaf(self, v):
+        return not self.out_e[v]
+
+    def wdown(self, e):
+        return self.ew[e] if self.weighted else np.float32(1.0 / float(len(self.in_e[self.ec[e]])))
+
+    def wup(self, e):
+        f32 = np.float32
+        W = self.ew[e] if self.weighted else f32(1.0 / float(len(self.in_e[self.ec[e]])))
+        p = self.ep[e]
+        return f32(W / self.wkids[p]) if p == self.root else f32(W / f32(self.wkids[p] + f32(1.0)))
+
+
+def dag_solve(dims, n_nodes, edges, data, weights=None, smooth=None, alpha=None, iterations=100, step=0.1,
+              cc=0.25):
+    """The DAG solver through the reference's own kernels, tasks in the order of
+    oracle/dag_oracle.cpp.  Arguments as oracle.oracle.dag_solve(); returns
+    {"u", "sink", "inc"}: [n, VZ, VY, VX] float32."""
+    import torch
+
+    K = ReferenceKernels()
+    g = DagGraph(n_nodes, edges, weights)
+    vx, vy, vz = (int(d) for d in dims)
+    V = vx * vy * vz
+    pad = vx * vy + 2 * NUMTHREADS
+    n = g.n
+    keep = []
+
+    def buf(init=None):
+        t = torch.zeros(V + 2 * pad, dtype=torch.float32, device="cuda")
+        if init is not None:
+            t[pad:pad + V] = torch.from_numpy(np.ascontiguousarray(init, dtype=np.float32).reshape(-1)).cuda()
+        keep.append(t)
+        return _Ptr(t.data_ptr() + 4 * pad)
+
+    leaves = [v for v in g.forward if g.leaf(v)]
+    sink = {v: buf() for v in range(n)}
+    fx, fy, fz, dv, lab, inc = ({} for _ in range(6))
+    for v in range(n):
+        if v != g.root:
+            fx[v], fy[v], fz[v], dv[v], lab[v], inc[v] = buf(), buf(), buf(), buf(), buf(), buf()
+    D = {l: buf(data[l]) for l in leaves}
+    S = {v: buf(smooth[v]) for v in range(n) if smooth is not None and smooth.get(v) is not None}
+    a = {v: float(np.float32((alpha or {}).get(v, 0.0))) for v in range(n)}
+    acc = buf()
+    dims2 = _Int2(vx, vy)
+    step = float(np.float32(step))
+    ccf = float(np.float32(cc))
+    icc = float(np.float32(1.0) / np.float32(cc))
+    src = sink[g.root]
+
+    # initialisation (vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:844-1045)
+    K.launch("copy", V, src, D[leaves[0]], V)
+    for l in leaves[1:]:
+        K.launch("min", V, src, D[l], V)
+    for v in g.forward:
+        if v != g.root:
+            K.launch("copy2", V, src, sink[v], inc[v], V)
+    for l in leaves:
+        K.launch("lbl", V, lab[l], sink[l], D[l], V)
+        K.launch("sum", V, acc, lab[l], V)
+    for l in leaves:
+        K.launch("divbuf", V, lab[l], acc, V)
+    for v in reversed(g.forward):
+        if v == g.root or g.leaf(v):
+            continue
+        K.launch("zero", V, lab[v], V)
+        for e in g.out_e[v]:
+            K.launch("sumscaled", V, lab[v], lab[g.ec[e]], float(g.wdown(e)), V)
+
+    shift = float(np.float32(1.0 / float(np.float32(np.float32(cc) * g.wkids[g.root]))))
+    T = int(iterations)
+    for t in range(T):
+        for v in g.forward:  # (1) UpdateSpatialFlowsTask
+            if v == g.root:
+                continue
+            K.launch("gradstep", V, sink[v], inc[v], dv[v], lab[v], step, icc, V)
+            K.launch("descent", V, dv[v], fx[v], fy[v], fz[v], dims2, V)
+            if v in S:
+                K.launch("magvari", V, dv[v], fx[v], fy[v], fz[v], S[v], a[v], dims2, V)
+            else:
+                K.launch("magconst", V, dv[v], fx[v], fy[v], fz[v], a[v], dims2, V)
+            K.launch("project", V, dv[v], fx[v], fy[v], fz[v], dims2, V)
+            K.launch("divergence", V, dv[v], fx[v], fy[v], fz[v], dims2, V)
+        K.launch("translate", V, src, 1.0, shift, V)  # (2) ResetSinkFlowRoot
+        for v in range(n):
+            if v == g.root:
+                continue
+            if g.leaf(v):  # ApplySinkPotentialLeafTask, UpdateLabelsTask
+                K.launch("leafsink", V, sink[v], inc[v], dv[v], lab[v], icc, V)
+                K.launch("capacity", V, sink[v], D[v], V)
+                K.launch("label", V, sink[v], inc[v], dv[v], lab[v], ccf, V)
+            else:  # ResetSinkFlowBranch
+                k = float(np.float32(1.0 / (float(g.wkids[v]) + 1.0)))
+                K.launch("resetsink", V, sink[v], inc[v], dv[v], lab[v], k, icc, V)
+        if t == T - 1:
+            break
+        for v in reversed(g.forward):  # (3) PushUpSourceFlows, branch UpdateLabelsTask
+            if v == g.root:
+                continue
+            for e in g.in_e[v]:
+                K.launch("pushup", V, sink[g.ep[e]], sink[v], inc[v], dv[v], lab[v], float(g.wup(e)), icc, V)
+            if not g.leaf(v):
+                K.launch("label", V, sink[v], inc[v], dv[v], lab[v], ccf, V)
+        for v in range(n):  # (4) ClearSourceBuffer, PushDownSinkFlows
+            if v == g.root:
+                continue
+            K.launch("zero", V, inc[v], V)
+            for e in g.in_e[v]:
+                K.launch("sumscaled", V, inc[v], sink[g.ep[e]], float(g.wdown(e)), V)
+    torch.cuda.synchronize()
+
+    def fetch(p):
+        return _as_tensor(keep, p, V, pad).cpu().numpy().reshape(vz, vy, vx)
+
+    out = {k: np.zeros((n, vz, vy, vx), dtype=np.float32) for k in ("u", "sink", "inc")}
+    for v in range(n):
+        out["sink"][v] = fetch(sink[v])
+        if v != g.root:
+            out["u"][v] = fetch(lab[v])
+            out["inc"][v] = fetch(inc[v])
+    return out

@@ -14,6 +14,10 @@
       ties, and the per-voxel terms of its energy decomposition
       (CUDA_hierarchicalmaxflowdecomp.cu) of seeded labellings, with and
       without a smoothness image (POST_CASES in tests/golden/cases.py).
+  python -m tests.golden.make_golden --ref-dag OUT.npz   (on a GPU)
+      the DAG solver through the reference's own kernels, its tasks
+      (vtkCudaMaxFlowSegmentationTask.cxx:309-492) in the order that
+      oracle/dag_oracle.cpp restates (DAG_CASES in tests/golden/cases.py).
 """
 import os
 import sys
@@ -69,6 +73,19 @@ def ref_post(path):
     np.savez_compressed(path, **out)
 
 
+def ref_dag(path):
+    from oracle import ref_kernels
+    from tests.golden.cases import DAG_CASES, dag_problem
+    out = {}
+    for name in DAG_CASES:
+        w = dag_problem(name)
+        res = ref_kernels.dag_solve(w.dims, w.n, w.edges, w.data, w.weights, w.smooth, w.alpha, w.iterations,
+                                    w.step, w.cc)
+        for k in ("u", "sink", "inc"):
+            out[name + "/" + k] = res[k].astype(np.float32)
+    np.savez_compressed(path, **out)
+
+
 if __name__ == "__main__":
     if "--ref-cpu" in sys.argv:
         ref_cpu(os.path.join(HERE, "ref_cpu_golden.npz"))
@@ -78,3 +95,6 @@ if __name__ == "__main__":
     if "--ref-post" in sys.argv:
         i = sys.argv.index("--ref-post")
         ref_post(sys.argv[i + 1] if i + 1 < len(sys.argv) else os.path.join(HERE, "ref_post_golden.npz"))
+    if "--ref-dag" in sys.argv:
+        i = sys.argv.index("--ref-dag")
+        ref_dag(sys.argv[i + 1] if i + 1 < len(sys.argv) else os.path.join(HERE, "ref_dag_golden.npz"))
