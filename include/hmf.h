@@ -69,6 +69,26 @@ typedef struct hmf_ctx hmf_ctx;
  * Device memory for the whole solver state is allocated here, once. */
 int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes,
                int semantics, int device);
+
+/* Create a solver for a directed acyclic graph of labels: the problem of
+ * vtkCudaDirectedAcyclicGraphMaxFlowSegmentation (its InitializeAlgorithm /
+ * RunAlgorithm, vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:150-286,
+ * over a vtkRootedDirectedAcyclicGraph).  Edge e runs from edge_parent[e] to
+ * edge_child[e]; edge order is the graph's edge order (a vertex's children are
+ * its out-edges in that order).  edge_weight: one positive weight per edge
+ * (the graph's "Weights" edge array) or NULL for none.  The single vertex
+ * without parents is the root; every vertex must be reachable from it and
+ * the graph acyclic (<= 64 vertices, <= 256 edges).  semantics must be
+ * HMF_SEMANTICS_REF_CUDA.  The reference's scheduler orders ready tasks at
+ * random; this library runs its task graph in one fixed order (the order of
+ * its weighted accumulations and, for a branch, its potential pushed up
+ * before its label update).  A vertex without hmf_set_smoothness_scalar has
+ * alpha 0, as the reference class reads its scalar map with operator[].
+ * Leaves are numbered in the graph's forward-iterator order (hmf_leaf_order).
+ * Every other call taking a context works on it, except the batch, adjoint
+ * and energy calls. */
+int hmf_create_dag(hmf_ctx** out, int vx, int vy, int vz, int n_nodes, int n_edges, const int* edge_parent,
+                   const int* edge_child, const float* edge_weight, int semantics, int device);
 int hmf_destroy(hmf_ctx* ctx);
 
 /* Data term (cost) of a leaf.  Replaces SetDataInputDataObject(idx, image)

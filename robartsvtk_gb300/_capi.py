@@ -45,6 +45,8 @@ SIGNATURES = [
     ("hmf_get_stats", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_last_error", ctypes.c_char_p, [_P]),
     ("hmf_create_batch", _I, [ctypes.POINTER(_P), _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _I, _I, _I]),
+    ("hmf_create_dag", _I, [ctypes.POINTER(_P), _I, _I, _I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                            ctypes.POINTER(ctypes.c_float), _I, _I]),
     ("hmf_num_volumes", _I, [_P]),
     ("hmf_batch_set_data", _I, [_P, _I, _I, _P, _I]),
     ("hmf_batch_set_smoothness", _I, [_P, _I, _I, _P, _I]),

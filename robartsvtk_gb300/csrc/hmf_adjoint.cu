@@ -545,6 +545,7 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
                       void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
   if (c->vols.size() != 1) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the adjoint supports single-volume contexts");
+  if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the adjoint is defined for trees (hmf_create), not graphs");
   if (c->semantics != HMF_SEMANTICS_REF_CUDA)
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "the adjoint is defined for the REF_CUDA semantics");
   if (!truth) return fail(c, HMF_ERR_INVALID_ARGUMENT, "ground-truth pointer is NULL");

@@ -17,6 +17,11 @@
 // whole concatenation and the flow kernel over a table of (volume, window)
 // work items, so a batch costs the same two launches per iteration as a
 // single volume.
+//
+// A context made by hmf_create_dag solves the directed-acyclic-graph problem
+// of vtkCudaDirectedAcyclicGraphMaxFlowSegmentation instead: the same flow
+// kernel (each node's "inc" is its own source buffer), then dag_sweep_kernel
+// (hmf_dag.cuh) per iteration.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +37,7 @@
 
 #include "../../include/hmf.h"
 #include "hmf_ctx.hpp"
+#include "hmf_dag.cuh"
 #include "hmf_flow_tma.cuh"
 #include "hmf_kernels.cuh"
 #include "hmf_tree_bulk.cuh"
@@ -108,6 +114,87 @@ int build_tree(hmf_ctx* c, const int* par, int n) {
   return HMF_OK;
 }
 
+// A rooted DAG (vtkRootedDirectedAcyclicGraph.cxx:145-243): one vertex
+// without parents, every vertex reachable, no cycle.  Levels are longest
+// paths from the root; the forward order visits them level by level, a child
+// entered from a parent one level up, children in edge order
+// (vtkRootedDirectedAcyclicGraphForwardIterator.cxx:95-120).  Parent and child
+// counts are weighted as vtkDirectedAcyclicGraphMaxFlowSegmentation.cxx:928-995
+// computes them.
+int build_dag(hmf_ctx* c, int n, int n_edges, const int* ep, const int* ec, const float* ew) {
+  if (!ep || !ec) return fail(c, HMF_ERR_TREE, "edge arrays are NULL");
+  if (n < 2 || n_edges < 1) return fail(c, HMF_ERR_TREE, "the graph needs a root, a leaf and an edge");
+  if (n > hmf::kMaxVertices)
+    return fail(c, HMF_ERR_TREE, "graphs of more than " + std::to_string(hmf::kMaxVertices) +
+                                     " vertices are not supported");
+  if (n_edges > hmf::kMaxDagEdges)
+    return fail(c, HMF_ERR_TREE, "graphs of more than " + std::to_string(hmf::kMaxDagEdges) +
+                                     " edges are not supported");
+  c->dag = true;
+  c->n = n;
+  c->e_parent.assign(ep, ep + n_edges);
+  c->e_child.assign(ec, ec + n_edges);
+  c->e_weighted = ew != nullptr;
+  c->e_weight.assign(n_edges, 1.0f);
+  if (ew) c->e_weight.assign(ew, ew + n_edges);
+  c->in_e.assign(n, {});
+  c->out_e.assign(n, {});
+  for (int e = 0; e < n_edges; ++e) {
+    if (ep[e] < 0 || ep[e] >= n || ec[e] < 0 || ec[e] >= n || ep[e] == ec[e])
+      return fail(c, HMF_ERR_TREE, "edge vertex out of range");
+    if (ew && !(ew[e] > 0.0f && ew[e] < INFINITY)) return fail(c, HMF_ERR_TREE, "edge weights must be positive");
+    c->out_e[ep[e]].push_back(e);
+    c->in_e[ec[e]].push_back(e);
+  }
+  c->root = -1;
+  for (int v = 0; v < n; ++v)
+    if (c->in_e[v].empty()) {
+      if (c->root >= 0) return fail(c, HMF_ERR_TREE, "the graph has more than one root");
+      c->root = v;
+    }
+  if (c->root < 0) return fail(c, HMF_ERR_TREE, "the graph has no root");
+  std::vector<int> indeg(n), topo{c->root}, level(n, 0);
+  for (int v = 0; v < n; ++v) indeg[v] = (int)c->in_e[v].size();
+  for (size_t i = 0; i < topo.size(); ++i)
+    for (int e : c->out_e[topo[i]]) {
+      const int k = ec[e];
+      level[k] = std::max(level[k], level[topo[i]] + 1);
+      if (--indeg[k] == 0) topo.push_back(k);
+    }
+  if ((int)topo.size() != n) return fail(c, HMF_ERR_TREE, "the graph has a cycle or an unreachable vertex");
+  std::vector<char> seen(n, 0);
+  c->preorder.assign(1, c->root);
+  seen[c->root] = 1;
+  for (size_t i = 0; i < c->preorder.size(); ++i) {
+    const int v = c->preorder[i];
+    for (int e : c->out_e[v]) {
+      const int k = ec[e];
+      if (level[k] != level[v] + 1 || seen[k]) continue;
+      seen[k] = 1;
+      c->preorder.push_back(k);
+    }
+  }
+  c->kids.assign(n, {});
+  c->parent.assign(n, -1);
+  for (int v = 0; v < n; ++v) {
+    for (int e : c->out_e[v]) c->kids[v].push_back(ec[e]);
+    if (!c->in_e[v].empty()) c->parent[v] = ep[c->in_e[v][0]];
+  }
+  c->leaves.clear();
+  for (int v : c->preorder)
+    if (c->kids[v].empty()) c->leaves.push_back(v);
+  c->n_parents.assign(n, 0.0f);
+  for (int v = 0; v < n; ++v)
+    for (int e : c->in_e[v]) c->n_parents[v] += c->e_weighted ? c->e_weight[e] : 1.0f;
+  c->wkids.assign(n, 0.0f);
+  for (int v = 0; v < n; ++v)
+    for (int e : c->out_e[v]) {
+      const float t = (float)((c->e_weighted ? (double)c->e_weight[e] : 1.0) / c->n_parents[ec[e]]);
+      c->wkids[v] += t * t;
+    }
+  return HMF_OK;
+}
+
 // Device memory plan: per non-root vertex 9 arrays (sink, label, div, two
 // sets of three flow components), the root's source flow; every array holds
 // all volumes.
@@ -115,7 +202,7 @@ int allocate_state(hmf_ctx* c) {
   const size_t arr = round_up((size_t)c->total * sizeof(float), 256);
   const int nonroot = c->n - 1;
   const int nvol = (int)c->vols.size();
-  c->arena_bytes = arr * (size_t)(9 * nonroot + 1) + 4096;
+  c->arena_bytes = arr * (size_t)((c->dag ? 10 : 9) * nonroot + 1) + 4096;
   CK(cudaMalloc(&c->arena, c->arena_bytes), "cudaMalloc(state)");
   CK(cudaMemset(c->arena, 0, c->arena_bytes), "cudaMemset(state)");
   char* p = c->arena;
@@ -127,6 +214,7 @@ int allocate_state(hmf_ctx* c) {
   c->sink.assign(c->n, nullptr);
   c->label.assign(c->n, nullptr);
   c->div.assign(c->n, nullptr);
+  c->inc.assign(c->n, nullptr);
   for (int s = 0; s < 2; ++s) {
     c->fx[s].assign(c->n, nullptr);
     c->fy[s].assign(c->n, nullptr);
@@ -137,6 +225,7 @@ int allocate_state(hmf_ctx* c) {
     if (v == c->root) continue;
     c->label[v] = take();
     c->div[v] = take();
+    if (c->dag) c->inc[v] = take();
     for (int s = 0; s < 2; ++s) {
       c->fx[s][v] = take();
       c->fy[s][v] = take();
@@ -148,6 +237,7 @@ int allocate_state(hmf_ctx* c) {
   CK(cudaMalloc(&c->d_tma, sizeof(hmf::FlowVertexTMA) * (size_t)nvol * nonroot), "cudaMalloc(tma table)");
   CK(cudaMalloc(&c->d_fvol, sizeof(hmf::FlowVolume) * nvol), "cudaMalloc(volume table)");
   CK(cudaMalloc(&c->d_tree, sizeof(hmf::TreeTable)), "cudaMalloc(tree table)");
+  if (c->dag) CK(cudaMalloc(&c->d_dag, sizeof(hmf::DagTable)), "cudaMalloc(graph table)");
   CK(cudaMalloc(&c->d_smooth_list, sizeof(float*) * hmf::kMaxVertices), "cudaMalloc(smooth list)");
   CK(cudaMalloc(&c->d_error, sizeof(int)), "cudaMalloc(error flag)");
   CK(cudaMemset(c->d_error, 0, sizeof(int)), "cudaMemset(error flag)");
@@ -401,7 +491,26 @@ int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t 
   return HMF_OK;
 }
 
+// Grid of the per-voxel DAG kernels: as many blocks as are resident at once.
+int dag_grid(hmf_ctx* c, const void* kernel, size_t smem) {
+  int per = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, hmf::kDagThreads, smem) != cudaSuccess || per < 1)
+    per = 1;
+  const long long blocks = (c->geo.vol + hmf::kDagThreads - 1) / hmf::kDagThreads;
+  return (int)std::max<long long>(1, std::min<long long>(blocks, (long long)c->sm_count * per));
+}
+
+int launch_dag_sweep(hmf_ctx* c, cudaStream_t s) {
+  const size_t smem = 4 * (size_t)c->n * hmf::kDagThreads * sizeof(float);
+  hmf::dag_sweep_kernel<<<dag_grid(c, (const void*)hmf::dag_sweep_kernel, smem), hmf::kDagThreads, smem, s>>>(
+      c->d_dag, c->geo.vol, c->dag_last ? 1 : 0);
+  CK(cudaGetLastError(), "dag_sweep_kernel launch");
+  ++c->launches;
+  return HMF_OK;
+}
+
 int launch_tree(hmf_ctx* c, cudaStream_t s) {
+  if (c->dag) return launch_dag_sweep(c, s);
   if (c->tree_kind == 0) return launch_tree_bulk_with(c, c->d_tree, s);
   if (c->tree_kind == 1) {
     const size_t smem4 = 4 * (size_t)c->n * hmf::kTree4Threads * sizeof(float4);
@@ -466,6 +575,60 @@ int timed(hmf_ctx* c, int kind, cudaStream_t s, int (*fn)(hmf_ctx*, cudaStream_t
   return HMF_OK;
 }
 
+// The graph table of dag_sweep_kernel / dag_init_kernel: entries in forward
+// order (root first), weights as the reference's tasks hold them
+// (vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:394-692, 957-1037):
+// push-down and label weight = edge weight, else 1/#parents; push-up weight =
+// that divided by the parent's weighted children (+1 for a branch); branch
+// reset weight 1/(weighted children + 1); root shift 1/(CC * weighted children).
+int prepare_dag_table(hmf_ctx* c, cudaStream_t s, const Staged& in) {
+  hmf::DagTable& T = c->h_dag;
+  std::memset(&T, 0, sizeof(T));
+  std::vector<int> ent(c->n, -1);
+  for (int i = 0; i < c->n; ++i) ent[c->preorder[i]] = i;
+  T.n = c->n;
+  T.cc = c->cc;
+  T.icc = 1.0f / c->cc;
+  T.shift = (float)(1.0 / (double)(c->cc * c->wkids[c->root]));
+  auto wdown = [&](int e) {
+    return c->e_weighted ? c->e_weight[e] : (float)(1.0 / (double)c->in_e[c->e_child[e]].size());
+  };
+  int pin = 0, pout = 0;
+  for (int i = 0; i < c->n; ++i) {
+    const int v = c->preorder[i];
+    hmf::DagEntry& E = T.e[i];
+    E.sink = c->sink[v];
+    E.leaf = c->kids[v].empty() && v != c->root;
+    if (v != c->root) {
+      E.inc = c->inc[v];
+      E.label = c->label[v];
+      E.div = c->div[v];
+      E.data = E.leaf ? in.data[v] : nullptr;
+      E.k = (float)(1.0 / ((double)c->wkids[v] + 1.0));
+    }
+    if (E.leaf) T.leaves[T.n_leaves++] = i;
+    E.first_in = pin;
+    for (int e : c->in_e[v]) {
+      const int p = c->e_parent[e];
+      const float W = c->e_weighted ? c->e_weight[e] : (float)(1.0 / (double)c->in_e[v].size());
+      T.in_parent[pin] = ent[p];
+      T.in_wdown[pin] = wdown(e);
+      T.in_wup[pin] = p == c->root ? W / c->wkids[p] : W / (c->wkids[p] + 1.0f);
+      ++pin;
+    }
+    E.n_in = pin - E.first_in;
+    E.first_out = pout;
+    for (int e : c->out_e[v]) {
+      T.out_child[pout] = ent[c->e_child[e]];
+      T.out_w[pout] = wdown(e);
+      ++pout;
+    }
+    E.n_out = pout - E.first_out;
+  }
+  CK(cudaMemcpyAsync(c->d_dag, &T, sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(graph table)");
+  return HMF_OK;
+}
+
 int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
   const int nvol = (int)c->vols.size();
   const int nonroot = c->n - 1;
@@ -484,7 +647,7 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
       f.py_out = c->fy[par ^ 1][v];
       f.pz_out = c->fz[par ^ 1][v];
       f.sink = c->sink[v];
-      f.inc = c->sink[c->parent[v]];
+      f.inc = c->dag ? c->inc[v] : c->sink[c->parent[v]];
       f.label = c->label[v];
       f.smooth = in.smooth[v];
       f.div = c->div[v];
@@ -515,7 +678,7 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
         }
         if (!rc) rc = encode_plane_map(c, &f.sink, c->sink[v] + V.off, V);
         if (!rc) rc = encode_plane_map(c, &f.label, c->label[v] + V.off, V);
-        if (!rc) rc = encode_plane_map(c, &f.inc, c->sink[c->parent[v]] + V.off, V);
+        if (!rc) rc = encode_plane_map(c, &f.inc, (c->dag ? c->inc[v] : c->sink[c->parent[v]]) + V.off, V);
         const bool has_s = in.smooth[v] && c->smooth[b][v].ptr;
         if (!rc && has_s) rc = encode_plane_map(c, &f.smooth, in.smooth[v] + V.off, V);
         if (rc) return rc;
@@ -527,6 +690,10 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
     CK(cudaMemcpyAsync(c->d_tma, tv.data(), sizeof(hmf::FlowVertexTMA) * tv.size(), cudaMemcpyHostToDevice, s),
        "cudaMemcpyAsync(tma table)");
   }
+  if (c->dag) {
+    int rc = prepare_dag_table(c, s, in);
+    if (rc) return rc;
+  } else {
   hmf::TreeTable& tt = c->h_tree;
   std::memset(&tt, 0, sizeof(tt));
   std::vector<int> entry(c->n, -1);
@@ -553,6 +720,7 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
   }
   for (size_t j = 0; j < c->leaves.size(); ++j) tt.leaves[j] = entry[c->leaves[j]];
   CK(cudaMemcpyAsync(c->d_tree, &tt, sizeof(tt), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(tree table)");
+  }
   c->n_smooth_list = (int)in.distinct.size();
   c->h_smooth_list = in.distinct;
   if (!in.distinct.empty())
@@ -563,6 +731,14 @@ int prepare_tables(hmf_ctx* c, cudaStream_t s, const Staged& in) {
 }
 
 int do_init(hmf_ctx* c, cudaStream_t s, int) {
+  if (c->dag) {
+    const size_t smem = (size_t)c->n * hmf::kDagThreads * sizeof(float);
+    hmf::dag_init_kernel<<<dag_grid(c, (const void*)hmf::dag_init_kernel, smem), hmf::kDagThreads, smem, s>>>(
+        c->d_dag, c->geo.vol);
+    CK(cudaGetLastError(), "dag_init_kernel launch");
+    ++c->launches;
+    return HMF_OK;
+  }
   const size_t smem = (size_t)c->n * kTreeThreads * sizeof(float);
   hmf::init_kernel<<<tree_grid(c), kTreeThreads, smem, s>>>(c->d_tree, c->geo, c->d_smooth_list,
                                                            c->n_smooth_list,
@@ -610,6 +786,12 @@ int configure_kernels(hmf_ctx* c) {
   HMF_TREE_N_ATTR(2) HMF_TREE_N_ATTR(3) HMF_TREE_N_ATTR(4) HMF_TREE_N_ATTR(5) HMF_TREE_N_ATTR(6)
   HMF_TREE_N_ATTR(7) HMF_TREE_N_ATTR(8)
 #undef HMF_TREE_N_ATTR
+  CK(cudaFuncSetAttribute(hmf::dag_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          4 * hmf::kMaxVertices * hmf::kDagThreads * (int)sizeof(float)),
+     "cudaFuncSetAttribute(dag_sweep_kernel)");
+  CK(cudaFuncSetAttribute(hmf::dag_init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          hmf::kMaxVertices * hmf::kDagThreads * (int)sizeof(float)),
+     "cudaFuncSetAttribute(dag_init_kernel)");
   return HMF_OK;
 }
 
@@ -694,10 +876,12 @@ int end_solve(hmf_ctx* c, cudaStream_t user) {
 
 using namespace hmfi;
 
-extern "C" {
+namespace {
 
-int hmf_create_batch(hmf_ctx** out, int n_volumes, const int* dims, const int* parent, int n_nodes,
-                     int semantics, int device) {
+// The common part of hmf_create_batch and hmf_create_dag: volumes, the graph
+// (`build`), device, stream, state, kernel attributes and the flow plan.
+template <class BuildGraph>
+int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics, int device, BuildGraph build) {
   g_create_error.clear();
   if (!out) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
@@ -731,13 +915,15 @@ int hmf_create_batch(hmf_ctx** out, int n_volumes, const int* dims, const int* p
   c->geo.pitch = n_volumes == 1 ? V0.pitch : 0;
   c->geo.plane = V0.plane;
   c->geo.vol = c->total;
-  int rc = build_tree(c, parent, n_nodes);
+  int rc = build(c);
   if (rc) {
     g_create_error = c->err;
     delete c;
     return rc;
   }
-  c->alpha.assign(c->n, 1.0);
+  // a DAG vertex without AddSmoothnessScalar has alpha 0: the CUDA DAG class
+  // reads its scalar map with operator[] (vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:365)
+  c->alpha.assign(c->n, c->dag ? 0.0 : 1.0);
   // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=quad|scalar select
   // the simpler kernels (same results), for comparisons.
   if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0 || n_volumes > 1;
@@ -791,6 +977,30 @@ int hmf_create_batch(hmf_ctx** out, int n_volumes, const int* dims, const int* p
   return HMF_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int hmf_create_batch(hmf_ctx** out, int n_volumes, const int* dims, const int* parent, int n_nodes,
+                     int semantics, int device) {
+  return create_context(out, n_volumes, dims, semantics, device,
+                        [&](hmf_ctx* c) { return build_tree(c, parent, n_nodes); });
+}
+
+int hmf_create_dag(hmf_ctx** out, int vx, int vy, int vz, int n_nodes, int n_edges, const int* edge_parent,
+                   const int* edge_child, const float* edge_weight, int semantics, int device) {
+  if (semantics == HMF_SEMANTICS_REF_CPU) {
+    g_create_error = "REF_CPU semantics is not available for graphs: the reference CPU class reads past its "
+                     "flow buffers (vtkMaxFlowSegmentationUtilities.cxx:197-200)";
+    if (out) *out = nullptr;
+    return HMF_ERR_INVALID_ARGUMENT;
+  }
+  const int dims[3] = {vx, vy, vz};
+  return create_context(out, 1, dims, semantics, device, [&](hmf_ctx* c) {
+    return build_dag(c, n_nodes, n_edges, edge_parent, edge_child, edge_weight);
+  });
+}
+
 int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
                int device) {
   const int dims[3] = {vx, vy, vz};
@@ -810,6 +1020,7 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->d_fvol) cudaFree(c->d_fvol);
   if (c->d_items) cudaFree(c->d_items);
   if (c->d_tree) cudaFree(c->d_tree);
+  if (c->d_dag) cudaFree(c->d_dag);
   if (c->d_smooth_list) cudaFree(c->d_smooth_list);
   if (c->d_error) cudaFree(c->d_error);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -887,8 +1098,10 @@ int hmf_solve(hmf_ctx* c, void* stream) {
     if (rc) return rc;
   } else if (c->timing) {
     for (int it = 0; it < c->iterations; ++it) {
+      c->dag_last = c->dag && it == c->iterations - 1;
       rc = timed(c, 0, s, do_flow, it & 1);
       if (!rc) rc = timed(c, 1, s, do_tree, 0);
+      c->dag_last = false;
       if (rc) return rc;
     }
   } else {
@@ -897,13 +1110,22 @@ int hmf_solve(hmf_ctx* c, void* stream) {
       if (!rc) rc = capture(c, 1, &c->graph_one);
       if (rc) return rc;
     }
-    for (int it = 0; it + 1 < c->iterations; it += 2) {
+    // a DAG's last iteration runs fewer tasks: launched on its own
+    const int graphed = c->dag ? std::max(0, c->iterations - 1) : c->iterations;
+    for (int it = 0; it + 1 < graphed; it += 2) {
       CK(cudaGraphLaunch(c->graph_pair, s), "cudaGraphLaunch");
       c->launches += 4;
     }
-    if (c->iterations & 1) {
+    if (graphed & 1) {
       CK(cudaGraphLaunch(c->graph_one, s), "cudaGraphLaunch");
       c->launches += 2;
+    }
+    if (c->dag && c->iterations > 0) {
+      rc = launch_flow(c, graphed & 1, s);
+      c->dag_last = true;
+      if (!rc) rc = launch_tree(c, s);
+      c->dag_last = false;
+      if (rc) return rc;
     }
   }
   // final flows live in set (iterations & 1); nothing else depends on parity

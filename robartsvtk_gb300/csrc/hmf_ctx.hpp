@@ -31,6 +31,16 @@ struct hmf_ctx {
   std::vector<std::vector<int>> kids;
   std::vector<int> preorder, postorder, leaves;  // leaves in DFS pre-order
 
+  // directed acyclic graph (hmf_create_dag): edges in edge order; kids, leaves
+  // and preorder above then hold out-edge children, leaves and nodes in the
+  // rooted DAG's forward-iterator order, parent the first parent
+  bool dag = false;
+  std::vector<int> e_parent, e_child;
+  std::vector<float> e_weight;
+  bool e_weighted = false;
+  std::vector<std::vector<int>> in_e, out_e;
+  std::vector<float> n_parents, wkids;  // weighted parent count, weighted children
+
   // parameters (vtkHierarchicalMaxFlowSegmentation.cxx:57-59)
   int iterations = 100;
   float step = 0.1f;
@@ -48,6 +58,7 @@ struct hmf_ctx {
   size_t arena_bytes = 0;
   std::vector<float*> sink, label, div;
   std::vector<float*> fx[2], fy[2], fz[2];
+  std::vector<float*> inc;  // DAG: each non-root node's own source buffer
   // input staging
   char* staging = nullptr;
   size_t staging_bytes = 0;
@@ -58,6 +69,8 @@ struct hmf_ctx {
   int n_items = 0;
   int zchunk = 0;  // planes per window column (0: not planned yet)
   hmf::TreeTable* d_tree = nullptr;
+  hmf::DagTable* d_dag = nullptr;
+  bool dag_last = false;  // the next sweep is the last iteration's
   bool use_tma = true;  // flow_tma_kernel (else the shared-memory ring flow_kernel)
   int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
   const float** d_smooth_list = nullptr;
@@ -83,6 +96,7 @@ struct hmf_ctx {
   std::vector<hmf::FlowVolume> h_fvol;
   std::vector<hmf::FlowItem> h_items;
   hmf::TreeTable h_tree{};
+  hmf::DagTable h_dag{};
   std::vector<const float*> h_smooth_list;
 
   // the staged inputs of the last solve (per vertex; for hmf_get_energy)

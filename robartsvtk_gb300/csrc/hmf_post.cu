@@ -300,6 +300,7 @@ int hmf_get_vote(hmf_ctx* c, int* out, int where, void* stream) { return hmf_bat
 int hmf_batch_get_energy(hmf_ctx* c, int volume, double* f0, double* f, int n) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
   if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
+  if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the energy decomposition is defined for trees, not graphs");
   if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
   DeviceGuard dg(c->device);
   hmf::EnergyTable tab;

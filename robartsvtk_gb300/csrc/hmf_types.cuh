@@ -57,6 +57,34 @@ struct TreeEntry {
   float inv_kids;       // 1.0f / (kids + 1) for branches, 1.0f / kids for the root
 };
 
+// Directed acyclic graphs (hmf_create_dag; kernels in hmf_dag.cuh): nodes as
+// entries in the rooted DAG's forward-iterator order, the root at entry 0.
+constexpr int kMaxDagEdges = 256;
+
+struct DagEntry {
+  float* sink;        // the root: its source flow
+  float* inc;         // own source buffer (nullptr for the root)
+  float* label;       // nullptr for the root
+  const float* div;   // nullptr for the root
+  const float* data;  // leaves: data term
+  float k;            // branches: 1 / (weighted children + 1)
+  int leaf;
+  int first_in, n_in;    // in-edges (parents) in edge order
+  int first_out, n_out;  // out-edges (children) in edge order
+};
+
+struct DagTable {
+  int n;  // entries (the root included)
+  int n_leaves;
+  float cc, icc, shift;  // shift = 1 / (CC * the root's weighted children)
+  int leaves[kMaxVertices];  // entry indices, forward order
+  int in_parent[kMaxDagEdges];
+  float in_wup[kMaxDagEdges], in_wdown[kMaxDagEdges];
+  int out_child[kMaxDagEdges];
+  float out_w[kMaxDagEdges];
+  DagEntry e[kMaxVertices];
+};
+
 struct TreeTable {
   int n;
   int n_leaves;

@@ -19,7 +19,7 @@ from . import _capi
 from ._capi import HMF_DEVICE, HMF_HOST, HMF_SEMANTICS_REF_CPU, HMF_SEMANTICS_REF_CUDA, HMFError, check
 
 __all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError",
-           "vote", "decomposition_energy"]
+           "vote", "decomposition_energy", "DAGSolver", "DirectedAcyclicGraphMaxFlowSegmentation"]
 
 REF_CUDA = HMF_SEMANTICS_REF_CUDA
 REF_CPU = HMF_SEMANTICS_REF_CPU
@@ -420,6 +420,43 @@ def decomposition_energy(dims, parent, data, labels, smooth=None, stream=None):
     return f0.value, np.array(f[:], dtype=np.float64)
 
 
+class DAGSolver(HMFSolver):
+    """One solver context for a directed acyclic graph of labels (the problem
+    of vtkCudaDirectedAcyclicGraphMaxFlowSegmentation): `n_nodes` vertices,
+    `edges` = [(parent, child), ...] in edge order, optional positive
+    per-edge `weights`.  Leaves are numbered in the graph's forward-iterator
+    order (`leaves`).  A vertex without set_smoothness_scalar has alpha 0, as
+    in the reference class.  The vote works on it; the adjoint, the energy
+    decomposition and batches are for trees."""
+
+    def __init__(self, dims, n_nodes, edges, weights=None, device: int = 0):
+        self._lib = _capi.load()
+        self.dims = tuple(int(d) for d in dims)
+        self.nvox = self.dims[0] * self.dims[1] * self.dims[2]
+        self.edges = [(int(p), int(c)) for p, c in edges]
+        self.weights = None if weights is None else [float(w) for w in weights]
+        n_edges = len(self.edges)
+        if self.weights is not None and len(self.weights) != n_edges:
+            raise ValueError("one weight per edge")
+        ep = (ctypes.c_int * max(n_edges, 1))(*[p for p, _ in self.edges])
+        ec = (ctypes.c_int * max(n_edges, 1))(*[c for _, c in self.edges])
+        ew = (ctypes.c_float * n_edges)(*self.weights) if self.weights is not None else None
+        first_parent = [-1] * int(n_nodes)
+        for p, c in reversed(self.edges):
+            if 0 <= c < len(first_parent):
+                first_parent[c] = p
+        self.parent = first_parent
+        ctx = ctypes.c_void_p()
+        check(self._lib.hmf_create_dag(ctypes.byref(ctx), *self.dims, int(n_nodes), n_edges, ep, ec, ew,
+                                       REF_CUDA, int(device)))
+        self._ctx = ctx
+        self._keep: dict = {}
+        n = self._lib.hmf_leaf_order(self._ctx, None, 0)
+        buf = (ctypes.c_int * max(n, 1))()
+        self._lib.hmf_leaf_order(self._ctx, buf, n)
+        self.leaves = [buf[i] for i in range(n)]
+
+
 class HierarchicalMaxFlowSegmentation:
     """Filter-style API with the reference's method names.
 
@@ -552,6 +589,71 @@ class HierarchicalMaxFlowSegmentation:
                 if p < 0:
                     continue
                 sol.set_smoothness_scalar(v, self.SmoothnessScalars.get(v, 1.0))
+                sol.set_smoothness(v, self._smooth.get(v))
+            sol.set_params(self.NumberOfIterations, self.StepSize, self.CC)
+            sol.solve(stream)
+            self._outputs = {leaf: sol.labels(leaf, stream=stream) for leaf in sol.leaves}
+        except HMFError as e:
+            return self._report(str(e))
+        return 1
+
+
+class DirectedAcyclicGraphMaxFlowSegmentation(HierarchicalMaxFlowSegmentation):
+    """Filter-style API of vtkCudaDirectedAcyclicGraphMaxFlowSegmentation
+    (Common/vtkRobartsCommon/vtkDirectedAcyclicGraphMaxFlowSegmentation.h:52-123)
+    with the same stand-ins as HierarchicalMaxFlowSegmentation: the
+    vtkRootedDirectedAcyclicGraph is given as (n_nodes, edges, weights) to
+    SetStructure, images are arrays.  Vertices without AddSmoothnessScalar
+    get alpha 0 (the CUDA class reads its scalar map with operator[])."""
+
+    def __init__(self):
+        super().__init__(REF_CUDA)
+
+    def SetStructure(self, n_nodes, edges, weights=None):
+        self.Structure = (int(n_nodes), [(int(p), int(c)) for p, c in edges],
+                          None if weights is None else [float(w) for w in weights])
+
+    SetHierarchy = SetStructure
+
+    def _report(self, msg: str) -> int:
+        self._error = msg
+        print("ERROR: DirectedAcyclicGraphMaxFlowSegmentation: " + msg, file=sys.stderr)
+        return -1
+
+    # RequestData / CheckInputConsistancy (vtkDirectedAcyclicGraphMaxFlowSegmentation.cxx:387-527, :574-1032)
+    def Update(self, stream=None) -> int:
+        self._error = ""
+        if not self.Structure:
+            return self._report("Structure must be provided.")
+        shape = None
+        for image in list(self._data.values()) + list(self._smooth.values()):
+            s = self._shape(image)
+            if len(s) != 3:
+                return self._report("Data type must be FLOAT and only have one component.")
+            if shape is None:
+                shape = s
+            elif s != shape:
+                return self._report("Inconsistant object extent.")
+        if shape is None:
+            return self._report("Missing data prior for leaf node.")
+        dims = (shape[2], shape[1], shape[0])
+        n_nodes, edges, weights = self.Structure
+        try:
+            key = (dims, n_nodes, tuple(edges), None if weights is None else tuple(weights))
+            if self._solver is None or getattr(self._solver, "_key", None) != key:
+                if self._solver is not None:
+                    self._solver.close()
+                self._solver = DAGSolver(dims, n_nodes, edges, weights, self.Device)
+                self._solver._key = key
+            sol = self._solver
+            for leaf in sol.leaves:
+                if leaf not in self._data:
+                    return self._report("Missing data prior for leaf node.")
+                sol.set_data(leaf, self._data[leaf])
+            for v in range(n_nodes):
+                if sol.parent[v] < 0:
+                    continue
+                sol.set_smoothness_scalar(v, self.SmoothnessScalars.get(v, 0.0))
                 sol.set_smoothness(v, self._smooth.get(v))
             sol.set_params(self.NumberOfIterations, self.StepSize, self.CC)
             sol.solve(stream)
