@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
     ap.add_argument("--adjoint-size", type=int, default=128)
     ap.add_argument("--adjoint-iterations", type=int, default=300)
+    ap.add_argument("--no-dag", action="store_true", help="skip the DAG solver measurement")
+    ap.add_argument("--dag-size", type=int, default=256)
+    ap.add_argument("--dag-iterations", type=int, default=100)
+    ap.add_argument("--profile-dag", action="store_true",
+                    help="one DAG solve (--dag-size, --dag-iterations): the command ncu wraps")
     ap.add_argument("--profile", action="store_true",
                     help="two solves (one warm, one profiled) and nothing else: the command ncu wraps")
     ap.add_argument("--profile-post", action="store_true",
@@ -387,6 +392,8 @@ def run_ours(args):
         out["batched"] = bench_batched(args, stream)
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = bench_adjoint(args, stream)
+    if rank == 0 and not args.no_dag:
+        out["dag"] = bench_dag(args, stream, None if args.no_cpu_baseline else host_threads())
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
     if rank == 0:
@@ -434,6 +441,117 @@ def bench_post(w, solver, device_stream):
         res[name] = {"ms": t, "bytes": b, "achieved_gbs": gbs, "frac": gbs / peak}
     res["energy"]["note"] = "one call: the sums zeroed, one kernel, the 8-byte-per-vertex sums read back, a stream sync"
     return res
+
+
+def dag_workload(size, iterations):
+    """The 256^3 tree4 phantom (ellipsoids_tree4) solved as a rooted DAG: the
+    tree's edges in vertex order plus B2 -> L1, so leaf L1 has two parents
+    (unweighted: push-down weight 1/2 each).  Vertices 0 root, 1 B1, 2 L0,
+    3 L1, 4 B2, 5 L2, 6 L3; smoothness image shared, alpha 1 on every vertex."""
+    from robartsvtk_gb300 import synthetic
+
+    w = synthetic.ellipsoids_tree4(seed=0, size=size, iterations=iterations)
+    edges = [(p, v) for v, p in enumerate(w.parent) if p >= 0] + [(4, 3)]
+    return w, edges
+
+
+def bench_dag(args, device_stream, cpu_threads):
+    """DAG solver throughput (voxel.label.iterations/s, device-resident
+    inputs, CUDA events) and the per-voxel graph sweep's roofline.  Sweep
+    algorithmic bytes per voxel: 4(7N + L + 2) (sink, source, divergence and
+    label of each non-root node read; sink, label and source written; each
+    data term read; the root's source read and written)."""
+    import torch
+
+    from robartsvtk_gb300 import DAGSolver
+
+    w, edges = dag_workload(args.dag_size, args.dag_iterations)
+    n = len(w.parent)
+    N, L = n - 1, len(w.leaves)
+    S = torch.from_numpy(next(iter(w.smooth.values()))).cuda()
+    d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
+    s = DAGSolver(w.dims, n, edges)
+    for leaf, t in d.items():
+        s.set_data(leaf, t)
+    for v in range(1, n):
+        s.set_smoothness(v, S)
+        s.set_smoothness_scalar(v, 1.0)
+    s.set_params(w.iterations, w.step, w.cc)
+    s.solve(device_stream)
+    device_stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 2
+    e0.record(device_stream)
+    for _ in range(reps):
+        s.solve(device_stream)
+    e1.record(device_stream)
+    device_stream.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    s.set_timing(True)
+    s.solve(device_stream)
+    st = s.stats()
+    s.set_timing(False)
+    V = w.nvox
+    peak, _ = measured_peak_hbm()
+    sweep_b = 4.0 * V * (7 * N + L + 2)
+    flow_b = 44.0 * V * N
+    out = {"workload": "ellipsoids%d_tree4 as a DAG (+ edge B2->L1), %d iterations" % (args.dag_size, w.iterations),
+           "value": V * L * w.iterations / (ms / 1000.0), "unit": UNIT, "ms_per_solve": ms,
+           "launches": st["launches"],
+           "flow_kernel": {"avg_ms": st["flow_ms"], "bytes": flow_b, "achieved_gbs": flow_b / st["flow_ms"] / 1e6,
+                           "frac": flow_b / st["flow_ms"] / 1e6 / peak},
+           "dag_sweep_kernel": {"avg_ms": st["tree_ms"], "bytes": sweep_b,
+                                "achieved_gbs": sweep_b / st["tree_ms"] / 1e6,
+                                "frac": sweep_b / st["tree_ms"] / 1e6 / peak},
+           "dag_init_kernel_ms": st["init_ms"]}
+    s.close()
+    if cpu_threads:
+        out["cpu_baseline"] = cpu_dag_sample(w, edges, cpu_threads)
+    return out
+
+
+def cpu_dag_sample(w, edges, threads, iters=2):
+    """The DAG oracle (the same fixed task order, FP32, OpenMP) on the host
+    cores: the full volume for `iters` iterations, initialisation excluded.
+    The reference's own CPU DAG class is not a baseline: its flow magnitude
+    reads past its buffers."""
+    from oracle import oracle as O
+
+    n = len(w.parent)
+    alpha = {v: 1.0 for v in range(1, n)}
+
+    def run(k):
+        t0 = time.perf_counter()
+        O.dag_solve(w.dims, n, edges, w.data, None, w.smooth, alpha, k, w.step, w.cc, threads=threads)
+        return time.perf_counter() - t0
+
+    t = max(run(iters) - run(0), 1e-6)
+    return {"value": w.nvox * len(w.leaves) * iters / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "full %dx%dx%d volume, %d iterations (initialisation excluded)" % (*w.dims, iters)}
+
+
+def run_profile_dag(args):
+    import torch
+
+    from robartsvtk_gb300 import DAGSolver
+
+    w, edges = dag_workload(args.dag_size, args.dag_iterations)
+    n = len(w.parent)
+    s = DAGSolver(w.dims, n, edges)
+    keep = [torch.from_numpy(a).cuda() for a in w.data.values()]
+    for leaf, t in zip(w.data, keep):
+        s.set_data(leaf, t)
+    S = torch.from_numpy(next(iter(w.smooth.values()))).cuda()
+    for v in range(1, n):
+        s.set_smoothness(v, S)
+        s.set_smoothness_scalar(v, 1.0)
+    s.set_params(w.iterations, w.step, w.cc)
+    s.solve()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_dag": list(w.dims), "iterations": w.iterations, "launches": s.stats()["launches"]}))
+    s.close()
+    return 0
 
 
 def bench_batched(args, device_stream):
@@ -620,6 +738,8 @@ def main():
         return run_profile(args)
     if args.profile_post:
         return run_profile_post(args)
+    if args.profile_dag:
+        return run_profile_dag(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -501,6 +501,20 @@ int dag_grid(hmf_ctx* c, const void* kernel, size_t smem) {
 }
 
 int launch_dag_sweep(hmf_ctx* c, cudaStream_t s) {
+  if (!c->dag_simple) {
+    const int A = hmf::dag_bulk_arrays(c->n, (int)c->leaves.size());
+    const int vc = hmf::dag_bulk_chunk(A);
+    const int smem = hmf::dag_bulk_smem_bytes(A);
+    int per = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, hmf::dag_bulk_kernel, vc, smem) != cudaSuccess || per < 1)
+      per = 1;
+    const long long chunks = (c->geo.vol + vc - 1) / vc;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(chunks, (long long)c->sm_count * per));
+    hmf::dag_bulk_kernel<<<grid, vc, smem, s>>>(c->d_dag, c->geo.vol, c->dag_last ? 1 : 0, c->d_error);
+    CK(cudaGetLastError(), "dag_bulk_kernel launch");
+    ++c->launches;
+    return HMF_OK;
+  }
   const size_t smem = 4 * (size_t)c->n * hmf::kDagThreads * sizeof(float);
   hmf::dag_sweep_kernel<<<dag_grid(c, (const void*)hmf::dag_sweep_kernel, smem), hmf::kDagThreads, smem, s>>>(
       c->d_dag, c->geo.vol, c->dag_last ? 1 : 0);
@@ -789,6 +803,9 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::dag_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           4 * hmf::kMaxVertices * hmf::kDagThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(dag_sweep_kernel)");
+  CK(cudaFuncSetAttribute(hmf::dag_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          128 + hmf::kDagBulkSmemBudget),
+     "cudaFuncSetAttribute(dag_bulk_kernel)");
   CK(cudaFuncSetAttribute(hmf::dag_init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::kMaxVertices * hmf::kDagThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(dag_init_kernel)");
@@ -924,6 +941,7 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
   // a DAG vertex without AddSmoothnessScalar has alpha 0: the CUDA DAG class
   // reads its scalar map with operator[] (vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:365)
   c->alpha.assign(c->n, c->dag ? 0.0 : 1.0);
+  if (const char* e = std::getenv("HMF_DAG_KERNEL")) c->dag_simple = std::strcmp(e, "simple") == 0;
   // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=quad|scalar select
   // the simpler kernels (same results), for comparisons.
   if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0 || n_volumes > 1;

@@ -71,6 +71,7 @@ struct hmf_ctx {
   hmf::TreeTable* d_tree = nullptr;
   hmf::DagTable* d_dag = nullptr;
   bool dag_last = false;  // the next sweep is the last iteration's
+  bool dag_simple = false;  // dag_sweep_kernel instead of dag_bulk_kernel (HMF_DAG_KERNEL=simple)
   bool use_tma = true;  // flow_tma_kernel (else the shared-memory ring flow_kernel)
   int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
   const float** d_smooth_list = nullptr;

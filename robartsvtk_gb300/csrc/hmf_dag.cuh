@@ -23,10 +23,20 @@
 //
 // Entries are the nodes in the rooted DAG's forward-iterator order (level by
 // level from the root; vtkRootedDirectedAcyclicGraphForwardIterator.cxx:95-120),
-// the root at entry 0.  Each thread owns one voxel and keeps the nodes' values
-// in shared-memory columns [quantity][entry][thread].
+// the root at entry 0.
+//
+// dag_bulk_kernel (the default) streams the volume through shared memory:
+// a persistent CTA walks chunks of VC voxels, brings every array the sweep
+// reads (per non-root node sink, source, divergence, label; each leaf's data
+// term; the root's source) into one of two stages with one cp.async.bulk per
+// array, completed by an mbarrier, and each thread sweeps one voxel of the
+// staged chunk in place while the next chunk is in flight.  dag_sweep_kernel
+// is the same arithmetic reading global memory directly, each thread keeping
+// the nodes' values in shared-memory columns [quantity][entry][thread]
+// (HMF_DAG_KERNEL=simple).
 #pragma once
 
+#include "hmf_async.cuh"
 #include "hmf_types.cuh"
 
 namespace hmf {
@@ -151,6 +161,151 @@ __global__ void __launch_bounds__(kDagThreads)
       if (!last) E.inc[i] = C(e);
     }
   }
+}
+
+// Staged arrays of dag_bulk_kernel: non-root entry e >= 1 -> sink 4(e-1),
+// source 4(e-1)+1, divergence 4(e-1)+2, label 4(e-1)+3; leaf j's data term
+// 4(n-1)+j; the root's source 4(n-1)+n_leaves.
+__host__ __device__ inline int dag_bulk_arrays(int n, int n_leaves) { return 4 * (n - 1) + n_leaves + 1; }
+constexpr int kDagBulkStages = 2;
+constexpr int kDagBulkSmemBudget = 64 * 1024;  // both stages: three CTAs per SM
+
+// Chunk length (voxels, one per thread): the largest power of two <= 256
+// whose stages fit the budget (at least 32).
+__host__ __device__ inline int dag_bulk_chunk(int arrays) {
+  int vc = 256;
+  while (vc > 32 && kDagBulkStages * arrays * vc * 4 > kDagBulkSmemBudget) vc /= 2;
+  return vc;
+}
+
+__host__ __device__ inline int dag_bulk_smem_bytes(int arrays) {
+  return 128 + kDagBulkStages * arrays * dag_bulk_chunk(arrays) * 4;
+}
+
+__global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_vox, int last,
+                                int* __restrict__ error_flag) {
+  __shared__ DagTable T;
+  __shared__ int abort_cta;
+  __shared__ int leaf_slot[kMaxVertices];  // entry -> staged data slot
+  extern __shared__ __align__(128) unsigned char db_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(db_raw);  // [kDagBulkStages]
+  float* const stage0 = reinterpret_cast<float*>(db_raw + 128);
+  dag_copy_table(T, table);
+  if (threadIdx.x == 0) {
+    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    if (smem_addr(db_raw) & 15) {
+      abort_cta = 1;
+      if (error_flag) atomicOr(error_flag, 4);
+    }
+    for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (abort_cta) return;
+  const int n = T.n, nl = T.n_leaves;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) leaf_slot[e] = -1;
+  __syncthreads();
+  for (int j = threadIdx.x; j < nl; j += blockDim.x) leaf_slot[T.leaves[j]] = 4 * (n - 1) + j;
+  __syncthreads();
+  const int A = dag_bulk_arrays(n, nl);
+  const int VC = dag_bulk_chunk(A);
+  const int root_slot = 4 * (n - 1) + nl;
+  const long long nchunks = (n_vox + VC - 1) / VC;
+  const float cc = T.cc, icc = T.icc;
+
+  auto issue = [&](long long chunk, int s) {  // thread 0 only
+    const long long v0 = chunk * VC;
+    const unsigned bytes = (unsigned)(min((long long)VC, n_vox - v0) * 4);
+    float* dst = stage0 + (size_t)s * A * VC;
+    mbar_expect_tx(&bars[s], bytes * (unsigned)A);
+    for (int e = 1; e < n; ++e) {
+      const DagEntry& E = T.e[e];
+      float* d = dst + (size_t)(4 * (e - 1)) * VC;
+      bulk_load(d, E.sink + v0, bytes, &bars[s]);
+      bulk_load(d + VC, E.inc + v0, bytes, &bars[s]);
+      bulk_load(d + 2 * VC, E.div + v0, bytes, &bars[s]);
+      bulk_load(d + 3 * VC, E.label + v0, bytes, &bars[s]);
+    }
+    for (int j = 0; j < nl; ++j)
+      bulk_load(dst + (size_t)(4 * (n - 1) + j) * VC, T.e[T.leaves[j]].data + v0, bytes, &bars[s]);
+    bulk_load(dst + (size_t)root_slot * VC, T.e[0].sink + v0, bytes, &bars[s]);
+  };
+
+  bool timed_out = false;
+  int nissued[kDagBulkStages] = {0, 0};  // kept by thread 0
+  long long chunk = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  }
+  for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
+    const int s = j & 1;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    const long long v0 = chunk * VC;
+    const int len = (int)min((long long)VC, n_vox - v0);
+    const int q = threadIdx.x;
+    if (q < len) {
+      float* st = stage0 + (size_t)s * A * VC + q;
+      auto S = [&](int e) -> float& { return st[(e ? 4 * (e - 1) : root_slot) * VC]; };
+      auto C = [&](int e) -> float& { return st[(4 * (e - 1) + 1) * VC]; };
+      auto D = [&](int e) -> float& { return st[(4 * (e - 1) + 2) * VC]; };
+      auto U = [&](int e) -> float& { return st[(4 * (e - 1) + 3) * VC]; };
+      // (2)
+      S(0) = 1.0f * S(0) + T.shift;
+      for (int e = 1; e < n; ++e) {
+        const float c = C(e), d = D(e), u = U(e);
+        if (leaf_slot[e] >= 0) {
+          float v = (c - d) + u * icc;
+          const float cap = st[leaf_slot[e] * VC];
+          v = (v < 0.0f) ? 0.0f : v;
+          v = (v > cap) ? cap : v;
+          S(e) = v;
+          U(e) = __saturatef(u + cc * ((c - d) - v));
+        } else {
+          const float k = T.e[e].k;
+          S(e) = (1.0f - k) * S(e) + k * ((c - d) + u * icc);
+        }
+      }
+      if (!last) {
+        // (3) deepest first: every push into a node precedes its own
+        for (int e = n - 1; e >= 1; --e) {
+          const DagEntry& E = T.e[e];
+          const float sv = S(e), c = C(e), d = D(e), u = U(e);
+          const float pot = ((sv - c) + d) - u * icc;
+          for (int k = E.first_in; k < E.first_in + E.n_in; ++k) {
+            float& ps = S(T.in_parent[k]);
+            ps = ps + T.in_wup[k] * pot;
+          }
+          if (leaf_slot[e] < 0) U(e) = __saturatef(u + cc * ((c - d) - sv));
+        }
+        // (4)
+        for (int e = 1; e < n; ++e) {
+          const DagEntry& E = T.e[e];
+          float c = 0.0f;
+          for (int k = E.first_in; k < E.first_in + E.n_in; ++k) c = c + T.in_wdown[k] * S(T.in_parent[k]);
+          C(e) = c;
+        }
+      }
+      const long long i = v0 + q;
+      T.e[0].sink[i] = S(0);
+      for (int e = 1; e < n; ++e) {
+        const DagEntry& E = T.e[e];
+        E.sink[i] = S(e);
+        E.label[i] = U(e);
+        if (!last) E.inc[i] = C(e);
+      }
+    }
+    // The sweep wrote into stage s with ordinary stores; order them before
+    // the bulk copy that refills the stage (async proxy).
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+  }
+  if (timed_out && error_flag) atomicOr(error_flag, 2);
+  if (threadIdx.x == 0 && timed_out)
+    for (int s = 0; s < kDagBulkStages; ++s)
+      if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
 }
 
 }  // namespace hmf

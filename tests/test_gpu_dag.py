@@ -57,8 +57,18 @@ def assert_exact(g, o, what):
             what, v, np.abs(s - o["sink"][v]).max())
 
 
+@pytest.fixture(params=["bulk", "simple"])
+def dag_kernel(request, monkeypatch):
+    """The bulk-staged graph sweep (default) and the direct one."""
+    if request.param == "simple":
+        monkeypatch.setenv("HMF_DAG_KERNEL", "simple")
+    else:
+        monkeypatch.delenv("HMF_DAG_KERNEL", raising=False)
+    return request.param
+
+
 @pytest.mark.parametrize("name", sorted(DAG_CASES))
-def test_dag_matches_oracle_and_reference_kernels(name):
+def test_dag_matches_oracle_and_reference_kernels(name, dag_kernel):
     w = dag_problem(name)
     g = gpu_solve(w)
     assert_exact(g, oracle_solve(w), name)
@@ -82,12 +92,12 @@ DIAMOND = [(0, 1), (0, 2), (1, 3), (2, 3), (1, 4), (2, 5)]
 
 
 @pytest.mark.parametrize("dims", [(37, 29, 21), (61, 45, 37), (1, 7, 11), (55, 1, 9), (28, 27, 1), (5, 4, 3)])
-def test_dag_shapes(dims):
+def test_dag_shapes(dims, dag_kernel):
     w = random_dag(3, dims, 6, DIAMOND, iterations=17, smooth_nodes=(2, 3))
     assert_exact(gpu_solve(w), oracle_solve(w), str(dims))
 
 
-def test_dag_many_iterations_deep_graph_and_weights():
+def test_dag_many_iterations_deep_graph_and_weights(dag_kernel):
     # three levels, a skip edge from the root, a leaf with three parents
     edges = [(0, 1), (0, 2), (1, 3), (2, 3), (1, 4), (3, 5), (3, 6), (4, 6), (2, 6), (0, 7), (4, 8)]
     weights = [1.0, 0.5, 0.7, 1.3, 1.0, 0.9, 0.4, 0.8, 1.1, 2.0, 0.6]
@@ -110,7 +120,7 @@ def test_dag_timing_path_and_device_inputs_agree():
 
 
 @pytest.mark.parametrize("iterations", [0, 1, 2])
-def test_dag_few_iterations(iterations):
+def test_dag_few_iterations(iterations, dag_kernel):
     w = random_dag(9, (13, 11, 7), 6, DIAMOND, iterations=iterations, smooth_nodes=(4,))
     assert_exact(gpu_solve(w), oracle_solve(w), "T=%d" % iterations)
 
