@@ -224,6 +224,41 @@ int hmf_decomposition_energy(int vx, int vy, int vz, const int* parent, int n_no
 int hmf_get_energy(hmf_ctx* ctx, double* f0, double* f, int n);
 int hmf_batch_get_energy(hmf_ctx* ctx, int volume, double* f0, double* f, int n);
 
+/* Data term of vtkImageDataTerm (Common/vtkRobartsCommon/vtkImageDataTerm.cxx:62-470),
+ * per voxel of float32 images in1 (and optionally in2, same size):
+ *   HMF_DATA_TERM_CONSTANT  C1                       (entropy: -log C1)
+ *   HMF_DATA_TERM_LOGISTIC  1/(1+e^-(K1(x1-C1))) [x 1/(1+e^-(K2(x2-C2)))]   (entropy: -log of it)
+ *   HMF_DATA_TERM_GAUSSIAN  e^-(((x1-C1)/K1)^2/2 [+ ((x2-C2)/K2)^2/2])        (entropy: the exponent)
+ *   HMF_DATA_TERM_SPIKE     x1 == K1 ? C1 : C2, one image only
+ * in the reference's double arithmetic and its constant handling (one
+ * image: the spike's second value is C1 unless entropy takes logarithms;
+ * two images: no normalisation).  normalize rescales one-image results by
+ * in1's range as the reference does.  The numeric codes are the reference's
+ * VTK_CONSTANT .. VTK_SPIKE; note that its SetOperationToGaussian selects
+ * VTK_SPIKE and SetOperationToSpike VTK_GAUSSIAN (vtkImageDataTerm.h).
+ * Synchronous for host buffers.  Returns a status. */
+#define HMF_DATA_TERM_CONSTANT 0
+#define HMF_DATA_TERM_LOGISTIC 1
+#define HMF_DATA_TERM_GAUSSIAN 2
+#define HMF_DATA_TERM_SPIKE 3
+int hmf_data_term(int op, int entropy, int normalize, double k1, double c1, double k2, double c2, const float* in1,
+                  const float* in2, long long n_voxels, float* out, int where, void* stream);
+
+/* Maximum-likelihood data term of vtkImageLogLikelihood
+ * (Common/vtkRobartsCommon/vtkImageLogLikelihood.cxx:140-250): voxels where
+ * at least required_agreement of the non-NULL int32 label maps equal
+ * label_id are the seeds; a histogram of the float32 image (1 or 2
+ * interleaved components) over the seeds with bins of `resolution`; per voxel
+ * -log(bin frequency + 1e-10), -log(1e-10) outside the histogram, divided by
+ * -log(1e-10) if normalize; 1 everywhere without seeds.  The bin count is the
+ * reference's (int)(max - min/resolution) + 1; inputs whose seeds would fall
+ * past it (where the reference writes out of bounds) are rejected.
+ * Synchronous.  Returns a status. */
+#define HMF_MAX_LABEL_MAPS 32
+int hmf_log_likelihood(const float* image, int components, const int* const* label_maps, int n_label_maps,
+                       long long n_voxels, int label_id, float resolution, double required_agreement, int normalize,
+                       float* out, int where, void* stream);
+
 /* Message of the last failed call on ctx (or, when ctx is NULL, of the last
  * failed hmf_create or hmf_solve_noalloc on this thread). */
 const char* hmf_last_error(const hmf_ctx* ctx);

@@ -11,5 +11,8 @@ from .segmentation import (REF_CPU, REF_CUDA, DAGSolver, DirectedAcyclicGraphMax
                            HierarchicalMaxFlowSegmentation, HMFBatchSolver, HMFError, HMFSolver,
                            decomposition_energy, vote)
 
+from .dataterm import ImageDataTerm, ImageLogLikelihood, data_term, log_likelihood  # noqa: F401
+
 __all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError",
-           "vote", "decomposition_energy", "DAGSolver", "DirectedAcyclicGraphMaxFlowSegmentation"]
+           "vote", "decomposition_energy", "DAGSolver", "DirectedAcyclicGraphMaxFlowSegmentation",
+           "data_term", "log_likelihood", "ImageDataTerm", "ImageLogLikelihood"]

@@ -45,6 +45,10 @@ SIGNATURES = [
     ("hmf_get_stats", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_last_error", ctypes.c_char_p, [_P]),
     ("hmf_create_batch", _I, [ctypes.POINTER(_P), _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _I, _I, _I]),
+    ("hmf_data_term", _I, [_I, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, _P,
+                           ctypes.c_longlong, _P, _I, _P]),
+    ("hmf_log_likelihood", _I, [_P, _I, ctypes.POINTER(_P), _I, ctypes.c_longlong, _I, ctypes.c_float,
+                                ctypes.c_double, _I, _P, _I, _P]),
     ("hmf_create_dag", _I, [ctypes.POINTER(_P), _I, _I, _I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I),
                             ctypes.POINTER(ctypes.c_float), _I, _I]),
     ("hmf_num_volumes", _I, [_P]),
