@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--adjoint-size", type=int, default=128)
     ap.add_argument("--adjoint-iterations", type=int, default=300)
     ap.add_argument("--no-dag", action="store_true", help="skip the DAG solver measurement")
+    ap.add_argument("--no-dataterm", action="store_true", help="skip the data-term producer measurement")
     ap.add_argument("--dag-size", type=int, default=256)
     ap.add_argument("--dag-iterations", type=int, default=100)
     ap.add_argument("--profile-dag", action="store_true",
@@ -392,6 +393,8 @@ def run_ours(args):
         out["batched"] = bench_batched(args, stream)
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = bench_adjoint(args, stream)
+    if rank == 0 and not args.no_dataterm:
+        out["dataterm"] = bench_dataterm(args, stream)
     if rank == 0 and not args.no_dag:
         out["dag"] = bench_dag(args, stream, None if args.no_cpu_baseline else host_threads())
     if rank == 0 and not args.no_cpu_baseline:
@@ -441,6 +444,54 @@ def bench_post(w, solver, device_stream):
         res[name] = {"ms": t, "bytes": b, "achieved_gbs": gbs, "frac": gbs / peak}
     res["energy"]["note"] = "one call: the sums zeroed, one kernel, the 8-byte-per-vertex sums read back, a stream sync"
     return res
+
+
+def bench_dataterm(args, device_stream):
+    """The data-term producers on the 256^3 phantom image, device-resident:
+    a Gaussian entropy cost of one image, normalised (hmf_data_term; bytes 8V:
+    one float read, one written, plus one read for the range), and the
+    log-likelihood cost from 4 int32 label maps (hmf_log_likelihood; bytes
+    4V(3 + 2*4): the maps and the image read in the seed scan and the
+    histogram pass, the image read and the cost written in the last pass).
+    CUDA events, the best of 3 calls."""
+    import torch
+
+    from robartsvtk_gb300 import data_term, log_likelihood
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    n = args.size
+    img = (torch.rand((n, n, n), generator=g, device="cuda") * 200.0).floor()
+    maps = [(torch.rand((n, n, n), generator=g, device="cuda") < 0.3).to(torch.int32) for _ in range(4)]
+    peak, _ = measured_peak_hbm()
+    V = n ** 3
+
+    def best(fn):
+        fn()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return min(times)
+
+    out = torch.empty_like(img)
+    t_dt = best(lambda: data_term(2, img, k1=20.0, c1=100.0, entropy=True, normalize=True, out=out))
+    t_ll = best(lambda: log_likelihood(img, maps, label_id=1, resolution=1.0, required_agreement=0.5, out=out))
+    b_dt = 12.0 * V
+    b_ll = 4.0 * V * (3 + 2 * 4)
+    return {"workload": "%d^3 float image, 4 int32 label maps" % n,
+            "data_term_gaussian_entropy_normalised": {"ms": t_dt, "bytes": b_dt, "achieved_gbs": b_dt / t_dt / 1e6,
+                                                      "frac": b_dt / t_dt / 1e6 / peak,
+                                                      "note": "double-precision exp/log as the reference computes"},
+            "log_likelihood": {"ms": t_ll, "bytes": b_ll, "achieved_gbs": b_ll / t_ll / 1e6,
+                               "frac": b_ll / t_ll / 1e6 / peak,
+                               "note": "three passes with two host synchronisations (range, histogram size)"}}
 
 
 def dag_workload(size, iterations):
