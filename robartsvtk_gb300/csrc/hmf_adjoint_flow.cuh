@@ -17,7 +17,10 @@
 // k-2 and the old-flow adjoints on k-3 (two __syncthreads per plane).  Input
 // planes arrive by cp.async.bulk.tensor into mbarrier rings two planes ahead;
 // one thread waits for them, before a barrier; every wait is bounded and a
-// time-out sets the error flag.
+// time-out sets the error flag.  The plane copies are spread over the
+// warps' first lanes (one array each, one mbarrier arrival per array), and
+// the steady planes of the march -- every stage active, no z boundary near --
+// run a copy of the step compiled without those tests.
 #pragma once
 
 #include <cuda.h>
@@ -135,7 +138,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       abort_cta = 1;
       if (fp.error_flag) atomicOr(fp.error_flag, 4);
     }
-    for (int s = 0; s < kAfMainSlots; ++s) mbar_init(&mbars[s], 1);
+    for (int s = 0; s < kAfMainSlots; ++s) mbar_init(&mbars[s], (unsigned)narr);
     for (int s = 0; s < kAfPzSlots; ++s) mbar_init(&zbars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -148,23 +151,18 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
 
   auto mslot = [&](int p) { return mslots + ((p - kstart) % kAfMainSlots) * (kAfMainArrays * kAfPlane); };
   auto zslot = [&](int p) { return zslots + ((p - kstart) % kAfPzSlots) * kAfPlane; };
-  auto issue_main = [&](int p) {  // thread 0 only
-    uint64_t* bar = &mbars[(p - kstart) % kAfMainSlots];
-    float* dst = mslot(p);
-    mbar_expect_tx(bar, (unsigned)(narr * kAfBoxX * kAfBoxY * 4));
-    const int yy = y0 - 3;
-    tma_load_plane(dst + 0 * kAfPlane, &V->px, xs, yy, p, bar);
-    tma_load_plane(dst + 1 * kAfPlane, &V->py, xs, yy, p, bar);
-    tma_load_plane(dst + 2 * kAfPlane, &V->s, xs, yy, p, bar);
-    tma_load_plane(dst + 3 * kAfPlane, &V->c, xs, yy, p, bar);
-    tma_load_plane(dst + 4 * kAfPlane, &V->u, xs, yy, p, bar);
-    tma_load_plane(dst + 5 * kAfPlane, &V->pb[par][0], xs, yy, p, bar);
-    tma_load_plane(dst + 6 * kAfPlane, &V->pb[par][1], xs, yy, p, bar);
-    tma_load_plane(dst + 7 * kAfPlane, &V->pb[par][2], xs, yy, p, bar);
-    tma_load_plane(dst + 8 * kAfPlane, &V->dbp, xs, yy, p, bar);
-    if (has_s) tma_load_plane(dst + 9 * kAfPlane, &V->smooth, xs, yy, p, bar);
+  // Array a of plane p into the main ring (px, py, s, c, u, Pb x/y/z, dbp, S):
+  // one thread per array, each with its own expect_tx.
+  auto main_map = [&](int a) -> const CUtensorMap* {
+    return a < 5 ? &V->px + (a < 2 ? a : a + 1) : a < 8 ? &V->pb[par][a - 5] : a == 8 ? &V->dbp : &V->smooth;
   };
-  auto issue_pz = [&](int p) {  // thread 0 only
+  auto issue_main_array = [&](int p, int a, const CUtensorMap* map) {
+    uint64_t* bar = &mbars[(p - kstart) % kAfMainSlots];
+    mbar_expect_tx(bar, (unsigned)(kAfBoxX * kAfBoxY * 4));
+    tma_load_plane(mslot(p) + a * kAfPlane, map, xs, y0 - 3, p, bar);
+  };
+  const CUtensorMap* const warp_map = main_map(warp < narr ? warp : 0);
+  auto issue_pz = [&](int p) {  // one thread
     uint64_t* bar = &zbars[(p - kstart) % kAfPzSlots];
     mbar_expect_tx(bar, (unsigned)(kAfBoxX * kAfBoxY * 4));
     tma_load_plane(zslot(p), &V->pz, xs, y0 - 3, p, bar);
@@ -184,7 +182,8 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     wait0(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1));
   };
   if (threadIdx.x == 0) {
-    for (int p = kstart; p <= min(kstart + 1, kA_end); ++p) issue_main(p);
+    for (int p = kstart; p <= min(kstart + 1, kA_end); ++p)
+      for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
     for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
     wait_main0(kstart);
     wait_pz0(kstart);
@@ -222,14 +221,16 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     long long go = (long long)(kstart - 2) * G.plane;  // plane offset of gb outputs (plane k-2)
     long long fo = (long long)(kstart - 3) * G.plane;  // ... of old-flow outputs (plane k-3)
 
-    for (int k = kstart; k <= kend; ++k) {
-      const bool doA = k <= kA_end;
+    // returns false when the march stops (a copy wait ran out)
+    auto zstep = [&](const int k, auto stag) -> bool {
+      constexpr bool ST = decltype(stag)::value;  // a steady plane: every stage, no z boundary near
+      const bool doA = ST || k <= kA_end;
       const int kc = k - 1;
-      const bool doC = kc >= kstart && kc <= min(ze, G.vz - 1);
+      const bool doC = ST || (kc >= kstart && kc <= min(ze, G.vz - 1));
       const int ko = k - 2;
-      const bool doE = ko >= kstart && ko <= ze - 1;
+      const bool doE = ST || (ko >= kstart && ko <= ze - 1);
       const int kf = k - 3;
-      const bool doF = kf >= zs && kf < ze;
+      const bool doF = ST || (kf >= zs && kf < ze);
       const int kb = k & 1;  // exchange-row parity of plane k
 
       // ---- stage A: g(k) (kern_CalcGradStep on the recomputed divergence)
@@ -239,7 +240,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       for (int j = 0; j < kAfR; ++j)
         g[j] = px[j] = py[j] = pz[j] = Pbx[j] = Pby[j] = Pbz[j] = dbp[j] = dbpl[j] = dbpu[j] = Sk[j] = 0.f;
       if (doA) {
-        const bool has_next = k + 1 < G.vz;
+        const bool has_next = ST || k + 1 < G.vz;
         const int znext = zsi + 1 == kAfPzSlots ? 0 : zsi + 1;
         const float* zn = zslots + znext * kAfPlane;
 #pragma unroll
@@ -247,7 +248,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
           const int e = si[j];
           px[j] = cur[e];
           py[j] = cur[kAfPlane + e];
-          pz[j] = have_pz ? pzn_c[j] : zc[e];
+          pz[j] = (ST || have_pz) ? pzn_c[j] : zc[e];
           const float pxr = cur[e + 1];
           const float pyd = cur[kAfPlane + e + kAfBoxX];
           const float pzn = has_next ? zn[e] : 0.f;
@@ -271,9 +272,9 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       }
       XG_L[xw] = g[kAfR - 1];
       __syncthreads();  // (1)
-      if (threadIdx.x == 0) {
-        if (k + 2 <= kA_end) issue_main(k + 2);
-        if (k + 3 <= kpz_end) issue_pz(k + 3);
+      if (lane == 0) {
+        if (warp < narr && k + 2 <= kA_end) issue_main_array(k + 2, warp, warp_map);
+        if (warp == kAfWarps - 1 && k + 3 <= kpz_end) issue_pz(k + 3);
       }
 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow) and the total adjoint t(k)
@@ -289,10 +290,10 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
           const bool vyp = INT || ypos[j];
           ppx_n[j] = (vin && vxpos) ? px[j] - (g[j] - gxm) : 0.f;
           ppy_n[j] = (vin && vyp) ? py[j] - (g[j] - gym) : 0.f;
-          ppz_n[j] = (vin && k > 0) ? pz[j] - (g[j] - gprev[j]) : 0.f;
+          ppz_n[j] = (vin && (ST || k > 0)) ? pz[j] - (g[j] - gprev[j]) : 0.f;
           tx_n[j] = vin ? (Pbx[j] + dbp[j]) - (vxpos ? dbpl[j] : 0.f) : 0.f;
           ty_n[j] = vin ? (Pby[j] + dbp[j]) - (vyp ? dbpu[j] : 0.f) : 0.f;
-          tz_n[j] = vin ? (Pbz[j] + dbp[j]) - (k > 0 ? dbp_prev[j] : 0.f) : 0.f;
+          tz_n[j] = vin ? (Pbz[j] + dbp[j]) - ((ST || k > 0) ? dbp_prev[j] : 0.f) : 0.f;
           if (doA) {
             gprev[j] = g[j];
             dbp_prev[j] = dbp[j];
@@ -307,7 +308,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       {
         const float pdown = XPPY_F[(kb ^ 1) * kAfX + xw + 32];
         const float tdown = XTY_F[(kb ^ 1) * kAfX + xw + 32];
-        const bool znl = kc != G.vz - 1;
+        const bool znl = ST || kc != G.vz - 1;
 #pragma unroll
         for (int j = 0; j < kAfR; ++j) {
           const float pxr = __shfl_down_sync(FULL, ppx_c[j], 1);
@@ -337,11 +338,11 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
                 if (vxnl) mb = mb + (txr * 0.5f) * pxr;
                 if (vyp) mb = mb + (ty_c[j] * 0.5f) * ppy_c[j];
                 if (vyn) mb = mb + (tyd * 0.5f) * pyd;
-                if (kc > 0) mb = mb + (tz_c[j] * 0.5f) * ppz_c[j];
+                if (ST || kc > 0) mb = mb + (tz_c[j] * 0.5f) * ppz_c[j];
                 if (znl) mb = mb + (tz_n[j] * 0.5f) * ppz_n[j];
                 m[j] = lim / Fm;
                 f2b[j] = -mb * lim / (4.0f * Fm * Fm * Fm);
-                if (rown[j] && kc >= zs && kc < ze) asum += (double)(mb / Fm * (has_s ? S_c[j] : 1.0f));
+                if (rown[j] && (ST || kc >= zs) && kc < ze) asum += (double)(mb / Fm * (has_s ? S_c[j] : 1.0f));
               }
             }
           }
@@ -354,7 +355,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
         if (k + 2 < G.vz && k + 2 <= kpz_end) wait_pz0(k + 2);
       }
       __syncthreads();  // (2)
-      if (stop) break;
+      if (stop) return false;
 
       // ---- stage D: q(k-1), the adjoint of p'
       float qx_n[kAfR], qy_n[kAfR], qz_n[kAfR];
@@ -370,7 +371,8 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
           if (doC && (INT || rin[j])) {
             qx_n[j] = vxpos ? (tx_c[j] * 0.5f) * (m[j] + mxm) + (2.0f * ppx_c[j]) * (f2b[j] + fxm) : 0.f;
             qy_n[j] = (INT || ypos[j]) ? (ty_c[j] * 0.5f) * (m[j] + mym) + (2.0f * ppy_c[j]) * (f2b[j] + fym) : 0.f;
-            qz_n[j] = kc > 0 ? (tz_c[j] * 0.5f) * (m[j] + m_prev[j]) + (2.0f * ppz_c[j]) * (f2b[j] + f_prev[j]) : 0.f;
+            qz_n[j] = (ST || kc > 0) ? (tz_c[j] * 0.5f) * (m[j] + m_prev[j]) + (2.0f * ppz_c[j]) * (f2b[j] + f_prev[j])
+                                      : 0.f;
           }
           if (doC) {
             m_prev[j] = m[j];
@@ -393,9 +395,9 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
             float gb = -((qx_e[j] + qy_e[j]) + qz_e[j]);
             if (vxnl) gb = gb + qxr;
             if (INT || ynl[j]) gb = gb + qyd;
-            if (ko != G.vz - 1) gb = gb + qz_n[j];
+            if (ST || ko != G.vz - 1) gb = gb + qz_n[j];
             dbo[j] = step * gb;
-            if (rown[j] && ko >= zs) ogb[go + rowoff[j]] = gb;
+            if (rown[j] && (ST || ko >= zs)) ogb[go + rowoff[j]] = gb;
           }
         }
         XD_L[kb * kAfX + xw] = dbo[kAfR - 1];  // plane k-2
@@ -412,7 +414,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
             const long long o = fo + rowoff[j];
             ox[o] = (qx_f[j] + dbo_f[j]) - (vxpos ? dxl : 0.f);
             oy[o] = (qy_f[j] + dbo_f[j]) - ((INT || ypos[j]) ? dyu : 0.f);
-            oz[o] = (qz_f[j] + dbo_f[j]) - (kf > 0 ? dbo_ff[j] : 0.f);
+            oz[o] = (qz_f[j] + dbo_f[j]) - ((ST || kf > 0) ? dbo_ff[j] : 0.f);
           }
         }
       }
@@ -442,7 +444,14 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       zc = zslots + zsi * kAfPlane;
       go += G.plane;
       fo += G.plane;
-    }
+      return true;
+    };
+    const int k_lo = zs + 4, k_hi = min(ze + 1, G.vz - 2);
+    int k = kstart;
+    bool go_on = true;
+    for (; go_on && k <= kend && k < k_lo; ++k) go_on = zstep(k, BoolTag<false>{});
+    for (; go_on && k <= k_hi; ++k) go_on = zstep(k, BoolTag<true>{});
+    for (; go_on && k <= kend; ++k) go_on = zstep(k, BoolTag<false>{});
   };
   if (interior) march(BoolTag<true>{});
   else march(BoolTag<false>{});
