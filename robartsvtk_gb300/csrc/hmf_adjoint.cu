@@ -192,8 +192,10 @@ float* pb_array(const AdjointState* S, const hmf_ctx* c, int parity, int v, int 
 }
 
 // Windows of at most 27 x 27 outputs spread evenly over the volume; z chunk:
-// the longest power of two (16 .. 64) that still gives two waves of one CTA
-// per SM.
+// the one that minimises waves x planes marched per CTA, with one CTA per SM
+// and the five halo planes the reverse chain reaches (3 low, 2 high) -- the
+// work of a wave is set by its longest CTA, so a last, partial wave costs as
+// much as a full one.
 int plan_reverse(hmf_ctx* c, cudaStream_t s) {
   AdjointState* S = c->adj;
   const auto& V = c->vols[0];
@@ -204,9 +206,17 @@ int plan_reverse(hmf_ctx* c, cudaStream_t s) {
   F.out_x = (V.vx + nx - 1) / nx;
   F.out_y = (V.vy + ny - 1) / ny;
   F.tiles_x = nx;
-  int z = 64;
-  while (z > 16 && (long long)nx * ny * ((V.vz + z - 1) / z) * (c->n - 1) < 2LL * c->sm_count) z /= 2;
-  F.zchunk = std::min(z, V.vz);
+  const long long per_chunk = (long long)nx * ny * (c->n - 1);
+  const int slots = std::max(1, c->sm_count);
+  int best_z = V.vz;
+  double best = 1e300;
+  for (int z = V.vz; z >= 4; --z) {
+    const long long chunks = (V.vz + z - 1) / z;
+    const long long waves = (per_chunk * chunks + slots - 1) / slots;
+    const double cost = (double)waves * (double)(z + 5);
+    if (cost < best) best = cost, best_z = z;
+  }
+  F.zchunk = std::min(best_z, V.vz);
   const int chunks = (V.vz + F.zchunk - 1) / F.zchunk;
   S->h_aitems.clear();
   for (int zc = 0; zc < chunks; ++zc)
