@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--no-dataterm", action="store_true", help="skip the data-term producer measurement")
     ap.add_argument("--dag-size", type=int, default=256)
     ap.add_argument("--dag-iterations", type=int, default=100)
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="two adjoint solves (--adjoint-size, --adjoint-iterations, every state kept): "
+                         "the command ncu wraps")
     ap.add_argument("--profile-dag", action="store_true",
                     help="one DAG solve (--dag-size, --dag-iterations): the command ncu wraps")
     ap.add_argument("--profile", action="store_true",
@@ -582,6 +585,28 @@ def cpu_dag_sample(w, edges, threads, iters=2):
             "sample": "full %dx%dx%d volume, %d iterations (initialisation excluded)" % (*w.dims, iters)}
 
 
+def run_profile_adjoint(args):
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver, synthetic
+
+    w = synthetic.ellipsoids_flat4(seed=3, size=args.adjoint_size, iterations=args.adjoint_iterations)
+    d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
+    truth = torch.from_numpy(w.truth.astype("int32")).cuda()
+    s = HMFSolver(w.dims, w.parent)
+    for leaf, t in d.items():
+        s.set_data(leaf, t)
+    for v, a in w.alpha.items():
+        s.set_smoothness_scalar(v, a)
+    s.set_params(w.iterations, w.step, w.cc)
+    losses = [s.solve_adjoint(truth) for _ in range(2)]
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_adjoint": list(w.dims), "iterations": w.iterations, "loss": losses[-1],
+                      "plan": s.adjoint_plan()}))
+    s.close()
+    return 0
+
+
 def run_profile_dag(args):
     import torch
 
@@ -791,6 +816,8 @@ def main():
         return run_profile_post(args)
     if args.profile_dag:
         return run_profile_dag(args)
+    if args.profile_adjoint:
+        return run_profile_adjoint(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
