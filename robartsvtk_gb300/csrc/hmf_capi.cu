@@ -501,6 +501,29 @@ int dag_grid(hmf_ctx* c, const void* kernel, size_t smem) {
 }
 
 int launch_dag_sweep(hmf_ctx* c, cudaStream_t s) {
+  if (!c->dag_simple && !c->dag_generic && c->dag_reg_ok) {
+    const int smem = hmf::dag_bulk_n_smem_bytes(c->n);
+    const long long chunks = (c->geo.vol + hmf::kDagNVc - 1) / hmf::kDagNVc;
+    auto launch = [&](auto kernel) {
+      int per = 1;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, hmf::kDagNVc, smem) != cudaSuccess || per < 1)
+        per = 1;
+      const int grid = (int)std::max<long long>(1, std::min<long long>(chunks, (long long)c->sm_count * per));
+      kernel<<<grid, hmf::kDagNVc, smem, s>>>(c->h_dagreg, c->geo.vol, c->dag_last ? 1 : 0, c->d_error);
+    };
+    switch (c->n) {
+      case 2: launch(hmf::dag_bulk_n_kernel<2>); break;
+      case 3: launch(hmf::dag_bulk_n_kernel<3>); break;
+      case 4: launch(hmf::dag_bulk_n_kernel<4>); break;
+      case 5: launch(hmf::dag_bulk_n_kernel<5>); break;
+      case 6: launch(hmf::dag_bulk_n_kernel<6>); break;
+      case 7: launch(hmf::dag_bulk_n_kernel<7>); break;
+      default: launch(hmf::dag_bulk_n_kernel<8>); break;
+    }
+    CK(cudaGetLastError(), "dag_bulk_n_kernel launch");
+    ++c->launches;
+    return HMF_OK;
+  }
   if (!c->dag_simple) {
     const int A = hmf::dag_bulk_arrays(c->n, (int)c->leaves.size());
     const int vc = hmf::dag_bulk_chunk(A);
@@ -640,6 +663,33 @@ int prepare_dag_table(hmf_ctx* c, cudaStream_t s, const Staged& in) {
     E.n_out = pout - E.first_out;
   }
   CK(cudaMemcpyAsync(c->d_dag, &T, sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(graph table)");
+  // the same graph as kernel parameters of dag_bulk_n_kernel (small graphs
+  // whose edges are all distinct)
+  hmf::DagRegParams& R = c->h_dagreg;
+  std::memset(&R, 0, sizeof(R));
+  c->dag_reg_ok = c->n <= hmf::kDagRegMax;
+  for (int i = 0; i < c->n && c->dag_reg_ok; ++i) {
+    const hmf::DagEntry& E = T.e[i];
+    R.sink[i] = E.sink;
+    R.inc[i] = E.inc;
+    R.label[i] = E.label;
+    R.div[i] = E.div;
+    R.data[i] = E.data;
+    R.k[i] = E.k;
+    if (E.leaf) R.leaf_mask |= 1u << i;
+    R.n_in[i] = E.n_in;
+    for (int j = 0; j < E.n_in; ++j) {
+      const int p = T.in_parent[E.first_in + j];
+      if ((R.pmask[i] >> p) & 1u) c->dag_reg_ok = false;  // a repeated edge
+      R.pmask[i] |= 1u << p;
+      R.wup[i][p] = T.in_wup[E.first_in + j];
+      R.wdown_ord[i][j] = T.in_wdown[E.first_in + j];
+      R.parent_ord[i][j] = p;
+    }
+  }
+  R.cc = T.cc;
+  R.icc = T.icc;
+  R.shift = T.shift;
   return HMF_OK;
 }
 
@@ -803,6 +853,13 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::dag_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           4 * hmf::kMaxVertices * hmf::kDagThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(dag_sweep_kernel)");
+#define HMF_DAG_N_ATTR(N)                                                                    \
+  CK(cudaFuncSetAttribute(hmf::dag_bulk_n_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                          hmf::dag_bulk_n_smem_bytes(N)),                                    \
+     "cudaFuncSetAttribute(dag_bulk_n_kernel)");
+  HMF_DAG_N_ATTR(2) HMF_DAG_N_ATTR(3) HMF_DAG_N_ATTR(4) HMF_DAG_N_ATTR(5) HMF_DAG_N_ATTR(6)
+  HMF_DAG_N_ATTR(7) HMF_DAG_N_ATTR(8)
+#undef HMF_DAG_N_ATTR
   CK(cudaFuncSetAttribute(hmf::dag_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           128 + hmf::kDagBulkSmemBudget),
      "cudaFuncSetAttribute(dag_bulk_kernel)");
@@ -941,7 +998,10 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
   // a DAG vertex without AddSmoothnessScalar has alpha 0: the CUDA DAG class
   // reads its scalar map with operator[] (vtkCudaDirectedAcyclicGraphMaxFlowSegmentation.cxx:365)
   c->alpha.assign(c->n, c->dag ? 0.0 : 1.0);
-  if (const char* e = std::getenv("HMF_DAG_KERNEL")) c->dag_simple = std::strcmp(e, "simple") == 0;
+  if (const char* e = std::getenv("HMF_DAG_KERNEL")) {
+    c->dag_simple = std::strcmp(e, "simple") == 0;
+    c->dag_generic = std::strcmp(e, "generic") == 0;
+  }
   // Kernel selection.  HMF_FLOW_KERNEL=ring / HMF_TREE_KERNEL=quad|scalar select
   // the simpler kernels (same results), for comparisons.
   if (const char* e = std::getenv("HMF_FLOW_KERNEL")) c->use_tma = std::strcmp(e, "ring") != 0 || n_volumes > 1;

@@ -71,7 +71,8 @@ struct hmf_ctx {
   hmf::TreeTable* d_tree = nullptr;
   hmf::DagTable* d_dag = nullptr;
   bool dag_last = false;  // the next sweep is the last iteration's
-  bool dag_simple = false;  // dag_sweep_kernel instead of dag_bulk_kernel (HMF_DAG_KERNEL=simple)
+  bool dag_simple = false;   // dag_sweep_kernel (HMF_DAG_KERNEL=simple)
+  bool dag_generic = false;  // dag_bulk_kernel even for small graphs (HMF_DAG_KERNEL=generic)
   bool use_tma = true;  // flow_tma_kernel (else the shared-memory ring flow_kernel)
   int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
   const float** d_smooth_list = nullptr;
@@ -98,6 +99,8 @@ struct hmf_ctx {
   std::vector<hmf::FlowItem> h_items;
   hmf::TreeTable h_tree{};
   hmf::DagTable h_dag{};
+  hmf::DagRegParams h_dagreg{};
+  bool dag_reg_ok = false;  // h_dagreg describes the graph (<= 8 nodes, no repeated edge)
   std::vector<const float*> h_smooth_list;
 
   // the staged inputs of the last solve (per vertex; for hmf_get_energy)

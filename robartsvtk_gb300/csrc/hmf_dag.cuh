@@ -308,4 +308,144 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
 }
 
+// dag_bulk_kernel for graphs of N <= 8 entries without repeated edges: the
+// graph in kernel parameters, staged slots at compile-time offsets (entry
+// e >= 1: sink 4(e-1), source +1, divergence +2, label +3, data term
+// 4(N-1) + e-1; the root's source 5(N-1)), so the per-voxel program reads no
+// table.  Same arithmetic and order as dag_bulk_kernel.
+constexpr int kDagNVc = 256;
+__host__ __device__ constexpr int dag_bulk_n_arrays(int N) { return 5 * (N - 1) + 1; }
+__host__ __device__ constexpr int dag_bulk_n_smem_bytes(int N) {
+  return 128 + kDagBulkStages * dag_bulk_n_arrays(N) * kDagNVc * 4;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kDagNVc)
+    dag_bulk_n_kernel(const __grid_constant__ DagRegParams P, long long n_vox, int last, int* __restrict__ error_flag) {
+  constexpr int A = dag_bulk_n_arrays(N);
+  constexpr int VC = kDagNVc;
+  constexpr int ROOT = 5 * (N - 1);
+  __shared__ int abort_cta;
+  extern __shared__ __align__(128) unsigned char dn_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(dn_raw);
+  float* const stage0 = reinterpret_cast<float*>(dn_raw + 128);
+  if (threadIdx.x == 0) {
+    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    if (smem_addr(dn_raw) & 15) {
+      abort_cta = 1;
+      if (error_flag) atomicOr(error_flag, 4);
+    }
+    for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (abort_cta) return;
+  const float cc = P.cc, icc = P.icc;
+  const long long nchunks = (n_vox + VC - 1) / VC;
+  auto slot_s = [](int e) { return e ? 4 * (e - 1) : ROOT; };
+
+  auto issue = [&](long long chunk, int s) {  // thread 0 only
+    const long long v0 = chunk * VC;
+    const unsigned bytes = (unsigned)(min((long long)VC, n_vox - v0) * 4);
+    float* dst = stage0 + (size_t)s * A * VC;
+    unsigned arrays = 4 * (N - 1) + 1;
+#pragma unroll
+    for (int e = 1; e < N; ++e) arrays += (P.leaf_mask >> e) & 1u;
+    mbar_expect_tx(&bars[s], bytes * arrays);
+#pragma unroll
+    for (int e = 1; e < N; ++e) {
+      float* d = dst + (4 * (e - 1)) * VC;
+      bulk_load(d, P.sink[e] + v0, bytes, &bars[s]);
+      bulk_load(d + VC, P.inc[e] + v0, bytes, &bars[s]);
+      bulk_load(d + 2 * VC, P.div[e] + v0, bytes, &bars[s]);
+      bulk_load(d + 3 * VC, P.label[e] + v0, bytes, &bars[s]);
+      if ((P.leaf_mask >> e) & 1u) bulk_load(dst + (4 * (N - 1) + e - 1) * VC, P.data[e] + v0, bytes, &bars[s]);
+    }
+    bulk_load(dst + ROOT * VC, P.sink[0] + v0, bytes, &bars[s]);
+  };
+
+  bool timed_out = false;
+  int nissued[kDagBulkStages] = {0, 0};  // kept by thread 0
+  long long chunk = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  }
+  for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
+    const int s = j & 1;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    const long long v0 = chunk * VC;
+    const int len = (int)min((long long)VC, n_vox - v0);
+    const int q = threadIdx.x;
+    if (q < len) {
+      float* st = stage0 + (size_t)s * A * VC + q;
+      float S[N], C[N], D[N], U[N];
+      S[0] = st[ROOT * VC];
+#pragma unroll
+      for (int e = 1; e < N; ++e) {
+        S[e] = st[(4 * (e - 1)) * VC];
+        C[e] = st[(4 * (e - 1) + 1) * VC];
+        D[e] = st[(4 * (e - 1) + 2) * VC];
+        U[e] = st[(4 * (e - 1) + 3) * VC];
+      }
+      // (2)
+      S[0] = 1.0f * S[0] + P.shift;
+#pragma unroll
+      for (int e = 1; e < N; ++e) {
+        const float c = C[e], d = D[e], u = U[e];
+        if ((P.leaf_mask >> e) & 1u) {
+          float v = (c - d) + u * icc;
+          const float cap = st[(4 * (N - 1) + e - 1) * VC];
+          v = (v < 0.0f) ? 0.0f : v;
+          v = (v > cap) ? cap : v;
+          S[e] = v;
+          U[e] = __saturatef(u + cc * ((c - d) - v));
+        } else {
+          S[e] = (1.0f - P.k[e]) * S[e] + P.k[e] * ((c - d) + u * icc);
+        }
+      }
+      if (!last) {
+        // (3) deepest first; a node's parents precede it in forward order
+#pragma unroll
+        for (int e = N - 1; e >= 1; --e) {
+          const float pot = ((S[e] - C[e]) + D[e]) - U[e] * icc;
+#pragma unroll
+          for (int p = 0; p < e; ++p)
+            if ((P.pmask[e] >> p) & 1u) S[p] = S[p] + P.wup[e][p] * pot;
+          if (!((P.leaf_mask >> e) & 1u)) U[e] = __saturatef(U[e] + cc * ((C[e] - D[e]) - S[e]));
+        }
+        // (4) parents in in-edge order
+#pragma unroll
+        for (int e = 1; e < N; ++e) {
+          float c = 0.0f;
+          for (int k = 0; k < P.n_in[e]; ++k) {
+            const int p = P.parent_ord[e][k];
+            float sp = S[0];
+#pragma unroll
+            for (int w = 1; w < e; ++w) sp = (w == p) ? S[w] : sp;
+            c = c + P.wdown_ord[e][k] * sp;
+          }
+          C[e] = c;
+        }
+      }
+      const long long i = v0 + q;
+      P.sink[0][i] = S[0];
+#pragma unroll
+      for (int e = 1; e < N; ++e) {
+        P.sink[e][i] = S[e];
+        P.label[e][i] = U[e];
+        if (!last) P.inc[e][i] = C[e];
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();  // stage s is free again
+    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+  }
+  if (timed_out && error_flag) atomicOr(error_flag, 2);
+  if (threadIdx.x == 0 && timed_out)
+    for (int s = 0; s < kDagBulkStages; ++s)
+      if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+}
+
 }  // namespace hmf

@@ -85,6 +85,26 @@ struct DagTable {
   DagEntry e[kMaxVertices];
 };
 
+// The graph of dag_bulk_n_kernel<N> (N <= 8 entries, no repeated edge), in
+// kernel parameters: entry e's staged arrays, its parents as a bit mask with
+// per-pair weights, and its parents in in-edge order for the push-down sum.
+constexpr int kDagRegMax = 8;
+struct DagRegParams {
+  float* sink[kDagRegMax];  // entry 0: the root's source
+  float* inc[kDagRegMax];
+  float* label[kDagRegMax];
+  const float* div[kDagRegMax];
+  const float* data[kDagRegMax];
+  float k[kDagRegMax];                    // branch reset weights
+  float wup[kDagRegMax][kDagRegMax];      // [child][parent] push-up weight
+  float wdown_ord[kDagRegMax][kDagRegMax];  // [child][j] push-down weight of its j-th in-edge
+  int parent_ord[kDagRegMax][kDagRegMax];   // [child][j] parent entry of its j-th in-edge
+  int n_in[kDagRegMax];
+  unsigned pmask[kDagRegMax];  // bit p: entry p is a parent
+  unsigned leaf_mask;
+  float cc, icc, shift;
+};
+
 struct TreeTable {
   int n;
   int n_leaves;

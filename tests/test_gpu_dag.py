@@ -57,13 +57,14 @@ def assert_exact(g, o, what):
             what, v, np.abs(s - o["sink"][v]).max())
 
 
-@pytest.fixture(params=["bulk", "simple"])
+@pytest.fixture(params=["default", "generic", "simple"])
 def dag_kernel(request, monkeypatch):
-    """The bulk-staged graph sweep (default) and the direct one."""
-    if request.param == "simple":
-        monkeypatch.setenv("HMF_DAG_KERNEL", "simple")
-    else:
+    """The default graph sweep (graph in kernel parameters for up to 8
+    nodes), the table-driven bulk-staged one and the direct one."""
+    if request.param == "default":
         monkeypatch.delenv("HMF_DAG_KERNEL", raising=False)
+    else:
+        monkeypatch.setenv("HMF_DAG_KERNEL", request.param)
     return request.param
 
 
