@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
-    for (int s = 0; s < 2; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < 2; ++s) mbar_init(&bars[s], N);  // one arrival per vertex lane
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -78,21 +78,21 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
   const long long arr = S.arr;
   const long long nchunks = (G.vol + kSwVc - 1) / kSwVc;
 
-  auto issue = [&](long long chunk, int s) {  // thread 0 only
+  // Vertex v's arrays of a chunk, issued by lane v of warp 0 (each lane its
+  // own expected bytes, before its copies complete against them).
+  auto issue = [&](long long chunk, int s, int v) {
     const long long v0 = chunk * kSwVc;
     const unsigned len = (unsigned)min((long long)kSwVc, G.vol - v0);
     uint64_t* bar = &bars[s];
     float* dst = stage0 + (size_t)s * kStage;
-    unsigned total = 0;  // expected bytes first (the copies complete against it)
-    for (int v = 0; v < N; ++v) {
+    {
       const bool nr = v != root, leaf = T.n_kids[v] == 0;
-      total += len * 4 * (3 + (nr ? 4 : 0)) + (leaf ? len * 8 : 0);
+      mbar_expect_tx(bar, len * 4 * (3 + (nr ? 4 : 0)) + (leaf ? len * 8 : 0));
     }
-    mbar_expect_tx(bar, total);
     auto ld = [&](int kind, int v, const float* src) {
       bulk_load(dst + (size_t)(kind * N + v) * kSwVc, src + v0, len * 4, bar);
     };
-    for (int v = 0; v < N; ++v) {
+    {
       const long long b = T.sbase[v];
       const bool nr = v != root, leaf = T.n_kids[v] == 0;
       ld(kSwSBN, v, S.sbn + v * arr);
@@ -112,9 +112,9 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
   bool timed_out = false;
   int nissued[2] = {0, 0};
   long long chunk = blockIdx.x;
-  if (threadIdx.x == 0) {
-    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
-    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  if (threadIdx.x < N) {
+    if (chunk < nchunks) issue(chunk, 0, threadIdx.x), ++nissued[0];
+    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1, threadIdx.x), ++nissued[1];
   }
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
@@ -259,7 +259,8 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
     // refills it (async proxy)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+    if (threadIdx.x < N && chunk + 2LL * gridDim.x < nchunks)
+      issue(chunk + 2LL * gridDim.x, s, threadIdx.x), ++nissued[s];
   }
   if (timed_out && error_flag) atomicOr(error_flag, 2);
   if (threadIdx.x == 0 && timed_out)
