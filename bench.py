@@ -59,6 +59,14 @@ def parse():
                     help="one DAG solve (--dag-size, --dag-iterations): the command ncu wraps")
     ap.add_argument("--profile", action="store_true",
                     help="two solves (one warm, one profiled) and nothing else: the command ncu wraps")
+    ap.add_argument("--large", action="store_true",
+                    help="the 512x512x384 tree8 workload (400 iterations): forward solve and the adjoint under "
+                         "the automatic memory plan, one JSON line, nothing else (minutes)")
+    ap.add_argument("--large-iterations", type=int, default=400)
+    ap.add_argument("--large-dims", default="512,512,384", help="VX,VY,VZ of --large (a smaller case for profiles)")
+    ap.add_argument("--profile-large", action="store_true",
+                    help="two forward solves of the --large workload (--large-dims, --large-iterations): the "
+                         "command ncu wraps")
     ap.add_argument("--profile-post", action="store_true",
                     help="one solve, then two votes and two energy evaluations of its labels: the command ncu wraps")
     return ap.parse_args()
@@ -585,6 +593,132 @@ def cpu_dag_sample(w, edges, threads, iters=2):
             "sample": "full %dx%dx%d volume, %d iterations (initialisation excluded)" % (*w.dims, iters)}
 
 
+def backward_bytes_per_step(w):
+    """Compulsory bytes of one backward step (the sweep reverse and the flow
+    reverse): sweep reads per vertex the two sink adjoint parts and the sink
+    after, the data term (leaves) or the sink before (others), per non-root
+    vertex the label adjoint, gb, the label before and the divergence after,
+    per leaf the data gradient (double); writes per vertex the new sink
+    adjoint, per non-root vertex the label and divergence adjoints, per leaf
+    the data gradient.  Flow reverse per non-root vertex: 10 reads, 4 writes."""
+    n, L = len(w.parent), len(w.leaves)
+    sweep = (2 * n + n + 4 * (n - 1) + 2 * L) + (n + 2 * (n - 1) + 2 * L)
+    flow = 14 * (n - 1)
+    return 4.0 * w.nvox * (sweep + flow)
+
+
+def run_large(args):
+    """512x512x384 CT-like phantom, tree root -> 2 -> 4 -> 8 (14 non-root
+    vertices, 8 leaves), one shared per-voxel smoothness image, 400
+    iterations: one forward solve, then hmf_solve_adjoint with the automatic
+    plan (every state kept if it fits, else the fewest-forward-iterations
+    schedule over the state slots that fit in 85% of the free HBM).  Inputs
+    are resident on the device; times are CUDA events on one stream."""
+    import numpy as np
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver, synthetic
+
+    t0 = time.time()
+    dims = tuple(int(v) for v in args.large_dims.split(","))
+    w = synthetic.ellipsoids_tree8(seed=5, dims=dims, iterations=args.large_iterations)
+    gen_s = time.time() - t0
+    stream = torch.cuda.Stream()
+    peak, peak_kind = measured_peak_hbm()
+    d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
+    S = torch.from_numpy(next(iter(w.smooth.values()))).cuda()
+    s = HMFSolver(w.dims, w.parent)
+    # phantom class k is leaf 7 + k; the adjoint's truth indexes s.leaves
+    order = np.array([s.leaves.index(leaf) for leaf in sorted(w.data)], dtype=np.int32)
+    truth = torch.from_numpy(order[w.truth]).cuda()
+    for leaf, t in d.items():
+        s.set_data(leaf, t)
+    for v in w.smooth:
+        s.set_smoothness(v, S)
+    for v, a in w.alpha.items():
+        s.set_smoothness_scalar(v, a)
+
+    def timed(fn):
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1), r
+
+    s.set_params(5, w.step, w.cc)
+    s.solve(stream)  # warm-up (tables, first launches)
+    s.set_params(w.iterations, w.step, w.cc)
+    t_fwd, _ = timed(lambda: s.solve(stream))
+    T = w.iterations
+    # per-kernel averages of a short solve with per-launch events
+    s.set_params(min(T, 10), w.step, w.cc)
+    s.set_timing(True)
+    s.solve(stream)
+    kstats = s.stats()
+    s.set_timing(False)
+    s.set_params(T, w.step, w.cc)
+    vli = w.nvox * len(w.leaves) * T
+    b_iter = survey_bytes_per_iteration(w)
+    # the adjoint may use the free device memory but a margin (the library's
+    # default budget is 85% of it): every state slot saves forward passes
+    free_b, _ = torch.cuda.mem_get_info()
+    s.set_adjoint_memory(max_bytes=max(0, free_b - (6 << 30)))
+    t_adj, loss = timed(lambda: s.solve_adjoint(truth, stream=stream))
+    plan = s.adjoint_plan()
+    t_it = t_fwd / T
+    t_bwd = t_adj - plan["forward_iterations"] * t_it
+    b_bwd = backward_bytes_per_step(w)
+    out = {
+        "workload": "ellipsoids%dx%dx%d_tree8" % tuple(w.dims), "volume": list(w.dims), "vertices": len(w.parent),
+        "leaves": len(w.leaves), "iterations": T, "data": "synthetic (seeded phantom)", "generate_s": gen_s,
+        "forward": {"ms": t_fwd, "value": vli / (t_fwd / 1000.0), "unit": "voxel*label*iter/s",
+                    "bytes_per_iteration": b_iter, "achieved_gbs": b_iter * T / (t_fwd / 1000.0) / 1e9,
+                    "frac": b_iter * T / (t_fwd / 1000.0) / 1e9 / peak,
+                    "flow_kernel_ms": kstats["flow_ms"], "tree_kernel_ms": kstats["tree_ms"]},
+        "adjoint": {"ms": t_adj, "ratio_to_forward": t_adj / t_fwd, "loss": loss, **plan,
+                    "device_bytes": s.device_bytes(),
+                    "backward_ms": t_bwd,
+                    "backward_note": "adjoint time minus the schedule's forward iterations at the forward solve's "
+                                     "per-iteration time",
+                    "backward_value": vli / (t_bwd / 1000.0),
+                    "backward_bytes_per_step": b_bwd,
+                    "backward_achieved_gbs": b_bwd * T / (t_bwd / 1000.0) / 1e9,
+                    "backward_frac": b_bwd * T / (t_bwd / 1000.0) / 1e9 / peak},
+        "peak_gbs": peak, "peak_source": peak_kind,
+    }
+    s.close()
+    print(json.dumps(out))
+    return 0
+
+
+def run_profile_large(args):
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver, synthetic
+
+    dims = tuple(int(v) for v in args.large_dims.split(","))
+    w = synthetic.ellipsoids_tree8(seed=5, dims=dims, iterations=args.large_iterations)
+    d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
+    S = torch.from_numpy(next(iter(w.smooth.values()))).cuda()
+    s = HMFSolver(w.dims, w.parent)
+    for leaf, t in d.items():
+        s.set_data(leaf, t)
+    for v in w.smooth:
+        s.set_smoothness(v, S)
+    for v, a in w.alpha.items():
+        s.set_smoothness_scalar(v, a)
+    s.set_params(w.iterations, w.step, w.cc)
+    for _ in range(2):
+        s.solve()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_large": list(w.dims), "iterations": w.iterations, "launches": s.stats()["launches"]}))
+    s.close()
+    return 0
+
+
 def run_profile_adjoint(args):
     import torch
 
@@ -818,6 +952,10 @@ def main():
         return run_profile_dag(args)
     if args.profile_adjoint:
         return run_profile_adjoint(args)
+    if args.large:
+        return run_large(args)
+    if args.profile_large:
+        return run_profile_large(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

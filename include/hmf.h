@@ -173,9 +173,14 @@ int hmf_autotune(hmf_ctx* ctx, void* stream);
  * leaf data term (per voxel, double) and hmf_get_alpha_gradient dL/dalpha for
  * every vertex's smoothness weight; labels and sinks read as after hmf_solve.
  * Forward states are kept in HBM every checkpoint_every iterations and the
- * states in between recomputed segment by segment (0 = automatic: keep every
- * state when they fit in 85% of the free device memory, else checkpoints
- * every ceil(sqrt(iterations))).  The call returns after the backward pass
+ * states in between recomputed segment by segment (ceil(T/k) + k state
+ * slots).  checkpoint_every = 0 is automatic: every state is kept when T + 1
+ * state slots fit in the memory budget (85% of the free device memory, or
+ * hmf_set_adjoint_memory's), else the budget's slots are scheduled for the
+ * fewest forward iterations (a revolve-style binomial schedule: states kept
+ * and recomputed recursively; fails with HMF_ERR_OUT_OF_MEMORY when too few
+ * slots fit for T iterations).  One state slot holds 6(n_nodes-1)+1 arrays
+ * of the padded volume.  The call returns after the backward pass
  * (it synchronises c's stream to read the loss).  Kinks follow the forward
  * code: saturate and the leaf capacity clamp pass gradients strictly inside
  * their linear ranges, the projection multiplier only where |p| > alpha*S. */
@@ -188,6 +193,26 @@ int hmf_get_alpha_gradient(hmf_ctx* ctx, double* out, int n);
 /* The checkpoint interval the last hmf_solve_adjoint used and how many of its
  * segments were recomputed. */
 int hmf_get_adjoint_plan(const hmf_ctx* ctx, int* checkpoint_every, int* recomputed_segments);
+/* Memory budget of later hmf_solve_adjoint calls with checkpoint_every = 0:
+ * at most max_bytes of device memory for the adjoint's arrays (0: 85% of the
+ * free device memory) and at most max_state_slots state slots (0: no cap).
+ * The analogue of the reference's MaxGPUUsage
+ * (vtkCudaHierarchicalMaxFlowSegmentation2.h:74-82), for the adjoint. */
+int hmf_set_adjoint_memory(hmf_ctx* ctx, long long max_bytes, int max_state_slots);
+/* The schedule the last hmf_solve_adjoint ran: state slots, forward
+ * iterations (first pass included; T when every state is kept) and backward
+ * steps (T). */
+int hmf_get_adjoint_schedule(const hmf_ctx* ctx, int* state_slots, long long* forward_iterations,
+                             long long* backward_steps);
+/* The schedule itself, host only (no device work): checkpoint_every > 0 gives
+ * the fixed-interval schedule, 0 the fewest-forward-iterations schedule over
+ * state_slots slots.  Writes up to `capacity` actions of four ints (kind: 0
+ * forward iteration t from slot a to slot b, 1 loss on x_T in slot a, 2
+ * backward step of iteration t with x_t in slot a and x_{t+1} in slot b;
+ * t; a; b; x_0 starts in slot 0) and returns the number of actions, or
+ * HMF_ERR_OUT_OF_MEMORY when no schedule exists with that many slots. */
+long long hmf_adjoint_schedule(int iterations, int state_slots, int checkpoint_every, int* actions,
+                               long long capacity);
 
 /* ---- Vote and energy (the steps after a solve) ----------------------------
  * hmf_vote replaces CUDA_CIV_COMPUTE (CUDA_imagevote.h, the vtkCudaImageVote

@@ -9,10 +9,10 @@ package binds it and mirrors the reference's filter API.
 """
 from .segmentation import (REF_CPU, REF_CUDA, DAGSolver, DirectedAcyclicGraphMaxFlowSegmentation,  # noqa: F401
                            HierarchicalMaxFlowSegmentation, HMFBatchSolver, HMFError, HMFSolver,
-                           decomposition_energy, vote)
+                           adjoint_schedule, decomposition_energy, vote)
 
 from .dataterm import ImageDataTerm, ImageLogLikelihood, data_term, log_likelihood  # noqa: F401
 
 __all__ = ["HMFSolver", "HMFBatchSolver", "HierarchicalMaxFlowSegmentation", "REF_CUDA", "REF_CPU", "HMFError",
            "vote", "decomposition_energy", "DAGSolver", "DirectedAcyclicGraphMaxFlowSegmentation",
-           "data_term", "log_likelihood", "ImageDataTerm", "ImageLogLikelihood"]
+           "data_term", "log_likelihood", "ImageDataTerm", "ImageLogLikelihood", "adjoint_schedule"]

@@ -61,6 +61,10 @@ SIGNATURES = [
     ("hmf_get_data_gradient", _I, [_P, _I, _P, _I, _P]),
     ("hmf_get_alpha_gradient", _I, [_P, ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_get_adjoint_plan", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("hmf_set_adjoint_memory", _I, [_P, ctypes.c_longlong, _I]),
+    ("hmf_get_adjoint_schedule", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_longlong),
+                                      ctypes.POINTER(ctypes.c_longlong)]),
+    ("hmf_adjoint_schedule", ctypes.c_longlong, [_I, _I, _I, ctypes.POINTER(_I), ctypes.c_longlong]),
     ("hmf_vote", _I, [_I, ctypes.POINTER(_P), ctypes.POINTER(_I), ctypes.c_longlong, _I, _P, _I, _P]),
     ("hmf_get_vote", _I, [_P, _P, _I, _P]),
     ("hmf_batch_get_vote", _I, [_P, _I, _P, _I, _P]),

@@ -2,25 +2,26 @@
 // include/hmf.h (no counterpart in the reference, which only solves forward).
 //
 // Forward: the solver's own kernels (flow_tma_kernel, tree_bulk_kernel) run
-// over per-iteration tables that read the state of iteration t from its slot
-// and write the state of t+1 into the next slot, so keeping a state costs no
-// copy.  States at multiples of k go to checkpoint slots C_m; the others go
-// to segment slots S_1..S_k (state a+j of the segment starting at a in S_j).
-// Backward: segment by segment from the last, the segment's inner states are
-// recomputed into S_j with the same tables (bit-identical to the first pass),
-// then one backward step per iteration runs from the segment's last
-// iteration to its first: adj_sweep_kernel (trees of up to 8 vertices;
-// adj_tree_kernel beyond) reverses the sink/label sweep of all vertices, and
+// over tables that read the state x_t from one state slot and write x_{t+1}
+// into another, so keeping a state costs no copy.  Which slots, and which
+// states are recomputed later, is the schedule (hmf_schedule.hpp): every
+// state kept when HBM holds T + 1 slots; a fixed checkpoint interval k when
+// the caller asks for one (ceil(T/k) checkpoint slots + k segment slots);
+// otherwise the schedule with the fewest forward iterations over the slots
+// that fit.  Recomputed states are bit-identical to the first pass (same
+// kernels, same inputs).  One backward step per iteration, from the last to
+// the first: adj_sweep_kernel (trees of up to 8 vertices; adj_tree_kernel
+// beyond) reverses the sink/label sweep of all vertices, and
 // adj_flow_tma_kernel reverses the flow step of every vertex
 // (HMF_ADJOINT_KERNEL=chain selects adj_tree_kernel and the unfused
-// per-vertex kernels of hmf_adjoint.cuh instead; same results).  With k >= iterations (the default
-// when HBM holds every state) nothing is recomputed.  Memory:
-// (ceil(T/k) + k) slots of 6(n-1)+1 arrays, plus 13n+11 float arrays and one
-// double array per leaf.
+// per-vertex kernels of hmf_adjoint.cuh instead; same results).  Memory:
+// the schedule's slots of 6(n-1)+1 arrays, plus 13n float arrays (+11 for
+// the unfused kernels) and one double array per leaf.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -29,6 +30,7 @@
 #include "hmf_adjoint_flow.cuh"
 #include "hmf_adjoint_sweep.cuh"
 #include "hmf_ctx.hpp"
+#include "hmf_schedule.hpp"
 
 using namespace hmfi;
 
@@ -40,13 +42,16 @@ constexpr int kAdjTemps = 11;  // g, ppx, ppy, ppz, m, Fm, F2b, qx, qy, qz, dbo
 }  // namespace
 
 struct AdjointState {
-  int k = 0, iterations = 0;
+  int iterations = 0;
   int A = 0;          // arrays per state slot
   long long arr = 0;  // floats per array (multiple of 64)
-  int n_ckpt = 0, n_seg = 0;
+  int n_slots = 0;
+  AdjSchedule sched;
+  std::vector<int> fwd_table;  // per action: index of its forward tables (forward actions)
+  int n_pairs = 0;             // distinct (read slot, write slot) pairs of the forward actions
   char* arena = nullptr;
   size_t bytes = 0;
-  float* slots = nullptr;             // C_0..C_{n_ckpt-1}, S_1..S_k
+  float* slots = nullptr;             // n_slots state slots
   float* sb[2] = {nullptr, nullptr};  // [v*arr] sweep part of the sinks' adjoint (ping-pong)
   float* ub[2] = {nullptr, nullptr};  // [v*arr] sweep part of the labels' adjoint
   float* gb = nullptr;                // [v*arr] adjoint of g of the flow reverse
@@ -59,9 +64,9 @@ struct AdjointState {
   double* scal = nullptr;             // [0] loss, [1 + v] alpha gradient
   const float** d_ctx = nullptr;      // solver arrays in slot order (null: not copied)
   hmf::AdjTree* d_tree = nullptr;
-  // per-transition forward tables: iteration t reads slot src(t), writes dst(t)
-  hmf::FlowVertexTMA* d_tflow = nullptr;  // [t][n-1]
-  hmf::TreeTable* d_ttree = nullptr;      // [t]
+  // forward tables per (read slot, write slot) pair
+  hmf::FlowVertexTMA* d_tflow = nullptr;  // [pair][n-1]
+  hmf::TreeTable* d_ttree = nullptr;      // [pair]
   int table_cap = 0;
   std::vector<hmf::FlowVertexTMA> h_tflow;
   std::vector<hmf::TreeTable> h_ttree;
@@ -97,20 +102,6 @@ float* slot_array(const AdjointState* S, int slot, int index) {
   return slot_ptr(S, slot) + (size_t)index * S->arr;
 }
 
-// slot ids: C_m = m, S_j = n_ckpt + j - 1 (j >= 1)
-int ckpt_id(const AdjointState* S, int m) { return m; }
-int seg_id(const AdjointState* S, int j) { return S->n_ckpt + j - 1; }
-// the slots iteration t reads and writes
-int src_slot(const AdjointState* S, int t) {
-  const int a = (t / S->k) * S->k;
-  return t == a ? ckpt_id(S, a / S->k) : seg_id(S, t - a);
-}
-int dst_slot(const AdjointState* S, int t) {
-  const int a = (t / S->k) * S->k;
-  if ((t + 1) % S->k == 0 && t + 1 < S->iterations) return ckpt_id(S, (t + 1) / S->k);
-  return seg_id(S, t + 1 - a);
-}
-
 int grid_for(const hmf_ctx* c, long long n) {
   return (int)std::max<long long>(1, std::min<long long>((n + kAdjThreads - 1) / kAdjThreads, (long long)c->sm_count * 16));
 }
@@ -121,20 +112,51 @@ int plan(hmf_ctx* c, int T, int k_req) {
   const int A = hmf::kAdjPerVertex * (c->n - 1) + 1;
   const size_t slot_bytes = (size_t)A * arr * sizeof(float);
   const int L = (int)c->leaves.size();
-  const size_t fixed = ((size_t)(13 * c->n + kAdjTemps) * arr) * sizeof(float) + (size_t)L * arr * sizeof(double) +
+  const int temps = S->chain ? kAdjTemps : 0;  // scratch of the unfused reverse kernels only
+  const size_t fixed = ((size_t)(13 * c->n + temps) * arr) * sizeof(float) + (size_t)L * arr * sizeof(double) +
                        (size_t)arr * sizeof(int) + 4096;
-  int k = k_req;
-  if (k <= 0) {
+  // state slots that fit: the caller's byte budget, else 85% of the free
+  // device memory (the held arena is reusable); the caller's slot cap
+  double budget = (double)c->adj_max_bytes;
+  if (budget <= 0.0) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
-    const double budget = 0.85 * (double)(free_b + S->bytes);  // the held arena is reusable
-    k = (double)(T + 1) * slot_bytes + fixed <= budget ? std::max(T, 1)
-                                                       : std::max(1, (int)std::ceil(std::sqrt((double)T)));
+    budget = 0.85 * (double)(free_b + S->bytes);
   }
-  k = std::max(1, std::min(k, std::max(T, 1)));
-  const int n_ckpt = std::max(1, (T + k - 1) / k);
-  const int n_seg = k;
-  const size_t need = (size_t)(n_ckpt + n_seg) * slot_bytes + fixed;
+  long long fit = budget > (double)fixed ? (long long)((budget - (double)fixed) / (double)slot_bytes) : 0;
+  if (c->adj_max_slots > 0) fit = std::min<long long>(fit, c->adj_max_slots);
+  if (k_req > 0) {
+    S->sched = schedule_fixed(T, k_req);
+    if (c->adj_max_slots > 0 && S->sched.slots > c->adj_max_slots) {
+      char msg[160];
+      std::snprintf(msg, sizeof(msg), "checkpoint interval %d needs %d state slots, more than the %d allowed",
+                    k_req, S->sched.slots, c->adj_max_slots);
+      return fail(c, HMF_ERR_OUT_OF_MEMORY, msg);
+    }
+  } else if (fit >= (long long)T + 1) {
+    S->sched = schedule_fixed(T, T);  // every state kept
+  } else if (!schedule_fewest(T, (int)fit, &S->sched)) {
+    char msg[200];
+    std::snprintf(msg, sizeof(msg),
+                  "%lld state slots of %.1f MB fit in the adjoint's device memory budget; %d iterations need more",
+                  fit, (double)slot_bytes / 1048576.0, T);
+    return fail(c, HMF_ERR_OUT_OF_MEMORY, msg);
+  }
+  const int n_slots = S->sched.slots;
+  // forward tables per distinct (read slot, write slot) pair
+  {
+    std::vector<int> pair_id((size_t)n_slots * n_slots, -1);
+    S->fwd_table.assign(S->sched.actions.size(), -1);
+    S->n_pairs = 0;
+    for (size_t i = 0; i < S->sched.actions.size(); ++i) {
+      const AdjAction& x = S->sched.actions[i];
+      if (x.kind != kActForward) continue;
+      int& id = pair_id[(size_t)x.a * n_slots + x.b];
+      if (id < 0) id = S->n_pairs++;
+      S->fwd_table[i] = id;
+    }
+  }
+  const size_t need = (size_t)n_slots * slot_bytes + fixed;
   if (need > S->bytes) {
     if (S->arena) cudaFree(S->arena);
     S->arena = nullptr;
@@ -143,39 +165,37 @@ int plan(hmf_ctx* c, int T, int k_req) {
     CK(cudaMemset(S->arena, 0, need), "cudaMemset(adjoint state)");
     S->bytes = need;
   }
-  S->k = k;
   S->iterations = T;
   S->A = A;
   S->arr = arr;
-  S->n_ckpt = n_ckpt;
-  S->n_seg = n_seg;
+  S->n_slots = n_slots;
   char* p = S->arena;
   auto takef = [&](size_t arrays) {
     float* r = reinterpret_cast<float*>(p);
     p += arrays * arr * sizeof(float);
     return r;
   };
-  S->slots = takef((size_t)(n_ckpt + n_seg) * A);
+  S->slots = takef((size_t)n_slots * A);
   for (int q = 0; q < 2; ++q) S->sb[q] = takef(c->n);
   for (int q = 0; q < 2; ++q) S->ub[q] = takef(c->n);
   S->gb = takef(c->n);
   S->dbp = takef(c->n);
   S->Pb = takef(6 * (size_t)c->n);
-  S->tmp = takef(kAdjTemps);
+  S->tmp = temps ? takef(temps) : nullptr;
   S->Db = reinterpret_cast<double*>(p);
   p += (size_t)L * arr * sizeof(double);
   S->truth = reinterpret_cast<int*>(p);
-  if (T > S->table_cap) {
+  if (S->n_pairs > S->table_cap) {
     if (S->d_tflow) cudaFree(S->d_tflow);
     if (S->d_ttree) cudaFree(S->d_ttree);
     S->d_tflow = nullptr;
     S->d_ttree = nullptr;
     S->table_cap = 0;
-    CK(cudaMalloc(&S->d_tflow, sizeof(hmf::FlowVertexTMA) * (size_t)T * (c->n - 1)), "cudaMalloc(adjoint flow tables)");
-    CK(cudaMalloc(&S->d_ttree, sizeof(hmf::TreeTable) * (size_t)T), "cudaMalloc(adjoint tree tables)");
-    S->table_cap = T;
+    CK(cudaMalloc(&S->d_tflow, sizeof(hmf::FlowVertexTMA) * (size_t)S->n_pairs * (c->n - 1)),
+       "cudaMalloc(adjoint flow tables)");
+    CK(cudaMalloc(&S->d_ttree, sizeof(hmf::TreeTable) * (size_t)S->n_pairs), "cudaMalloc(adjoint tree tables)");
+    S->table_cap = S->n_pairs;
   }
-  const int n_slots = n_ckpt + n_seg;
   if (n_slots > S->aflow_cap) {
     if (S->d_aflow) cudaFree(S->d_aflow);
     S->d_aflow = nullptr;
@@ -240,7 +260,7 @@ int plan_reverse(hmf_ctx* c, cudaStream_t s) {
 // Reverse-kernel tables, one per state slot (the state before the iteration).
 int build_reverse_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
   AdjointState* S = c->adj;
-  const int nv = c->n - 1, n_slots = S->n_ckpt + S->n_seg;
+  const int nv = c->n - 1, n_slots = S->n_slots;
   const auto& V = c->vols[0];
   const int rows = hmf::kAfBoxY;
   S->h_aflow.assign((size_t)n_slots * nv, hmf::AdjFlowVertex{});
@@ -287,24 +307,26 @@ int copy_state(hmf_ctx* c, float* slot, bool to_slot, cudaStream_t s) {
   return HMF_OK;
 }
 
-// Tables of iteration t: the flow kernel reads the flows, sinks and labels of
-// slot src(t) and writes the flows and divergence of slot dst(t); the sweep
-// reads slot src(t)'s sinks and labels and dst(t)'s divergence and writes
-// dst(t)'s sinks and labels.
+// Tables of a forward iteration from slot a to slot b (the same for every
+// iteration t): the flow kernel reads the flows, sinks and labels of slot a
+// and writes the flows and divergence of slot b; the sweep reads slot a's
+// sinks and labels and b's divergence and writes b's sinks and labels.
 int build_transition_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
   AdjointState* S = c->adj;
-  const int T = S->iterations, nv = c->n - 1;
+  const int P = S->n_pairs, nv = c->n - 1;
   const auto& V = c->vols[0];
-  S->h_tflow.assign((size_t)T * nv, hmf::FlowVertexTMA{});
-  S->h_ttree.assign((size_t)T, hmf::TreeTable{});
-  std::vector<int> entry(c->n, -1);
-  for (int i = 0; i < c->n; ++i) entry[c->postorder[i]] = i;
-  for (int t = 0; t < T; ++t) {
-    const int a = src_slot(S, t), b = dst_slot(S, t);
+  S->h_tflow.assign((size_t)P * nv, hmf::FlowVertexTMA{});
+  S->h_ttree.assign((size_t)P, hmf::TreeTable{});
+  std::vector<char> done((size_t)P, 0);
+  for (size_t i = 0; i < S->sched.actions.size(); ++i) {
+    const int pr = S->fwd_table[i];
+    if (pr < 0 || done[pr]) continue;
+    done[pr] = 1;
+    const int a = S->sched.actions[i].a, b = S->sched.actions[i].b;
     int j = 0;
     for (int v : c->preorder) {
       if (v == c->root) continue;
-      hmf::FlowVertexTMA& f = S->h_tflow[(size_t)t * nv + j++];
+      hmf::FlowVertexTMA& f = S->h_tflow[(size_t)pr * nv + j++];
       std::memset(&f, 0, sizeof(f));
       const int base = slot_base(c, v), pbase = slot_base(c, c->parent[v]);
       int rc = HMF_OK;
@@ -323,7 +345,7 @@ int build_transition_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
       f.div = slot_array(S, b, base + hmf::kAdjDiv);
       f.alpha = (float)c->alpha[v];  // stored as float, as the reference does (.cxx:692)
     }
-    hmf::TreeTable& tt = S->h_ttree[t];
+    hmf::TreeTable& tt = S->h_ttree[pr];
     tt = c->h_tree;  // the solver's own table: tree, constants, data terms
     for (int i = 0; i < c->n; ++i) {
       const int v = c->postorder[i];
@@ -337,7 +359,7 @@ int build_transition_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
       E.div = slot_array(S, b, base + hmf::kAdjDiv);
     }
   }
-  if (T > 0) {
+  if (P > 0) {
     CK(cudaMemcpyAsync(S->d_tflow, S->h_tflow.data(), sizeof(hmf::FlowVertexTMA) * S->h_tflow.size(),
                        cudaMemcpyHostToDevice, s),
        "cudaMemcpyAsync(adjoint flow tables)");
@@ -348,10 +370,11 @@ int build_transition_tables(hmf_ctx* c, const Staged& staged, cudaStream_t s) {
   return HMF_OK;
 }
 
-int forward_iteration(hmf_ctx* c, int t, cudaStream_t s) {
+// one forward iteration with the tables of pair `pair`
+int forward_iteration(hmf_ctx* c, int pair, cudaStream_t s) {
   AdjointState* S = c->adj;
-  int rc = launch_flow_tma_with(c, S->d_tflow + (size_t)t * (c->n - 1), 0, s);
-  if (!rc) rc = launch_tree_bulk_with(c, S->d_ttree + t, s);
+  int rc = launch_flow_tma_with(c, S->d_tflow + (size_t)pair * (c->n - 1), 0, s);
+  if (!rc) rc = launch_tree_bulk_with(c, S->d_ttree + pair, s);
   return rc;
 }
 
@@ -613,41 +636,35 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
   CK(cudaMemsetAsync(S->Db, 0, c->leaves.size() * arr * sizeof(double), s), "cudaMemsetAsync(gradients)");
   CK(cudaMemsetAsync(S->scal, 0, sizeof(double) * (1 + hmf::kMaxVertices), s), "cudaMemsetAsync(scalars)");
 
-  // ---- forward pass: the initial state into C_0, then every iteration
-  // writes its successor's slot
-  const int k = S->k;
-  const int a_last = T > 0 ? ((T - 1) / k) * k : 0;
-  rc = copy_state(c, slot_ptr(S, ckpt_id(S, 0)), true, s);
-  for (int t = 0; t < T && !rc; ++t) rc = forward_iteration(c, t, s);
-  if (rc) return rc;
-  const int final_slot = T > 0 ? dst_slot(S, T - 1) : ckpt_id(S, 0);
-  // the final sinks and labels into the solver's arrays (hmf_get_labels / _sink)
-  rc = copy_state(c, slot_ptr(S, final_slot), false, s);
-  if (rc) return rc;
-  // ---- loss on the final labels; it seeds the label adjoints of the leaves
-  {
-    hmf::AdjLoss Lo;
-    std::memset(&Lo, 0, sizeof(Lo));
-    Lo.n_leaves = (int)c->leaves.size();
-    for (int j = 0; j < Lo.n_leaves; ++j) {
-      Lo.u[j] = slot_array(S, final_slot, slot_base(c, c->leaves[j]) + hmf::kAdjLabel);
-      Lo.ub[j] = S->ub[0] + (size_t)c->leaves[j] * arr;
-    }
-    Lo.n_voxels = (double)dense;
-    Lo.eps = eps;
-    hmf::adj_loss_kernel<<<grid_for(c, c->geo.vol), kAdjThreads, 0, s>>>(Lo, S->truth, c->geo, S->scal, c->d_error);
-    CK(cudaGetLastError(), "adj_loss_kernel launch");
-    ++c->launches;
-  }
-  // ---- backward, segment by segment
+  // ---- the schedule: x_0 into slot 0, then forward iterations, the loss
+  // where x_T is reached (it seeds the label adjoints of the leaves) and the
+  // backward steps from T-1 down to 0, with recomputations in between
+  rc = copy_state(c, slot_ptr(S, 0), true, s);
   int cur = 0;
-  for (int a = a_last; a >= 0 && T > 0 && !rc; a -= k) {
-    const int b = std::min(a + k, T);
-    if (a != a_last)
-      for (int t = a; t + 2 <= b && !rc; ++t) rc = forward_iteration(c, t, s);  // states a+1 .. b-1
-    for (int t = b - 1; t >= a && !rc; --t) {
-      rc = backward_step(c, staged, src_slot(S, t), dst_slot(S, t), cur, s);
+  for (size_t i = 0; i < S->sched.actions.size() && !rc; ++i) {
+    const AdjAction& x = S->sched.actions[i];
+    if (x.kind == kActForward) {
+      rc = forward_iteration(c, S->fwd_table[i], s);
+    } else if (x.kind == kActBackward) {
+      rc = backward_step(c, staged, x.a, x.b, cur, s);
       cur ^= 1;
+    } else {
+      // the final sinks and labels into the solver's arrays (hmf_get_labels / _sink)
+      rc = copy_state(c, slot_ptr(S, x.a), false, s);
+      if (rc) break;
+      hmf::AdjLoss Lo;
+      std::memset(&Lo, 0, sizeof(Lo));
+      Lo.n_leaves = (int)c->leaves.size();
+      for (int j = 0; j < Lo.n_leaves; ++j) {
+        Lo.u[j] = slot_array(S, x.a, slot_base(c, c->leaves[j]) + hmf::kAdjLabel);
+        Lo.ub[j] = S->ub[0] + (size_t)c->leaves[j] * arr;
+      }
+      Lo.n_voxels = (double)dense;
+      Lo.eps = eps;
+      hmf::adj_loss_kernel<<<grid_for(c, c->geo.vol), kAdjThreads, 0, s>>>(Lo, S->truth, c->geo, S->scal,
+                                                                          c->d_error);
+      CK(cudaGetLastError(), "adj_loss_kernel launch");
+      ++c->launches;
     }
   }
   if (rc) return rc;
@@ -714,9 +731,50 @@ int hmf_get_alpha_gradient(hmf_ctx* c, double* out, int n) {
 int hmf_get_adjoint_plan(const hmf_ctx* c, int* checkpoint_every, int* recomputed_segments) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
   if (!c->adj) return HMF_ERR_STATE;
-  if (checkpoint_every) *checkpoint_every = c->adj->k;
-  if (recomputed_segments) *recomputed_segments = c->adj->n_ckpt - 1;
+  if (checkpoint_every) *checkpoint_every = c->adj->sched.k;
+  if (recomputed_segments) *recomputed_segments = c->adj->sched.recomputed_segments;
   return HMF_OK;
+}
+
+int hmf_set_adjoint_memory(hmf_ctx* c, long long max_bytes, int max_state_slots) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (max_bytes < 0 || max_state_slots < 0)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "adjoint memory limits must be >= 0 (0: no limit)");
+  c->adj_max_bytes = max_bytes;
+  c->adj_max_slots = max_state_slots;
+  return HMF_OK;
+}
+
+int hmf_get_adjoint_schedule(const hmf_ctx* c, int* state_slots, long long* forward_iterations,
+                             long long* backward_steps) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!c->adj) return HMF_ERR_STATE;
+  const AdjSchedule& sc = c->adj->sched;
+  if (state_slots) *state_slots = sc.slots;
+  if (forward_iterations) *forward_iterations = sc.forward;
+  if (backward_steps) {
+    long long nb = 0;
+    for (const auto& x : sc.actions) nb += x.kind == kActBackward;
+    *backward_steps = nb;
+  }
+  return HMF_OK;
+}
+
+long long hmf_adjoint_schedule(int iterations, int state_slots, int checkpoint_every, int* actions,
+                               long long capacity) {
+  if (iterations < 0 || checkpoint_every < 0 || capacity < 0 || (capacity > 0 && !actions))
+    return HMF_ERR_INVALID_ARGUMENT;
+  AdjSchedule sc;
+  if (checkpoint_every > 0) sc = schedule_fixed(iterations, checkpoint_every);
+  else if (!schedule_fewest(iterations, state_slots, &sc)) return HMF_ERR_OUT_OF_MEMORY;
+  const long long n = (long long)sc.actions.size();
+  for (long long i = 0; i < n && i < capacity; ++i) {
+    actions[4 * i + 0] = sc.actions[i].kind;
+    actions[4 * i + 1] = sc.actions[i].t;
+    actions[4 * i + 2] = sc.actions[i].a;
+    actions[4 * i + 3] = sc.actions[i].b;
+  }
+  return n;
 }
 
 }  // extern "C"

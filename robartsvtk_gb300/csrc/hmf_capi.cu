@@ -482,6 +482,8 @@ int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t 
     hmf::tree_bulk_n_kernel<N><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error); \
     break;
     HMF_TREE_N(2) HMF_TREE_N(3) HMF_TREE_N(4) HMF_TREE_N(5) HMF_TREE_N(6) HMF_TREE_N(7) HMF_TREE_N(8)
+    HMF_TREE_N(9) HMF_TREE_N(10) HMF_TREE_N(11) HMF_TREE_N(12) HMF_TREE_N(13) HMF_TREE_N(14) HMF_TREE_N(15)
+    HMF_TREE_N(16)
 #undef HMF_TREE_N
     default:
       hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);
@@ -848,7 +850,8 @@ int configure_kernels(hmf_ctx* c) {
                           hmf::tree_bulk_smem_bytes(N)),                                      \
      "cudaFuncSetAttribute(tree_bulk_n_kernel)");
   HMF_TREE_N_ATTR(2) HMF_TREE_N_ATTR(3) HMF_TREE_N_ATTR(4) HMF_TREE_N_ATTR(5) HMF_TREE_N_ATTR(6)
-  HMF_TREE_N_ATTR(7) HMF_TREE_N_ATTR(8)
+  HMF_TREE_N_ATTR(7) HMF_TREE_N_ATTR(8) HMF_TREE_N_ATTR(9) HMF_TREE_N_ATTR(10) HMF_TREE_N_ATTR(11)
+  HMF_TREE_N_ATTR(12) HMF_TREE_N_ATTR(13) HMF_TREE_N_ATTR(14) HMF_TREE_N_ATTR(15) HMF_TREE_N_ATTR(16)
 #undef HMF_TREE_N_ATTR
   CK(cudaFuncSetAttribute(hmf::dag_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           4 * hmf::kMaxVertices * hmf::kDagThreads * (int)sizeof(float)),

@@ -109,6 +109,8 @@ struct hmf_ctx {
 
   // reverse-mode state of hmf_solve_adjoint (hmf_adjoint.cu), created on demand
   struct AdjointState* adj = nullptr;
+  long long adj_max_bytes = 0;  // hmf_set_adjoint_memory (0: 85% of the free device memory)
+  int adj_max_slots = 0;        // (0: no cap)
 
   std::string err;
 };

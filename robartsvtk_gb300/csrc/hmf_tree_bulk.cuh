@@ -166,7 +166,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
   }
 }
 
-// The same sweep for trees of N <= 8 entries (the root last, entries in
+// The same sweep for trees of N <= 16 entries (the root last, entries in
 // post-order).  The tree's shape is read once per CTA into registers -- per
 // entry the staged offset of its parent's sink, a bit mask of its children,
 // 1/(kids+1) and the output pointers -- and the chunk length is a

@@ -185,10 +185,26 @@ class HMFSolver:
         return np.array(buf[:], dtype=np.float64)
 
     def adjoint_plan(self) -> dict:
+        """The schedule of the last solve_adjoint: checkpoint interval (0 for
+        the fewest-forward-iterations schedule), recomputed segments, state
+        slots, forward iterations run (first pass included) and backward
+        steps."""
         k = ctypes.c_int()
         r = ctypes.c_int()
         check(self._lib.hmf_get_adjoint_plan(self._ctx, ctypes.byref(k), ctypes.byref(r)), self._ctx)
-        return {"checkpoint_every": k.value, "recomputed_segments": r.value}
+        slots = ctypes.c_int()
+        fwd = ctypes.c_longlong()
+        bwd = ctypes.c_longlong()
+        check(self._lib.hmf_get_adjoint_schedule(self._ctx, ctypes.byref(slots), ctypes.byref(fwd),
+                                                 ctypes.byref(bwd)), self._ctx)
+        return {"checkpoint_every": k.value, "recomputed_segments": r.value, "state_slots": slots.value,
+                "forward_iterations": fwd.value, "backward_steps": bwd.value}
+
+    def set_adjoint_memory(self, max_bytes: int = 0, max_state_slots: int = 0) -> None:
+        """Budget of later automatic (checkpoint_every=0) adjoint plans: device
+        bytes for the adjoint's arrays (0: 85% of the free memory) and a cap on
+        state slots (0: none)."""
+        check(self._lib.hmf_set_adjoint_memory(self._ctx, int(max_bytes), int(max_state_slots)), self._ctx)
 
     def stats(self):
         launches = ctypes.c_longlong()
@@ -353,6 +369,21 @@ def _fetch_energy(call, n, ctx):
     check(call(ctypes.byref(f0), f, n), ctx)
     return f0.value, np.array(f[:], dtype=np.float64)
 
+
+
+def adjoint_schedule(iterations: int, state_slots: int = 0, checkpoint_every: int = 0):
+    """The adjoint's schedule as a list of (kind, t, a, b) actions (host
+    only): kind 0 = forward iteration t from slot a to slot b, 1 = loss on
+    x_T in slot a, 2 = backward step of iteration t with x_t in slot a and
+    x_{t+1} in slot b.  checkpoint_every > 0: fixed interval; 0: fewest
+    forward iterations over `state_slots` slots.  None when infeasible."""
+    lib = _capi.load()
+    n = lib.hmf_adjoint_schedule(int(iterations), int(state_slots), int(checkpoint_every), None, 0)
+    if n < 0:
+        return None
+    buf = (ctypes.c_int * (4 * n))()
+    lib.hmf_adjoint_schedule(int(iterations), int(state_slots), int(checkpoint_every), buf, n)
+    return [tuple(buf[4 * i:4 * i + 4]) for i in range(n)]
 
 def vote(inputs, values=None, semantics: int = REF_CUDA, out=None, stream=None):
     """Label vote over equally sized float32 images (numpy on the host or

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from robartsvtk_gb300 import REF_CPU, HMFBatchSolver, HMFError, HMFSolver
+from robartsvtk_gb300 import REF_CPU, HMFBatchSolver, HMFError, HMFSolver, adjoint_schedule
 from robartsvtk_gb300.synthetic import random_tree_problem
 
 pytestmark = pytest.mark.gpu
@@ -36,8 +36,10 @@ def solver_for(w):
     return s
 
 
-def run_gpu(w, truth, checkpoint_every=0):
+def run_gpu(w, truth, checkpoint_every=0, max_slots=0):
     with solver_for(w) as s:
+        if max_slots:
+            s.set_adjoint_memory(max_state_slots=max_slots)
         loss = s.solve_adjoint(truth, checkpoint_every=checkpoint_every)
         dD = {l: s.data_gradient(l) for l in s.leaves}
         da = s.alpha_gradient()
@@ -84,12 +86,38 @@ def test_adjoint_checkpointing_recomputes_exactly(k, reverse_kernel):
     w, truth = problem(11, (33, 20, 17), iterations=13)
     o = run_oracle(w, truth)
     g = run_gpu(w, truth, checkpoint_every=k)
-    assert g["plan"] == {"checkpoint_every": k, "recomputed_segments": (13 + k - 1) // k - 1}
+    n_ckpt = (13 + k - 1) // k
+    assert g["plan"]["checkpoint_every"] == k and g["plan"]["recomputed_segments"] == n_ckpt - 1
+    assert g["plan"]["state_slots"] == n_ckpt + k
+    assert g["plan"]["forward_iterations"] == 13 + (n_ckpt - 1) * (k - 1)
+    assert g["plan"]["backward_steps"] == 13
     assert_matches(g, o, w, "k=%d" % k)
     # the labels read after the adjoint are the forward solve's
     f = O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, w.iterations, w.step, w.cc)
     for v, u in g["u"].items():
         assert np.array_equal(u, f["u"][v].astype(np.float32)), v
+
+
+@pytest.mark.parametrize("slots", [3, 4, 6])
+def test_adjoint_fewest_forward_schedule_recomputes_exactly(slots, reverse_kernel):
+    """Too few state slots for every state: the revolve-style schedule keeps
+    and recomputes states recursively; the gradients do not change."""
+    w, truth = problem(13, (33, 20, 17), iterations=13)
+    g = run_gpu(w, truth, max_slots=slots)
+    sched = adjoint_schedule(13, slots)
+    assert g["plan"]["checkpoint_every"] == 0 and g["plan"]["state_slots"] == slots
+    assert g["plan"]["forward_iterations"] == sum(1 for a in sched if a[0] == 0) > 13
+    assert_matches(g, run_oracle(w, truth), w, "slots=%d" % slots)
+
+
+def test_adjoint_config5_tree_with_few_slots():
+    """The 15-vertex tree of the large workload (root -> 2 -> 4 -> 8), whose
+    sweep reverse takes the table-driven kernel, under a 5-slot schedule."""
+    parent = [-1, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6]
+    w, truth = problem(17, (26, 21, 15), parent=parent, iterations=11, smooth_nodes=(1, 4, 9))
+    g = run_gpu(w, truth, max_slots=5)
+    assert g["plan"]["state_slots"] == 5
+    assert_matches(g, run_oracle(w, truth), w, "tree8, 5 slots")
 
 
 def test_adjoint_flat_tree_without_smoothness_images(reverse_kernel):
@@ -150,6 +178,13 @@ def test_adjoint_errors():
             s.data_gradient(1)
         with pytest.raises(HMFError, match="eps"):
             s.solve_adjoint(truth, eps=0.0)
+        s.set_adjoint_memory(max_state_slots=2)  # x_0 and one more: no schedule for 3 iterations
+        with pytest.raises(HMFError, match="state slots"):
+            s.solve_adjoint(truth)
+        with pytest.raises(HMFError, match="more than the 2 allowed"):
+            s.solve_adjoint(truth, checkpoint_every=1)
+        with pytest.raises(HMFError, match=">= 0"):
+            s.set_adjoint_memory(max_bytes=-1)
     with HMFSolver(w.dims, w.parent, semantics=REF_CPU) as s:
         with pytest.raises(HMFError, match="REF_CUDA"):
             s.solve_adjoint(truth)
