@@ -161,6 +161,10 @@ int hmf_batch_get_sink(hmf_ctx* ctx, int volume, int node, float* out, int where
  * for contexts of the same shape (volume sizes, tree size, device) created
  * later in the process.  Inputs must be set; the labels are not kept. */
 int hmf_autotune(hmf_ctx* ctx, void* stream);
+/* The flow kernel's z-chunk length (planes each CTA marches): set it (z >= 1;
+ * 0 restores the default plan) or read the current one. */
+int hmf_set_zchunk(hmf_ctx* ctx, int z);
+int hmf_get_zchunk(const hmf_ctx* ctx);
 
 /* ---- Adjoint (reverse mode) -----------------------------------------------
  * No counterpart in the reference, which only solves forward.  Solves like

@@ -282,23 +282,29 @@ int plan_flow(hmf_ctx* c, int zchunk) {
   return HMF_OK;
 }
 
-// Default z chunk: the longest power of two (>= 16 planes) that still gives
-// the launch a few waves of two CTAs per SM.
+// Default z chunk.  A CTA marches its chunk's planes plus three halo planes,
+// so long chunks waste less; but the windows of one wave of CTAs share their
+// halo planes, parent sinks and smoothness images with the windows of the
+// next wave only while those planes are still in L2, and a wave's L2
+// footprint grows with its chunk length (~7 MB per plane for two CTAs per
+// SM).  Measured on GB300: chunks of ~48 planes are fastest while a z chunk
+// takes at most a few waves; when it takes many (the windows of a wave
+// cover about one row of the volume, so every row boundary is crossed
+// between waves) ~24 planes are, up to 2.2x faster than whole-volume chunks.
+// Chunks are balanced: the longest volume is cut into equal chunks.
 int default_zchunk(const hmf_ctx* c) {
-  const long long target = (long long)c->sm_count * 2 * 3;
+  const long long slots = (long long)c->sm_count * 2;  // two flow CTAs per SM
+  long long per_chunk = 0;                             // CTAs of one z chunk of every volume
   int maxz = 1;
-  for (const auto& V : c->vols) maxz = std::max(maxz, V.vz);
-  int z = 16;
-  while (z < maxz) z *= 2;
-  for (;; z /= 2) {
-    long long ctas = 0;
-    for (const auto& V : c->vols) {
-      const long long tiles = (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
-                              ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY);
-      ctas += tiles * ((V.vz + std::min(z, V.vz) - 1) / std::min(z, V.vz)) * (c->n - 1);
-    }
-    if (ctas >= target || z <= 16) return z;
+  for (const auto& V : c->vols) {
+    const long long tiles = (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
+                            ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY);
+    per_chunk += tiles * (c->n - 1);
+    maxz = std::max(maxz, V.vz);
   }
+  const int target = per_chunk > 8 * slots ? 24 : 48;
+  const int chunks = std::max(1, (maxz + target - 1) / target);
+  return (maxz + chunks - 1) / chunks;
 }
 
 // cuTensorMapEncodeTiled, fetched through the runtime so that the library
@@ -1223,15 +1229,17 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   int best_z = c->zchunk;
   double best_ms = 1e30;
   int rc = HMF_OK;
-  for (int z = 16; rc == HMF_OK; z *= 2) {
-    rc = plan_flow(c, std::min(z, maxz));
+  // candidates 16, 24, 32, 48, 64, 96, ... up to the longest volume
+  for (int i = 0; rc == HMF_OK; ++i) {
+    const int z = std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
+    rc = plan_flow(c, z);
     if (rc) break;
     c->iterations = 4;
     c->timing = true;
     rc = hmf_solve(c, stream);
     if (rc) break;
     const double ms = c->kind_count[0] ? c->kind_ms[0] / (double)c->kind_count[0] : 1e30;
-    if (ms < best_ms) best_ms = ms, best_z = std::min(z, maxz);
+    if (ms < best_ms) best_ms = ms, best_z = z;
     if (z >= maxz) break;
   }
   c->iterations = saved_iters;
@@ -1248,6 +1256,18 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   g_tune_cache[tune_key(c)] = best_z;
   return HMF_OK;
 }
+
+int hmf_set_zchunk(hmf_ctx* c, int z) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (z < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the z chunk must be >= 0 (0: default plan)");
+  DeviceGuard dg(c->device);
+  drop_graphs(c);
+  int maxz = 1;
+  for (const auto& V : c->vols) maxz = std::max(maxz, V.vz);
+  return plan_flow(c, z ? std::min(z, maxz) : default_zchunk(c));
+}
+
+int hmf_get_zchunk(const hmf_ctx* c) { return c ? c->zchunk : HMF_ERR_INVALID_ARGUMENT; }
 
 int hmf_batch_get_labels(hmf_ctx* c, int volume, int node, float* out, int where, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;

@@ -104,6 +104,18 @@ class HMFSolver:
     def set_timing(self, enabled: bool) -> None:
         check(self._lib.hmf_set_timing(self._ctx, 1 if enabled else 0), self._ctx)
 
+    def set_zchunk(self, z: int) -> None:
+        """Planes each flow-kernel CTA marches (0: the default plan)."""
+        check(self._lib.hmf_set_zchunk(self._ctx, int(z)), self._ctx)
+
+    def zchunk(self) -> int:
+        return int(self._lib.hmf_get_zchunk(self._ctx))
+
+    def autotune(self, stream=None) -> None:
+        """Time the flow kernel for each candidate z chunk on the current
+        inputs and keep the fastest (hmf_autotune)."""
+        check(self._lib.hmf_autotune(self._ctx, _stream_handle(stream)), self._ctx)
+
     # -- run ------------------------------------------------------------
     def solve(self, stream=None) -> None:
         check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)

@@ -223,3 +223,29 @@ def test_large_tree_uses_small_chunks():
     parent = [-1] + [0] * 4 + [1, 1, 2, 2, 3, 3, 4, 4] + [5, 5, 6, 6, 7, 7, 8]
     w = random_tree_problem(32, (40, 21, 13), parent, iterations=6, smooth_nodes=(3, 9))
     assert_same(run_gpu(w), oracle(w), "20-vertex tree")
+
+
+@pytest.mark.parametrize("z", [1, 2, 3, 5, 16, 0])
+def test_z_chunk_lengths_are_bitexact(z):
+    """The flow kernel's work plan does not change results: chunks of a few
+    planes (halo planes of both neighbours recomputed), the default plan and
+    the 15-vertex tree of the large workload."""
+    for dims, parent in (((45, 30, 23), [-1, 0, 0, 1, 1, 2, 2]),
+                         ((33, 29, 19), [-1, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6])):
+        w = random_tree_problem(41, dims, parent, iterations=7, smooth_nodes=(1, 4))
+        with HMFSolver(w.dims, w.parent) as s:
+            for leaf, d in w.data.items():
+                s.set_data(leaf, d)
+            for v, S in w.smooth.items():
+                s.set_smoothness(v, S)
+            for v, a in w.alpha.items():
+                s.set_smoothness_scalar(v, a)
+            s.set_params(w.iterations, w.step, w.cc)
+            s.set_zchunk(z)
+            assert s.zchunk() == (z if z else s.zchunk()) and 1 <= s.zchunk() <= dims[2]
+            s.solve()
+            ref = oracle(w)
+            for v in range(len(parent)):
+                assert np.array_equal(s.sink(v), ref["sink"][v].astype(np.float32)), (z, dims, v)
+                if parent[v] >= 0:
+                    assert np.array_equal(s.labels(v), ref["u"][v].astype(np.float32)), (z, dims, v)
