@@ -5,12 +5,13 @@
 //
 // A persistent CTA walks chunks of 256 consecutive voxels of the pitched
 // layout (padding columns included: their values are finite and never read
-// back).  For every chunk thread 0 issues one cp.async.bulk per input array
-// -- per vertex the sweep parts of the later state's sink and label
+// back).  For every chunk lane v of warp 0 issues vertex v's cp.async.bulk
+// copies, one per input array -- per vertex the sweep parts of the later state's sink and label
 // adjoints, the later flow reverse's gb, the sink and label before the
 // iteration, the sink and divergence after it, the data term and the
 // accumulated data-term gradient (double) -- into one of two shared-memory
-// stages, so the next chunk streams in while this one is reversed.  Stage
+// stages; a stage is refilled as soon as its chunk has been read into
+// registers, so two chunks stream in while one is reversed.  Stage
 // slots sit at fixed [quantity][vertex] positions (absent quantities are not
 // copied and not read), so every shared-memory offset is a compile-time
 // constant; one thread reverses one voxel with all per-vertex values in
@@ -123,11 +124,11 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
     const long long v0 = chunk * kSwVc;
     const int len = (int)min((long long)kSwVc, G.vol - v0);
     const int q = threadIdx.x;
+    float SBN[N], UB[N], GB[N], AS[N], AU[N], BS[N], BD[N], D[N];
+    double DB[N];
+    bool hit[N];
     if (q < len) {
       auto at = [&](int kind, int v) { return st[(kind * N + v) * kSwVc + q]; };
-      float SBN[N], UB[N], GB[N], AS[N], AU[N], BS[N], BD[N], D[N];
-      double DB[N];
-      bool hit[N];
 #pragma unroll
       for (int v = 0; v < N; ++v) {
         const bool nr = v != root, leaf = T.n_kids[v] == 0;
@@ -142,6 +143,16 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
         BD[v] = nr ? at(kSwBD, v) : 0.f;
         hit[v] = false;
       }
+    }
+    // Every value of the chunk is in registers now: stage s is free.  Order
+    // these generic reads before the bulk copies that refill it (async
+    // proxy), then issue the chunk after next, so that two chunks stream in
+    // while this one is reversed.
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x < N && chunk + 2LL * gridDim.x < nchunks)
+      issue(chunk + 2LL * gridDim.x, s, threadIdx.x), ++nissued[s];
+    if (q < len) {
       // full adjoints of the later state: sinks (sweep part, then the flow
       // part vertex by vertex in id order: own +step*gb, children's -step*gb)
       // and labels (sweep part - step*icc*gb)
@@ -255,12 +266,6 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
         if (hit[v]) T.Db[v][i] = DB[v];
       }
     }
-    // order this chunk's generic reads of stage s before the bulk copy that
-    // refills it (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (threadIdx.x < N && chunk + 2LL * gridDim.x < nchunks)
-      issue(chunk + 2LL * gridDim.x, s, threadIdx.x), ++nissued[s];
   }
   if (timed_out && error_flag) atomicOr(error_flag, 2);
   if (threadIdx.x == 0 && timed_out)
