@@ -105,6 +105,23 @@ def test_energy_standalone_matches_oracle():
     np.testing.assert_allclose(fd, o["f"], rtol=1e-11, atol=0)
 
 
+@pytest.mark.parametrize("dims", [(1, 1, 1), (1, 7, 5), (33, 9, 3), (64, 17, 70), (5, 40, 1), (40, 1, 33),
+                                  (97, 23, 41)])
+def test_energy_march_shapes(dims):
+    """The z-marching kernel's tiles (32 x 8 columns) and z chunks on ragged
+    and degenerate volumes: partial tiles, one-voxel axes, chunk borders."""
+    rng = np.random.default_rng(sum(dims))
+    shape = dims[::-1]
+    leaves = [3, 4, 5, 6]
+    lab = {l: rng.random(shape).astype(np.float32) for l in leaves}
+    dat = {l: rng.random(shape).astype(np.float32) for l in leaves}
+    sm = {2: rng.random(shape).astype(np.float32), 5: rng.random(shape).astype(np.float32)}
+    o = O.energy(dims, PARENT, dat, lab, sm)
+    f0, f = decomposition_energy(dims, PARENT, dat, lab, sm)
+    assert abs(f0 - o["f0"]) <= 1e-11 * abs(o["f0"])
+    np.testing.assert_allclose(f, o["f"], rtol=1e-11, atol=1e-30)
+
+
 def test_energy_large_tree_and_dense_quads():
     """Eleven non-root vertices (past the register-resident kernels' eight) and
     rows a multiple of four wide (the four-voxel vote)."""
