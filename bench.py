@@ -254,9 +254,9 @@ def run_ours(args):
     import numpy as np
     import torch
 
-    from robartsvtk_gb300 import HMFSolver
+    from robartsvtk_gb300 import HMFSolver, replicas
 
-    rank, world, local = dist_env()
+    rank, world, local = replicas.rank_env()
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -289,8 +289,7 @@ def run_ours(args):
     for _ in range(max(3, args.warmup)):
         solver.solve(stream)
     stream.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
@@ -304,15 +303,12 @@ def run_ours(args):
     e1.record(stream)
     stream.synchronize()
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier()
     clock_info = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * units_per_step / (ms / 1000.0)
+    ms_rank = e0.elapsed_time(e1) / args.steps
+    # every rank solved its own volume: the job's units over its slowest rank's time
+    value = replicas.job_throughput(units_per_step, ms_rank, "cuda")
+    ms = replicas.max_over_ranks(ms_rank, "cuda")
 
     # ---- per-kernel device times (events around every launch) -------------
     solver.set_timing(True)
@@ -344,8 +340,7 @@ def run_ours(args):
             solver.labels(leaf, out=h_out[leaf], stream=stream)
 
     e2e_step()
-    if dist:
-        dist.barrier()
+    replicas.barrier()
     e_steps = max(2, min(args.steps, 3))
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
@@ -355,12 +350,9 @@ def run_ours(args):
         e2e_step()
     e3.record(stream)
     stream.synchronize()
-    e2e_ms = e2.elapsed_time(e3) / e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * units_per_step / (e2e_ms / 1000.0)
+    e2e_rank_ms = e2.elapsed_time(e3) / e_steps
+    e2e_value = replicas.job_throughput(units_per_step, e2e_rank_ms, "cuda")
+    e2e_ms = replicas.max_over_ranks(e2e_rank_ms, "cuda")
 
     # ---- roofline -----------------------------------------------------------
     peak, peak_kind = measured_peak_hbm()
