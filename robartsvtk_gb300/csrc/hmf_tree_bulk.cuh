@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
-    for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], A);  // one arrival per staged array
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -223,25 +223,30 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
   const float icc = T.icc, cc = T.cc, w0r = T.root_init;
   const long long nchunks = (G.vol + VC - 1) / VC;
 
-  auto issue = [&](long long chunk, int s) {  // thread 0 only
+  // Staged array a of a chunk is copied by thread a (a < A), each copy with
+  // its own expected bytes and mbarrier arrival: per entry e < R its
+  // divergence (3e), label (3e+1) and sink or data term (3e+2); the source
+  // flow (3R).
+  const int ta = threadIdx.x;
+  const float* asrc = nullptr;
+  if (ta < 3 * R) {
+    const TreeEntry& E = T.e[ta / 3];
+    asrc = ta % 3 == 0 ? E.div : ta % 3 == 1 ? E.label : (E.n_kids ? E.sink : E.data);
+  } else if (ta == 3 * R) {
+    asrc = T.e[R].sink;
+  }
+  auto issue = [&](long long chunk, int s) {  // threads 0 .. A-1
     const long long v0 = chunk * VC;
     const unsigned bytes = (unsigned)(min((long long)VC, G.vol - v0) * 4);
     uint64_t* bar = &bars[s];
-    float* dst = reinterpret_cast<float*>(stage0 + s * A * Q);
-    mbar_expect_tx(bar, bytes * (unsigned)A);
-    for (int e = 0; e < R; ++e) {
-      const TreeEntry& E = T.e[e];
-      bulk_load(dst + (3 * e) * VC, E.div + v0, bytes, bar);
-      bulk_load(dst + (3 * e + 1) * VC, E.label + v0, bytes, bar);
-      bulk_load(dst + (3 * e + 2) * VC, (E.n_kids ? E.sink : E.data) + v0, bytes, bar);
-    }
-    bulk_load(dst + (3 * R) * VC, T.e[R].sink + v0, bytes, bar);
+    mbar_expect_tx(bar, bytes);
+    bulk_load(reinterpret_cast<float*>(stage0 + s * A * Q) + ta * VC, asrc + v0, bytes, bar);
   };
 
   bool timed_out = false;
-  int nissued[kTreeBulkStages] = {0, 0};  // kept by thread 0
+  int nissued[kTreeBulkStages] = {0, 0};  // kept by every issuing thread
   long long chunk = blockIdx.x;
-  if (threadIdx.x == 0) {
+  if (ta < A) {
     if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
     if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
   }
@@ -270,15 +275,24 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
         } else {
           const float w0 = e == R ? w0r : 0.0f;
           float4 W = make_float4(w0, w0, w0, w0);
+          auto add_child = [&](int k) {
+            const float4 sc = b[ss(k) * Q], dc = b[(3 * k) * Q], uc = b[(3 * k + 1) * Q];
+            W.x = ((W.x + sc.x) + dc.x) - uc.x * icc;
+            W.y = ((W.y + sc.y) + dc.y) - uc.y * icc;
+            W.z = ((W.z + sc.z) + dc.z) - uc.z * icc;
+            W.w = ((W.w + sc.w) + dc.w) - uc.w * icc;
+          };
+          if constexpr (N <= 8) {
 #pragma unroll
-          for (int k = 0; k < e; ++k)
-            if (kmask[e] >> k & 1u) {
-              const float4 sc = b[ss(k) * Q], dc = b[(3 * k) * Q], uc = b[(3 * k + 1) * Q];
-              W.x = ((W.x + sc.x) + dc.x) - uc.x * icc;
-              W.y = ((W.y + sc.y) + dc.y) - uc.y * icc;
-              W.z = ((W.z + sc.z) + dc.z) - uc.z * icc;
-              W.w = ((W.w + sc.w) + dc.w) - uc.w * icc;
-            }
+            for (int k = 0; k < e; ++k)
+              if (kmask[e] >> k & 1u) add_child(k);
+          } else {
+            // children in increasing entry order, as a loop over the mask's
+            // set bits: unrolling all N^2 (entry, child) pairs overflows the
+            // instruction cache for large trees
+#pragma unroll 1
+            for (unsigned m = kmask[e]; m; m &= m - 1u) add_child(__ffs(m) - 1);
+          }
           if (e != R) {
             const float4 inc = b[poff[e]], d = b[(3 * e) * Q], u = b[(3 * e + 1) * Q];
             W.x = ((W.x + inc.x) - d.x) + u.x * icc;
@@ -306,7 +320,7 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // stage s is free again
-    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+    if (ta < A && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
   if (timed_out && error_flag) atomicOr(error_flag, 2);
   if (threadIdx.x == 0 && timed_out)
