@@ -335,7 +335,10 @@ __global__ void __launch_bounds__(kDagNVc)
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
-    for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], 1);
+    // one arrival per copied array: 4 per non-root node, the data term of
+    // each leaf, the root sink
+    const unsigned narr = 4u * (N - 1) + 1u + (unsigned)__popc(P.leaf_mask & ((1u << N) - 2u));
+    for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], narr);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -345,30 +348,32 @@ __global__ void __launch_bounds__(kDagNVc)
   const long long nchunks = (n_vox + VC - 1) / VC;
   auto slot_s = [](int e) { return e ? 4 * (e - 1) : ROOT; };
 
-  auto issue = [&](long long chunk, int s) {  // thread 0 only
+  // Staged slot a of a chunk is copied by thread a, with its own expected
+  // bytes and mbarrier arrival: node e's sink, source, divergence and label
+  // (slots 4(e-1) .. 4(e-1)+3), a leaf's data term (4(N-1) + e-1; absent for
+  // branches: no copy, no arrival), the root sink (ROOT).
+  const int ta = threadIdx.x;
+  const float* asrc = nullptr;
+  if (ta < 4 * (N - 1)) {
+    const int e = ta / 4 + 1, kind = ta % 4;
+    asrc = kind == 0 ? P.sink[e] : kind == 1 ? P.inc[e] : kind == 2 ? P.div[e] : P.label[e];
+  } else if (ta < ROOT) {
+    const int e = ta - 4 * (N - 1) + 1;
+    if ((P.leaf_mask >> e) & 1u) asrc = P.data[e];
+  } else if (ta == ROOT) {
+    asrc = P.sink[0];
+  }
+  auto issue = [&](long long chunk, int s) {  // threads with a slot to fill
     const long long v0 = chunk * VC;
     const unsigned bytes = (unsigned)(min((long long)VC, n_vox - v0) * 4);
-    float* dst = stage0 + (size_t)s * A * VC;
-    unsigned arrays = 4 * (N - 1) + 1;
-#pragma unroll
-    for (int e = 1; e < N; ++e) arrays += (P.leaf_mask >> e) & 1u;
-    mbar_expect_tx(&bars[s], bytes * arrays);
-#pragma unroll
-    for (int e = 1; e < N; ++e) {
-      float* d = dst + (4 * (e - 1)) * VC;
-      bulk_load(d, P.sink[e] + v0, bytes, &bars[s]);
-      bulk_load(d + VC, P.inc[e] + v0, bytes, &bars[s]);
-      bulk_load(d + 2 * VC, P.div[e] + v0, bytes, &bars[s]);
-      bulk_load(d + 3 * VC, P.label[e] + v0, bytes, &bars[s]);
-      if ((P.leaf_mask >> e) & 1u) bulk_load(dst + (4 * (N - 1) + e - 1) * VC, P.data[e] + v0, bytes, &bars[s]);
-    }
-    bulk_load(dst + ROOT * VC, P.sink[0] + v0, bytes, &bars[s]);
+    mbar_expect_tx(&bars[s], bytes);
+    bulk_load(stage0 + (size_t)s * A * VC + (size_t)ta * VC, asrc + v0, bytes, &bars[s]);
   };
 
   bool timed_out = false;
-  int nissued[kDagBulkStages] = {0, 0};  // kept by thread 0
+  int nissued[kDagBulkStages] = {0, 0};  // kept by every issuing thread
   long long chunk = blockIdx.x;
-  if (threadIdx.x == 0) {
+  if (asrc) {
     if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
     if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
   }
@@ -440,7 +445,7 @@ __global__ void __launch_bounds__(kDagNVc)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // stage s is free again
-    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+    if (asrc && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
   if (timed_out && error_flag) atomicOr(error_flag, 2);
   if (threadIdx.x == 0 && timed_out)
