@@ -15,8 +15,9 @@
 // adj_flow_tma_kernel reverses the flow step of every vertex
 // (HMF_ADJOINT_KERNEL=chain selects adj_tree_kernel and the unfused
 // per-vertex kernels of hmf_adjoint.cuh instead; same results).  Memory:
-// the schedule's slots of 6(n-1)+1 arrays, plus 13n float arrays (+11 for
-// the unfused kernels) and one double array per leaf.
+// the schedule's slots of 6(n-1)+1 arrays, plus 7n float arrays (+11 for
+// the unfused kernels) and one double array per leaf; the second set of flow
+// adjoints uses the solver's second flow set.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,11 +53,19 @@ struct AdjointState {
   char* arena = nullptr;
   size_t bytes = 0;
   float* slots = nullptr;             // n_slots state slots
-  float* sb[2] = {nullptr, nullptr};  // [v*arr] sweep part of the sinks' adjoint (ping-pong)
-  float* ub[2] = {nullptr, nullptr};  // [v*arr] sweep part of the labels' adjoint
+  // [v*arr] sweep part of the sinks' / labels' adjoint.  The sweep reverse
+  // reads and writes them voxel by voxel (every read of a voxel before its
+  // write, in the same thread), so the old and new parts share one array:
+  // sb[1] == sb[0], ub[1] == ub[0].
+  float* sb[2] = {nullptr, nullptr};
+  float* ub[2] = {nullptr, nullptr};
   float* gb = nullptr;                // [v*arr] adjoint of g of the flow reverse
   float* dbp = nullptr;               // [v*arr]
-  float* Pb = nullptr;                // [((parity*n + v)*3 + axis)*arr], two sets
+  // Adjoint of the flows, two sets (the reverse flow kernel reads one and
+  // writes the other: its windows read halos their neighbours write).  Set 0
+  // is Pb [(v*3 + axis)*arr]; set 1 is the solver's second flow set, idle
+  // while the adjoint runs (the forward iterations use the state slots).
+  float* Pb = nullptr;
   int pb_par = 0;                     // the set holding the current adjoint of the flows
   float* tmp = nullptr;               // kAdjTemps arrays
   double* Db = nullptr;               // [leaf index * arr]
@@ -113,7 +122,7 @@ int plan(hmf_ctx* c, int T, int k_req) {
   const size_t slot_bytes = (size_t)A * arr * sizeof(float);
   const int L = (int)c->leaves.size();
   const int temps = S->chain ? kAdjTemps : 0;  // scratch of the unfused reverse kernels only
-  const size_t fixed = ((size_t)(13 * c->n + temps) * arr) * sizeof(float) + (size_t)L * arr * sizeof(double) +
+  const size_t fixed = ((size_t)(7 * c->n + temps) * arr) * sizeof(float) + (size_t)L * arr * sizeof(double) +
                        (size_t)arr * sizeof(int) + 4096;
   // state slots that fit: the caller's byte budget, else 85% of the free
   // device memory (the held arena is reusable); the caller's slot cap
@@ -176,11 +185,11 @@ int plan(hmf_ctx* c, int T, int k_req) {
     return r;
   };
   S->slots = takef((size_t)n_slots * A);
-  for (int q = 0; q < 2; ++q) S->sb[q] = takef(c->n);
-  for (int q = 0; q < 2; ++q) S->ub[q] = takef(c->n);
+  S->sb[0] = S->sb[1] = takef(c->n);
+  S->ub[0] = S->ub[1] = takef(c->n);
   S->gb = takef(c->n);
   S->dbp = takef(c->n);
-  S->Pb = takef(6 * (size_t)c->n);
+  S->Pb = takef(3 * (size_t)c->n);
   S->tmp = temps ? takef(temps) : nullptr;
   S->Db = reinterpret_cast<double*>(p);
   p += (size_t)L * arr * sizeof(double);
@@ -208,7 +217,8 @@ int plan(hmf_ctx* c, int T, int k_req) {
 }
 
 float* pb_array(const AdjointState* S, const hmf_ctx* c, int parity, int v, int axis) {
-  return S->Pb + ((size_t)(parity * c->n + v) * 3 + axis) * S->arr;
+  if (parity == 0) return S->Pb + ((size_t)v * 3 + axis) * S->arr;
+  return axis == 0 ? c->fx[1][v] : axis == 1 ? c->fy[1][v] : c->fz[1][v];  // null for the root (no flows)
 }
 
 // Windows of at most 27 x 27 outputs spread evenly over the volume; z chunk:
@@ -630,8 +640,9 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
   CK(cudaMemcpyAsync(S->truth, truth, dense * sizeof(int),
                      where == HMF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s),
      "cudaMemcpyAsync(truth)");
-  // zero the adjoints (sb, ub, gb, dbp and both Pb sets are contiguous) and accumulators
-  CK(cudaMemsetAsync(S->sb[0], 0, (size_t)13 * n * arr * sizeof(float), s), "cudaMemsetAsync(adjoints)");
+  // zero the adjoints (sb, ub, gb, dbp and the first Pb set are contiguous; the
+  // second set is written before it is read) and accumulators
+  CK(cudaMemsetAsync(S->sb[0], 0, (size_t)7 * n * arr * sizeof(float), s), "cudaMemsetAsync(adjoints)");
   S->pb_par = 0;
   CK(cudaMemsetAsync(S->Db, 0, c->leaves.size() * arr * sizeof(double), s), "cudaMemsetAsync(gradients)");
   CK(cudaMemsetAsync(S->scal, 0, sizeof(double) * (1 + hmf::kMaxVertices), s), "cudaMemsetAsync(scalars)");
