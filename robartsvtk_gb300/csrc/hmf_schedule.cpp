@@ -20,7 +20,10 @@
 #include "hmf_schedule.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
+#include <map>
+#include <mutex>
 
 namespace hmfi {
 namespace {
@@ -230,8 +233,43 @@ AdjSchedule schedule_fixed(int T, int k) {
   return S;
 }
 
+// The dynamic program costs about T^2 * min(S, T) / 3 steps (~20-30 ns each
+// on a host core).  Beyond kDpMaxWork steps, checkpoints every k <= sqrt(T)
+// iterations are used instead when they fit (about two forward passes, close
+// to the optimum with that many slots); the dynamic program runs only when
+// they do not.  Schedules are cached per (T, S): a training loop calls the
+// adjoint with the same iteration count and memory budget again and again.
+constexpr double kDpMaxWork = 5.0e7;
+
+bool schedule_fewest_uncached(int T, int slots, AdjSchedule* out);
+
 bool schedule_fewest(int T, int slots, AdjSchedule* out) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, AdjSchedule> cache;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find({T, slots});
+    if (it != cache.end()) {
+      *out = it->second;
+      return true;
+    }
+  }
+  if (!schedule_fewest_uncached(T, slots, out)) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  if (cache.size() > 64) cache.clear();
+  cache[{T, slots}] = *out;
+  return true;
+}
+
+bool schedule_fewest_uncached(int T, int slots, AdjSchedule* out) {
   if (T < 0 || slots < 1) return false;
+  if (T > 0 && slots < T + 1 && (double)T * T * std::min(slots, T) / 3.0 > kDpMaxWork) {
+    for (int k = std::max(1, (int)std::ceil(std::sqrt((double)T))); k >= 1; --k)
+      if ((T + k - 1) / k + k <= slots) {
+        *out = schedule_fixed(T, k);
+        return true;
+      }
+  }
   AdjSchedule S;
   if (T == 0) {
     S.slots = 1;
@@ -256,13 +294,8 @@ bool schedule_fewest(int T, int slots, AdjSchedule* out) {
 }
 
 long long schedule_fewest_cost(int T, int slots) {
-  if (T < 0 || slots < 1) return -1;
-  if (T == 0) return 0;
-  if (slots >= T + 1) return T;
-  Dp dp;
-  dp.solve(T, slots);
-  const long long c = dp.P(T, slots - 1);
-  return c >= kInf ? -1 : c;
+  AdjSchedule sc;
+  return schedule_fewest(T, slots, &sc) ? sc.forward : -1;
 }
 
 }  // namespace hmfi

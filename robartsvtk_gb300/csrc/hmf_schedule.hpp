@@ -45,7 +45,9 @@ struct AdjSchedule {
 AdjSchedule schedule_fixed(int T, int k);
 
 // Fewest forward iterations with at most `slots` state slots; false when no
-// schedule exists (T >= 2 needs at least 3 slots; few slots limit T).
+// schedule exists (T >= 2 needs at least 3 slots).  For long runs
+// (T^2 * min(slots, T) / 3 above 5e7) checkpoints every k <= sqrt(T)
+// iterations are used instead when they fit.  Cached per (T, slots).
 bool schedule_fewest(int T, int slots, AdjSchedule* out);
 
 // Forward iterations of schedule_fewest(T, slots), -1 when infeasible.
