@@ -288,23 +288,38 @@ int plan_flow(hmf_ctx* c, int zchunk) {
 // next wave only while those planes are still in L2, and a wave's L2
 // footprint grows with its chunk length (~7 MB per plane for two CTAs per
 // SM).  Measured on GB300: chunks of ~48 planes are fastest while a z chunk
-// takes at most a few waves; when it takes many (the windows of a wave
-// cover about one row of the volume, so every row boundary is crossed
-// between waves) ~24 planes are, up to 2.2x faster than whole-volume chunks.
-// Chunks are balanced: the longest volume is cut into equal chunks.
+// takes at most a few waves; when it takes many (the windows of a wave cover
+// about one row of the volume, so every row boundary is crossed between
+// waves) ~24 planes are, up to 2.2x faster than whole-volume chunks.  Within
+// that cap the chunk count minimises waves x (planes + 3 halo + ~4 planes'
+// worth of per-CTA set-up): small volumes get short chunks, so that their
+// few windows still spread over the SMs.  Chunks are balanced (the deepest
+// volume cut into equal chunks).
 int default_zchunk(const hmf_ctx* c) {
-  const long long slots = (long long)c->sm_count * 2;  // two flow CTAs per SM
-  long long per_chunk = 0;                             // CTAs of one z chunk of every volume
+  const long long slots = std::max(1, c->sm_count) * 2LL;  // two flow CTAs per SM
+  long long per_chunk = 0;                                  // CTAs of one z chunk of every volume
   int maxz = 1;
   for (const auto& V : c->vols) {
-    const long long tiles = (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
-                            ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY);
-    per_chunk += tiles * (c->n - 1);
+    per_chunk += (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
+                 ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY) * (c->n - 1);
     maxz = std::max(maxz, V.vz);
   }
-  const int target = per_chunk > 8 * slots ? 24 : 48;
-  const int chunks = std::max(1, (maxz + target - 1) / target);
-  return (maxz + chunks - 1) / chunks;
+  const int cap = per_chunk > 8 * slots ? 24 : 48;
+  int best_z = 1;
+  double best = 1e300;
+  for (int chunks = 1; chunks <= maxz; ++chunks) {
+    const int z = (maxz + chunks - 1) / chunks;
+    if (z > cap) continue;
+    long long ctas = 0;
+    for (const auto& V : c->vols) {
+      const int zv = std::min(z, V.vz);
+      ctas += (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
+              ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY) * ((V.vz + zv - 1) / zv) * (c->n - 1);
+    }
+    const double cost = (double)((ctas + slots - 1) / slots) * (double)(z + 7);
+    if (cost < best) best = cost, best_z = z;  // ties keep the longer chunk
+  }
+  return best_z;
 }
 
 // cuTensorMapEncodeTiled, fetched through the runtime so that the library
@@ -1229,9 +1244,11 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   int best_z = c->zchunk;
   double best_ms = 1e30;
   int rc = HMF_OK;
-  // candidates 16, 24, 32, 48, 64, 96, ... up to the longest volume
-  for (int i = 0; rc == HMF_OK; ++i) {
-    const int z = std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
+  // candidates: the default plan's chunk, then 16, 24, 32, 48, 64, 96, ...
+  // up to the longest volume
+  const int z_default = default_zchunk(c);
+  for (int i = -1; rc == HMF_OK; ++i) {
+    const int z = i < 0 ? z_default : std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
     rc = plan_flow(c, z);
     if (rc) break;
     c->iterations = 4;
@@ -1240,7 +1257,7 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
     if (rc) break;
     const double ms = c->kind_count[0] ? c->kind_ms[0] / (double)c->kind_count[0] : 1e30;
     if (ms < best_ms) best_ms = ms, best_z = z;
-    if (z >= maxz) break;
+    if (i >= 0 && z >= maxz) break;
   }
   c->iterations = saved_iters;
   c->timing = saved_timing;
