@@ -120,6 +120,14 @@ def test_adjoint_config5_tree_with_few_slots():
     assert_matches(g, run_oracle(w, truth), w, "tree8, 5 slots")
 
 
+def test_adjoint_twenty_vertex_tree(reverse_kernel):
+    """Twenty vertices (the staged sweep reverse for 9..32 vertices, leaves
+    at several depths, ids not in pre-order) and the unfused chain."""
+    parent = [-1, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 6, 6, 7, 8, 9, 9, 9]
+    w, truth = problem(23, (27, 19, 14), parent=parent, iterations=8, smooth_nodes=(2, 7, 13))
+    assert_matches(run_gpu(w, truth), run_oracle(w, truth), w, "tree20")
+
+
 def test_adjoint_flat_tree_without_smoothness_images(reverse_kernel):
     w, truth = problem(21, (40, 24, 18), parent=[-1, 0, 0, 0, 0], iterations=10, smooth_nodes=())
     assert_matches(run_gpu(w, truth), run_oracle(w, truth), w, "flat4")
