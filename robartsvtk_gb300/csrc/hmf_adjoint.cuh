@@ -190,9 +190,16 @@ __global__ void __launch_bounds__(kAdjTreeThreads) adj_tree_kernel(const AdjTree
   float* DBP = av + 4 * n * nb;
   const float cc = T.cc, icc = T.icc, step_icc = T.step * T.icc;
   const long long arr = S.arr;
+  const bool small = G.vol < (1LL << 31);  // 32-bit voxel coordinates
   for (long long i = (long long)blockIdx.x * nb + t; i < G.vol; i += (long long)gridDim.x * nb) {
-    int x, y, z;
-    if (!adj_coords(G, i, x, y, z)) continue;
+    if (small) {
+      const unsigned iu = (unsigned)i, r = iu % (unsigned)G.plane;
+      if (r % (unsigned)G.pitch >= (unsigned)G.vx) continue;  // a padding column
+    } else {
+      int x, y, z;
+      if (!adj_coords(G, i, x, y, z)) continue;
+    }
+#pragma unroll 4
     for (int v = 0; v < n; ++v) {
       SBN[v * nb + t] = adj_sink_adjoint(T, v, S.sbn, S.gbn, arr, i);
       SBO[v * nb + t] = 0.0f;
@@ -201,6 +208,7 @@ __global__ void __launch_bounds__(kAdjTreeThreads) adj_tree_kernel(const AdjTree
       if (v != root) DN[v * nb + t] = S.stB[((long long)T.sbase[v] + kAdjDiv) * arr + i];
     }
     // labels: u' = sat(u + cc*((s'_parent - d') - s'))
+#pragma unroll 4
     for (int v = 0; v < n; ++v) {
       if (v == root) continue;
       const int p = T.parent[v];
