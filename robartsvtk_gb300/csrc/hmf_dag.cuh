@@ -191,13 +191,15 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
   uint64_t* bars = reinterpret_cast<uint64_t*>(db_raw);  // [kDagBulkStages]
   float* const stage0 = reinterpret_cast<float*>(db_raw + 128);
   dag_copy_table(T, table);
+  __syncthreads();  // thread 0 reads the table below
   if (threadIdx.x == 0) {
     abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
     if (smem_addr(db_raw) & 15) {
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
-    for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], 1);
+    // one arrival per staged array (the copies are spread over the threads)
+    for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], (unsigned)dag_bulk_arrays(T.n, T.n_leaves));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -214,31 +216,34 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
   const long long nchunks = (n_vox + VC - 1) / VC;
   const float cc = T.cc, icc = T.icc;
 
-  auto issue = [&](long long chunk, int s) {  // thread 0 only
+  // Staged slot c of a chunk is copied by thread c (c, c + blockDim, ...),
+  // each copy with its own expected bytes and mbarrier arrival: entry e's
+  // sink, source, divergence and label (slots 4(e-1) .. 4(e-1)+3), leaf j's
+  // data term (4(n-1) + j), the root sink (root_slot).
+  auto slot_src = [&](int c) -> const float* {
+    if (c < 4 * (n - 1)) {
+      const DagEntry& E = T.e[c / 4 + 1];
+      const int kind = c % 4;
+      return kind == 0 ? E.sink : kind == 1 ? E.inc : kind == 2 ? E.div : E.label;
+    }
+    if (c < root_slot) return T.e[T.leaves[c - 4 * (n - 1)]].data;
+    return T.e[0].sink;
+  };
+  auto issue = [&](long long chunk, int s) {
     const long long v0 = chunk * VC;
     const unsigned bytes = (unsigned)(min((long long)VC, n_vox - v0) * 4);
     float* dst = stage0 + (size_t)s * A * VC;
-    mbar_expect_tx(&bars[s], bytes * (unsigned)A);
-    for (int e = 1; e < n; ++e) {
-      const DagEntry& E = T.e[e];
-      float* d = dst + (size_t)(4 * (e - 1)) * VC;
-      bulk_load(d, E.sink + v0, bytes, &bars[s]);
-      bulk_load(d + VC, E.inc + v0, bytes, &bars[s]);
-      bulk_load(d + 2 * VC, E.div + v0, bytes, &bars[s]);
-      bulk_load(d + 3 * VC, E.label + v0, bytes, &bars[s]);
+    for (int c = threadIdx.x; c < A; c += blockDim.x) {
+      mbar_expect_tx(&bars[s], bytes);
+      bulk_load(dst + (size_t)c * VC, slot_src(c) + v0, bytes, &bars[s]);
     }
-    for (int j = 0; j < nl; ++j)
-      bulk_load(dst + (size_t)(4 * (n - 1) + j) * VC, T.e[T.leaves[j]].data + v0, bytes, &bars[s]);
-    bulk_load(dst + (size_t)root_slot * VC, T.e[0].sink + v0, bytes, &bars[s]);
   };
 
   bool timed_out = false;
-  int nissued[kDagBulkStages] = {0, 0};  // kept by thread 0
+  int nissued[kDagBulkStages] = {0, 0};  // kept by every thread (thread 0 always issues)
   long long chunk = blockIdx.x;
-  if (threadIdx.x == 0) {
-    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
-    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
-  }
+  if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+  if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
     if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
@@ -300,7 +305,7 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
     // the bulk copy that refills the stage (async proxy).
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+    if (chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
   if (timed_out && error_flag) atomicOr(error_flag, 2);
   if (threadIdx.x == 0 && timed_out)

@@ -46,6 +46,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
 
   for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
+  __syncthreads();  // thread 0 reads the table below
   if (threadIdx.x == 0) {
     abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
     // bulk-copy destinations must be 16-byte aligned: refuse to run otherwise.
@@ -53,7 +54,8 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
-    for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], 1);
+    // one arrival per staged array (the copies are spread over the threads)
+    for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], (unsigned)(3 * (T.n - 1) + 1));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -70,28 +72,29 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
   // sink (branch) / data (leaf) 3e+2; the root's source flow -> 3(n-1)
   auto sink_slot = [&](int e) { return e == root ? 3 * root : 3 * e + 2; };
 
-  auto issue = [&](long long chunk, int s) {  // thread 0 only
+  // Staged array c of a chunk is copied by thread c (c, c + blockDim, ...),
+  // each copy with its own expected bytes and mbarrier arrival.
+  auto array_src = [&](int c) -> const float* {
+    if (c == 3 * root) return T.e[root].sink;
+    const TreeEntry& E = T.e[c / 3];
+    return c % 3 == 0 ? E.div : c % 3 == 1 ? E.label : (E.n_kids ? E.sink : E.data);
+  };
+  auto issue = [&](long long chunk, int s) {
     const long long v0 = chunk * vc;
     const unsigned bytes = (unsigned)(min((long long)vc, G.vol - v0) * 4);
     uint64_t* bar = &bars[s];
     float* dst = stage(s);
-    mbar_expect_tx(bar, bytes * (unsigned)arrays);
-    for (int e = 0; e < root; ++e) {
-      const TreeEntry& E = T.e[e];
-      bulk_load(dst + (size_t)(3 * e) * vc, E.div + v0, bytes, bar);
-      bulk_load(dst + (size_t)(3 * e + 1) * vc, E.label + v0, bytes, bar);
-      bulk_load(dst + (size_t)(3 * e + 2) * vc, (E.n_kids ? E.sink : E.data) + v0, bytes, bar);
+    for (int c = threadIdx.x; c < arrays; c += blockDim.x) {
+      mbar_expect_tx(bar, bytes);
+      bulk_load(dst + (size_t)c * vc, array_src(c) + v0, bytes, bar);
     }
-    bulk_load(dst + (size_t)(3 * root) * vc, T.e[root].sink + v0, bytes, bar);
   };
 
   bool timed_out = false;
-  int nissued[kTreeBulkStages] = {0, 0};  // kept by thread 0
+  int nissued[kTreeBulkStages] = {0, 0};  // kept by every thread (thread 0 always issues)
   long long chunk = blockIdx.x;
-  if (threadIdx.x == 0) {
-    if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
-    if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
-  }
+  if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
+  if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
     if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
@@ -154,7 +157,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
     // before the bulk copy that will refill the stage (async proxy).
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // stage s is free again
-    if (threadIdx.x == 0 && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
+    if (chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
   if (timed_out && error_flag) atomicOr(error_flag, 2);
   if (threadIdx.x == 0) {
