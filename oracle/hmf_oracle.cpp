@@ -32,6 +32,7 @@
 // pre-order exactly as CheckInputConsistancy does
 // (vtkHierarchicalMaxFlowSegmentation.cxx:383-398).
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -961,6 +962,68 @@ int ORACLE_ENTRY(int semantics, int precision, int threads, int vx, int vy, int 
 }
 
 #ifndef HMF_ORACLE_WITH_REFERENCE
+// REF_CUDA in FP32 from a given state: `iterations` iterations of the
+// restatement above (after its initialisation from the data terms when init
+// != 0) on the per-vertex state arrays [n_nodes * V] -- flows, divergence and
+// labels of the non-root vertices, the sinks of all (root: source flow) --
+// read and updated in place.  The building block of the slab simulation of a
+// sharded solve (each rank iterates its slab plus halo planes).
+int oracle_hmf_iterate(int threads, int vx, int vy, int vz, int n_nodes, const int* parent,
+                       const float* const* data, const float* const* smooth, const double* alpha, int init,
+                       int iterations, float step, float cc, float* fx, float* fy, float* fz, float* div,
+                       float* u, float* sink) {
+  g_err.clear();
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  if (vx <= 0 || vy <= 0 || vz <= 0) { g_err = "bad dimensions"; return -1; }
+  if ((long)vx * vy * vz > 0x7fffffffL) { g_err = "volume too large for the oracle"; return -1; }
+  Tree t;
+  if (!t.build(n_nodes, parent)) return -2;
+  CudaOracle<float> o(t, vx, vy, vz);
+  o.alloc();
+  o.data.assign(t.n, nullptr);
+  o.smooth.assign(t.n, nullptr);
+  o.alpha.assign(t.n, 1.0f);
+  for (int v = 0; v < t.n; ++v) {
+    o.data[v] = data ? data[v] : nullptr;
+    o.smooth[v] = smooth ? smooth[v] : nullptr;
+    o.alpha[v] = alpha ? (float)alpha[v] : 1.0f;
+  }
+  for (int v = 0; v < t.n; ++v) if (t.leaf(v) && !o.data[v]) { g_err = "missing data term for a leaf"; return -3; }
+  o.step = step;
+  o.cc = cc;
+  o.icc = 1.0f / cc;
+  o.root_work = 1.0f / cc;
+  const long V = o.V;
+  if (init) {
+    o.init();
+  } else {
+    for (int v = 0; v < t.n; ++v) {
+      std::copy(sink + (long)v * V, sink + (long)(v + 1) * V, o.sink[v].begin());
+      if (v == t.root) continue;
+      std::copy(fx + (long)v * V, fx + (long)(v + 1) * V, o.fx[v].begin());
+      std::copy(fy + (long)v * V, fy + (long)(v + 1) * V, o.fy[v].begin());
+      std::copy(fz + (long)v * V, fz + (long)(v + 1) * V, o.fz[v].begin());
+      std::copy(div + (long)v * V, div + (long)(v + 1) * V, o.div[v].begin());
+      std::copy(u + (long)v * V, u + (long)(v + 1) * V, o.u[v].begin());
+    }
+  }
+  for (int it = 0; it < iterations; ++it) o.solve(t.root);
+  for (int v = 0; v < t.n; ++v) {
+    std::copy(o.sink[v].begin(), o.sink[v].end(), sink + (long)v * V);
+    if (v == t.root) continue;
+    std::copy(o.fx[v].begin(), o.fx[v].end(), fx + (long)v * V);
+    std::copy(o.fy[v].begin(), o.fy[v].end(), fy + (long)v * V);
+    std::copy(o.fz[v].begin(), o.fz[v].end(), fz + (long)v * V);
+    std::copy(o.div[v].begin(), o.div[v].end(), div + (long)v * V);
+    std::copy(o.u[v].begin(), o.u[v].end(), u + (long)v * V);
+  }
+  return 0;
+}
+
 // Label vote over n_inputs float images of n voxels (the step after the
 // solve that turns label probabilities into one label per voxel).
 // semantics 0 = vtkCudaImageVote: the running maximum starts at input 0 and

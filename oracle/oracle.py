@@ -104,6 +104,49 @@ def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1,
                  data, smooth, alpha, iterations, step, cc, want_sink, want_div)
 
 
+def iterate(dims, parent, data, state, smooth=None, alpha=None, iterations=1, step=0.1, cc=0.25, init=False,
+            threads=0):
+    """REF_CUDA FP32 iterations from a given state, in place.  `state` = dict
+    of float32 arrays [n, VZ, VY, VX]: "fx", "fy", "fz", "div", "u" (non-root
+    rows used) and "sink" (every row; the root's is the source flow).  With
+    init=True the state is first initialised from the data terms."""
+    lib = port_library()
+    fn = lib.oracle_hmf_iterate
+    fn.restype = ctypes.c_int
+    vx, vy, vz = (int(d) for d in dims)
+    n = len(parent)
+    par = (ctypes.c_int * n)(*[int(p) for p in parent])
+    keep = []
+    dptr = (ctypes.c_void_p * n)()
+    sptr = (ctypes.c_void_p * n)()
+    for v in range(n):
+        if data.get(v) is not None:
+            a = np.ascontiguousarray(data[v], dtype=np.float32).reshape(-1)
+            keep.append(a)
+            dptr[v] = a.ctypes.data
+        if smooth and smooth.get(v) is not None:
+            a = np.ascontiguousarray(smooth[v], dtype=np.float32).reshape(-1)
+            keep.append(a)
+            sptr[v] = a.ctypes.data
+    al = (ctypes.c_double * n)(*[float((alpha or {}).get(v, 1.0)) for v in range(n)])
+    arrs = []
+    for k in ("fx", "fy", "fz", "div", "u", "sink"):
+        a = state[k]
+        if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"] or a.shape != (n, vz, vy, vx):
+            raise ValueError("state[%r] must be a C-contiguous float32 array of shape %r" % (k, (n, vz, vy, vx)))
+        arrs.append(a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    rc = fn(int(threads), vx, vy, vz, n, par, dptr, sptr if smooth else None, al, 1 if init else 0,
+            int(iterations), ctypes.c_float(step), ctypes.c_float(cc), *arrs)
+    if rc != 0:
+        raise RuntimeError("oracle error %d: %s" % (rc, lib.oracle_last_error().decode()))
+
+
+def new_state(dims, n):
+    """Zeroed state arrays for iterate()."""
+    vx, vy, vz = (int(d) for d in dims)
+    return {k: np.zeros((n, vz, vy, vx), np.float32) for k in ("fx", "fy", "fz", "div", "u", "sink")}
+
+
 def solve_reference_cpu(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1,
                         cc=0.25, want_sink=False, want_div=False):
     """REF_CPU through the reference's own compiled utility loops (single thread)."""
