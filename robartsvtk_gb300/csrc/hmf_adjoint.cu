@@ -142,9 +142,9 @@ int plan(hmf_ctx* c, int T, int k_req) {
                     k_req, S->sched.slots, c->adj_max_slots);
       return fail(c, HMF_ERR_OUT_OF_MEMORY, msg);
     }
-  } else if (fit >= (long long)T + 1) {
+  } else if (T > 0 && fit >= (long long)T + 1) {
     S->sched = schedule_fixed(T, T);  // every state kept
-  } else if (!schedule_fewest(T, (int)fit, &S->sched)) {
+  } else if (!schedule_fewest(T, (int)std::min<long long>(fit, INT32_MAX), &S->sched)) {
     char msg[200];
     std::snprintf(msg, sizeof(msg),
                   "%lld state slots of %.1f MB fit in the adjoint's device memory budget; %d iterations need more",
