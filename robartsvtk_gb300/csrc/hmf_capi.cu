@@ -297,13 +297,15 @@ int plan_flow(hmf_ctx* c, int zchunk) {
 // volume cut into equal chunks).
 int default_zchunk(const hmf_ctx* c) {
   const long long slots = std::max(1, c->sm_count) * 2LL;  // two flow CTAs per SM
-  long long per_chunk = 0;                                  // CTAs of one z chunk of every volume
+  long long per_chunk = 0;                                  // CTAs of one z chunk of the largest volume
   int maxz = 1;
   for (const auto& V : c->vols) {
-    per_chunk += (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
-                 ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY) * (c->n - 1);
+    per_chunk = std::max(per_chunk, (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
+                                        ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY) * (c->n - 1));
     maxz = std::max(maxz, V.vz);
   }
+  // a wave covers about one row of windows only when one volume's chunk
+  // takes many waves (a batch of small volumes puts whole volumes in a wave)
   const int cap = per_chunk > 8 * slots ? 24 : 48;
   int best_z = 1;
   double best = 1e300;
