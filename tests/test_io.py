@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from robartsvtk_gb300 import ghmf_segment
-from robartsvtk_gb300.io import Graph, read_metaimage, read_vtk_graph, write_metaimage, write_vtk_graph
+from robartsvtk_gb300.io import read_metaimage, read_vtk_graph, write_metaimage, write_vtk_graph
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.uint8, np.int16, np.uint16])
