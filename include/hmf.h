@@ -20,7 +20,10 @@
  *    memory of the context's GPU (HMF_DEVICE).  Input pointers are borrowed,
  *    as VTK borrows its input images: they must stay valid until the next
  *    hmf_solve() returns.  Host inputs are copied to the device inside
- *    hmf_solve(); device inputs are read in place.
+ *    hmf_solve(); device inputs are read in place.  A pointer passed as
+ *    HMF_DEVICE that is not device memory of the GPU the call runs on (or
+ *    managed memory) is refused with HMF_ERR_INVALID_ARGUMENT before any
+ *    kernel or copy touches it.
  *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  All work
  *    is ordered after the work already queued on it; calls return once the
  *    work is queued (hmf_get_labels to host memory returns after the copy).

@@ -596,6 +596,8 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
   if (!(eps > 0.0) || !(eps < 1.0)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "eps must lie in (0, 1)");
   if (checkpoint_every < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "checkpoint interval must be >= 0");
   DeviceGuard dg(c->device);
+  if (where == HMF_DEVICE)
+    if (int rc = check_device_pointer(c, truth, "ground truth")) return rc;
   if (!c->adj) c->adj = new AdjointState();
   AdjointState* S = c->adj;
   S->done = false;
@@ -719,6 +721,8 @@ int hmf_get_data_gradient(hmf_ctx* c, int leaf, double* out, int where, void* st
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   if (!c->adj || !c->adj->done) return fail(c, HMF_ERR_STATE, "hmf_solve_adjoint has not run");
   DeviceGuard dg(c->device);
+  if (where == HMF_DEVICE)
+    if (int rc = check_device_pointer(c, out, "data gradient output")) return rc;
   const AdjointState* S = c->adj;
   const int j = (int)(std::find(c->leaves.begin(), c->leaves.end(), leaf) - c->leaves.begin());
   const auto& V = c->vols[0];

@@ -64,6 +64,29 @@ int cuda_fail(hmf_ctx* c, cudaError_t e, const char* what) {
               std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+std::string device_pointer_problem(const void* p) {
+  if (!p) return "";
+  cudaPointerAttributes a{};
+  const cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return std::string("not a CUDA address (") + cudaGetErrorString(e) + ")";
+  }
+  if (a.type == cudaMemoryTypeManaged) return "";
+  if (a.type != cudaMemoryTypeDevice) return "host memory passed as device memory (HMF_DEVICE)";
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return "no current CUDA device";
+  if (a.device != dev)
+    return "memory of CUDA device " + std::to_string(a.device) + ", but the call runs on device " +
+           std::to_string(dev);
+  return "";
+}
+
+int check_device_pointer(hmf_ctx* c, const void* p, const char* what) {
+  const std::string why = device_pointer_problem(p);
+  return why.empty() ? HMF_OK : fail(c, HMF_ERR_INVALID_ARGUMENT, std::string(what) + ": " + why);
+}
+
 int build_tree(hmf_ctx* c, const int* par, int n) {
   if (!par) return fail(c, HMF_ERR_TREE, "tree parent array is NULL");
   if (n < 2) return fail(c, HMF_ERR_TREE, "the tree needs a root and at least one leaf");
@@ -914,6 +937,8 @@ int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* s
   if (!out) return fail(c, HMF_ERR_INVALID_ARGUMENT, "output pointer is NULL");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   DeviceGuard dg(c->device);
+  if (where == HMF_DEVICE)
+    if (int rc = check_device_pointer(c, out, "output")) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const auto& V = c->vols[b];
   CK(cudaMemcpy2DAsync(out, (size_t)V.vx * sizeof(float), src + V.off, (size_t)V.pitch * sizeof(float),
@@ -1144,6 +1169,10 @@ int hmf_batch_set_data(hmf_ctx* c, int volume, int node, const float* data, int 
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   if (!c->kids[node].empty())
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "data terms are only used for leaves");
+  if (where == HMF_DEVICE && data) {
+    DeviceGuard dg(c->device);
+    if (int rc = check_device_pointer(c, data, "data term")) return rc;
+  }
   c->data[volume][node] = {data, where};
   return HMF_OK;
 }
@@ -1158,6 +1187,10 @@ int hmf_batch_set_smoothness(hmf_ctx* c, int volume, int node, const float* smoo
   if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   if (node == c->root) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the root has no smoothness term");
+  if (where == HMF_DEVICE && smooth) {
+    DeviceGuard dg(c->device);
+    if (int rc = check_device_pointer(c, smooth, "smoothness image")) return rc;
+  }
   c->smooth[volume][node] = {smooth, where};
   return HMF_OK;
 }
@@ -1488,6 +1521,19 @@ extern "C" int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int 
   for (int v = 0; v < t.n; ++v)
     if (alpha && v != t.root && !(alpha[v] >= 0.0))
       return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "Cannot use a negative smoothness value.");
+  {  // the caller's buffers the kernels and copies will touch
+    std::vector<const void*> bufs;
+    for (int j = 0; j < t.n_leaves; ++j) bufs.push_back(data[t.leaves[j]]);
+    for (int v = 0; v < t.n; ++v)
+      if (v != t.root) {
+        if (smooth) bufs.push_back(smooth[v]);
+        if (labels) bufs.push_back(labels[v]);
+      }
+    for (const void* q : bufs) {
+      const std::string why = device_pointer_problem(q);
+      if (!why.empty()) return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, ("hmf_solve_noalloc: " + why).c_str());
+    }
+  }
   iterations = std::max(0, iterations);
   step_size = std::min(1.0f, std::max(0.0f, step_size));
   cc = std::min(1.0f, std::max(0.0f, cc));

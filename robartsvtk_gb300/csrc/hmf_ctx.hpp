@@ -120,6 +120,15 @@ namespace hmfi {
 int fail(hmf_ctx* c, int code, const std::string& msg);
 int cuda_fail(hmf_ctx* c, cudaError_t e, const char* what);
 
+// A buffer passed as HMF_DEVICE is read or written by kernels and device
+// copies, so it must be device memory of the current device or managed
+// memory.  device_pointer_problem returns "" when `p` (non-null) qualifies,
+// else the reason; check_device_pointer turns that into an error status, so
+// that a host buffer labelled as device memory is refused before any kernel
+// dereferences it.
+std::string device_pointer_problem(const void* p);
+int check_device_pointer(hmf_ctx* c, const void* p, const char* what);
+
 #define CK(call, what)                                  \
   do {                                                  \
     cudaError_t e_ = (call);                            \

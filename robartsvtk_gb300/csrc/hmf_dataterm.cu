@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -260,6 +261,9 @@ int hmf_data_term(int op, int entropy, int normalize, double k1, double c1, doub
   if (in2 && op == HMF_DATA_TERM_SPIKE)
     return fail(c, HMF_ERR_INVALID_ARGUMENT,
                 "the spike operation takes one image (the reference's two-image form writes no output)");
+  if (where == HMF_DEVICE)
+    for (const void* q : {(const void*)in1, (const void*)in2, (const void*)out})
+      if (int rc = check_device_pointer(c, q, "data-term buffer")) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   TermParams P{};
   P.op = op;
@@ -362,6 +366,12 @@ int hmf_log_likelihood(const float* image, int components, const int* const* lab
   if (!(resolution >= FLT_MIN)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "histogram resolution must be positive");
   if (!(required_agreement >= 0.0 && required_agreement <= 1.0))
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "required agreement must lie in [0, 1]");
+  if (where == HMF_DEVICE) {
+    if (int rc = check_device_pointer(c, image, "log-likelihood image")) return rc;
+    if (int rc = check_device_pointer(c, out, "log-likelihood output")) return rc;
+    for (int k = 0; k < n_label_maps; ++k)
+      if (int rc = check_device_pointer(c, label_maps[k], "label map")) return rc;
+  }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   LLParams P{};
   P.comps = components;

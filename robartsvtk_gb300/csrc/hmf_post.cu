@@ -190,6 +190,11 @@ int hmf_vote(int n_inputs, const float* const* inputs, const int* values, long l
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   for (int k = 0; k < n_inputs; ++k)
     if (!inputs[k]) return fail(c, HMF_ERR_MISSING_INPUT, "a vote input is NULL");
+  if (where == HMF_DEVICE) {
+    for (int k = 0; k < n_inputs; ++k)
+      if (int rc = check_device_pointer(c, inputs[k], "vote input")) return rc;
+    if (int rc = check_device_pointer(c, out, "vote output")) return rc;
+  }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   Scratch scratch;
   hmf::VoteInputs in;
@@ -241,8 +246,12 @@ int hmf_decomposition_energy(int vx, int vy, int vz, const int* parent, int n_no
     if (leaf && (!data || !data[v] || !labels || !labels[v]))
       return fail(c, HMF_ERR_MISSING_INPUT, "a leaf's data term or labelling is NULL");
     auto bring = [&](const float* src, const float** dst) -> int {
-      if (where == HMF_DEVICE) *dst = src;
-      else CK(scratch.copy_in(src, V, dst, s), "energy input copy");
+      if (where == HMF_DEVICE) {
+        if (int rc = check_device_pointer(c, src, "energy input")) return rc;
+        *dst = src;
+      } else {
+        CK(scratch.copy_in(src, V, dst, s), "energy input copy");
+      }
       return HMF_OK;
     };
     if (leaf) {
@@ -262,6 +271,8 @@ int hmf_batch_get_vote(hmf_ctx* c, int volume, int* out, int where, void* stream
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
   DeviceGuard dg(c->device);
+  if (where == HMF_DEVICE)
+    if (int rc = check_device_pointer(c, out, "vote output")) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const auto& V = c->vols[volume];
   hmf::VoteInputs in;

@@ -171,6 +171,29 @@ def test_negative_data_is_reported():
             s.labels(1)
 
 
+def test_host_memory_labelled_as_device_memory_is_refused():
+    """A host buffer passed as HMF_DEVICE is refused by the calls that take
+    it (none of these calls launches a kernel); device tensors still pass."""
+    import torch
+
+    from robartsvtk_gb300._capi import HMF_DEVICE
+    host = np.ones((4, 4, 4), np.float32)
+    with HMFSolver((4, 4, 4), [-1, 0, 0]) as s:
+        with pytest.raises(HMFError, match="host memory passed as device memory"):
+            s.set_data_pointer(1, host.ctypes.data, HMF_DEVICE)
+        rc = s._lib.hmf_set_smoothness(s._ctx, 1, host.ctypes.data, HMF_DEVICE)
+        assert rc != 0 and b"device memory" in s._lib.hmf_last_error(s._ctx)
+        dev = torch.ones((4, 4, 4), dtype=torch.float32, device="cuda")
+        s.set_data(1, dev)
+        s.set_data(2, dev)
+        s.set_smoothness(1, dev)
+        s.solve()
+        out = np.empty((4, 4, 4), np.float32)
+        rc = s._lib.hmf_get_labels(s._ctx, 1, out.ctypes.data, HMF_DEVICE, None)
+        assert rc != 0 and b"device memory" in s._lib.hmf_last_error(s._ctx)
+        assert np.all(np.isfinite(s.labels(1)))
+
+
 def test_filter_api_end_to_end():
     w = random_tree_problem(26, (12, 10, 8), [-1, 0, 0, 1, 1], iterations=20, smooth_nodes=(2,))
     f = HierarchicalMaxFlowSegmentation()
