@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--profile-large", action="store_true",
                     help="two forward solves of the --large workload (--large-dims, --large-iterations): the "
                          "command ncu wraps")
+    ap.add_argument("--profile-dataterm", action="store_true",
+                    help="two calls of each data-term producer on the --size image: the command ncu wraps")
     ap.add_argument("--profile-post", action="store_true",
                     help="one solve, then two votes and two energy evaluations of its labels: the command ncu wraps")
     return ap.parse_args()
@@ -449,6 +451,39 @@ def bench_post(w, solver, device_stream):
     return res
 
 
+def dataterm_inputs(n):
+    """The data-term producers' inputs, on the device: an n^3 image of
+    integers 0..199 and four int32 label maps (each voxel 1 with p = 0.3),
+    from a seeded torch generator."""
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    img = (torch.rand((n, n, n), generator=g, device="cuda") * 200.0).floor()
+    maps = [(torch.rand((n, n, n), generator=g, device="cuda") < 0.3).to(torch.int32) for _ in range(4)]
+    return img, maps
+
+
+def run_profile_dataterm(args):
+    """Two calls of each data-term producer on the --size image (the Gaussian
+    entropy cost, normalised, and the 4-map log-likelihood cost), device
+    resident: the command ncu wraps."""
+    import torch
+
+    from robartsvtk_gb300 import data_term, log_likelihood
+
+    img, maps = dataterm_inputs(args.size)
+    out = torch.empty_like(img)
+    for _ in range(2):
+        data_term(2, img, k1=20.0, c1=100.0, entropy=True, normalize=True, out=out)
+    for _ in range(2):
+        log_likelihood(img, maps, label_id=1, resolution=1.0, required_agreement=0.5, out=out)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_dataterm": "%d^3 float image, 4 int32 label maps" % args.size,
+                      "checksum": float(out.double().sum().item())}))
+    return 0
+
+
 def bench_dataterm(args, device_stream):
     """The data-term producers on the 256^3 phantom image, device-resident:
     a Gaussian entropy cost of one image, normalised (hmf_data_term; bytes 8V:
@@ -461,11 +496,8 @@ def bench_dataterm(args, device_stream):
 
     from robartsvtk_gb300 import data_term, log_likelihood
 
-    g = torch.Generator(device="cuda")
-    g.manual_seed(0)
     n = args.size
-    img = (torch.rand((n, n, n), generator=g, device="cuda") * 200.0).floor()
-    maps = [(torch.rand((n, n, n), generator=g, device="cuda") < 0.3).to(torch.int32) for _ in range(4)]
+    img, maps = dataterm_inputs(n)
     peak, _ = measured_peak_hbm()
     V = n ** 3
 
@@ -940,6 +972,8 @@ def main():
         return run_profile(args)
     if args.profile_post:
         return run_profile_post(args)
+    if args.profile_dataterm:
+        return run_profile_dataterm(args)
     if args.profile_dag:
         return run_profile_dag(args)
     if args.profile_adjoint:

@@ -121,7 +121,7 @@ __global__ void data_term_kernel(const TermParams P, const float* __restrict__ i
 
 struct LLParams {
   int comps, n_maps, actual_maps, label_id;
-  double agreement;
+  int min_agree;  // smallest agreeing count k with (double)k >= agreement * (double)actual_maps
   float resolution;
 };
 
@@ -129,11 +129,14 @@ struct LLMaps {
   const int* map[HMF_MAX_LABEL_MAPS];
 };
 
+// A seed: enough label maps mark voxel i with the label.  The reference's
+// test, (double)agree >= agreement * (double)actual_maps, is monotone in the
+// integer count, so the host turns it into the threshold min_agree.
 __device__ __forceinline__ bool ll_sample(const LLParams& P, const LLMaps& M, long long i) {
   int agree = 0;
   for (int k = 0; k < P.n_maps; ++k)
     if (M.map[k] && M.map[k][i] == P.label_id) ++agree;
-  return (double)agree >= P.agreement * (double)P.actual_maps;
+  return agree >= P.min_agree;
 }
 
 // sums: [0] samples; keys: [0..1] min, [2..3] max per component
@@ -176,43 +179,76 @@ struct Hist {
 
 __device__ __forceinline__ int ll_bin(float x, float mn, float res) { return (int)((x - mn) / res); }
 
-__global__ void ll_hist_kernel(const LLParams P, const LLMaps M, const Hist H, const float* __restrict__ img,
-                               long long n, unsigned int* hist) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    if (!ll_sample(P, M, i)) continue;
-    int b = ll_bin(img[P.comps * i], H.mn0, P.resolution);
-    if (P.comps == 2) b = b * H.sz1 + ll_bin(img[2 * i + 1], H.mn1, P.resolution);
-    atomicAdd(&hist[b], 1u);
+__device__ __forceinline__ int ll_seed_bin(const LLParams& P, const Hist& H, const float* __restrict__ img,
+                                           long long i) {
+  int b = ll_bin(img[P.comps * i], H.mn0, P.resolution);
+  if (P.comps == 2) b = b * H.sz1 + ll_bin(img[2 * i + 1], H.mn1, P.resolution);
+  return b;  // < bins: the host checked the seeds' range against the bin counts
+}
+
+// Histograms of up to kSharedBins bins (48 KB, the default dynamic shared
+// memory limit): each CTA counts its voxels in shared memory and adds its non-zero bins to the global histogram once (integer
+// counts, so the totals do not depend on the order).
+constexpr int kSharedBins = 12288;
+__global__ void ll_hist_shared_kernel(const LLParams P, const LLMaps M, const Hist H, const float* __restrict__ img,
+                                      long long n, int bins, unsigned int* hist) {
+  extern __shared__ unsigned int sh[];  // bins entries
+  for (int b = threadIdx.x; b < bins; b += blockDim.x) sh[b] = 0u;
+  __syncthreads();
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    if (ll_sample(P, M, i)) atomicAdd(&sh[ll_seed_bin(P, H, img, i)], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < bins; b += blockDim.x) {
+    const unsigned int v = sh[b];
+    if (v) atomicAdd(&hist[b], v);
   }
 }
 
-// hist[i] / (float)szSample + 1.0e-10, the counts kept as the reference's
-// float increments keep them (they stop growing at 2^24).
-__global__ void ll_freq_kernel(const unsigned int* __restrict__ hist, int bins, unsigned long long samples,
-                               float* __restrict__ freq) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < bins; i += gridDim.x * blockDim.x) {
-    const float cnt = (float)min(hist[i], 16777216u);
-    freq[i] = (float)((double)(cnt / (float)(int)samples) + 1.0e-10);
+// Larger histograms: global atomics.
+__global__ void ll_hist_kernel(const LLParams P, const LLMaps M, const Hist H, const float* __restrict__ img,
+                               long long n, unsigned int* hist) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    if (ll_sample(P, M, i)) atomicAdd(&hist[ll_seed_bin(P, H, img, i)], 1u);
+}
+
+// The cost of a voxel depends on its bin only, so it is evaluated once per
+// bin: frequency hist[i] / (float)szSample + 1.0e-10 (the counts kept as the
+// reference's float increments keep them: they stop growing at 2^24), cost
+// -log(frequency), divided by the cost of an empty bin, -log(1.0e-10), when
+// normalised.  cost[bins] is the cost of a voxel outside the histogram.
+__global__ void ll_cost_kernel(const unsigned int* __restrict__ hist, int bins, unsigned long long samples,
+                               int normalize, float* __restrict__ cost) {
+  const double floor_cost = -log(1.0e-10);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= bins; i += gridDim.x * blockDim.x) {
+    float o;
+    if (i < bins) {
+      const float cnt = (float)min(hist[i], 16777216u);
+      const float freq = (float)((double)(cnt / (float)(int)samples) + 1.0e-10);
+      o = (float)(-log((double)freq));
+    } else {
+      o = (float)floor_cost;
+    }
+    if (normalize) o = (float)((double)o / floor_cost);
+    cost[i] = o;
   }
 }
 
 __global__ void ll_out_kernel(const LLParams P, const Hist H, const float* __restrict__ img,
-                              const float* __restrict__ freq, int normalize, long long n, float* __restrict__ out) {
-  const double floor_cost = -log(1.0e-10);
+                              const float* __restrict__ cost, int bins, long long n, float* __restrict__ out) {
+  const float outside = cost[bins];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float x0 = img[P.comps * i];
     const int b0 = ll_bin(x0, H.mn0, P.resolution);
     float o;
     if (x0 < H.mn0 || b0 >= H.sz0) {
-      o = (float)floor_cost;
+      o = outside;
     } else if (P.comps == 1) {
-      o = (float)(-log((double)freq[b0]));
+      o = cost[b0];
     } else {
       const float x1 = img[2 * i + 1];
       const int b1 = ll_bin(x1, H.mn1, P.resolution);
-      o = (x1 < H.mn1 || b1 >= H.sz1) ? (float)floor_cost : (float)(-log((double)freq[b0 * H.sz1 + b1]));
+      o = (x1 < H.mn1 || b1 >= H.sz1) ? outside : cost[b0 * H.sz1 + b1];
     }
-    if (normalize) o = (float)((double)o / floor_cost);
     out[i] = o;
   }
 }
@@ -377,7 +413,6 @@ int hmf_log_likelihood(const float* image, int components, const int* const* lab
   P.comps = components;
   P.n_maps = n_label_maps;
   P.label_id = label_id;
-  P.agreement = required_agreement;
   P.resolution = resolution;
   LLMaps M{};
   Scratch sc;
@@ -389,6 +424,12 @@ int hmf_log_likelihood(const float* image, int components, const int* const* lab
     ++P.actual_maps;
     e = sc.bring(label_maps[k], (size_t)n_voxels, where, &M.map[k], s);
   }
+  P.min_agree = n_label_maps + 1;  // no count qualifies
+  for (int k = 0; k <= n_label_maps; ++k)
+    if ((double)k >= required_agreement * (double)P.actual_maps) {
+      P.min_agree = k;
+      break;
+    }
   if (e == cudaSuccess && where == HMF_HOST) e = sc.alloc(&dout, (size_t)n_voxels);
   unsigned long long* cnt = nullptr;
   unsigned int* keys = nullptr;
@@ -451,20 +492,24 @@ int hmf_log_likelihood(const float* image, int components, const int* const* lab
   const long long bins = (long long)H.sz0 * H.sz1;
   if (bins > (1LL << 28)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "histogram of more than 2^28 bins");
   unsigned int* hist = nullptr;
-  float* freq = nullptr;
+  float* cost = nullptr;
   e = sc.alloc(&hist, (size_t)bins);
-  if (e == cudaSuccess) e = sc.alloc(&freq, (size_t)bins);
+  if (e == cudaSuccess) e = sc.alloc(&cost, (size_t)bins + 1);
   if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * (size_t)bins, s);
   if (e == cudaSuccess) {
-    ll_hist_kernel<<<grid_for(n_voxels), kThreads, 0, s>>>(P, M, H, img, n_voxels, hist);
+    if (bins <= kSharedBins)
+      ll_hist_shared_kernel<<<grid_for(n_voxels), kThreads, sizeof(unsigned int) * (size_t)bins, s>>>(
+          P, M, H, img, n_voxels, (int)bins, hist);
+    else
+      ll_hist_kernel<<<grid_for(n_voxels), kThreads, 0, s>>>(P, M, H, img, n_voxels, hist);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    ll_freq_kernel<<<grid_for(bins), kThreads, 0, s>>>(hist, (int)bins, samples, freq);
+    ll_cost_kernel<<<grid_for(bins + 1), kThreads, 0, s>>>(hist, (int)bins, samples, normalize != 0, cost);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    ll_out_kernel<<<grid_for(n_voxels), kThreads, 0, s>>>(P, H, img, freq, normalize != 0, n_voxels, dout);
+    ll_out_kernel<<<grid_for(n_voxels), kThreads, 0, s>>>(P, H, img, cost, (int)bins, n_voxels, dout);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && where == HMF_HOST) {

@@ -85,7 +85,7 @@ def seeds(seed, shape, n_maps, label=2):
     return maps
 
 
-@pytest.mark.parametrize("agreement,normalize", [(0.8, False), (0.5, True), (1.0, False)])
+@pytest.mark.parametrize("agreement,normalize", [(0.8, False), (0.5, True), (1.0, False), (0.0, True)])
 def test_log_likelihood_one_component(agreement, normalize):
     shape = (31, 19, 13)
     img = np.round(image(5, shape, 0.0, 120.0))  # integral values, resolution 1
@@ -106,6 +106,18 @@ def test_log_likelihood_two_components_and_device():
     dev = log_likelihood(torch.from_numpy(img).cuda(), [torch.from_numpy(m.reshape(-1)).cuda() for m in maps],
                          label_id=1, resolution=2.0, required_agreement=0.6, components=2)
     assert_ulps(dev.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("hi,comps", [(20000.0, 1), (199.0, 2)])
+def test_log_likelihood_large_histograms(hi, comps):
+    """Histograms of more bins than one CTA's shared memory holds (20001 bins;
+    200 x 200) are counted with global atomics; same costs."""
+    shape = (23, 17, 11)
+    img = np.round(image(12, shape + ((comps,) if comps == 2 else ()), 0.0, hi)).reshape(-1)
+    maps = seeds(13, shape, 3, label=1)
+    want = DT.log_likelihood(img, maps, label_id=1, resolution=1.0, required_agreement=0.6, components=comps)
+    got = log_likelihood(img, maps, label_id=1, resolution=1.0, required_agreement=0.6, components=comps)
+    assert_ulps(got, want)
 
 
 def test_log_likelihood_no_seed_overflow_and_facade():
