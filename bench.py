@@ -157,7 +157,7 @@ def ncu_traffic():
     return None
 
 
-def survey_bytes_per_iteration(w):
+def compulsory_bytes_per_iteration(w):
     """Algorithmic bytes of one iteration, 4*V*(12*N + L + N_S + 2): every
     non-root vertex's three flows, divergence, sink and label read and written
     once, each data term and distinct smoothness image read once, the source
@@ -358,7 +358,7 @@ def run_ours(args):
 
     # ---- roofline -----------------------------------------------------------
     peak, peak_kind = measured_peak_hbm()
-    b_iter = survey_bytes_per_iteration(w)
+    b_iter = compulsory_bytes_per_iteration(w)
     it_ms = t_flow + t_tree
     achieved = b_iter / (it_ms / 1000.0) / 1e9
     flow_b, tree_b = kernel_bytes(w)
@@ -685,7 +685,7 @@ def run_large(args):
     s.set_timing(False)
     s.set_params(T, w.step, w.cc)
     vli = w.nvox * len(w.leaves) * T
-    b_iter = survey_bytes_per_iteration(w)
+    b_iter = compulsory_bytes_per_iteration(w)
     # the adjoint may use the free device memory but a margin (the library's
     # default budget is 85% of it): every state slot saves forward passes
     free_b, _ = torch.cuda.mem_get_info()
