@@ -46,6 +46,10 @@ namespace {
 
 thread_local std::string g_create_error;
 
+// Largest extent along one axis: row pitches (rounded up to 4 floats) and the
+// kernels' per-axis coordinates stay within int.
+constexpr int kMaxDim = 1 << 30;
+
 constexpr int kTX = 32, kTY = 8;
 constexpr int kTreeThreads = 256;
 
@@ -1011,9 +1015,12 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
   if (!out) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (n_volumes < 1 || !dims) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "a batch needs at least one volume");
-  for (int b = 0; b < n_volumes; ++b)
+  for (int b = 0; b < n_volumes; ++b) {
     if (dims[3 * b] <= 0 || dims[3 * b + 1] <= 0 || dims[3 * b + 2] <= 0)
       return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
+    if (dims[3 * b] > kMaxDim || dims[3 * b + 1] > kMaxDim || dims[3 * b + 2] > kMaxDim)
+      return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "volume dimensions above 2^30 are not supported");
+  }
   if (semantics != HMF_SEMANTICS_REF_CUDA && semantics != HMF_SEMANTICS_REF_CPU)
     return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "unknown semantics");
   hmf_ctx* c = new hmf_ctx();
@@ -1510,6 +1517,8 @@ extern "C" int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int 
                                  void* stream) {
   if (vx <= 0 || vy <= 0 || vz <= 0)
     return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
+  if (vx > kMaxDim || vy > kMaxDim || vz > kMaxDim)
+    return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "volume dimensions above 2^30 are not supported");
   if (semantics != HMF_SEMANTICS_REF_CUDA && semantics != HMF_SEMANTICS_REF_CPU)
     return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "unknown semantics");
   if (!data) return noalloc_fail(HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");

@@ -64,6 +64,10 @@ def test_create_rejects_bad_dims_and_semantics(hmf_lib):
     par = (ctypes.c_int * 3)(-1, 0, 0)
     assert hmf_lib.hmf_create(ctypes.byref(ctx), 0, 4, 4, par, 3, 0, 0) == -1
     assert hmf_lib.hmf_create(ctypes.byref(ctx), 4, 4, 4, par, 3, 7, 0) == -1
+    assert hmf_lib.hmf_create(ctypes.byref(ctx), (1 << 30) + 1, 4, 4, par, 3, 0, 0) == -1
+    assert b"2^30" in hmf_lib.hmf_last_error(None)
+    assert hmf_lib.hmf_create(ctypes.byref(ctx), 4, 4, 2**31 - 1, par, 3, 0, 0) == -1
+    assert not ctx.value
 
 
 def test_null_context_is_rejected(hmf_lib):
