@@ -231,6 +231,8 @@ int hmf_decomposition_energy(int vx, int vy, int vz, const int* parent, int n_no
                              double* f, void* stream) {
   hmf_ctx* c = nullptr;  // errors: hmf_last_error(NULL)
   if (vx <= 0 || vy <= 0 || vz <= 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume dimensions must be positive");
+  if (vx > (1 << 30) || vy > (1 << 30) || vz > (1 << 30))
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume dimensions above 2^30 are not supported");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
   hmf::EnergyTable tab;
   std::vector<int> entry;

@@ -68,6 +68,10 @@ def test_create_rejects_bad_dims_and_semantics(hmf_lib):
     assert b"2^30" in hmf_lib.hmf_last_error(None)
     assert hmf_lib.hmf_create(ctypes.byref(ctx), 4, 4, 2**31 - 1, par, 3, 0, 0) == -1
     assert not ctx.value
+    f0 = ctypes.c_double()
+    f = (ctypes.c_double * 3)()
+    assert hmf_lib.hmf_decomposition_energy((1 << 30) + 1, 1, 1, par, 3, None, None, None, 0,
+                                            ctypes.byref(f0), f, None) == -1
 
 
 def test_null_context_is_rejected(hmf_lib):
