@@ -320,6 +320,16 @@ def run_ours(args):
     t_flow, t_tree, t_init = st["flow_ms"], st["tree_ms"], st["init_ms"]
     post = bench_post(w, solver, stream)
 
+    # ---- the FP32 labels' distance from the same iteration in FP64 --------
+    # (outside the timed region: hmf_solve_fp64 on the same context and
+    # inputs, then the comparison on the device)
+    t0 = time.perf_counter()
+    solver.solve_fp64(stream)
+    fp64 = solver.fp64_error(stream)
+    fp64["seconds"] = time.perf_counter() - t0
+    fp64["what"] = ("max over leaves and voxels of |u_fp32 - u_fp64| after all %d iterations; argmax leaf "
+                    "agreement between the two" % w.iterations)
+
     # ---- end to end through the public API with pinned host buffers -------
     h_data = {leaf: torch.from_numpy(d).pin_memory() for leaf, d in w.data.items()}
     h_smooth_obj = {}
@@ -392,6 +402,9 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clock_info,
         "roofline": roofline,
+        "fp64_max_abs_err": fp64["max_abs_err"],
+        "argmax_agreement": fp64["argmax_agreement"],
+        "fp64": fp64,
         "post": post,
     }
     if rank == 0 and not args.no_batched:

@@ -169,6 +169,27 @@ int hmf_autotune(hmf_ctx* ctx, void* stream);
 int hmf_set_zchunk(hmf_ctx* ctx, int z);
 int hmf_get_zchunk(const hmf_ctx* ctx);
 
+/* ---- Bounded copy waits ----------------------------------------------------
+ * No counterpart in the reference, whose kernels have no waits.  The
+ * kernels that stream their inputs through shared memory (TMA / bulk copies
+ * completed on mbarriers) bound every wait: a wait that runs out makes the
+ * kernel stop issuing copies, wait (0.5 s at most) for the copies still in
+ * flight into its shared memory, and leave; the call then returns
+ * HMF_ERR_CUDA ("... timed out ...") and the context stays usable.
+ *  - hmf_set_wait_limit: the bound (ns) of the flow kernels' waits, forward
+ *    and reverse (0: the default 0.5 s).  The sweep kernels keep 0.5 s.
+ *  - hmf_inject_wait_stall: makes one CTA of the next launch of `kernel`
+ *    wait on a barrier that no copy completes, so that its bounded wait runs
+ *    out on healthy hardware: the failure path on demand, for tests (-1
+ *    cancels).  A solve with a pending request runs its launches one by one
+ *    instead of replaying its CUDA graph. */
+#define HMF_STALL_FLOW 0
+#define HMF_STALL_SWEEP 1
+#define HMF_STALL_REVERSE_FLOW 2
+#define HMF_STALL_REVERSE_SWEEP 3
+int hmf_set_wait_limit(hmf_ctx* ctx, long long limit_ns);
+int hmf_inject_wait_stall(hmf_ctx* ctx, int kernel);
+
 /* ---- Adjoint (reverse mode) -----------------------------------------------
  * No counterpart in the reference, which only solves forward.  Solves like
  * hmf_solve (REF_CUDA semantics, single-volume contexts) and differentiates
@@ -220,6 +241,42 @@ int hmf_get_adjoint_schedule(const hmf_ctx* ctx, int* state_slots, long long* fo
  * HMF_ERR_OUT_OF_MEMORY when no schedule exists with that many slots. */
 long long hmf_adjoint_schedule(int iterations, int state_slots, int checkpoint_every, int* actions,
                                long long capacity);
+
+/* ---- Reference precision (FP64) -------------------------------------------
+ * No counterpart in the reference, which computes in FP32 only.  The error
+ * of an FP32 solve against the exact solution of the same iteration is
+ * measured by running the REF_CUDA iteration of hmf_solve
+ * (CUDA_hierarchicalmaxflow.cu:124-456 in the launch order of
+ * vtkCudaHierarchicalMaxFlowSegmentation.cxx:106-476, initialisation
+ * :547-658) in FP64 on the GPU: every operation in the reference's order, in
+ * double; step and CC are the FP32 parameters widened, 1/CC and
+ * 1/(children+1) are formed in double, alpha is the FP32-stored scalar
+ * widened.  Single-volume REF_CUDA tree contexts only.  The FP64 state (six
+ * doubles per non-root vertex and voxel) is allocated by the first call and
+ * kept with the context.
+ *  - hmf_solve_fp64: initialise and iterate in FP64 on the context's current
+ *    inputs and parameters (queued on `stream`).
+ *  - hmf_get_labels_fp64: the FP64 labelling of a non-root vertex
+ *    (VX*VY*VZ doubles).
+ *  - hmf_fp64_error: max over leaves and voxels of |u_fp32 - u_fp64| between
+ *    the last hmf_solve and the last hmf_solve_fp64, and the fraction of
+ *    voxels whose argmax leaf (first maximum) agrees.  Synchronous.
+ *  - hmf_fp64_loss: the adjoint's loss -(1/V) sum_i log(max(u_{truth_i}, eps))
+ *    on the FP64 labels (truth as for hmf_solve_adjoint).  Synchronous.
+ *  - hmf_set_fp64_probe: inputs of later FP64 solves that differ from the
+ *    FP32 inputs, for finite differences: HMF_FP64_PROBE_DATA sets the data
+ *    term of leaf `node` at dense voxel index `voxel` (x fastest) to `value`
+ *    (double); HMF_FP64_PROBE_ALPHA sets the smoothness weight of vertex
+ *    `node` to `value` (double, not rounded to float); HMF_FP64_PROBE_NONE
+ *    clears both.  One data probe at a time. */
+#define HMF_FP64_PROBE_NONE 0
+#define HMF_FP64_PROBE_DATA 1
+#define HMF_FP64_PROBE_ALPHA 2
+int hmf_solve_fp64(hmf_ctx* ctx, void* stream);
+int hmf_get_labels_fp64(hmf_ctx* ctx, int node, double* out, int where, void* stream);
+int hmf_fp64_error(hmf_ctx* ctx, double* max_abs_err, double* argmax_agreement, void* stream);
+int hmf_fp64_loss(hmf_ctx* ctx, const int* truth, int where, double eps, double* loss, void* stream);
+int hmf_set_fp64_probe(hmf_ctx* ctx, int kind, int node, long long voxel, double value);
 
 /* ---- Vote and energy (the steps after a solve) ----------------------------
  * hmf_vote replaces CUDA_CIV_COMPUTE (CUDA_imagevote.h, the vtkCudaImageVote

@@ -16,6 +16,13 @@ HMF_HOST = 0
 HMF_DEVICE = 1
 HMF_SEMANTICS_REF_CUDA = 0
 HMF_SEMANTICS_REF_CPU = 1
+HMF_STALL_FLOW = 0
+HMF_STALL_SWEEP = 1
+HMF_STALL_REVERSE_FLOW = 2
+HMF_STALL_REVERSE_SWEEP = 3
+HMF_FP64_PROBE_NONE = 0
+HMF_FP64_PROBE_DATA = 1
+HMF_FP64_PROBE_ALPHA = 2
 
 ERRORS = {
     -1: "HMF_ERR_INVALID_ARGUMENT",
@@ -75,6 +82,13 @@ SIGNATURES = [
                                       ctypes.POINTER(ctypes.c_double), _P]),
     ("hmf_get_energy", _I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_batch_get_energy", _I, [_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
+    ("hmf_set_wait_limit", _I, [_P, ctypes.c_longlong]),
+    ("hmf_inject_wait_stall", _I, [_P, _I]),
+    ("hmf_solve_fp64", _I, [_P, _P]),
+    ("hmf_get_labels_fp64", _I, [_P, _I, _P, _I, _P]),
+    ("hmf_fp64_error", _I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _P]),
+    ("hmf_fp64_loss", _I, [_P, _P, _I, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _P]),
+    ("hmf_set_fp64_probe", _I, [_P, _I, _I, ctypes.c_longlong, ctypes.c_double]),
     ("hmf_solve_noalloc", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                ctypes.POINTER(ctypes.c_double), _I, ctypes.c_float, ctypes.c_float,
                                ctypes.POINTER(_P), _P]),

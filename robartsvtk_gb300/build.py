@@ -1,7 +1,8 @@
 """Builds libhmf_gb300.so in-tree (robartsvtk_gb300/_build/) for sm_103a.
 
-Six translation units (the solver, its adjoint and its schedules, the vote
-and energy, the data-term producers, the C++ facade), compiled
+Seven translation units (the solver, its FP64 evaluation, its adjoint and
+its schedules, the vote and energy, the data-term producers, the C++
+facade), compiled
 in parallel with nvcc and linked into one shared library that exports the C
 ABI of include/hmf.h and the C++ facade of csrc/hmf_segmentation.hpp.  The
 kernel units are compiled with -fmad=false so the FP32 arithmetic follows the
@@ -26,6 +27,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompi
 UNITS = {
     "hmf_capi.o": ("hmf_capi.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     "hmf_adjoint.o": ("hmf_adjoint.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
+    "hmf_fp64.o": ("hmf_fp64.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     "hmf_post.o": ("hmf_post.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     "hmf_dataterm.o": ("hmf_dataterm.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
                                            "-Xcompiler", "-ffp-contract=off"]),

@@ -473,6 +473,7 @@ int backward_step(hmf_ctx* c, const Staged& staged, int slotA, int slotB, int cu
     const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
     bool pre = true;  // vertex ids in pre-order: the sink pass runs in id order
     for (int k = 0; k < n; ++k) pre = pre && c->preorder[k] == k;
+    if (int rc = maybe_request_stall(c, HMF_STALL_REVERSE_SWEEP, s)) return rc;
     switch (n * 2 + (pre ? 1 : 0)) {
 #define HMF_SWEEP_CASE(N)                                                                                  \
   case 2 * N:                                                                                              \
@@ -497,6 +498,8 @@ int backward_step(hmf_ctx* c, const Staged& staged, int slotA, int slotB, int cu
     fp.vols = S->d_avol;
     fp.items = S->d_aitems;
     fp.error_flag = c->d_error;
+    fp.wait_limit_ns = c->wait_limit_ns;
+    if (int rc = maybe_request_stall(c, HMF_STALL_REVERSE_FLOW, s)) return rc;
     const dim3 grid((unsigned)S->n_aitems * (unsigned)(n - 1));
     hmf::adj_flow_tma_kernel<<<grid, hmf::kAfThreads, hmf::kAfSmemBytes, s>>>(
         S->d_aflow + (size_t)slotA * (n - 1), fp);

@@ -63,6 +63,7 @@ struct AdjFlowParams {
   const FlowVolume* vols;
   const FlowItem* items;
   int* error_flag;
+  unsigned long long wait_limit_ns;  // bound of every copy wait (kTmaWaitLimitNs unless a caller sets it)
 };
 
 __global__ void __launch_bounds__(kAfThreads, 1)
@@ -73,6 +74,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   float* xp = zslots + kAfPzSlots * kAfPlane;                            // [11][18][32]
   uint64_t* mbars = reinterpret_cast<uint64_t*>(xp + kAfXPlanes * kAfX); // [3]
   uint64_t* zbars = mbars + kAfMainSlots;                                // [4]
+  uint64_t* stall_bar = zbars + kAfPzSlots;                              // [1] never completed (a requested stall)
   // exchange rows: *_L = the last row of each warp (read by the next warp as
   // its y-1 neighbour), *_F = the first row (read by the previous warp as y+1)
   float* XG_L = xp;
@@ -82,7 +84,7 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   float* XF_L = xp + 6 * kAfX;
   float* XQY_F = xp + 7 * kAfX;   // [2]
   float* XD_L = xp + 9 * kAfX;    // [2]
-  __shared__ int abort_cta;
+  __shared__ int abort_cta, stall_cta;
   __shared__ int stop;
   __shared__ double red[kAfWarps];
 
@@ -133,13 +135,16 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   const int xw = (warp + 1) * 32 + lane;  // this warp's entry in an exchange row
 
   if (threadIdx.x == 0) {
-    abort_cta = fp.error_flag ? (*(volatile int*)fp.error_flag & 2) : 0;
+    const int flag = fp.error_flag ? *(volatile int*)fp.error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(fp.error_flag, flag);
     if (smem_addr(af_raw) & 127) {  // TMA destinations must be 128-byte aligned
       abort_cta = 1;
       if (fp.error_flag) atomicOr(fp.error_flag, 4);
     }
     for (int s = 0; s < kAfMainSlots; ++s) mbar_init(&mbars[s], (unsigned)narr);
     for (int s = 0; s < kAfPzSlots; ++s) mbar_init(&zbars[s], 1);
+    mbar_init(stall_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     stop = 0;
@@ -173,8 +178,9 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   // barrier: the CTA leaves the march, drains its copies and reports.
   auto wait0 = [&](uint64_t* bar, unsigned parity) {  // thread 0 only
     if (stop) return;
-    if (!mbar_wait_bounded(bar, parity, kTmaWaitLimitNs)) stop = 1;
+    if (!mbar_wait_bounded(bar, parity, fp.wait_limit_ns)) stop = 1;
   };
+  int k_stop = -1;  // the step at which the march stopped (-1: it ran to the end)
   auto wait_main0 = [&](int p) {
     wait0(&mbars[(p - kstart) % kAfMainSlots], (unsigned)(((p - kstart) / kAfMainSlots) & 1));
   };
@@ -188,6 +194,8 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     wait_main0(kstart);
     wait_pz0(kstart);
     if (kstart + 1 < G.vz) wait_pz0(kstart + 1);
+    // the failure path on demand: a wait on a barrier that no copy completes
+    if (stall_cta) wait0(stall_bar, 0);
   }
   __syncthreads();
 
@@ -355,7 +363,10 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
         if (k + 2 < G.vz && k + 2 <= kpz_end) wait_pz0(k + 2);
       }
       __syncthreads();  // (2)
-      if (stop) return false;
+      if (stop) {
+        k_stop = k;
+        return false;
+      }
 
       // ---- stage D: q(k-1), the adjoint of p'
       float qx_n[kAfR], qy_n[kAfR], qz_n[kAfR];
@@ -468,12 +479,18 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   }
   if (timed_out && threadIdx.x == 0) {
     if (fp.error_flag) atomicOr(fp.error_flag, 2);
-    // copies still in flight into this CTA's shared memory must land before it
-    // exits: wait (bounded) for the last plane of each slot
-    for (int p = max(kstart, kA_end - kAfMainSlots + 1); p <= kA_end; ++p)
+    // Copies still in flight into this CTA's shared memory must land before
+    // it exits.  Up to step k_stop the main ring was filled to plane
+    // k_stop + 2 and the pz ring to k_stop + 3 (the initial issue: kstart + 1,
+    // kstart + 2), each slot holding at most one pending phase: wait for the
+    // last plane issued into each slot, with the default bound.
+    const int ks = k_stop >= 0 ? k_stop : kstart;
+    const int l_main = min(max(ks + 2, kstart + 1), kA_end);
+    const int l_pz = min(max(ks + 3, kstart + 2), kpz_end);
+    for (int p = max(kstart, l_main - kAfMainSlots + 1); p <= l_main; ++p)
       mbar_wait_bounded(&mbars[(p - kstart) % kAfMainSlots], (unsigned)(((p - kstart) / kAfMainSlots) & 1),
                         kTmaWaitLimitNs);
-    for (int p = max(kstart, kpz_end - kAfPzSlots + 1); p <= kpz_end; ++p)
+    for (int p = max(kstart, l_pz - kAfPzSlots + 1); p <= l_pz; ++p)
       mbar_wait_bounded(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1),
                         kTmaWaitLimitNs);
   }

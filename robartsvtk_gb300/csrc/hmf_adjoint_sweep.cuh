@@ -53,21 +53,25 @@ template <int N, bool PRE>
 __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restrict__ table, const Geometry G,
                                                           const AdjSweep S, int* __restrict__ error_flag) {
   __shared__ AdjTree T;
-  __shared__ int abort_cta;
+  __shared__ int abort_cta, stall_cta, stop_cta;
   extern __shared__ __align__(128) unsigned char sw_raw[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sw_raw);  // [2]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sw_raw);  // [2], then the stall barrier
   float* stage0 = reinterpret_cast<float*>(sw_raw + 128);
   constexpr int kStage = kSwKinds * N * kSwVc;  // floats per stage
 
   for (int i = threadIdx.x; i < (int)(sizeof(AdjTree) / 4); i += blockDim.x)
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
   if (threadIdx.x == 0) {
-    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    const int flag = error_flag ? *(volatile int*)error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(error_flag, flag);
+    stop_cta = 0;
     if (smem_addr(sw_raw) & 15) {  // bulk-copy destinations must be 16-byte aligned
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
     for (int s = 0; s < 2; ++s) mbar_init(&bars[s], N);  // one arrival per vertex lane
+    mbar_init(&bars[2], 1);  // completed by nothing: a requested stall waits on it
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -117,9 +121,17 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
     if (chunk < nchunks) issue(chunk, 0, threadIdx.x), ++nissued[0];
     if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1, threadIdx.x), ++nissued[1];
   }
+  // a requested stall: a wait that runs out, so the time-out path runs
+  if (threadIdx.x == 0 && stall_cta && !mbar_wait_bounded(&bars[2], 0, kTmaWaitLimitNs)) {
+    timed_out = true;
+    *(volatile int*)&stop_cta = 1;
+  }
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
-    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) {
+      timed_out = true;
+      *(volatile int*)&stop_cta = 1;
+    }
     const float* st = stage0 + (size_t)s * kStage;
     const long long v0 = chunk * kSwVc;
     const int len = (int)min((long long)kSwVc, G.vol - v0);
@@ -150,6 +162,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
     // while this one is reversed.
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
+    if (stop_cta) break;  // a copy wait ran out: no further copies
     if (threadIdx.x < N && chunk + 2LL * gridDim.x < nchunks)
       issue(chunk + 2LL * gridDim.x, s, threadIdx.x), ++nissued[s];
     if (q < len) {
@@ -267,10 +280,15 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
       }
     }
   }
-  if (timed_out && error_flag) atomicOr(error_flag, 2);
-  if (threadIdx.x == 0 && timed_out)
+  __syncthreads();
+  // Copies into this CTA's shared memory must have landed before it exits:
+  // after a time-out each issuing thread waits (bounded) for the last copy it
+  // issued into each stage (nothing is issued after stop_cta).
+  if (stop_cta) {
+    if (threadIdx.x == 0 && error_flag) atomicOr(error_flag, 2);
     for (int s = 0; s < 2; ++s)
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+  }
 }
 
 }  // namespace hmf

@@ -59,6 +59,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   return true;
 }
 
+// Error-flag bit of a requested stall: the first CTA of a copy-pipeline
+// kernel that finds it set clears it and, before its first copy wait, waits
+// on an mbarrier that nothing completes, so that the bounded wait runs out
+// and the kernel's time-out path (stop issuing, drain the copies in flight,
+// report) runs on healthy hardware.  Set by the host only on request
+// (hmf_inject_wait_stall).
+constexpr int kStallRequest = 1 << 16;
+
+// Thread 0 of a CTA, given the error flag's value read at kernel start:
+// whether this CTA takes the stall request (exactly one CTA does).
+__device__ __forceinline__ bool take_stall_request(int* error_flag, int flag) {
+  return error_flag && (flag & kStallRequest) && (atomicAnd(error_flag, ~kStallRequest) & kStallRequest);
+}
+
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(

@@ -473,6 +473,18 @@ int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out) {
 
 int launch_flow_tma(hmf_ctx* c, int parity, cudaStream_t s) { return launch_flow_tma_with(c, c->d_tma, parity, s); }
 
+namespace {
+__global__ void request_stall_kernel(int* error_flag) { atomicOr(error_flag, hmf::kStallRequest); }
+}  // namespace
+
+int maybe_request_stall(hmf_ctx* c, int kind, cudaStream_t s) {
+  if (c->stall_kind != kind) return HMF_OK;
+  c->stall_kind = -1;
+  request_stall_kernel<<<1, 1, 0, s>>>(c->d_error);
+  CK(cudaGetLastError(), "request_stall_kernel launch");
+  return HMF_OK;
+}
+
 int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s) {
   hmf::FlowTmaParams fp;
   fp.step = c->step;
@@ -482,6 +494,8 @@ int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity
   fp.vols = c->d_fvol;
   fp.items = c->d_items;
   fp.error_flag = c->d_error;
+  fp.wait_limit_ns = c->wait_limit_ns;
+  if (int rc = maybe_request_stall(c, HMF_STALL_FLOW, s)) return rc;
   const dim3 grid((unsigned)c->n_items * (unsigned)(c->n - 1), 1, 1);
   hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(table, fp);
   CK(cudaGetLastError(), "flow_tma_kernel launch");
@@ -526,6 +540,7 @@ int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t 
   const long long chunks = (c->geo.vol + vc - 1) / vc;
   const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
   const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
+  if (int rc = maybe_request_stall(c, HMF_STALL_SWEEP, s)) return rc;
   switch (c->n) {
 #define HMF_TREE_N(N)                                                                 \
   case N:                                                                             \
@@ -553,6 +568,8 @@ int dag_grid(hmf_ctx* c, const void* kernel, size_t smem) {
 }
 
 int launch_dag_sweep(hmf_ctx* c, cudaStream_t s) {
+  if (!c->dag_simple)
+    if (int rc = maybe_request_stall(c, HMF_STALL_SWEEP, s)) return rc;
   if (!c->dag_simple && !c->dag_generic && c->dag_reg_ok) {
     const int smem = hmf::dag_bulk_n_smem_bytes(c->n);
     const long long chunks = (c->geo.vol + hmf::kDagNVc - 1) / hmf::kDagNVc;
@@ -928,6 +945,7 @@ bool valid_volume(const hmf_ctx* c, int b) { return c && b >= 0 && b < (int)c->v
 int check_error_flag(hmf_ctx* c) {
   int flag = 0;
   CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  flag &= ~hmf::kStallRequest;  // a stall request no kernel took
   if (flag & 4) return fail(c, HMF_ERR_CUDA, "shared-memory staging area misaligned; results are invalid");
   if (flag & 2) return fail(c, HMF_ERR_CUDA, "an asynchronous-copy wait timed out; results are invalid");
   if (flag & 1)
@@ -1163,6 +1181,7 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->ev_t0) cudaEventDestroy(c->ev_t0);
   if (c->ev_t1) cudaEventDestroy(c->ev_t1);
   adjoint_free(c);
+  fp64_free(c);
   if (c->d_post) cudaFree(c->d_post);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1240,7 +1259,7 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   if (c->semantics == HMF_SEMANTICS_REF_CPU) {
     rc = timed(c, 1, s, do_refcpu, 0);
     if (rc) return rc;
-  } else if (c->timing) {
+  } else if (c->timing || c->stall_kind >= 0) {
     for (int it = 0; it < c->iterations; ++it) {
       c->dag_last = c->dag && it == c->iterations - 1;
       rc = timed(c, 0, s, do_flow, it & 1);
@@ -1328,6 +1347,24 @@ int hmf_set_zchunk(hmf_ctx* c, int z) {
 
 int hmf_get_zchunk(const hmf_ctx* c) { return c ? c->zchunk : HMF_ERR_INVALID_ARGUMENT; }
 
+int hmf_set_wait_limit(hmf_ctx* c, long long limit_ns) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (limit_ns < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the wait limit must be >= 0 (0: default)");
+  const unsigned long long v = limit_ns ? (unsigned long long)limit_ns : hmf::kTmaWaitLimitNs;
+  if (v == c->wait_limit_ns) return HMF_OK;
+  DeviceGuard dg(c->device);
+  drop_graphs(c);  // the captured launches carry the old bound
+  c->wait_limit_ns = v;
+  return HMF_OK;
+}
+
+int hmf_inject_wait_stall(hmf_ctx* c, int kernel) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (kernel < -1 || kernel > HMF_STALL_REVERSE_SWEEP) return fail(c, HMF_ERR_INVALID_ARGUMENT, "unknown kernel");
+  c->stall_kind = kernel;
+  return HMF_OK;
+}
+
 int hmf_batch_get_labels(hmf_ctx* c, int volume, int node, float* out, int where, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
   if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
@@ -1364,7 +1401,7 @@ int hmf_leaf_order(const hmf_ctx* c, int* out, int cap) {
 
 size_t hmf_device_bytes(const hmf_ctx* c) {
   if (!c) return 0;
-  return c->arena_bytes + c->staging_bytes + adjoint_bytes(c) + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
+  return c->arena_bytes + c->staging_bytes + adjoint_bytes(c) + fp64_bytes(c) + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
          sizeof(hmf::FlowVertexTMA) * c->vols.size() * (c->n - 1) + sizeof(hmf::TreeTable) +
          sizeof(hmf::FlowItem) * c->h_items.size();
 }

@@ -85,6 +85,10 @@ struct hmf_ctx {
   cudaGraphExec_t graph_pair = nullptr;  // two iterations (both flow parities)
   cudaGraphExec_t graph_one = nullptr;   // one iteration, parity 0
 
+  // failure-path controls (hmf_set_wait_limit, hmf_inject_wait_stall)
+  unsigned long long wait_limit_ns = hmf::kTmaWaitLimitNs;
+  int stall_kind = -1;  // HMF_STALL_* of the next launch of that kind that is to stall (-1: none)
+
   bool timing = false;
   long long launches = 0;
   double kind_ms[3] = {0, 0, 0};
@@ -109,6 +113,9 @@ struct hmf_ctx {
 
   // reverse-mode state of hmf_solve_adjoint (hmf_adjoint.cu), created on demand
   struct AdjointState* adj = nullptr;
+  // FP64 evaluation of the same iteration (hmf_fp64.cu), created on demand
+  struct Fp64State* f64 = nullptr;
+
   long long adj_max_bytes = 0;  // hmf_set_adjoint_memory (0: 85% of the free device memory)
   int adj_max_slots = 0;        // (0: no cap)
 
@@ -155,6 +162,10 @@ struct Staged {
   std::vector<const float*> distinct;  // bases of the smoothness groups
 };
 
+// Device arrays of the inputs over the concatenation of the volumes (host
+// inputs and unaligned or pitched device inputs copied into staging arrays),
+// queued on `s`.
+int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out);
 // Joins the caller's stream, stages the inputs, writes the kernel tables,
 // zeroes the parity-0 flows and runs the initialisation kernel on c->stream.
 int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged);
@@ -171,6 +182,9 @@ int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ct
                      int rows = hmf::kTmaRows);
 bool valid_vertex(const hmf_ctx* c, int v);
 bool valid_volume(const hmf_ctx* c, int b);
+// When c->stall_kind == kind: queue on `s` the request that makes the next
+// copy-pipeline kernel stall once (its bounded wait runs out), and clear it.
+int maybe_request_stall(hmf_ctx* c, int kind, cudaStream_t s);
 // Error flag set by the kernels (bit 0 negative input, 1 wait time-out,
 // 2 misaligned staging, 3 label index out of range), as a status.
 int check_error_flag(hmf_ctx* c);
@@ -178,5 +192,8 @@ int check_error_flag(hmf_ctx* c);
 // hmf_adjoint.cu
 void adjoint_free(hmf_ctx* c);
 size_t adjoint_bytes(const hmf_ctx* c);
+// hmf_fp64.cu
+void fp64_free(hmf_ctx* c);
+size_t fp64_bytes(const hmf_ctx* c);
 
 }  // namespace hmfi

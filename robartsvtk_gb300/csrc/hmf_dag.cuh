@@ -185,7 +185,7 @@ __host__ __device__ inline int dag_bulk_smem_bytes(int arrays) {
 __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_vox, int last,
                                 int* __restrict__ error_flag) {
   __shared__ DagTable T;
-  __shared__ int abort_cta;
+  __shared__ int abort_cta, stall_cta, stop_cta;
   __shared__ int leaf_slot[kMaxVertices];  // entry -> staged data slot
   extern __shared__ __align__(128) unsigned char db_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(db_raw);  // [kDagBulkStages]
@@ -193,13 +193,17 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
   dag_copy_table(T, table);
   __syncthreads();  // thread 0 reads the table below
   if (threadIdx.x == 0) {
-    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    const int flag = error_flag ? *(volatile int*)error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(error_flag, flag);
+    stop_cta = 0;
     if (smem_addr(db_raw) & 15) {
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
     // one arrival per staged array (the copies are spread over the threads)
     for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], (unsigned)dag_bulk_arrays(T.n, T.n_leaves));
+    mbar_init(&bars[kDagBulkStages], 1);  // completed by nothing: a requested stall waits on it
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -244,9 +248,17 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
   long long chunk = blockIdx.x;
   if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
   if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  // a requested stall: a wait that runs out, so the time-out path runs
+  if (threadIdx.x == 0 && stall_cta && !mbar_wait_bounded(&bars[kDagBulkStages], 0, kTmaWaitLimitNs)) {
+    timed_out = true;
+    *(volatile int*)&stop_cta = 1;
+  }
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
-    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) {
+      timed_out = true;
+      *(volatile int*)&stop_cta = 1;
+    }
     const long long v0 = chunk * VC;
     const int len = (int)min((long long)VC, n_vox - v0);
     const int q = threadIdx.x;
@@ -305,12 +317,18 @@ __global__ void dag_bulk_kernel(const DagTable* __restrict__ table, long long n_
     // the bulk copy that refills the stage (async proxy).
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
+    if (stop_cta) break;  // a copy wait ran out: no further copies
     if (chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
-  if (timed_out && error_flag) atomicOr(error_flag, 2);
-  if (threadIdx.x == 0 && timed_out)
+  __syncthreads();
+  // Copies into this CTA's shared memory must have landed before it exits:
+  // after a time-out each issuing thread waits (bounded) for the last copy it
+  // issued into each stage (nothing is issued after stop_cta).
+  if (stop_cta) {
+    if (threadIdx.x == 0 && error_flag) atomicOr(error_flag, 2);
     for (int s = 0; s < kDagBulkStages; ++s)
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+  }
 }
 
 // dag_bulk_kernel for graphs of N <= 8 entries without repeated edges: the
@@ -330,12 +348,15 @@ __global__ void __launch_bounds__(kDagNVc)
   constexpr int A = dag_bulk_n_arrays(N);
   constexpr int VC = kDagNVc;
   constexpr int ROOT = 5 * (N - 1);
-  __shared__ int abort_cta;
+  __shared__ int abort_cta, stall_cta, stop_cta;
   extern __shared__ __align__(128) unsigned char dn_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(dn_raw);
   float* const stage0 = reinterpret_cast<float*>(dn_raw + 128);
   if (threadIdx.x == 0) {
-    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    const int flag = error_flag ? *(volatile int*)error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(error_flag, flag);
+    stop_cta = 0;
     if (smem_addr(dn_raw) & 15) {
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
@@ -344,6 +365,7 @@ __global__ void __launch_bounds__(kDagNVc)
     // each leaf, the root sink
     const unsigned narr = 4u * (N - 1) + 1u + (unsigned)__popc(P.leaf_mask & ((1u << N) - 2u));
     for (int s = 0; s < kDagBulkStages; ++s) mbar_init(&bars[s], narr);
+    mbar_init(&bars[kDagBulkStages], 1);  // completed by nothing: a requested stall waits on it
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -382,9 +404,17 @@ __global__ void __launch_bounds__(kDagNVc)
     if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
     if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
   }
+  // a requested stall: a wait that runs out, so the time-out path runs
+  if (threadIdx.x == 0 && stall_cta && !mbar_wait_bounded(&bars[kDagBulkStages], 0, kTmaWaitLimitNs)) {
+    timed_out = true;
+    *(volatile int*)&stop_cta = 1;
+  }
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
-    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) {
+      timed_out = true;
+      *(volatile int*)&stop_cta = 1;
+    }
     const long long v0 = chunk * VC;
     const int len = (int)min((long long)VC, n_vox - v0);
     const int q = threadIdx.x;
@@ -450,12 +480,18 @@ __global__ void __launch_bounds__(kDagNVc)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // stage s is free again
+    if (stop_cta) break;  // a copy wait ran out: no further copies
     if (asrc && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
-  if (timed_out && error_flag) atomicOr(error_flag, 2);
-  if (threadIdx.x == 0 && timed_out)
+  __syncthreads();
+  // Copies into this CTA's shared memory must have landed before it exits:
+  // after a time-out each issuing thread waits (bounded) for the last copy it
+  // issued into each stage (nothing is issued after stop_cta).
+  if (stop_cta) {
+    if (threadIdx.x == 0 && error_flag) atomicOr(error_flag, 2);
     for (int s = 0; s < kDagBulkStages; ++s)
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+  }
 }
 
 }  // namespace hmf

@@ -57,7 +57,9 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   float* xP = xm + 256;                                           // [2][8][32] P_y(k-2), row 0
   uint64_t* mbars = reinterpret_cast<uint64_t*>(xP + 512);       // [3]
   uint64_t* zbars = mbars + kTmaMainSlots;                        // [4]
+  uint64_t* stall_bar = zbars + kTmaPzSlots;                      // [1] never completed (a requested stall)
   __shared__ int abort_cta;
+  __shared__ int stop_cta;  // a copy wait ran out: the CTA stops issuing, drains its copies and leaves
 
   // blockIdx.x = vertex + n_vertices * item: the vertices of one window run
   // side by side, so a parent sink and a shared smoothness image read by
@@ -114,8 +116,11 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   // If a previous launch already timed out waiting for its copies, the whole
   // CTA returns (one read, shared by all threads), so that a broken
   // configuration fails fast instead of slowly.
+  __shared__ int stall_cta;
   if (threadIdx.x == 0) {
-    abort_cta = fp.error_flag ? (*(volatile int*)fp.error_flag & 2) : 0;
+    const int flag = fp.error_flag ? *(volatile int*)fp.error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(fp.error_flag, flag);
     // TMA destinations must be 128-byte aligned: refuse to run otherwise.
     if (smem_addr(smem_raw) & 127) {
       abort_cta = 1;
@@ -125,6 +130,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     // own expect_tx) by the lane 0 of its own warp
     for (int s = 0; s < kTmaMainSlots; ++s) mbar_init(&mbars[s], (unsigned)narr);
     for (int s = 0; s < kTmaPzSlots; ++s) mbar_init(&zbars[s], 1);
+    mbar_init(stall_bar, 1);
+    stop_cta = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -148,10 +155,17 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     mbar_expect_tx(bar, (unsigned)(kTmaPlane * 4));
     tma_load_plane(zslot(p), &V->flow_in[par][2], xs, y0 - 2, p, bar);
   };
+  // A wait that runs out raises stop_cta before the CTA barrier that follows
+  // every step's waits; after that barrier all threads see it, nobody issues
+  // another copy, and the march ends.
   bool timed_out = false;
+  int k_stop = -1;  // the step at which the march stopped (-1: it ran to the end)
   auto wait_on = [&](uint64_t* bar, unsigned parity) {
     if (timed_out) return;  // results are void already; do not wait again
-    if (!mbar_wait_bounded(bar, parity, kTmaWaitLimitNs)) timed_out = true;
+    if (!mbar_wait_bounded(bar, parity, fp.wait_limit_ns)) {
+      timed_out = true;
+      *(volatile int*)&stop_cta = 1;
+    }
   };
   auto wait_main = [&](int p) {
     wait_on(&mbars[(p - kstart) % kTmaMainSlots], (unsigned)(((p - kstart) / kTmaMainSlots) & 1));
@@ -164,6 +178,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     for (int p = kstart; p <= min(kstart + 1, kmain_end); ++p)
       for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
     for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
+    // the failure path on demand: a wait on a barrier that no copy completes
+    if (stall_cta) wait_on(stall_bar, 0);
   }
 
   // A window whose 32 x 32 columns/rows all lie strictly inside the volume
@@ -185,7 +201,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     }
     bool have_pz = false;  // pzn_c holds pz of plane k (loaded in step k-1)
 
-    auto zstep = [&](const int k, auto stag) {
+    // returns false when the march stops (a copy wait ran out)
+    auto zstep = [&](const int k, auto stag) -> bool {
       constexpr bool ST = decltype(stag)::value;
       const bool doA = ST || k <= kmain_end;                                   // g(k), p'(k)
       const int kc = k - 1;
@@ -239,6 +256,10 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       xpy[warp * 32 + lane] = ppy[0];
       xP[((k & 1) * 8 + warp) * 32 + lane] = Py[0];
       __syncthreads();  // (1)
+      if (stop_cta) {
+        k_stop = k;
+        return false;
+      }
       // the copies two planes ahead, spread over the warps' first lanes
       if (lane == 0) {
         if (warp < narr && k + 2 <= kmain_end) issue_main_array(k + 2, warp, warp_map);
@@ -345,24 +366,31 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         Py[r] = nPy[r];
         Pz[r] = nPz[r];
       }
+      return true;
     };
 
     const int k_lo = zs + 2, k_hi = min(ze + 1, G.vz - 2);
     int k = kstart;
-    for (; k <= kend && k < k_lo; ++k) zstep(k, BoolTag<false>{});
-    for (; k <= k_hi; ++k) zstep(k, BoolTag<true>{});
-    for (; k <= kend; ++k) zstep(k, BoolTag<false>{});
+    bool go_on = true;
+    for (; go_on && k <= kend && k < k_lo; ++k) go_on = zstep(k, BoolTag<false>{});
+    for (; go_on && k <= k_hi; ++k) go_on = zstep(k, BoolTag<true>{});
+    for (; go_on && k <= kend; ++k) go_on = zstep(k, BoolTag<false>{});
   };
   if (interior) march(BoolTag<true>{});
   else march(BoolTag<false>{});
-  if (timed_out) {
+  if (k_stop >= 0 && threadIdx.x == 0) {
     if (fp.error_flag) atomicOr(fp.error_flag, 2);
-    // Let copies still in flight into this CTA's shared memory land (bounded)
-    // before the CTA exits: the last plane issued into each slot.
-    for (int p = max(kstart, kmain_end - kTmaMainSlots + 1); p <= kmain_end; ++p)
+    // Copies still in flight into this CTA's shared memory must land before
+    // it exits.  Up to step k_stop the main ring was filled to plane
+    // k_stop + 1 and the pz ring to k_stop + 2 (the initial issue: kstart + 1,
+    // kstart + 2), each slot holding at most one pending phase: wait for the
+    // last plane issued into each slot, with the default bound.
+    const int l_main = min(max(k_stop + 1, kstart + 1), kmain_end);
+    const int l_pz = min(max(k_stop + 2, kstart + 2), kpz_end);
+    for (int p = max(kstart, l_main - kTmaMainSlots + 1); p <= l_main; ++p)
       mbar_wait_bounded(&mbars[(p - kstart) % kTmaMainSlots],
                         (unsigned)(((p - kstart) / kTmaMainSlots) & 1), kTmaWaitLimitNs);
-    for (int p = max(kstart, kpz_end - kTmaPzSlots + 1); p <= kpz_end; ++p)
+    for (int p = max(kstart, l_pz - kTmaPzSlots + 1); p <= l_pz; ++p)
       mbar_wait_bounded(&zbars[(p - kstart) % kTmaPzSlots], (unsigned)(((p - kstart) / kTmaPzSlots) & 1),
                         kTmaWaitLimitNs);
   }

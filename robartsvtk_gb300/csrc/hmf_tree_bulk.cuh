@@ -39,16 +39,19 @@ __host__ __device__ constexpr int tree_bulk_smem_bytes(int n) {
 
 __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag) {
   __shared__ TreeTable T;
-  __shared__ int abort_cta;
+  __shared__ int abort_cta, stall_cta, stop_cta;
   extern __shared__ __align__(128) unsigned char tb_raw[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tb_raw);  // [2]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tb_raw);  // [2], then the stall barrier
   float* stage0 = reinterpret_cast<float*>(tb_raw + 128);
 
   for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
   __syncthreads();  // thread 0 reads the table below
   if (threadIdx.x == 0) {
-    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    const int flag = error_flag ? *(volatile int*)error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(error_flag, flag);
+    stop_cta = 0;
     // bulk-copy destinations must be 16-byte aligned: refuse to run otherwise.
     if (smem_addr(tb_raw) & 15) {
       abort_cta = 1;
@@ -56,6 +59,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
     }
     // one arrival per staged array (the copies are spread over the threads)
     for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], (unsigned)(3 * (T.n - 1) + 1));
+    mbar_init(&bars[kTreeBulkStages], 1);  // completed by nothing: a requested stall waits on it
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -90,14 +94,25 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
     }
   };
 
+  // A wait that runs out raises stop_cta; after the CTA barrier that ends the
+  // chunk every thread sees it and the loop ends before another copy is
+  // issued, so the copies in flight are exactly the last one of each stage.
   bool timed_out = false;
+  auto wait_stage = [&](uint64_t* bar, unsigned parity) {
+    if (timed_out) return;
+    if (!mbar_wait_bounded(bar, parity, kTmaWaitLimitNs)) {
+      timed_out = true;
+      *(volatile int*)&stop_cta = 1;
+    }
+  };
   int nissued[kTreeBulkStages] = {0, 0};  // kept by every thread (thread 0 always issues)
   long long chunk = blockIdx.x;
   if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
   if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
+  if (threadIdx.x == 0 && stall_cta) wait_stage(&bars[kTreeBulkStages], 0);
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
-    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    wait_stage(&bars[s], (unsigned)((j >> 1) & 1));
     float* st = stage(s);
     const long long v0 = chunk * vc;
     const int len = (int)min((long long)vc, G.vol - v0);
@@ -157,15 +172,16 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
     // before the bulk copy that will refill the stage (async proxy).
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // stage s is free again
+    if (stop_cta) break;
     if (chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
-  if (timed_out && error_flag) atomicOr(error_flag, 2);
-  if (threadIdx.x == 0) {
-    // Copies into this CTA's shared memory must have landed before it exits;
-    // after a time-out wait for the last one of each stage (bounded).
-    if (timed_out)
-      for (int s = 0; s < kTreeBulkStages; ++s)
-        if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+  __syncthreads();
+  if (stop_cta && threadIdx.x == 0) {
+    if (error_flag) atomicOr(error_flag, 2);
+    // Copies into this CTA's shared memory must have landed before it exits:
+    // wait (bounded) for the last one issued into each stage.
+    for (int s = 0; s < kTreeBulkStages; ++s)
+      if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
   }
 }
 
@@ -183,20 +199,24 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
   constexpr int VC = tree_bulk_chunk(N);
   constexpr int Q = VC / 4;  // float4 per staged array
   __shared__ TreeTable T;
-  __shared__ int abort_cta;
+  __shared__ int abort_cta, stall_cta, stop_cta;
   extern __shared__ __align__(128) unsigned char tb_raw[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tb_raw);  // [2]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tb_raw);  // [2], then the stall barrier
   float4* stage0 = reinterpret_cast<float4*>(tb_raw + 128);
 
   for (int i = threadIdx.x; i < (int)(sizeof(TreeTable) / 4); i += blockDim.x)
     reinterpret_cast<int*>(&T)[i] = reinterpret_cast<const int*>(table)[i];
   if (threadIdx.x == 0) {
-    abort_cta = error_flag ? (*(volatile int*)error_flag & 2) : 0;
+    const int flag = error_flag ? *(volatile int*)error_flag : 0;
+    abort_cta = flag & 2;
+    stall_cta = take_stall_request(error_flag, flag);
+    stop_cta = 0;
     if (smem_addr(tb_raw) & 15) {
       abort_cta = 1;
       if (error_flag) atomicOr(error_flag, 4);
     }
     for (int s = 0; s < kTreeBulkStages; ++s) mbar_init(&bars[s], A);  // one arrival per staged array
+    mbar_init(&bars[kTreeBulkStages], 1);  // completed by nothing: a requested stall waits on it
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -246,16 +266,27 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
     bulk_load(reinterpret_cast<float*>(stage0 + s * A * Q) + ta * VC, asrc + v0, bytes, bar);
   };
 
+  // A wait that runs out raises stop_cta; after the CTA barrier that ends the
+  // chunk every thread sees it and the loop ends before another copy is
+  // issued, so the copies in flight are exactly the last one of each stage.
   bool timed_out = false;
+  auto wait_stage = [&](uint64_t* bar, unsigned parity) {
+    if (timed_out) return;
+    if (!mbar_wait_bounded(bar, parity, kTmaWaitLimitNs)) {
+      timed_out = true;
+      *(volatile int*)&stop_cta = 1;
+    }
+  };
   int nissued[kTreeBulkStages] = {0, 0};  // kept by every issuing thread
   long long chunk = blockIdx.x;
   if (ta < A) {
     if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
     if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, 1), ++nissued[1];
   }
+  if (threadIdx.x == 0 && stall_cta) wait_stage(&bars[kTreeBulkStages], 0);
   for (int j = 0; chunk < nchunks; ++j, chunk += gridDim.x) {
     const int s = j & 1;
-    if (!timed_out && !mbar_wait_bounded(&bars[s], (unsigned)((j >> 1) & 1), kTmaWaitLimitNs)) timed_out = true;
+    wait_stage(&bars[s], (unsigned)((j >> 1) & 1));
     const long long v0 = chunk * VC;
     const int len = (int)min((long long)VC, G.vol - v0);
     if ((int)threadIdx.x * 4 < len) {
@@ -323,12 +354,18 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // stage s is free again
+    if (stop_cta) break;
     if (ta < A && chunk + 2LL * gridDim.x < nchunks) issue(chunk + 2LL * gridDim.x, s), ++nissued[s];
   }
-  if (timed_out && error_flag) atomicOr(error_flag, 2);
-  if (threadIdx.x == 0 && timed_out)
+  __syncthreads();
+  // Copies into this CTA's shared memory must have landed before it exits:
+  // after a time-out every issuing thread waits (bounded) for the last copy
+  // it issued into each stage.
+  if (stop_cta && ta < A) {
+    if (threadIdx.x == 0 && error_flag) atomicOr(error_flag, 2);
     for (int s = 0; s < kTreeBulkStages; ++s)
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
+  }
 }
 
 }  // namespace hmf

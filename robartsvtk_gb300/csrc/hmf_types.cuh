@@ -168,6 +168,7 @@ struct FlowTmaParams {
   const FlowVolume* vols;
   const FlowItem* items;
   int* error_flag;
+  unsigned long long wait_limit_ns;  // bound of every copy wait (kTmaWaitLimitNs unless a caller sets it)
 };
 
 // Compile-time flag passed to generic lambdas (kernel specialisations).
@@ -176,8 +177,10 @@ struct BoolTag {
   static constexpr bool value = B;
 };
 
-// Bound of every mbarrier wait of the copy pipelines; a wait that runs out
-// sets the error flag instead of hanging.
+// Default bound of every mbarrier wait of the copy pipelines; a wait that
+// runs out sets the error flag instead of hanging.  The flow kernels take
+// their bound as a parameter (hmf_set_wait_limit); the drain after a
+// time-out always uses this one.
 constexpr uint64_t kTmaWaitLimitNs = 500000000ull;  // 0.5 s: far beyond any healthy copy
 
 }  // namespace hmf

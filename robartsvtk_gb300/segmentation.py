@@ -57,6 +57,19 @@ def _array_pointer(arr, nvox: int):
     raise TypeError("volumes must be numpy arrays or torch tensors")
 
 
+def _truth_pointer(truth, nvox: int):
+    """(pointer, where, keepalive) of an int32 class map (numpy or torch)."""
+    if isinstance(truth, np.ndarray):
+        if truth.dtype != np.int32 or not truth.flags["C_CONTIGUOUS"] or truth.size != nvox:
+            raise TypeError("truth must be a C-contiguous int32 array of the volume's size")
+        return truth.ctypes.data, HMF_HOST, truth
+    import torch
+
+    if truth.dtype != torch.int32 or not truth.is_contiguous() or truth.numel() != nvox:
+        raise TypeError("truth must be a contiguous int32 tensor of the volume's size")
+    return truth.data_ptr(), HMF_DEVICE if truth.is_cuda else HMF_HOST, truth
+
+
 class HMFSolver:
     """One solver context: a volume size (vx, vy, vz), a label tree given as a
     parent array, and a semantics (REF_CUDA or REF_CPU)."""
@@ -148,22 +161,61 @@ class HMFSolver:
         return _fetch_energy(lambda f0, f, n: self._lib.hmf_get_energy(self._ctx, f0, f, n), len(self.parent),
                              self._ctx)
 
+    # -- bounded copy waits --------------------------------------------------
+    def set_wait_limit(self, limit_ns: int = 0) -> None:
+        """Bound (ns) of the flow kernels' copy waits (0: the default 0.5 s)."""
+        check(self._lib.hmf_set_wait_limit(self._ctx, int(limit_ns)), self._ctx)
+
+    def inject_wait_stall(self, kernel: int) -> None:
+        """Make one CTA of the next launch of `kernel` (HMF_STALL_*) wait on a
+        barrier nothing completes, so its bounded wait runs out (-1 cancels)."""
+        check(self._lib.hmf_inject_wait_stall(self._ctx, int(kernel)), self._ctx)
+
+    # -- reference precision (FP64) ----------------------------------------
+    def solve_fp64(self, stream=None) -> None:
+        """The same REF_CUDA iteration in FP64 on the GPU (hmf_solve_fp64)."""
+        check(self._lib.hmf_solve_fp64(self._ctx, _stream_handle(stream)), self._ctx)
+
+    def labels_fp64(self, node: int, stream=None) -> np.ndarray:
+        """FP64 labelling of a non-root vertex, float64 [VZ, VY, VX]."""
+        out = np.empty((self.dims[2], self.dims[1], self.dims[0]), dtype=np.float64)
+        check(self._lib.hmf_get_labels_fp64(self._ctx, int(node), out.ctypes.data, HMF_HOST,
+                                            _stream_handle(stream)), self._ctx)
+        return out
+
+    def fp64_error(self, stream=None) -> dict:
+        """max |u_fp32 - u_fp64| over leaves and voxels between the last solve
+        and the last solve_fp64, and the fraction of voxels whose argmax leaf
+        agrees."""
+        mx = ctypes.c_double()
+        agree = ctypes.c_double()
+        check(self._lib.hmf_fp64_error(self._ctx, ctypes.byref(mx), ctypes.byref(agree), _stream_handle(stream)),
+              self._ctx)
+        return {"max_abs_err": mx.value, "argmax_agreement": agree.value}
+
+    def fp64_loss(self, truth, eps: float = 1e-6, stream=None) -> float:
+        """The adjoint's cross-entropy loss on the FP64 labels."""
+        ptr, where, keep = _truth_pointer(truth, self.nvox)
+        loss = ctypes.c_double()
+        check(self._lib.hmf_fp64_loss(self._ctx, ptr, where, float(eps), ctypes.byref(loss),
+                                      _stream_handle(stream)), self._ctx)
+        del keep
+        return loss.value
+
+    def set_fp64_probe(self, kind: int = _capi.HMF_FP64_PROBE_NONE, node: int = 0, voxel: int = 0,
+                       value: float = 0.0) -> None:
+        """Inputs of later FP64 solves that differ from the FP32 inputs (for
+        finite differences): a leaf's data term at one dense voxel index, or a
+        vertex's alpha, as a double; kind NONE clears them."""
+        check(self._lib.hmf_set_fp64_probe(self._ctx, int(kind), int(node), int(voxel), float(value)), self._ctx)
+
     # -- adjoint ----------------------------------------------------------
     def solve_adjoint(self, truth, checkpoint_every: int = 0, eps: float = 1e-6, stream=None) -> float:
         """Solve, then differentiate L = -(1/V) sum log(max(u_truth, eps)) of
         the final leaf labels.  truth: int32 [VZ, VY, VX] indices into
         `self.leaves` (numpy, or a torch tensor on the host or the device).
         Returns L; gradients via data_gradient() / alpha_gradient()."""
-        if isinstance(truth, np.ndarray):
-            if truth.dtype != np.int32 or not truth.flags["C_CONTIGUOUS"] or truth.size != self.nvox:
-                raise TypeError("truth must be a C-contiguous int32 array of the volume's size")
-            ptr, where, keep = truth.ctypes.data, HMF_HOST, truth
-        else:
-            import torch
-
-            if truth.dtype != torch.int32 or not truth.is_contiguous() or truth.numel() != self.nvox:
-                raise TypeError("truth must be a contiguous int32 tensor of the volume's size")
-            ptr, where, keep = truth.data_ptr(), HMF_DEVICE if truth.is_cuda else HMF_HOST, truth
+        ptr, where, keep = _truth_pointer(truth, self.nvox)
         loss = ctypes.c_double()
         check(self._lib.hmf_solve_adjoint(self._ctx, ptr, where, int(checkpoint_every), float(eps),
                                           ctypes.byref(loss), _stream_handle(stream)), self._ctx)
