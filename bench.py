@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--iterations", type=int, default=500)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own CUDA kernels on this GPU")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-sequential measurement")
     ap.add_argument("--batch-count", type=int, default=64)
     ap.add_argument("--batch-iterations", type=int, default=200)
@@ -213,6 +215,49 @@ def cpu_reference_sample(w, seconds: float, threads: int):
             "seconds": t, "iterations": iters}
 
 
+def cpu_ref_cuda_sample(w, seconds: float, threads: int):
+    """The oracle's REF_CUDA restatement (the algorithm the GPU path runs, in
+    the reference kernels' pass order) on all host threads: the full volume
+    for as many iterations as fit in ~`seconds`, initialisation subtracted."""
+    from oracle import oracle as O
+
+    def run(iters):
+        t0 = time.perf_counter()
+        O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, iters, w.step, w.cc, threads=threads)
+        return time.perf_counter() - t0
+
+    t_init = run(0)
+    t_one = max(run(1) - t_init, 1e-6)
+    iters = max(1, min(20, int(seconds / t_one)))
+    t = max(run(iters) - t_init, 1e-6)
+    L = len(w.leaves)
+    return {"value": w.nvox * L * iters / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "full %dx%dx%d volume, %d of %d iterations (initialisation excluded), REF_CUDA semantics, "
+                      "FP32, OpenMP" % (w.dims[0], w.dims[1], w.dims[2], iters, w.iterations),
+            "seconds": t, "iterations": iters}
+
+
+def reference_gpu_sample(w, iterations: int = 10):
+    """The reference's own HMF CUDA kernels (CUDA_hierarchicalmaxflow.cu and
+    CUDA_commonKernels.cu, compiled unmodified from the reference sources for
+    sm_103a into oracle/_ref/hmf_ref_kernels.cubin) on this GPU, launched in
+    the reference host code's order (vtkCudaHierarchicalMaxFlowSegmentation.cxx:106-476)
+    with every buffer resident: two untimed iterations, then `iterations`
+    timed with CUDA events (back to back, without the reference's
+    per-iteration stream synchronisation)."""
+    from oracle import ref_kernels
+
+    if not ref_kernels.available():
+        return {"unavailable": "the reference kernels' cubin was not built (the reference sources were absent)"}
+    r = ref_kernels.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, iterations=2, step=w.step, cc=w.cc,
+                          time_iterations=iterations, fetch_outputs=False)
+    ms = r["ms_per_iteration"]
+    return {"value": w.nvox * len(w.leaves) / (ms / 1000.0), "unit": UNIT, "ms_per_iteration": ms,
+            "launches_per_iteration": r["launches_per_iteration"],
+            "sample": "full %dx%dx%d volume, %d timed iterations after 2" % (w.dims[0], w.dims[1], w.dims[2],
+                                                                            iterations)}
+
+
 def host_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -234,15 +279,22 @@ def run_reference(args):
     for _ in range(max(0, args.warmup)):
         cpu_reference_sample(w, 0.5, threads)
     vals = []
+    secs = []
     last = None
     for _ in range(max(1, args.steps)):
         last = cpu_reference_sample(w, args.cpu_seconds / max(1, args.steps), threads)
         vals.append(last["value"])
+        secs.append(last["seconds"])
     vals.sort()
     value = vals[len(vals) // 2]
+    # A step is one bounded sample (a few iterations of the full volume):
+    # ms_per_step is its measured time; the full 500-iteration solve at that
+    # rate is stated apart.
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1000.0 * w.nvox * len(w.leaves) * w.iterations / value,
+           "ms_per_step": 1000.0 * sum(secs) / len(secs),
+           "step": "one bounded sample: %s" % last["sample"],
+           "extrapolated_ms_per_solve": 1000.0 * w.nvox * len(w.leaves) * w.iterations / value,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": WORKLOAD, "volume": list(w.dims), "vertices": len(w.parent),
                       "leaves": len(w.leaves), "iterations": w.iterations, "semantics": "REF_CPU"},
@@ -319,6 +371,25 @@ def run_ours(args):
     solver.set_timing(False)
     t_flow, t_tree, t_init = st["flow_ms"], st["tree_ms"], st["init_ms"]
     post = bench_post(w, solver, stream)
+
+    # ---- the convergence log's cost (max / mean |du| per iteration) -------
+    solver.set_convergence_log(True)
+    solver.solve(stream)
+    stream.synchronize()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(2):
+        solver.solve(stream)
+    g1.record(stream)
+    stream.synchronize()
+    ms_log = g0.elapsed_time(g1) / 2
+    conv = solver.convergence()
+    solver.set_convergence_log(False)
+    convergence = {"ms_per_step_with_log": ms_log, "ms_per_step_without": ms_rank,
+                   "overhead_frac": ms_log / ms_rank - 1.0,
+                   "final_max_change": float(conv["max"][-1]), "final_mean_change": float(conv["mean"][-1]),
+                   "max_change_every_100": [float(x) for x in conv["max"][::100]]}
 
     # ---- the FP32 labels' distance from the same iteration in FP64 --------
     # (outside the timed region: hmf_solve_fp64 on the same context and
@@ -405,6 +476,7 @@ def run_ours(args):
         "fp64_max_abs_err": fp64["max_abs_err"],
         "argmax_agreement": fp64["argmax_agreement"],
         "fp64": fp64,
+        "convergence_log": convergence,
         "post": post,
     }
     if rank == 0 and not args.no_batched:
@@ -417,6 +489,14 @@ def run_ours(args):
         out["dag"] = bench_dag(args, stream, None if args.no_cpu_baseline else host_threads())
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
+        cb = cpu_ref_cuda_sample(w, args.cpu_seconds, host_threads())
+        cb["ratio"] = value / cb["value"]
+        out["cpu_baseline_ref_cuda"] = cb
+    if rank == 0 and not args.no_reference_gpu:
+        rg = reference_gpu_sample(w)
+        if "value" in rg:
+            rg["ratio"] = value / rg["value"]
+        out["reference_gpu"] = rg
     if rank == 0:
         print(json.dumps(out))
     solver.close()

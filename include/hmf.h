@@ -169,6 +169,21 @@ int hmf_autotune(hmf_ctx* ctx, void* stream);
 int hmf_set_zchunk(hmf_ctx* ctx, int z);
 int hmf_get_zchunk(const hmf_ctx* ctx);
 
+/* ---- Convergence log --------------------------------------------------------
+ * No counterpart in the reference, which runs a fixed number of iterations
+ * and computes no convergence measure (its header gives the cost as the
+ * reason, vtkHierarchicalMaxFlowSegmentation.h:61-63).  With the log on,
+ * the label sweep of every iteration also reduces, over all non-root
+ * vertices and voxels, max |u_new - u_old| and the sum of |u_new - u_old|
+ * (warp shuffles and a few atomics per CTA inside the same kernel; no extra
+ * pass over memory).  hmf_get_convergence writes, for the iterations of the
+ * last hmf_solve (up to `capacity`), the maximum and the mean (the sum over
+ * (n_nodes - 1) x voxels) and returns the number of iterations logged.
+ * REF_CUDA tree contexts; a batch's volumes are pooled (each volume's VX a
+ * multiple of 4).  Toggling re-captures the iteration graphs. */
+int hmf_set_convergence_log(hmf_ctx* ctx, int enabled);
+int hmf_get_convergence(hmf_ctx* ctx, double* max_change, double* mean_change, int capacity);
+
 /* ---- Bounded copy waits ----------------------------------------------------
  * No counterpart in the reference, whose kernels have no waits.  The
  * kernels that stream their inputs through shared memory (TMA / bulk copies

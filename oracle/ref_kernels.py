@@ -123,9 +123,16 @@ class ReferenceKernels:
         self._ck(self.cu.cuLaunchKernel(self.fn[key], grid, 1, 1, NUMTHREADS, 1, 1, 0, stream, ptrs, None), key)
 
 
-def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1, cc=0.25):
+def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1, cc=0.25, time_iterations=0,
+          fetch_outputs=True):
     """REF_CUDA through the reference's own kernels.  Arguments as
-    oracle.oracle.solve(); returns {"u": [n, VZ, VY, VX] float32, "sink": ...}."""
+    oracle.oracle.solve(); returns {"u": [n, VZ, VY, VX] float32, "sink": ...}.
+
+    time_iterations > 0: after the `iterations` iterations, that many more
+    are timed with CUDA events on the launching stream (launched back to
+    back, without the per-iteration stream synchronisation of
+    vtkCudaHierarchicalMaxFlowSegmentation.cxx:681); the result then holds
+    "ms_per_iteration" and "launches_per_iteration"."""
     import torch
 
     K = ReferenceKernels()
@@ -251,6 +258,28 @@ def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1,
     for _ in range(int(iterations)):
         solve_node(root)
     torch.cuda.synchronize()
+    timing = {}
+    if time_iterations > 0:
+        count = [0]
+        launch = K.launch
+
+        def counted(*a):
+            count[0] += 1
+            launch(*a)
+
+        K.launch = counted
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(int(time_iterations)):
+            solve_node(root)
+        e1.record()
+        torch.cuda.synchronize()
+        K.launch = launch
+        timing = {"ms_per_iteration": e0.elapsed_time(e1) / time_iterations,
+                  "launches_per_iteration": count[0] / time_iterations}
+    if not fetch_outputs:
+        return timing
 
     def fetch(p):
         return _as_tensor(keep, p, V, pad).cpu().numpy().reshape(vz, vy, vx)
@@ -261,7 +290,7 @@ def solve(dims, parent, data, smooth=None, alpha=None, iterations=100, step=0.1,
         s[v] = fetch(sink[v])
         if v != root:
             u[v] = fetch(lab[v])
-    return {"u": u, "sink": s}
+    return {"u": u, "sink": s, **timing}
 
 
 def _as_tensor(keep, ptr, V, pad):

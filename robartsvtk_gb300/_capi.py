@@ -82,6 +82,8 @@ SIGNATURES = [
                                       ctypes.POINTER(ctypes.c_double), _P]),
     ("hmf_get_energy", _I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_batch_get_energy", _I, [_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
+    ("hmf_set_convergence_log", _I, [_P, _I]),
+    ("hmf_get_convergence", _I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _I]),
     ("hmf_set_wait_limit", _I, [_P, ctypes.c_longlong]),
     ("hmf_inject_wait_stall", _I, [_P, _I]),
     ("hmf_solve_fp64", _I, [_P, _P]),

@@ -446,6 +446,11 @@ int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out) {
       if (!src[b].first) continue;
       const auto& V = c->vols[b];
       const cudaMemcpyKind kind = src[b].second == HMF_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+      if (V.pitch == V.vx) {  // unpadded rows: one linear copy (a 2-D copy moves row by row)
+        CK(cudaMemcpyAsync(dst + V.off, src[b].first, (size_t)V.vol * sizeof(float), kind, s),
+           "cudaMemcpyAsync(input)");
+        continue;
+      }
       CK(cudaMemcpy2DAsync(dst + V.off, (size_t)V.pitch * sizeof(float), src[b].first, (size_t)V.vx * sizeof(float),
                            (size_t)V.vx * sizeof(float), (size_t)V.vy * V.vz, kind, s),
          "cudaMemcpy2DAsync(input)");
@@ -534,24 +539,42 @@ int tree_grid(hmf_ctx* c) {
   return (int)std::min<long long>(blocks, (long long)c->sm_count * 16);
 }
 
-int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s) {
+// The convergence log's device view (the arena of hmf_set_convergence_log).
+hmf::GapLog gap_view(const hmf_ctx* c) {
+  hmf::GapLog g{};
+  g.counter = reinterpret_cast<unsigned int*>(c->d_gap);
+  g.max_bits = g.counter + 2;
+  g.sum = reinterpret_cast<double*>(c->d_gap + round_up(8 + 4 * (size_t)c->gap_cap, 8));
+  g.capacity = c->gap_cap;
+  g.vx = c->vols[0].vx;
+  g.pitch = c->vols.size() == 1 && c->vols[0].pitch != c->vols[0].vx ? c->vols[0].pitch : 0;
+  return g;
+}
+
+size_t gap_bytes(int cap) { return round_up(8 + 4 * (size_t)cap, 8) + 8 * (size_t)cap; }
+
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log) {
   const int smem = hmf::tree_bulk_smem_bytes(c->n);
   const int vc = hmf::tree_bulk_chunk(c->n);
   const long long chunks = (c->geo.vol + vc - 1) / vc;
   const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
   const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
   if (int rc = maybe_request_stall(c, HMF_STALL_SWEEP, s)) return rc;
+  const hmf::GapLog gap = gap_log ? gap_view(c) : hmf::GapLog{};
   switch (c->n) {
-#define HMF_TREE_N(N)                                                                 \
-  case N:                                                                             \
-    hmf::tree_bulk_n_kernel<N><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error); \
+#define HMF_TREE_N(N)                                                                             \
+  case N:                                                                                         \
+    if (gap_log)                                                                                  \
+      hmf::tree_bulk_n_kernel<N, true><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error, gap); \
+    else                                                                                          \
+      hmf::tree_bulk_n_kernel<N, false><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);    \
     break;
     HMF_TREE_N(2) HMF_TREE_N(3) HMF_TREE_N(4) HMF_TREE_N(5) HMF_TREE_N(6) HMF_TREE_N(7) HMF_TREE_N(8)
     HMF_TREE_N(9) HMF_TREE_N(10) HMF_TREE_N(11) HMF_TREE_N(12) HMF_TREE_N(13) HMF_TREE_N(14) HMF_TREE_N(15)
     HMF_TREE_N(16)
 #undef HMF_TREE_N
     default:
-      hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);
+      hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error, gap);
   }
   CK(cudaGetLastError(), "tree_bulk_kernel launch");
   ++c->launches;
@@ -617,7 +640,7 @@ int launch_dag_sweep(hmf_ctx* c, cudaStream_t s) {
 
 int launch_tree(hmf_ctx* c, cudaStream_t s) {
   if (c->dag) return launch_dag_sweep(c, s);
-  if (c->tree_kind == 0) return launch_tree_bulk_with(c, c->d_tree, s);
+  if (c->tree_kind == 0) return launch_tree_bulk_with(c, c->d_tree, s, c->gap_on);
   if (c->tree_kind == 1) {
     const size_t smem4 = 4 * (size_t)c->n * hmf::kTree4Threads * sizeof(float4);
     const long long quads = c->geo.vol / 4;
@@ -912,9 +935,12 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::tree_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           128 + hmf::kTreeBulkSmemBudget),
      "cudaFuncSetAttribute(tree_bulk_kernel)");
-#define HMF_TREE_N_ATTR(N)                                                                    \
-  CK(cudaFuncSetAttribute(hmf::tree_bulk_n_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                          hmf::tree_bulk_smem_bytes(N)),                                      \
+#define HMF_TREE_N_ATTR(N)                                                                           \
+  CK(cudaFuncSetAttribute(hmf::tree_bulk_n_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                          hmf::tree_bulk_smem_bytes(N)),                                             \
+     "cudaFuncSetAttribute(tree_bulk_n_kernel)");                                                    \
+  CK(cudaFuncSetAttribute(hmf::tree_bulk_n_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                          hmf::tree_bulk_smem_bytes(N)),                                             \
      "cudaFuncSetAttribute(tree_bulk_n_kernel)");
   HMF_TREE_N_ATTR(2) HMF_TREE_N_ATTR(3) HMF_TREE_N_ATTR(4) HMF_TREE_N_ATTR(5) HMF_TREE_N_ATTR(6)
   HMF_TREE_N_ATTR(7) HMF_TREE_N_ATTR(8) HMF_TREE_N_ATTR(9) HMF_TREE_N_ATTR(10) HMF_TREE_N_ATTR(11)
@@ -963,10 +989,14 @@ int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* s
     if (int rc = check_device_pointer(c, out, "output")) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const auto& V = c->vols[b];
-  CK(cudaMemcpy2DAsync(out, (size_t)V.vx * sizeof(float), src + V.off, (size_t)V.pitch * sizeof(float),
-                       (size_t)V.vx * sizeof(float), (size_t)V.vy * V.vz,
-                       where == HMF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s),
-     "cudaMemcpy2DAsync(output)");
+  const cudaMemcpyKind kind = where == HMF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (V.pitch == V.vx) {  // unpadded rows: one linear copy
+    CK(cudaMemcpyAsync(out, src + V.off, (size_t)V.vol * sizeof(float), kind, s), "cudaMemcpyAsync(output)");
+  } else {
+    CK(cudaMemcpy2DAsync(out, (size_t)V.vx * sizeof(float), src + V.off, (size_t)V.pitch * sizeof(float),
+                         (size_t)V.vx * sizeof(float), (size_t)V.vy * V.vz, kind, s),
+       "cudaMemcpy2DAsync(output)");
+  }
   if (where == HMF_HOST) {
     CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(output)");
     return check_error_flag(c);
@@ -1183,6 +1213,7 @@ int hmf_destroy(hmf_ctx* c) {
   adjoint_free(c);
   fp64_free(c);
   if (c->d_post) cudaFree(c->d_post);
+  if (c->d_gap) cudaFree(c->d_gap);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return HMF_OK;
@@ -1256,6 +1287,20 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   Staged staged;
   int rc = begin_solve(c, user, staged);
   if (rc) return rc;
+  c->gap_logged = 0;
+  if (c->gap_on && c->semantics == HMF_SEMANTICS_REF_CUDA) {
+    if (c->gap_cap < c->iterations) {  // a longer log: new arena, graphs re-captured with it
+      drop_graphs(c);
+      if (c->d_gap) cudaFree(c->d_gap);
+      c->d_gap = nullptr;
+      c->gap_cap = 0;
+      const int cap = std::max(c->iterations, 64);
+      CK(cudaMalloc(&c->d_gap, gap_bytes(cap)), "cudaMalloc(convergence log)");
+      c->gap_cap = cap;
+    }
+    CK(cudaMemsetAsync(c->d_gap, 0, gap_bytes(c->gap_cap), s), "cudaMemsetAsync(convergence log)");
+    c->gap_logged = c->iterations;
+  }
   if (c->semantics == HMF_SEMANTICS_REF_CPU) {
     rc = timed(c, 1, s, do_refcpu, 0);
     if (rc) return rc;
@@ -1346,6 +1391,53 @@ int hmf_set_zchunk(hmf_ctx* c, int z) {
 }
 
 int hmf_get_zchunk(const hmf_ctx* c) { return c ? c->zchunk : HMF_ERR_INVALID_ARGUMENT; }
+
+int hmf_set_convergence_log(hmf_ctx* c, int enabled) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (enabled) {
+    if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the convergence log is for label trees (hmf_create)");
+    if (c->semantics != HMF_SEMANTICS_REF_CUDA)
+      return fail(c, HMF_ERR_INVALID_ARGUMENT, "the convergence log needs REF_CUDA semantics");
+    if (c->tree_kind != 0)
+      return fail(c, HMF_ERR_INVALID_ARGUMENT, "the convergence log runs in the staged sweep kernels only");
+    if (c->vols.size() > 1)
+      for (const auto& V : c->vols)
+        if (V.pitch != V.vx)
+          return fail(c, HMF_ERR_INVALID_ARGUMENT,
+                      "the convergence log of a batch needs every volume's VX to be a multiple of 4");
+  }
+  if ((enabled != 0) == c->gap_on) return HMF_OK;
+  DeviceGuard dg(c->device);
+  drop_graphs(c);  // the captured sweeps differ
+  c->gap_on = enabled != 0;
+  return HMF_OK;
+}
+
+int hmf_get_convergence(hmf_ctx* c, double* max_change, double* mean_change, int capacity) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (capacity < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "capacity must be >= 0");
+  const int n = std::min(capacity, c->gap_logged);
+  if (n == 0) return c->gap_logged;
+  DeviceGuard dg(c->device);
+  const hmf::GapLog g = gap_view(c);
+  std::vector<unsigned int> bits(n);
+  std::vector<double> sums(n);
+  CK(cudaMemcpyAsync(bits.data(), g.max_bits, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "cudaMemcpyAsync(convergence log)");
+  CK(cudaMemcpyAsync(sums.data(), g.sum, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "cudaMemcpyAsync(convergence log)");
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize(convergence log)");
+  double voxels = 0;
+  for (const auto& V : c->vols) voxels += (double)V.vx * V.vy * V.vz;
+  const double count = voxels * (double)(c->n - 1);
+  for (int i = 0; i < n; ++i) {
+    float f;
+    std::memcpy(&f, &bits[i], 4);
+    if (max_change) max_change[i] = f;
+    if (mean_change) mean_change[i] = sums[i] / count;
+  }
+  return c->gap_logged;
+}
 
 int hmf_set_wait_limit(hmf_ctx* c, long long limit_ns) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
@@ -1766,9 +1858,11 @@ extern "C" int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int 
           "cudaMemcpy2DAsync(labels)");
     }
   }
-  NCK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  // the flag is read on the caller's stream, so the wait covers that stream
+  // only (a plain cudaMemcpy would wait for every blocking stream)
   int flag = 0;
-  NCK(cudaMemcpy(&flag, d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  NCK(cudaMemcpyAsync(&flag, d_error, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(error flag)");
+  NCK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   if (flag)
     return noalloc_fail(HMF_ERR_INVALID_ARGUMENT,
                         "Data prior and smoothness must be non-negative (the solve ran on invalid input)");

@@ -89,6 +89,12 @@ struct hmf_ctx {
   unsigned long long wait_limit_ns = hmf::kTmaWaitLimitNs;
   int stall_kind = -1;  // HMF_STALL_* of the next launch of that kind that is to stall (-1: none)
 
+  // convergence log (hmf_set_convergence_log): per iteration max and sum of |u_new - u_old|
+  bool gap_on = false;
+  char* d_gap = nullptr;  // counter[2], max bits[gap_cap], sums[gap_cap]
+  int gap_cap = 0;
+  int gap_logged = 0;     // iterations logged by the last solve
+
   bool timing = false;
   long long launches = 0;
   double kind_ms[3] = {0, 0, 0};
@@ -176,7 +182,7 @@ int launch_flow(hmf_ctx* c, int parity, cudaStream_t s);
 int launch_tree(hmf_ctx* c, cudaStream_t s);
 // The TMA flow kernel and the bulk sweep over caller-built tables.
 int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s);
-int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s);
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log = false);
 // Tensor map of one pitched volume block; box = kTmaBoxX columns x `rows` rows.
 int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V,
                      int rows = hmf::kTmaRows);

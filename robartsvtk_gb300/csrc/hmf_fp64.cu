@@ -298,9 +298,14 @@ __global__ void f64_compare_kernel(const F64Compare C, const Geometry G, unsigne
   }
 }
 
-// L = -(1/V) sum_i log(max(u_{leaf(truth_i)}(i), eps)) on the FP64 labels.
-__global__ void f64_loss_kernel(const F64Compare C, const int* __restrict__ truth, const Geometry G, double eps,
-                                double n_voxels, double* loss, int* bad_flag) {
+// L = -(1/V) sum_i log(max(u_{leaf(truth_i)}(i), eps)) on the FP64 labels,
+// summed in a fixed order (per block, then over the blocks on the host), so
+// that two solves that differ in a few voxels give losses whose difference
+// comes from those voxels only -- what a finite difference needs.
+constexpr int kF64LossThreads = 256;
+__global__ void __launch_bounds__(kF64LossThreads)
+f64_loss_kernel(const F64Compare C, const int* __restrict__ truth, const Geometry G, double eps, double n_voxels,
+                double* partial, int* bad_flag) {
   double acc = 0.0;
   int bad = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < G.vol;
@@ -316,8 +321,15 @@ __global__ void f64_loss_kernel(const F64Compare C, const int* __restrict__ trut
     acc -= log(u > eps ? u : eps) / n_voxels;
   }
   if (bad) atomicOr(bad_flag, 1);
+  __shared__ double warp_sum[kF64LossThreads / 32];
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
+  if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int w = 0; w < kF64LossThreads / 32; ++w) b += warp_sum[w];
+    partial[blockIdx.x] = b;
+  }
 }
 
 }  // namespace
@@ -330,6 +342,7 @@ struct Fp64State {
   hmf::F64Table* d_table = nullptr;
   unsigned long long* d_red = nullptr;  // [0] max bits, [1] agreeing voxels, [2] loss (double), [3] flag
   int* d_truth = nullptr;               // hmf_fp64_loss's copy of a host class map
+  double* d_partial = nullptr;          // hmf_fp64_loss's per-block sums
   std::vector<double*> sink, u;         // per vertex id
   hmf::F64Table h_table{};
   bool solved = false;
@@ -348,6 +361,7 @@ void fp64_free(hmf_ctx* c) {
   if (c->f64->d_table) cudaFree(c->f64->d_table);
   if (c->f64->d_red) cudaFree(c->f64->d_red);
   if (c->f64->d_truth) cudaFree(c->f64->d_truth);
+  if (c->f64->d_partial) cudaFree(c->f64->d_partial);
   delete c->f64;
   c->f64 = nullptr;
 }
@@ -603,16 +617,23 @@ int hmf_fp64_loss(hmf_ctx* c, const int* truth, int where, double eps, double* l
        "cudaMemcpyAsync(truth)");
     d_truth = F->d_truth;
   }
-  CK(cudaMemsetAsync(F->d_red + 2, 0, 2 * sizeof(unsigned long long), s), "cudaMemsetAsync(FP64 loss)");
-  hmf::f64_loss_kernel<<<fp64_grid(c), kF64Threads, 0, s>>>(fp64_compare_table(c), d_truth, c->geo, eps,
-                                                             (double)nvox, reinterpret_cast<double*>(F->d_red + 2),
-                                                             reinterpret_cast<int*>(F->d_red + 3));
+  const int grid = fp64_grid(c);
+  if (!F->d_partial) CK(cudaMalloc(&F->d_partial, (size_t)c->sm_count * 8 * sizeof(double)), "cudaMalloc(FP64 sums)");
+  CK(cudaMemsetAsync(F->d_red + 3, 0, sizeof(unsigned long long), s), "cudaMemsetAsync(FP64 flag)");
+  hmf::f64_loss_kernel<<<grid, hmf::kF64LossThreads, 0, s>>>(fp64_compare_table(c), d_truth, c->geo, eps,
+                                                              (double)nvox, F->d_partial,
+                                                              reinterpret_cast<int*>(F->d_red + 3));
   CK(cudaGetLastError(), "f64_loss_kernel launch");
-  unsigned long long h[2] = {0, 0};
-  CK(cudaMemcpyAsync(h, F->d_red + 2, sizeof(h), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(FP64 loss)");
+  std::vector<double> part(grid);
+  unsigned long long flag = 0;
+  CK(cudaMemcpyAsync(part.data(), F->d_partial, sizeof(double) * grid, cudaMemcpyDeviceToHost, s),
+     "cudaMemcpyAsync(FP64 loss)");
+  CK(cudaMemcpyAsync(&flag, F->d_red + 3, sizeof(flag), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(FP64 flag)");
   CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(FP64 loss)");
-  if (h[1] & 1u) return fail(c, HMF_ERR_INVALID_ARGUMENT, "a ground-truth class index is not a leaf index");
-  std::memcpy(loss, &h[0], sizeof(double));
+  if (flag & 1u) return fail(c, HMF_ERR_INVALID_ARGUMENT, "a ground-truth class index is not a leaf index");
+  double sum = 0.0;
+  for (double v : part) sum += v;
+  *loss = sum;
   return hand_back(c, user);
 }
 

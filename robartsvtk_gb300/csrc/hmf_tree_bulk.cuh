@@ -22,6 +22,20 @@
 namespace hmf {
 
 constexpr int kTreeBulkStages = 2;
+
+// Convergence log of a solve: per iteration, max and sum over non-root
+// vertices and voxels of |u_new - u_old|, reduced inside the label sweep
+// (warp shuffles, one pair of atomics per warp, the iteration advanced by
+// the CTA that finishes last).  Padding columns (x >= vx of each row of
+// `pitch` elements; pitch 0: none) are left out.
+struct GapLog {
+  unsigned int* max_bits;  // [capacity] float bits (non-negative floats order as unsigned ints)
+  double* sum;             // [capacity]
+  unsigned int* counter;   // [0] iteration of the next sweep, [1] CTAs finished with the current one
+  int capacity;
+  int vx, pitch;
+  int pad_;
+};
 constexpr int kTreeBulkSmemBudget = 200 * 1024;
 
 // Chunk length (voxels) for a tree of n entries: the largest power of two
@@ -37,7 +51,34 @@ __host__ __device__ constexpr int tree_bulk_smem_bytes(int n) {
   return 128 + kTreeBulkStages * (3 * (n - 1) + 1) * tree_bulk_chunk(n) * 4;
 }
 
-__global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag) {
+// End of a sweep launch with the convergence log on (every thread of the
+// CTA): warp-shuffle max and sum, one pair of atomics per warp into this
+// iteration's entries, then the CTA's finish count; the CTA that finishes
+// last advances the iteration.  Every CTA reads the iteration before its own
+// finish count, so all CTAs of one launch log into the same entry.
+__device__ __forceinline__ void gap_log_commit(const GapLog& gap, float gmax, float gsum) {
+  const unsigned it = *(volatile unsigned*)&gap.counter[0];
+  for (int o = 16; o > 0; o >>= 1) {
+    gmax = fmaxf(gmax, __shfl_down_sync(0xffffffffu, gmax, o));
+    gsum += __shfl_down_sync(0xffffffffu, gsum, o);
+  }
+  if ((threadIdx.x & 31) == 0 && it < (unsigned)gap.capacity) {
+    atomicMax(&gap.max_bits[it], __float_as_uint(gmax));
+    atomicAdd(&gap.sum[it], (double)gsum);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&gap.counter[1], 1u) == gridDim.x - 1) {
+      gap.counter[1] = 0;
+      __threadfence();
+      atomicAdd(&gap.counter[0], 1u);
+    }
+  }
+}
+
+__global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag,
+                                 const GapLog gap = GapLog{}) {
   __shared__ TreeTable T;
   __shared__ int abort_cta, stall_cta, stop_cta;
   extern __shared__ __align__(128) unsigned char tb_raw[];
@@ -105,6 +146,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
       *(volatile int*)&stop_cta = 1;
     }
   };
+  float gmax = 0.0f, gsum = 0.0f;  // convergence log: this thread's max and sum of |u_new - u_old|
   int nissued[kTreeBulkStages] = {0, 0};  // kept by every thread (thread 0 always issues)
   long long chunk = blockIdx.x;
   if (chunk < nchunks) issue(chunk, 0), ++nissued[0];
@@ -155,6 +197,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
         }
       }
       const long long i = v0 + q;
+      const int nvalid = gap.pitch ? min(4, max(0, gap.vx - (int)(i % gap.pitch))) : 4;
       for (int e = 0; e < root; ++e) {
         const TreeEntry& E = T.e[e];
         const float4 inc = at(sink_slot(E.parent)), d = at(3 * e), sk = at(3 * e + 2), u = at(3 * e + 1);
@@ -163,6 +206,12 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
         o.y = __saturatef(u.y + cc * ((inc.y - d.y) - sk.y));
         o.z = __saturatef(u.z + cc * ((inc.z - d.z) - sk.z));
         o.w = __saturatef(u.w + cc * ((inc.w - d.w) - sk.w));
+        if (gap.max_bits) {
+          const float a0 = nvalid > 0 ? fabsf(o.x - u.x) : 0.0f, a1 = nvalid > 1 ? fabsf(o.y - u.y) : 0.0f;
+          const float a2 = nvalid > 2 ? fabsf(o.z - u.z) : 0.0f, a3 = nvalid > 3 ? fabsf(o.w - u.w) : 0.0f;
+          gmax = fmaxf(gmax, fmaxf(fmaxf(a0, a1), fmaxf(a2, a3)));
+          gsum += (a0 + a1) + (a2 + a3);
+        }
         *reinterpret_cast<float4*>(E.label_out + i) = o;
         *reinterpret_cast<float4*>(E.sink_out + i) = sk;
       }
@@ -183,6 +232,7 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
     for (int s = 0; s < kTreeBulkStages; ++s)
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
   }
+  if (gap.max_bits) gap_log_commit(gap, gmax, gsum);
 }
 
 // The same sweep for trees of N <= 16 entries (the root last, entries in
@@ -191,9 +241,10 @@ __global__ void tree_bulk_kernel(const TreeTable* __restrict__ table, const Geom
 // 1/(kids+1) and the output pointers -- and the chunk length is a
 // compile-time constant, so every staged array is an immediate offset from
 // one shared-memory base and the per-voxel code reads no table.
-template <int N>
+template <int N, bool GAP = false>
 __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
-    tree_bulk_n_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag) {
+    tree_bulk_n_kernel(const TreeTable* __restrict__ table, const Geometry G, int* __restrict__ error_flag,
+                       const GapLog gap = GapLog{}) {
   constexpr int R = N - 1;  // the root entry
   constexpr int A = 3 * R + 1;
   constexpr int VC = tree_bulk_chunk(N);
@@ -277,6 +328,7 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
       *(volatile int*)&stop_cta = 1;
     }
   };
+  float gmax = 0.0f, gsum = 0.0f;  // convergence log: this thread's max and sum of |u_new - u_old|
   int nissued[kTreeBulkStages] = {0, 0};  // kept by every issuing thread
   long long chunk = blockIdx.x;
   if (ta < A) {
@@ -339,6 +391,10 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
       }
       // ---- labels, then every new sink and label to global memory
       const long long i = v0 + threadIdx.x * 4;
+      int nvalid = 4;  // voxels of the quad inside the volume (rows are padded to 4 floats)
+      if constexpr (GAP) {
+        if (gap.pitch) nvalid = min(4, max(0, gap.vx - (int)(i % gap.pitch)));
+      }
 #pragma unroll
       for (int e = 0; e < R; ++e) {
         const float4 inc = b[poff[e]], d = b[(3 * e) * Q], sk = b[(3 * e + 2) * Q], u = b[(3 * e + 1) * Q];
@@ -347,6 +403,13 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
         o.y = __saturatef(u.y + cc * ((inc.y - d.y) - sk.y));
         o.z = __saturatef(u.z + cc * ((inc.z - d.z) - sk.z));
         o.w = __saturatef(u.w + cc * ((inc.w - d.w) - sk.w));
+        if constexpr (GAP) {
+          const float a0 = fabsf(o.x - u.x), a1 = nvalid > 1 ? fabsf(o.y - u.y) : 0.0f;
+          const float a2 = nvalid > 2 ? fabsf(o.z - u.z) : 0.0f, a3 = nvalid > 3 ? fabsf(o.w - u.w) : 0.0f;
+          const float q0 = nvalid > 0 ? a0 : 0.0f;
+          gmax = fmaxf(gmax, fmaxf(fmaxf(q0, a1), fmaxf(a2, a3)));
+          gsum += (q0 + a1) + (a2 + a3);
+        }
         *reinterpret_cast<float4*>(lout[e] + i) = o;
         *reinterpret_cast<float4*>(sout[e] + i) = sk;
       }
@@ -366,6 +429,7 @@ __global__ void __launch_bounds__(tree_bulk_chunk(N) / 4)
     for (int s = 0; s < kTreeBulkStages; ++s)
       if (nissued[s]) mbar_wait_bounded(&bars[s], (unsigned)((nissued[s] - 1) & 1), kTmaWaitLimitNs);
   }
+  if constexpr (GAP) gap_log_commit(gap, gmax, gsum);
 }
 
 }  // namespace hmf

@@ -161,6 +161,19 @@ class HMFSolver:
         return _fetch_energy(lambda f0, f, n: self._lib.hmf_get_energy(self._ctx, f0, f, n), len(self.parent),
                              self._ctx)
 
+    # -- convergence log ----------------------------------------------------
+    def set_convergence_log(self, enabled: bool) -> None:
+        """Per-iteration max / mean |u_new - u_old| reduced inside the sweep."""
+        check(self._lib.hmf_set_convergence_log(self._ctx, 1 if enabled else 0), self._ctx)
+
+    def convergence(self) -> dict:
+        """{"max": [...], "mean": [...]} per iteration of the last solve."""
+        n = check(self._lib.hmf_get_convergence(self._ctx, None, None, 0), self._ctx)
+        mx = (ctypes.c_double * max(n, 1))()
+        mean = (ctypes.c_double * max(n, 1))()
+        check(self._lib.hmf_get_convergence(self._ctx, mx, mean, n), self._ctx)
+        return {"max": np.array(mx[:n]), "mean": np.array(mean[:n])}
+
     # -- bounded copy waits --------------------------------------------------
     def set_wait_limit(self, limit_ns: int = 0) -> None:
         """Bound (ns) of the flow kernels' copy waits (0: the default 0.5 s)."""
@@ -350,6 +363,13 @@ class HMFBatchSolver:
 
     def solve(self, stream=None) -> None:
         check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
+
+    def set_convergence_log(self, enabled: bool) -> None:
+        """Per-iteration max / mean |u_new - u_old| over all volumes."""
+        HMFSolver.set_convergence_log(self, enabled)
+
+    def convergence(self) -> dict:
+        return HMFSolver.convergence(self)
 
     def labels(self, volume: int, node: int, out=None, stream=None):
         if out is None:

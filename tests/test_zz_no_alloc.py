@@ -18,8 +18,8 @@ from robartsvtk_gb300.synthetic import random_tree_problem
 pytestmark = pytest.mark.gpu
 
 
-def _context_labels(w):
-    with HMFSolver(w.dims, w.parent) as s:
+def _context_labels(w, semantics=0):
+    with HMFSolver(w.dims, w.parent, semantics) as s:
         for leaf, d in w.data.items():
             s.set_data(leaf, d)
         for v, S in w.smooth.items():
@@ -31,7 +31,7 @@ def _context_labels(w):
         return {v: s.labels(v) for v in range(len(w.parent)) if w.parent[v] >= 0}
 
 
-def _noalloc_labels(w, semantics=0):
+def _noalloc_labels(w, semantics=0, stream=None):
     import torch
     lib = _capi.load()
     n = len(w.parent)
@@ -53,8 +53,9 @@ def _noalloc_labels(w, semantics=0):
         labels[v] = t.data_ptr()
     par = (ctypes.c_int * n)(*w.parent)
     torch.cuda.synchronize()
+    handle = stream.cuda_stream if stream is not None else None
     rc = lib.hmf_solve_noalloc(*w.dims, par, n, semantics, data, smooth, alpha, w.iterations, w.step, w.cc,
-                               labels, None)
+                               labels, handle)
     assert rc == 0, lib.hmf_last_error(None)
     return {v: t.cpu().numpy() for v, t in outs.items()}
 
@@ -80,3 +81,36 @@ def test_noalloc_rejects_a_problem_beyond_its_scratch():
     rc = lib.hmf_solve_noalloc(*dims, par, 5, 0, data, None, None, 10, 0.1, 0.25, None, None)
     assert rc == -1
     assert b"64 MiB" in lib.hmf_last_error(None)
+
+
+def test_noalloc_ref_cpu_semantics_and_a_caller_stream():
+    """REF_CPU semantics (the per-voxel leaf iteration of the reference's CPU
+    class) on a caller's non-default stream, twice in a row, against the
+    allocating path."""
+    import torch
+    w = random_tree_problem(43, (29, 17, 13), [-1, 0, 0, 1, 1, 1], iterations=25, smooth_nodes=(1,))
+    ref = _context_labels(w, semantics=1)
+    stream = torch.cuda.Stream()
+    for _ in range(2):
+        got = _noalloc_labels(w, semantics=1, stream=stream)
+        for v in ref:
+            assert np.array_equal(got[v], ref[v]), v
+
+
+def test_noalloc_reports_negative_input():
+    """A negative data term is reported after the solve (the reference
+    rejects such inputs), and the next call with valid input succeeds."""
+    import torch
+    lib = _capi.load()
+    w = random_tree_problem(44, (12, 9, 7), [-1, 0, 0], iterations=4)
+    bad = {k: v.copy() for k, v in w.data.items()}
+    bad[1][3, 4, 5] = -1.0
+    w_bad = random_tree_problem(44, (12, 9, 7), [-1, 0, 0], iterations=4)
+    w_bad.data = bad
+    with pytest.raises(AssertionError):
+        _noalloc_labels(w_bad)
+    assert b"non-negative" in lib.hmf_last_error(None)
+    ref = _context_labels(w)
+    got = _noalloc_labels(w)
+    for v in ref:
+        assert np.array_equal(got[v], ref[v]), v
