@@ -929,9 +929,18 @@ def bench_batched(args, device_stream):
         device_stream.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    t_batch = timed(lambda: batch.solve(device_stream), 2)
-    t_seq = timed(lambda: [s.solve(device_stream) for s in singles], 1)
+    t_batch = timed(lambda: batch.solve(device_stream), 3)
+    t_seq = timed(lambda: [s.solve(device_stream) for s in singles], 3)
     launches = batch.stats()["launches"]
+    # what one persistent launch could save over the graph replay: the time
+    # the replayed solve spends outside the kernels (launch gaps), from the
+    # kernels' own event times in a solve launched one by one
+    batch.set_timing(True)
+    batch.solve(device_stream)
+    st = batch.stats()
+    batch.set_timing(False)
+    iters = ws[0].iterations
+    kernel_ms = iters * (st["flow_ms"] + st["tree_ms"]) + st["init_ms"]
     for s in singles:
         s.close()
     batch.close()
@@ -940,7 +949,11 @@ def bench_batched(args, device_stream):
             "voxels": sum(w.nvox for w in ws),
             "value": units / (t_batch / 1000.0), "sequential_value": units / (t_seq / 1000.0), "unit": UNIT,
             "ms_batched": t_batch, "ms_sequential": t_seq, "speedup_vs_sequential": t_seq / t_batch,
-            "launches_per_batched_solve": launches}
+            "repetitions": 3,
+            "launches_per_batched_solve": launches,
+            "kernel_ms_per_batched_solve": kernel_ms,
+            "outside_kernels_frac": max(0.0, 1.0 - kernel_ms / t_batch),
+            "flow_window": batch.flow_window, "zchunk": batch.zchunk()}
 
 
 def bench_adjoint(args, device_stream):

@@ -159,15 +159,24 @@ int hmf_batch_get_labels(hmf_ctx* ctx, int volume, int node, float* out, int whe
 int hmf_batch_get_sink(hmf_ctx* ctx, int volume, int node, float* out, int where, void* stream);
 
 /* Autotuner (no counterpart in the reference): times a few iterations of the
- * flow kernel for each candidate z-chunk length (planes per CTA column) on the
- * context's current inputs, keeps the fastest for this context and caches it
- * for contexts of the same shape (volume sizes, tree size, device) created
- * later in the process.  Inputs must be set; the labels are not kept. */
+ * flow kernel for each window shape (hmf_set_flow_window) and candidate
+ * z-chunk length (planes per CTA column) on the context's current inputs,
+ * keeps the fastest for this context and caches it for contexts of the same
+ * shape created later (key: SM count, semantics, tree shape, volume sizes
+ * rounded up to multiples of 16).  The cache lives for the process; with the
+ * environment variable HMF_AUTOTUNE_CACHE naming a file it is also read from
+ * and appended to that file.  Inputs must be set; the labels are not kept. */
 int hmf_autotune(hmf_ctx* ctx, void* stream);
 /* The flow kernel's z-chunk length (planes each CTA marches): set it (z >= 1;
  * 0 restores the default plan) or read the current one. */
 int hmf_set_zchunk(hmf_ctx* ctx, int z);
 int hmf_get_zchunk(const hmf_ctx* ctx);
+/* The flow kernel's window: 32 columns x `rows` rows per CTA, rows 32 (two
+ * CTAs of 8 warps per SM) or 64 (one CTA of 16 warps per SM, fewer halo rows
+ * per output); 0 restores the default.  hmf_autotune times both shapes.  The
+ * z chunk returns to its default plan for the shape. */
+int hmf_set_flow_window(hmf_ctx* ctx, int rows);
+int hmf_get_flow_window(const hmf_ctx* ctx);
 
 /* ---- Convergence log --------------------------------------------------------
  * No counterpart in the reference, which runs a fixed number of iterations

@@ -271,9 +271,12 @@ int allocate_state(hmf_ctx* c) {
   return HMF_OK;
 }
 
-// Flow-kernel work plan for a given z-chunk length: windows of at most 28 x 27
-// outputs spread evenly over each volume, z split into chunks of `zchunk`
-// planes.  Items enumerate volume, then z chunk, then window, so that windows
+// Output rows of one flow window of the context's shape.
+int flow_max_out_y(const hmf_ctx* c) { return 4 * c->flow_warps - 5; }
+
+// Flow-kernel work plan for a given z-chunk length: windows of at most
+// 28 x (4W - 5) outputs spread evenly over each volume, z split into chunks
+// of `zchunk` planes.  Items enumerate volume, then z chunk, then window, so that windows
 // that share halos run side by side.
 int plan_flow(hmf_ctx* c, int zchunk) {
   c->h_fvol.assign(c->vols.size(), hmf::FlowVolume{});
@@ -288,7 +291,7 @@ int plan_flow(hmf_ctx* c, int zchunk) {
     F.G.plane = V.plane;
     F.G.vol = V.vol;
     const int nx = (V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX;
-    const int ny = (V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY;
+    const int ny = (V.vy + flow_max_out_y(c) - 1) / flow_max_out_y(c);
     F.out_x = (V.vx + nx - 1) / nx;
     F.out_y = (V.vy + ny - 1) / ny;
     F.tiles_x = nx;
@@ -323,12 +326,13 @@ int plan_flow(hmf_ctx* c, int zchunk) {
 // few windows still spread over the SMs.  Chunks are balanced (the deepest
 // volume cut into equal chunks).
 int default_zchunk(const hmf_ctx* c) {
-  const long long slots = std::max(1, c->sm_count) * 2LL;  // two flow CTAs per SM
+  const int oy = flow_max_out_y(c);
+  const long long slots = std::max(1, c->sm_count) * (c->flow_warps <= 8 ? 2LL : 1LL);  // flow CTAs per SM
   long long per_chunk = 0;                                  // CTAs of one z chunk of the largest volume
   int maxz = 1;
   for (const auto& V : c->vols) {
     per_chunk = std::max(per_chunk, (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
-                                        ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY) * (c->n - 1));
+                                        ((V.vy + oy - 1) / oy) * (c->n - 1));
     maxz = std::max(maxz, V.vz);
   }
   // a wave covers about one row of windows only when one volume's chunk
@@ -343,7 +347,7 @@ int default_zchunk(const hmf_ctx* c) {
     for (const auto& V : c->vols) {
       const int zv = std::min(z, V.vz);
       ctas += (long long)((V.vx + hmf::kTmaMaxOutX - 1) / hmf::kTmaMaxOutX) *
-              ((V.vy + hmf::kTmaMaxOutY - 1) / hmf::kTmaMaxOutY) * ((V.vz + zv - 1) / zv) * (c->n - 1);
+              ((V.vy + oy - 1) / oy) * ((V.vz + zv - 1) / zv) * (c->n - 1);
     }
     const double cost = (double)((ctas + slots - 1) / slots) * (double)(z + 7);
     if (cost < best) best = cost, best_z = z;  // ties keep the longer chunk
@@ -378,6 +382,7 @@ int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ct
   if (!fn) return fail(c, HMF_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
   const cuuint64_t dims[3] = {(cuuint64_t)V.vx, (cuuint64_t)V.vy, (cuuint64_t)V.vz};
   const cuuint64_t strides[2] = {(cuuint64_t)V.pitch * 4, (cuuint64_t)V.plane * 4};
+  if (rows <= 0) rows = 4 * c->flow_warps;
   const cuuint32_t box[3] = {(cuuint32_t)hmf::kTmaBoxX, (cuuint32_t)rows, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
@@ -502,7 +507,10 @@ int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity
   fp.wait_limit_ns = c->wait_limit_ns;
   if (int rc = maybe_request_stall(c, HMF_STALL_FLOW, s)) return rc;
   const dim3 grid((unsigned)c->n_items * (unsigned)(c->n - 1), 1, 1);
-  hmf::flow_tma_kernel<<<grid, hmf::kTmaThreads, hmf::kTmaSmemBytes, s>>>(table, fp);
+  if (c->flow_warps == 16)
+    hmf::flow_tma_kernel<16><<<grid, hmf::FlowTmaShape<16>::kThreads, hmf::FlowTmaShape<16>::kSmemBytes, s>>>(table, fp);
+  else
+    hmf::flow_tma_kernel<8><<<grid, hmf::FlowTmaShape<8>::kThreads, hmf::FlowTmaShape<8>::kSmemBytes, s>>>(table, fp);
   CK(cudaGetLastError(), "flow_tma_kernel launch");
   ++c->launches;
   return HMF_OK;
@@ -927,7 +935,11 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(init_kernel)");
-  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hmf::kTmaSmemBytes),
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          hmf::FlowTmaShape<8>::kSmemBytes),
+     "cudaFuncSetAttribute(flow_tma_kernel)");
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          hmf::FlowTmaShape<16>::kSmemBytes),
      "cudaFuncSetAttribute(flow_tma_kernel)");
   CK(cudaFuncSetAttribute(hmf::tree4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           4 * hmf::kTree4MaxVertices * hmf::kTree4Threads * (int)sizeof(float4)),
@@ -1004,14 +1016,52 @@ int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* s
   return HMF_OK;
 }
 
-// Process-wide cache of tuned z chunks, keyed by the work shape.
+// Cache of tuned flow plans (window warps, z chunk), keyed by the work
+// shape: SM count, tree (vertex count and the children count of every
+// vertex in pre-order), semantics and the volume sizes, each axis rounded up
+// to a multiple of 16 (sizes in one bucket share window counts within one
+// and the same z-chunk choices).  Process-wide; with HMF_AUTOTUNE_CACHE set
+// to a file path it is also read from and appended to that file (one
+// "key warps zchunk" line per tuned shape), so later processes reuse it.
+struct TunedPlan {
+  int warps, zchunk;
+};
 std::mutex g_tune_mutex;
-std::map<std::string, int> g_tune_cache;
+std::map<std::string, TunedPlan> g_tune_cache;
+bool g_tune_file_read = false;
 
 std::string tune_key(const hmf_ctx* c) {
-  std::string k = std::to_string(c->sm_count) + "/" + std::to_string(c->n) + "/" + std::to_string(c->semantics);
-  for (const auto& V : c->vols) k += "/" + std::to_string(V.vx) + "x" + std::to_string(V.vy) + "x" + std::to_string(V.vz);
+  std::string k = std::to_string(c->sm_count) + "/" + std::to_string(c->semantics) + "/n" + std::to_string(c->n) + ":";
+  for (int v : c->preorder) k += std::to_string(c->kids[v].size()) + ",";
+  for (const auto& V : c->vols)
+    k += "/" + std::to_string((V.vx + 15) / 16 * 16) + "x" + std::to_string((V.vy + 15) / 16 * 16) + "x" +
+         std::to_string((V.vz + 15) / 16 * 16);
   return k;
+}
+
+// with g_tune_mutex held
+void tune_file_read() {
+  if (g_tune_file_read) return;
+  g_tune_file_read = true;
+  const char* path = std::getenv("HMF_AUTOTUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  char key[4096];
+  int w, z;
+  while (std::fscanf(f, "%4095s %d %d", key, &w, &z) == 3)
+    if ((w == 8 || w == 16) && z >= 1) g_tune_cache[key] = TunedPlan{w, z};
+  std::fclose(f);
+}
+
+// with g_tune_mutex held
+void tune_file_append(const std::string& key, const TunedPlan& t) {
+  const char* path = std::getenv("HMF_AUTOTUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%s %d %d\n", key.c_str(), t.warps, t.zchunk);
+  std::fclose(f);
 }
 
 int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged) {
@@ -1146,8 +1196,12 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
       int z = 0;
       {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
+        tune_file_read();
         auto it = g_tune_cache.find(tune_key(c));
-        if (it != g_tune_cache.end()) z = it->second;
+        if (it != g_tune_cache.end()) {
+          c->flow_warps = it->second.warps;
+          z = it->second.zchunk;
+        }
       }
       rc = plan_flow(c, z ? z : default_zchunk(c));
     }
@@ -1347,38 +1401,57 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   const bool saved_timing = c->timing;
   int maxz = 1;
   for (const auto& V : c->vols) maxz = std::max(maxz, V.vz);
-  int best_z = c->zchunk;
+  TunedPlan best{c->flow_warps, c->zchunk};
   double best_ms = 1e30;
   int rc = HMF_OK;
-  // candidates: the default plan's chunk, then 16, 24, 32, 48, 64, 96, ...
-  // up to the longest volume
-  const int z_default = default_zchunk(c);
-  for (int i = -1; rc == HMF_OK; ++i) {
-    const int z = i < 0 ? z_default : std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
-    rc = plan_flow(c, z);
+  // candidates, for each window shape (32 x 32 and 32 x 64): the default
+  // plan's chunk, then 16, 24, 32, 48, 64, 96, ... up to the longest volume
+  for (int w : {8, 16}) {
+    c->flow_warps = w;
+    const int z_default = default_zchunk(c);
+    for (int i = -1; rc == HMF_OK; ++i) {
+      const int z = i < 0 ? z_default : std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
+      rc = plan_flow(c, z);
+      if (rc) break;
+      c->iterations = 4;
+      c->timing = true;
+      rc = hmf_solve(c, stream);
+      if (rc) break;
+      const double ms = c->kind_count[0] ? c->kind_ms[0] / (double)c->kind_count[0] : 1e30;
+      if (ms < best_ms) best_ms = ms, best = TunedPlan{w, z};
+      if (i >= 0 && z >= maxz) break;
+    }
     if (rc) break;
-    c->iterations = 4;
-    c->timing = true;
-    rc = hmf_solve(c, stream);
-    if (rc) break;
-    const double ms = c->kind_count[0] ? c->kind_ms[0] / (double)c->kind_count[0] : 1e30;
-    if (ms < best_ms) best_ms = ms, best_z = z;
-    if (i >= 0 && z >= maxz) break;
   }
   c->iterations = saved_iters;
   c->timing = saved_timing;
   c->solved = false;
+  c->flow_warps = best.warps;
   if (rc) return rc;
   {
     DeviceGuard dg(c->device);
     drop_graphs(c);
-    rc = plan_flow(c, best_z);
+    rc = plan_flow(c, best.zchunk);
   }
   if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
-  g_tune_cache[tune_key(c)] = best_z;
+  const std::string key = tune_key(c);
+  g_tune_cache[key] = best;
+  tune_file_append(key, best);
   return HMF_OK;
 }
+
+int hmf_set_flow_window(hmf_ctx* c, int rows) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (rows != 0 && rows != 32 && rows != 64)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "flow window rows must be 32 or 64 (0: default)");
+  DeviceGuard dg(c->device);
+  drop_graphs(c);
+  c->flow_warps = rows == 64 ? 16 : 8;
+  return plan_flow(c, default_zchunk(c));
+}
+
+int hmf_get_flow_window(const hmf_ctx* c) { return c ? 4 * c->flow_warps : HMF_ERR_INVALID_ARGUMENT; }
 
 int hmf_set_zchunk(hmf_ctx* c, int z) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;

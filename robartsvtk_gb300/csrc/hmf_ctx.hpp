@@ -68,6 +68,7 @@ struct hmf_ctx {
   hmf::FlowItem* d_items = nullptr;
   int n_items = 0;
   int zchunk = 0;  // planes per window column (0: not planned yet)
+  int flow_warps = 8;  // flow_tma_kernel<W>: windows of 32 x 4W (hmf_set_flow_window)
   hmf::TreeTable* d_tree = nullptr;
   hmf::DagTable* d_dag = nullptr;
   bool dag_last = false;  // the next sweep is the last iteration's
@@ -183,9 +184,9 @@ int launch_tree(hmf_ctx* c, cudaStream_t s);
 // The TMA flow kernel and the bulk sweep over caller-built tables.
 int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s);
 int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log = false);
-// Tensor map of one pitched volume block; box = kTmaBoxX columns x `rows` rows.
-int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V,
-                     int rows = hmf::kTmaRows);
+// Tensor map of one pitched volume block; box = kTmaBoxX columns x `rows`
+// rows (0: the rows of the context's flow window).
+int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V, int rows = 0);
 bool valid_vertex(const hmf_ctx* c, int v);
 bool valid_volume(const hmf_ctx* c, int b);
 // When c->stall_kind == kind: queue on `s` the request that makes the next

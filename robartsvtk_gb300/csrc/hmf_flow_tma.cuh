@@ -6,7 +6,8 @@
 // kern_Divergence of CUDA_hierarchicalmaxflow.cu:233-456, operation by
 // operation), organised for sm_103a:
 //
-//  * A CTA owns a 32 x 32 (x, y) window of one vertex and marches along z.
+//  * A CTA owns a 32 x 4W (x, y) window of one vertex (W = 8 or 16 warps)
+//    and marches along z.
 //    Lane l of every warp is column x0-2+l, so x neighbours move by warp
 //    shuffles; warp w holds rows 4w..4w+3 of the window in registers, so y
 //    neighbours inside a warp are registers and only the rows on a warp
@@ -18,7 +19,8 @@
 //    being computed.  Every mbarrier wait is bounded: on time-out the kernel
 //    sets an error flag instead of hanging.
 //  * The stencil chain needs two halo columns/rows on the low side and up to
-//    two on the high side, so a window yields up to 28 x 27 outputs.
+//    two (columns) / three (rows) on the high side, so a window yields up to
+//    28 x (4W - 5) outputs: 28 x 27 or 28 x 59.
 #pragma once
 
 #include <cuda.h>
@@ -44,18 +46,22 @@ __device__ __forceinline__ float projection_multiplier(float h, float lim) {
   return (F > lim) ? lim / F : 1.0f;
 }
 
-__global__ void __launch_bounds__(kTmaThreads, 2)
+// W warps per CTA: the window is 32 columns x 4W rows (FlowTmaShape<W>).
+template <int W>
+__global__ void __launch_bounds__(FlowTmaShape<W>::kThreads, FlowTmaShape<W>::kCtasPerSm)
 flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams fp) {
+  constexpr int kPlane = FlowTmaShape<W>::kPlane;  // floats per staged array plane
+  constexpr int kRows = FlowTmaShape<W>::kRows;
   // Pointers into the shared window are formed by pointer arithmetic only,
   // so the compiler keeps them in the shared address space (32-bit LDS/STS).
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float* mslots = reinterpret_cast<float*>(smem_raw);            // [3][6][32][36]
-  float* zslots = mslots + kTmaMainSlots * kTmaMainArrays * kTmaPlane;  // [4][32][36]
-  float* xg = zslots + kTmaPzSlots * kTmaPlane;                   // [8][32]  g(k), row 3 of each warp
-  float* xpy = xg + 256;                                          // [8][32]  p'_y(k-1), row 0
-  float* xm = xpy + 256;                                          // [8][32]  m(k-1), row 3
-  float* xP = xm + 256;                                           // [2][8][32] P_y(k-2), row 0
-  uint64_t* mbars = reinterpret_cast<uint64_t*>(xP + 512);       // [3]
+  float* zslots = mslots + kTmaMainSlots * kTmaMainArrays * kPlane;  // [4][rows][36]
+  float* xg = zslots + kTmaPzSlots * kPlane;                      // [W][32]  g(k), row 3 of each warp
+  float* xpy = xg + W * 32;                                       // [W][32]  p'_y(k-1), row 0
+  float* xm = xpy + W * 32;                                       // [W][32]  m(k-1), row 3
+  float* xP = xm + W * 32;                                        // [2][W][32] P_y(k-2), row 0
+  uint64_t* mbars = reinterpret_cast<uint64_t*>(xP + 2 * W * 32);  // [3]
   uint64_t* zbars = mbars + kTmaMainSlots;                        // [4]
   uint64_t* stall_bar = zbars + kTmaPzSlots;                      // [1] never completed (a requested stall)
   __shared__ int abort_cta;
@@ -138,21 +144,21 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   __syncthreads();
   if (abort_cta) return;
 
-  auto mslot = [&](int p) { return mslots + ((p - kstart) % kTmaMainSlots) * (kTmaMainArrays * kTmaPlane); };
-  auto zslot = [&](int p) { return zslots + ((p - kstart) % kTmaPzSlots) * kTmaPlane; };
+  auto mslot = [&](int p) { return mslots + ((p - kstart) % kTmaMainSlots) * (kTmaMainArrays * kPlane); };
+  auto zslot = [&](int p) { return zslots + ((p - kstart) % kTmaPzSlots) * kPlane; };
   // Array a of plane p into the main ring (a: 0, 1 flows x, y; 2 sink;
   // 3 label; 4 parent sink; 5 smoothness -- the order of FlowVertexTMA's
   // maps).  One thread per array.
   auto main_map = [&](int a) -> const CUtensorMap* { return a < 2 ? &V->flow_in[par][a] : &V->sink + (a - 2); };
   auto issue_main_array = [&](int p, int a, const CUtensorMap* map) {
     uint64_t* bar = &mbars[(p - kstart) % kTmaMainSlots];
-    mbar_expect_tx(bar, (unsigned)(kTmaPlane * 4));
-    tma_load_plane(mslot(p) + a * kTmaPlane, map, xs, y0 - 2, p, bar);
+    mbar_expect_tx(bar, (unsigned)(kPlane * 4));
+    tma_load_plane(mslot(p) + a * kPlane, map, xs, y0 - 2, p, bar);
   };
   const CUtensorMap* const warp_map = main_map(warp < narr ? warp : 0);  // this warp's array in the loop
   auto issue_pz = [&](int p) {  // one thread
     uint64_t* bar = &zbars[(p - kstart) % kTmaPzSlots];
-    mbar_expect_tx(bar, (unsigned)(kTmaPlane * 4));
+    mbar_expect_tx(bar, (unsigned)(kPlane * 4));
     tma_load_plane(zslot(p), &V->flow_in[par][2], xs, y0 - 2, p, bar);
   };
   // A wait that runs out raises stop_cta before the CTA barrier that follows
@@ -185,7 +191,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   // A window whose 32 x 32 columns/rows all lie strictly inside the volume
   // (not on its first or last column/row) needs none of the x / y boundary
   // masks; it runs a copy of the march with those tests folded away.
-  const bool interior = x0 - 2 >= 1 && x0 + 29 <= G.vx - 2 && y0 - 2 >= 1 && y0 + 29 <= G.vy - 2;
+  const bool interior = x0 - 2 >= 1 && x0 + 29 <= G.vx - 2 && y0 - 2 >= 1 && y0 + kRows - 3 <= G.vy - 2;
 
   // The z-march.  Steps k in [zs + 2, min(ze + 1, vz - 2)] are steady: every
   // stage runs and no z boundary is near, so the step is compiled a second
@@ -224,8 +230,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         const float* zn = has_next ? zslot(k + 1) : zc;
         float pyv[5];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) pyv[r] = cur[kTmaPlane + (warp * 4 + r) * kTmaBoxX + off + lane];
-        pyv[4] = warp < 7 ? cur[kTmaPlane + (warp * 4 + 4) * kTmaBoxX + off + lane] : 0.f;
+        for (int r = 0; r < 4; ++r) pyv[r] = cur[kPlane + (warp * 4 + r) * kTmaBoxX + off + lane];
+        pyv[4] = warp < W - 1 ? cur[kPlane + (warp * 4 + 4) * kTmaBoxX + off + lane] : 0.f;
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int i = (warp * 4 + r) * kTmaBoxX + off + lane;
@@ -234,8 +240,8 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
           const float pxr = cur[i + 1];
           const float pyd = pyv[r + 1];
           const float pzn = zn[i];
-          const float sk = cur[2 * kTmaPlane + i], u = cur[3 * kTmaPlane + i], c = cur[4 * kTmaPlane + i];
-          Scur[r] = has_s ? cur[5 * kTmaPlane + i] : 0.f;
+          const float sk = cur[2 * kPlane + i], u = cur[3 * kPlane + i], c = cur[4 * kPlane + i];
+          Scur[r] = has_s ? cur[5 * kPlane + i] : 0.f;
           float d = (px + py) + pz;
           if (INT || xnl) d = d - pxr;
           if (INT || ynl[r]) d = d - pyd;
@@ -254,7 +260,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       }
       xg[warp * 32 + lane] = g[3];
       xpy[warp * 32 + lane] = ppy[0];
-      xP[((k & 1) * 8 + warp) * 32 + lane] = Py[0];
+      xP[((k & 1) * W + warp) * 32 + lane] = Py[0];
       __syncthreads();  // (1)
       if (stop_cta) {
         k_stop = k;
@@ -263,7 +269,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       // the copies two planes ahead, spread over the warps' first lanes
       if (lane == 0) {
         if (warp < narr && k + 2 <= kmain_end) issue_main_array(k + 2, warp, warp_map);
-        if (warp == 7 && k + 3 <= kpz_end) issue_pz(k + 3);
+        if (warp == W - 1 && k + 3 <= kpz_end) issue_pz(k + 3);
       }
 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow)
@@ -287,7 +293,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       // above its bound (projection_multiplier's test), behind one warp vote.
       float m[4], h[4], lim[4];
       bool slow[4];
-      const float pdown = warp < 7 ? xpy[(warp + 1) * 32 + lane] : 0.f;
+      const float pdown = warp < W - 1 ? xpy[(warp + 1) * 32 + lane] : 0.f;
       const bool znl = ST || kc != G.vz - 1;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
@@ -336,7 +342,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       }
 
       // ---- stage E: divergence of P(k-2) (kern_Divergence), store P(k-2) and div(k-2)
-      const float Pdown = warp < 7 ? xP[((k & 1) * 8 + warp + 1) * 32 + lane] : 0.f;
+      const float Pdown = warp < W - 1 ? xP[((k & 1) * W + warp + 1) * 32 + lane] : 0.f;
       const bool zonl = ST || ko != G.vz - 1;
       const long long zoff = (long long)ko * G.plane;
 #pragma unroll

@@ -133,6 +133,22 @@ constexpr int kTmaSmemBytes =
                               (kTmaMainSlots * kTmaMainArrays + kTmaPzSlots) * kTmaPlane * 4 +
                               (3 * 256 + 2 * 256) * 4 + 64;
 
+// Shape of flow_tma_kernel<W>: W warps of 4 register rows, a window of 32
+// columns x 4W rows (the TMA box is kTmaBoxX x 4W), 28 x (4W - 5) outputs.
+// W = 8: two CTAs per SM (~108 KB of shared memory each); W = 16: one CTA of
+// 16 warps per SM (~208 KB), half the halo rows per output.
+template <int W>
+struct FlowTmaShape {
+  static constexpr int kRows = 4 * W;
+  static constexpr int kThreads = 32 * W;
+  static constexpr int kPlane = kTmaBoxX * kRows;
+  static constexpr int kMaxOutY = kRows - 5;
+  static constexpr int kCtasPerSm = W <= 8 ? 2 : 1;
+  static constexpr int kSmemBytes = (kTmaMainSlots * kTmaMainArrays + kTmaPzSlots) * kPlane * 4 + 5 * kThreads * 4 + 64;
+};
+static_assert(FlowTmaShape<8>::kSmemBytes == kTmaSmemBytes, "the 32-row shape keeps its layout");
+static_assert(FlowTmaShape<16>::kSmemBytes <= 227 * 1024, "the 64-row shape fits one SM's shared memory");
+
 struct FlowVertexTMA {  // 64-byte aligned through its CUtensorMap members
   CUtensorMap flow_in[2][3];  // [parity][axis]: flows read in iterations of that parity
   CUtensorMap sink, label, inc, smooth;

@@ -124,6 +124,14 @@ class HMFSolver:
     def zchunk(self) -> int:
         return int(self._lib.hmf_get_zchunk(self._ctx))
 
+    def set_flow_window(self, rows: int) -> None:
+        """Flow-kernel window rows: 32 or 64 (0: default)."""
+        check(self._lib.hmf_set_flow_window(self._ctx, int(rows)), self._ctx)
+
+    @property
+    def flow_window(self) -> int:
+        return check(self._lib.hmf_get_flow_window(self._ctx), self._ctx)
+
     def autotune(self, stream=None) -> None:
         """Time the flow kernel for each candidate z chunk on the current
         inputs and keep the fastest (hmf_autotune)."""
@@ -363,6 +371,12 @@ class HMFBatchSolver:
 
     def solve(self, stream=None) -> None:
         check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
+
+    # the flow plan's controls, shared with HMFSolver
+    set_flow_window = HMFSolver.set_flow_window
+    flow_window = HMFSolver.flow_window
+    set_zchunk = HMFSolver.set_zchunk
+    zchunk = HMFSolver.zchunk
 
     def set_convergence_log(self, enabled: bool) -> None:
         """Per-iteration max / mean |u_new - u_old| over all volumes."""

@@ -88,6 +88,7 @@ def test_convergence_log_off_and_timed_path():
 def test_convergence_log_of_a_batch_pools_its_volumes():
     ws = [random_tree_problem(53 + k, d, [-1, 0, 0, 0], iterations=6) for k, d in
           enumerate([(16, 10, 9), (24, 7, 12)])]
+    ws[1].alpha = dict(ws[0].alpha)  # a batch shares one set of smoothness weights
     with HMFBatchSolver([w.dims for w in ws], ws[0].parent) as b:
         for k, w in enumerate(ws):
             for leaf, d in w.data.items():

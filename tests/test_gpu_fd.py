@@ -74,21 +74,26 @@ def test_adjoint_against_fp64_central_differences():
             rows.append(("alpha", v, -1, float(galpha[v]), lp, lm))
         s.set_fp64_probe(HMF_FP64_PROBE_NONE)
 
-    checked, kinks, worst, nonzero = 0, [], 0.0, 0
+    checked, kinks, worst, nonzero, bad = 0, [], 0.0, 0, []
     for kind, node, vox, g, lp, lm in rows:
         fd = (lp - lm) / (2 * H)
         fwd, bwd = (lp - L0) / H, (L0 - lm) / H
         scale = max(abs(fwd), abs(bwd), atol)
-        if abs(fwd - bwd) > KINK * scale:
-            kinks.append((kind, node, vox, g, fd, fwd, bwd))
-            continue
+        kink = abs(fwd - bwd) > KINK * scale
         err = abs(g - fd)
+        print("%-6s node %d voxel %8d  adjoint % .6e  fd % .6e  fwd % .6e  bwd % .6e  rel %.3g%s"
+              % (kind, node, vox, g, fd, fwd, bwd, err / (abs(fd) + atol), "  KINK" if kink else ""))
+        if kink:
+            kinks.append((kind, node, vox))
+            continue
         worst = max(worst, err / (abs(fd) + atol))
         nonzero += abs(fd) > atol
         checked += 1
-        assert err <= RTOL * abs(fd) + atol, (kind, node, vox, g, fd, fwd, bwd)
+        if err > RTOL * abs(fd) + atol:
+            bad.append((kind, node, vox, g, fd))
     print("FD check, 128^3 flat4, 300 iterations, checkpoints every %d (%d recomputed segments): loss fp32 %.9f, "
           "fp64 %.9f; %d probes checked (%d with |g| above %.1e), worst relative error %.3g; %d kink hits: %s"
           % (plan["checkpoint_every"], plan["recomputed_segments"], loss32, L0, checked, nonzero, atol, worst,
              len(kinks), kinks))
+    assert not bad, bad
     assert checked >= len(rows) // 2

@@ -20,9 +20,13 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 LABEL_TOL = 1e-4  # per-voxel max |u_gpu - u_oracle| accepted for end-to-end workloads
 
 
-def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None):
+def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None, window=0, zchunk=0):
     import torch
     with HMFSolver(w.dims, w.parent, semantics) as s:
+        if window:
+            s.set_flow_window(window)
+        if zchunk:
+            s.set_zchunk(zchunk)
         keep = []
         for leaf, d in w.data.items():
             if device_inputs:
@@ -83,6 +87,37 @@ def test_ref_cuda_bitexact_golden_cases(name):
 def test_ref_cuda_bitexact_shapes(dims, parent, smooth_nodes, iters):
     w = random_tree_problem(21, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
     assert_same(run_gpu(w), oracle(w), str(dims))
+
+
+@pytest.mark.parametrize("dims,parent,smooth_nodes,iters,zchunk", [
+    ((5, 4, 3), [-1, 0, 0, 0], (), 7, 0),
+    ((31, 17, 1), [-1, 0, 0, 0], (2,), 9, 0),
+    ((70, 130, 23), [-1, 0, 1, 2, 2, 1, 0], (3, 4), 6, 0),     # interior 64-row windows and partial ones
+    ((40, 64, 40), [-1, 0, 0, 1, 1, 2, 2], (1, 2, 3), 5, 7),  # exactly one window row, short z chunks
+    ((33, 61, 12), [-1, 0, 0, 0, 0], (), 6, 0),                # 61 rows: two windows of 59 + 2
+])
+def test_ref_cuda_bitexact_64_row_windows(dims, parent, smooth_nodes, iters, zchunk):
+    w = random_tree_problem(26, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
+    assert_same(run_gpu(w, window=64, zchunk=zchunk), oracle(w), "64 rows " + str(dims))
+
+
+def test_autotuned_plan_is_bitexact():
+    w = random_tree_problem(27, (90, 75, 33), [-1, 0, 0, 1, 1], iterations=8, smooth_nodes=(1,))
+    ref = oracle(w)
+    with HMFSolver(w.dims, w.parent) as s:
+        for leaf, d in w.data.items():
+            s.set_data(leaf, d)
+        for v, S in w.smooth.items():
+            s.set_smoothness(v, S)
+        for v, a in w.alpha.items():
+            s.set_smoothness_scalar(v, a)
+        s.set_params(w.iterations, w.step, w.cc)
+        s.autotune()
+        assert s.flow_window in (32, 64) and s.zchunk() >= 1
+        s.solve()
+        for v in range(len(w.parent)):
+            if w.parent[v] >= 0:
+                assert np.array_equal(s.labels(v), ref["u"][v].astype(np.float32)), v
 
 
 def test_ref_cuda_shared_smoothness_image():
