@@ -932,6 +932,7 @@ def bench_batched(args, device_stream):
     t_batch = timed(lambda: batch.solve(device_stream), 3)
     t_seq = timed(lambda: [s.solve(device_stream) for s in singles], 3)
     launches = batch.stats()["launches"]
+    plan = {"flow_window": batch.flow_window, "zchunk": batch.zchunk()}
     # what one persistent launch could save over the graph replay: the time
     # the replayed solve spends outside the kernels (launch gaps), from the
     # kernels' own event times in a solve launched one by one
@@ -953,7 +954,7 @@ def bench_batched(args, device_stream):
             "launches_per_batched_solve": launches,
             "kernel_ms_per_batched_solve": kernel_ms,
             "outside_kernels_frac": max(0.0, 1.0 - kernel_ms / t_batch),
-            "flow_window": batch.flow_window, "zchunk": batch.zchunk()}
+            **plan}
 
 
 def bench_adjoint(args, device_stream):

@@ -177,6 +177,14 @@ int hmf_get_zchunk(const hmf_ctx* ctx);
  * z chunk returns to its default plan for the shape. */
 int hmf_set_flow_window(hmf_ctx* ctx, int rows);
 int hmf_get_flow_window(const hmf_ctx* ctx);
+/* Slab pipeline of the replayed iterations (single volumes of label trees,
+ * REF_CUDA, convergence log off): each iteration's flow and sweep launches
+ * are cut at the flow plan's z chunks into per-slab graph nodes that wait
+ * only for the slabs their stencil touches, so sweeps overlap flows and
+ * consecutive iterations overlap.  Same arithmetic, bit-identical results.
+ * hmf_get_pipeline returns 1 when the next solve runs pipelined. */
+int hmf_set_pipeline(hmf_ctx* ctx, int enabled);
+int hmf_get_pipeline(const hmf_ctx* ctx);
 
 /* ---- Convergence log --------------------------------------------------------
  * No counterpart in the reference, which runs a fixed number of iterations

@@ -71,6 +71,8 @@ SIGNATURES = [
     ("hmf_set_adjoint_memory", _I, [_P, ctypes.c_longlong, _I]),
     ("hmf_set_zchunk", _I, [_P, _I]),
     ("hmf_get_zchunk", _I, [_P]),
+    ("hmf_set_pipeline", _I, [_P, _I]),
+    ("hmf_get_pipeline", _I, [_P]),
     ("hmf_set_flow_window", _I, [_P, _I]),
     ("hmf_get_flow_window", _I, [_P]),
     ("hmf_get_adjoint_schedule", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_longlong),

@@ -51,6 +51,7 @@ thread_local std::string g_create_error;
 constexpr int kMaxDim = 1 << 30;
 
 constexpr int kTX = 32, kTY = 8;
+constexpr int kPipelineIterations = 8;  // iterations per replayed graph of a pipelined solve (even)
 constexpr int kTreeThreads = 256;
 
 }  // namespace
@@ -496,17 +497,22 @@ int maybe_request_stall(hmf_ctx* c, int kind, cudaStream_t s) {
 }
 
 int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s) {
+  return launch_flow_tma_items(c, table, parity, 0, c->n_items, s);
+}
+
+int launch_flow_tma_items(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, int first_item, int n_items,
+                          cudaStream_t s) {
   hmf::FlowTmaParams fp;
   fp.step = c->step;
   fp.icc = 1.0f / c->cc;
   fp.parity = parity;
   fp.n_vertices = c->n - 1;
   fp.vols = c->d_fvol;
-  fp.items = c->d_items;
+  fp.items = c->d_items + first_item;
   fp.error_flag = c->d_error;
   fp.wait_limit_ns = c->wait_limit_ns;
   if (int rc = maybe_request_stall(c, HMF_STALL_FLOW, s)) return rc;
-  const dim3 grid((unsigned)c->n_items * (unsigned)(c->n - 1), 1, 1);
+  const dim3 grid((unsigned)n_items * (unsigned)(c->n - 1), 1, 1);
   if (c->flow_warps == 16)
     hmf::flow_tma_kernel<16><<<grid, hmf::FlowTmaShape<16>::kThreads, hmf::FlowTmaShape<16>::kSmemBytes, s>>>(table, fp);
   else
@@ -561,32 +567,38 @@ hmf::GapLog gap_view(const hmf_ctx* c) {
 
 size_t gap_bytes(int cap) { return round_up(8 + 4 * (size_t)cap, 8) + 8 * (size_t)cap; }
 
-int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log) {
+// The sweep over the elements [0, G.vol) of `table`'s arrays.
+int launch_tree_bulk_geo(hmf_ctx* c, const hmf::TreeTable* table, const hmf::Geometry& G, cudaStream_t s,
+                         bool gap_log) {
   const int smem = hmf::tree_bulk_smem_bytes(c->n);
   const int vc = hmf::tree_bulk_chunk(c->n);
-  const long long chunks = (c->geo.vol + vc - 1) / vc;
+  const long long chunks = (G.vol + vc - 1) / vc;
   const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
   const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
   if (int rc = maybe_request_stall(c, HMF_STALL_SWEEP, s)) return rc;
   const hmf::GapLog gap = gap_log ? gap_view(c) : hmf::GapLog{};
   switch (c->n) {
-#define HMF_TREE_N(N)                                                                             \
-  case N:                                                                                         \
-    if (gap_log)                                                                                  \
-      hmf::tree_bulk_n_kernel<N, true><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error, gap); \
-    else                                                                                          \
-      hmf::tree_bulk_n_kernel<N, false><<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error);    \
+#define HMF_TREE_N(N)                                                                        \
+  case N:                                                                                    \
+    if (gap_log)                                                                             \
+      hmf::tree_bulk_n_kernel<N, true><<<grid, vc / 4, smem, s>>>(table, G, c->d_error, gap); \
+    else                                                                                     \
+      hmf::tree_bulk_n_kernel<N, false><<<grid, vc / 4, smem, s>>>(table, G, c->d_error);    \
     break;
     HMF_TREE_N(2) HMF_TREE_N(3) HMF_TREE_N(4) HMF_TREE_N(5) HMF_TREE_N(6) HMF_TREE_N(7) HMF_TREE_N(8)
     HMF_TREE_N(9) HMF_TREE_N(10) HMF_TREE_N(11) HMF_TREE_N(12) HMF_TREE_N(13) HMF_TREE_N(14) HMF_TREE_N(15)
     HMF_TREE_N(16)
 #undef HMF_TREE_N
     default:
-      hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, c->geo, c->d_error, gap);
+      hmf::tree_bulk_kernel<<<grid, vc / 4, smem, s>>>(table, G, c->d_error, gap);
   }
   CK(cudaGetLastError(), "tree_bulk_kernel launch");
   ++c->launches;
   return HMF_OK;
+}
+
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log) {
+  return launch_tree_bulk_geo(c, table, c->geo, s, gap_log);
 }
 
 // Grid of the per-voxel DAG kernels: as many blocks as are resident at once.
@@ -672,12 +684,120 @@ int record_iteration(hmf_ctx* c, int parity, cudaStream_t s) {
   return launch_tree(c, s);
 }
 
+// ---- z-slab pipeline of the replayed iterations ---------------------------
+// With the pipeline on (hmf_set_pipeline) a single volume's iteration is cut
+// at the flow plan's z chunks into slabs: the flow launch of a slab runs its
+// chunk's work items, the sweep launch of a slab its planes' elements, each
+// a graph node with only the dependencies the stencil needs --
+//   sweep(t, k) after flow(t, k-1 .. k+1): the flows of the neighbouring
+//     slabs read this slab's halo planes of sinks and labels, which the sweep
+//     replaces;
+//   flow(t+1, k) after sweep(t, k-1 .. k+1): it reads those planes' new
+//     sinks and labels, and it overwrites the flow set that flow(t, k +- 1)
+//     read as halo (both before those sweeps).
+// So the sweeps of some slabs run beside the flows of others (the flow
+// kernel leaves HBM bandwidth unused, the sweep needs little besides it),
+// and the next iteration's first slabs start before this one's last.  The
+// arithmetic is unchanged: results are bit-identical.
+bool pipeline_active(const hmf_ctx* c) {
+  return c->pipeline && c->vols.size() == 1 && !c->dag && c->use_tma && c->tree_kind == 0 && !c->gap_on &&
+         c->semantics == HMF_SEMANTICS_REF_CUDA && c->n_items > 0;
+}
+
+// Per-slab sweep tables: the solver's table with every array pointer moved
+// to the slab's first plane (its inputs may move between solves, so they are
+// written before every pipelined solve, into the array the graphs point at).
+int upload_slab_tables(hmf_ctx* c, cudaStream_t s) {
+  const auto& V = c->vols[0];
+  const int K = c->n_slabs, zc = c->h_fvol[0].zchunk;
+  c->h_tree_slabs.assign(K, c->h_tree);
+  for (int k = 0; k < K; ++k) {
+    const long long base = (long long)k * zc * V.plane;
+    hmf::TreeTable& T = c->h_tree_slabs[k];
+    for (int e = 0; e < T.n; ++e) {
+      hmf::TreeEntry& E = T.e[e];
+      if (E.sink) E.sink += base;
+      if (E.label) E.label += base;
+      if (E.sink_out) E.sink_out += base;
+      if (E.label_out) E.label_out += base;
+      if (E.div) E.div += base;
+      if (E.data) E.data += base;
+    }
+  }
+  CK(cudaMemcpyAsync(c->d_tree_slabs, c->h_tree_slabs.data(), sizeof(hmf::TreeTable) * K, cudaMemcpyHostToDevice, s),
+     "cudaMemcpyAsync(slab tables)");
+  return HMF_OK;
+}
+
+// Slabs of the current plan (one per z chunk), their tables' device array,
+// streams and events (made when the graphs are captured).
+int prepare_slabs(hmf_ctx* c, cudaStream_t s) {
+  const auto& V = c->vols[0];
+  const int zc = c->h_fvol[0].zchunk;
+  const int K = (V.vz + zc - 1) / zc;
+  c->slab_tiles = c->n_items / K;
+  c->slab_geo.assign(K, c->geo);
+  for (int k = 0; k < K; ++k) {
+    const long long z0 = (long long)k * zc, z1 = std::min<long long>(V.vz, z0 + zc);
+    c->slab_geo[k].vol = (z1 - z0) * V.plane;
+  }
+  if (c->d_tree_slabs) cudaFree(c->d_tree_slabs);
+  c->d_tree_slabs = nullptr;
+  CK(cudaMalloc(&c->d_tree_slabs, sizeof(hmf::TreeTable) * K), "cudaMalloc(slab tables)");
+  c->n_slabs = K;
+  if (int rc = upload_slab_tables(c, s)) return rc;
+  while ((int)c->slab_streams.size() < K) {
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate(slab)");
+    c->slab_streams.push_back(st);
+    cudaEvent_t ef = nullptr, es = nullptr;
+    CK(cudaEventCreateWithFlags(&ef, cudaEventDisableTiming), "cudaEventCreate(slab)");
+    CK(cudaEventCreateWithFlags(&es, cudaEventDisableTiming), "cudaEventCreate(slab)");
+    c->slab_ev_flow.push_back(ef);
+    c->slab_ev_sweep.push_back(es);
+  }
+  return HMF_OK;
+}
+
+// Records n_iter iterations as slab nodes on the slab streams, forked from
+// and joined back to c->stream (which is being captured).
+int record_slab_iterations(hmf_ctx* c, int n_iter) {
+  const int K = c->n_slabs;
+  cudaStream_t origin = c->stream;
+  CK(cudaEventRecord(c->ev_join, origin), "cudaEventRecord(fork)");
+  for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(c->slab_streams[k], c->ev_join, 0), "cudaStreamWaitEvent(fork)");
+  for (int t = 0; t < n_iter; ++t) {
+    for (int k = 0; k < K; ++k) {
+      cudaStream_t st = c->slab_streams[k];
+      if (t > 0)  // sweep(t-1, k) precedes on this stream
+        for (int j = std::max(0, k - 1); j <= std::min(K - 1, k + 1); ++j)
+          if (j != k) CK(cudaStreamWaitEvent(st, c->slab_ev_sweep[j], 0), "cudaStreamWaitEvent(sweep)");
+      if (int rc = launch_flow_tma_items(c, c->d_tma, t & 1, k * c->slab_tiles, c->slab_tiles, st)) return rc;
+      CK(cudaEventRecord(c->slab_ev_flow[k], st), "cudaEventRecord(flow)");
+    }
+    for (int k = 0; k < K; ++k) {
+      cudaStream_t st = c->slab_streams[k];
+      for (int j = std::max(0, k - 1); j <= std::min(K - 1, k + 1); ++j)
+        if (j != k) CK(cudaStreamWaitEvent(st, c->slab_ev_flow[j], 0), "cudaStreamWaitEvent(flow)");
+      if (int rc = launch_tree_bulk_geo(c, c->d_tree_slabs + k, c->slab_geo[k], st, false)) return rc;
+      CK(cudaEventRecord(c->slab_ev_sweep[k], st), "cudaEventRecord(sweep)");
+    }
+  }
+  for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(origin, c->slab_ev_sweep[k], 0), "cudaStreamWaitEvent(join)");
+  return HMF_OK;
+}
+
 int capture(hmf_ctx* c, int n_iter, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
+  const bool slabs = pipeline_active(c);
+  if (slabs)
+    if (int rc = prepare_slabs(c, c->stream)) return rc;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
   long long before = c->launches;
   int rc = HMF_OK;
-  for (int i = 0; i < n_iter && rc == HMF_OK; ++i) rc = record_iteration(c, i & 1, c->stream);
+  if (slabs) rc = record_slab_iterations(c, n_iter);
+  else
+    for (int i = 0; i < n_iter && rc == HMF_OK; ++i) rc = record_iteration(c, i & 1, c->stream);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->launches = before;
   if (rc) {
@@ -695,7 +815,8 @@ void drop_graphs(hmf_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
   if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
-  c->graph_pair = c->graph_one = nullptr;
+  if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
+  c->graph_pair = c->graph_one = c->graph_many = nullptr;
 }
 
 int timed(hmf_ctx* c, int kind, cudaStream_t s, int (*fn)(hmf_ctx*, cudaStream_t, int), int arg) {
@@ -1251,6 +1372,11 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
   if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
+  if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
+  if (c->d_tree_slabs) cudaFree(c->d_tree_slabs);
+  for (auto st : c->slab_streams) cudaStreamDestroy(st);
+  for (auto ev : c->slab_ev_flow) cudaEventDestroy(ev);
+  for (auto ev : c->slab_ev_sweep) cudaEventDestroy(ev);
   if (c->arena) cudaFree(c->arena);
   if (c->staging) cudaFree(c->staging);
   if (c->d_flow[0]) cudaFree(c->d_flow[0]);
@@ -1370,17 +1496,29 @@ int hmf_solve(hmf_ctx* c, void* stream) {
     if (!c->graph_pair) {
       rc = capture(c, 2, &c->graph_pair);
       if (!rc) rc = capture(c, 1, &c->graph_one);
+      // a pipelined solve replays several iterations per graph, so that the
+      // pipeline drains (at a graph's end) rarely
+      if (!rc && pipeline_active(c)) rc = capture(c, kPipelineIterations, &c->graph_many);
       if (rc) return rc;
     }
     // a DAG's last iteration runs fewer tasks: launched on its own
     const int graphed = c->dag ? std::max(0, c->iterations - 1) : c->iterations;
-    for (int it = 0; it + 1 < graphed; it += 2) {
+    const long long per_iter = pipeline_active(c) ? 2LL * c->n_slabs : 2;
+    if (pipeline_active(c))
+      if (int rc2 = upload_slab_tables(c, s)) return rc2;
+    int it0 = 0;
+    if (c->graph_many)
+      for (; it0 + kPipelineIterations <= graphed; it0 += kPipelineIterations) {
+        CK(cudaGraphLaunch(c->graph_many, s), "cudaGraphLaunch");
+        c->launches += per_iter * kPipelineIterations;
+      }
+    for (int it = it0; it + 1 < graphed; it += 2) {
       CK(cudaGraphLaunch(c->graph_pair, s), "cudaGraphLaunch");
-      c->launches += 4;
+      c->launches += 2 * per_iter;
     }
-    if (graphed & 1) {
+    if ((graphed - it0) & 1) {
       CK(cudaGraphLaunch(c->graph_one, s), "cudaGraphLaunch");
-      c->launches += 2;
+      c->launches += per_iter;
     }
     if (c->dag && c->iterations > 0) {
       rc = launch_flow(c, graphed & 1, s);
@@ -1440,6 +1578,17 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   tune_file_append(key, best);
   return HMF_OK;
 }
+
+int hmf_set_pipeline(hmf_ctx* c, int enabled) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if ((enabled != 0) == c->pipeline) return HMF_OK;
+  DeviceGuard dg(c->device);
+  drop_graphs(c);
+  c->pipeline = enabled != 0;
+  return HMF_OK;
+}
+
+int hmf_get_pipeline(const hmf_ctx* c) { return c ? (pipeline_active(c) ? 1 : 0) : HMF_ERR_INVALID_ARGUMENT; }
 
 int hmf_set_flow_window(hmf_ctx* c, int rows) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;

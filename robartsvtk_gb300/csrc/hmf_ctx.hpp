@@ -85,6 +85,16 @@ struct hmf_ctx {
   cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
   cudaGraphExec_t graph_pair = nullptr;  // two iterations (both flow parities)
   cudaGraphExec_t graph_one = nullptr;   // one iteration, parity 0
+  cudaGraphExec_t graph_many = nullptr;  // pipelined solves: several iterations per replay
+
+  // z-slab pipeline of the replayed iterations (hmf_set_pipeline)
+  bool pipeline = false;
+  int n_slabs = 0, slab_tiles = 0;
+  std::vector<hmf::Geometry> slab_geo;
+  std::vector<hmf::TreeTable> h_tree_slabs;
+  hmf::TreeTable* d_tree_slabs = nullptr;
+  std::vector<cudaStream_t> slab_streams;
+  std::vector<cudaEvent_t> slab_ev_flow, slab_ev_sweep;
 
   // failure-path controls (hmf_set_wait_limit, hmf_inject_wait_stall)
   unsigned long long wait_limit_ns = hmf::kTmaWaitLimitNs;
@@ -183,6 +193,8 @@ int launch_flow(hmf_ctx* c, int parity, cudaStream_t s);
 int launch_tree(hmf_ctx* c, cudaStream_t s);
 // The TMA flow kernel and the bulk sweep over caller-built tables.
 int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s);
+int launch_flow_tma_items(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, int first_item, int n_items,
+                          cudaStream_t s);
 int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log = false);
 // Tensor map of one pitched volume block; box = kTmaBoxX columns x `rows`
 // rows (0: the rows of the context's flow window).

@@ -124,6 +124,14 @@ class HMFSolver:
     def zchunk(self) -> int:
         return int(self._lib.hmf_get_zchunk(self._ctx))
 
+    def set_pipeline(self, enabled: bool) -> None:
+        """Per-slab graph nodes so that sweeps overlap flows (same results)."""
+        check(self._lib.hmf_set_pipeline(self._ctx, 1 if enabled else 0), self._ctx)
+
+    @property
+    def pipeline(self) -> bool:
+        return check(self._lib.hmf_get_pipeline(self._ctx), self._ctx) == 1
+
     def set_flow_window(self, rows: int) -> None:
         """Flow-kernel window rows: 32 or 64 (0: default)."""
         check(self._lib.hmf_set_flow_window(self._ctx, int(rows)), self._ctx)

@@ -20,13 +20,15 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 LABEL_TOL = 1e-4  # per-voxel max |u_gpu - u_oracle| accepted for end-to-end workloads
 
 
-def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None, window=0, zchunk=0):
+def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None, window=0, zchunk=0, pipeline=False):
     import torch
     with HMFSolver(w.dims, w.parent, semantics) as s:
         if window:
             s.set_flow_window(window)
         if zchunk:
             s.set_zchunk(zchunk)
+        if pipeline:
+            s.set_pipeline(True)
         keep = []
         for leaf, d in w.data.items():
             if device_inputs:
@@ -99,6 +101,41 @@ def test_ref_cuda_bitexact_shapes(dims, parent, smooth_nodes, iters):
 def test_ref_cuda_bitexact_64_row_windows(dims, parent, smooth_nodes, iters, zchunk):
     w = random_tree_problem(26, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
     assert_same(run_gpu(w, window=64, zchunk=zchunk), oracle(w), "64 rows " + str(dims))
+
+
+@pytest.mark.parametrize("dims,parent,smooth_nodes,iters,zchunk,window", [
+    ((40, 30, 50), [-1, 0, 0, 1, 1, 2, 2], (1, 2), 19, 7, 0),    # 8 slabs, 19 iterations: 8 + 8 + 2 + 1
+    ((33, 61, 23), [-1, 0, 0, 0], (), 10, 5, 64),                # 5 slabs of 5 planes, the last of 3
+    ((64, 16, 40), [-1, 0, 0, 1, 1, 2, 2], (1, 3, 5), 9, 0, 0),   # the default plan's chunks
+    ((20, 12, 6), [-1, 0, 0], (), 4, 0, 0),                      # a single slab
+])
+def test_ref_cuda_bitexact_slab_pipeline(dims, parent, smooth_nodes, iters, zchunk, window):
+    w = random_tree_problem(28, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
+    assert_same(run_gpu(w, window=window, zchunk=zchunk, pipeline=True), oracle(w), "pipelined " + str(dims))
+
+
+def test_slab_pipeline_with_device_inputs_that_move():
+    """The per-slab tables follow inputs that move between solves."""
+    import torch
+    w = random_tree_problem(29, (36, 20, 30), [-1, 0, 0, 1, 1], iterations=9, smooth_nodes=(1,))
+    ref = oracle(w)
+    with HMFSolver(w.dims, w.parent) as s:
+        s.set_zchunk(6)
+        s.set_pipeline(True)
+        for v, a in w.alpha.items():
+            s.set_smoothness_scalar(v, a)
+        s.set_params(w.iterations, w.step, w.cc)
+        for attempt in range(2):
+            keep = [torch.from_numpy(d).cuda() for d in w.data.values()]  # new device buffers each time
+            for leaf, t in zip(w.data, keep):
+                s.set_data(leaf, t)
+            for v, S in w.smooth.items():
+                s.set_smoothness(v, S)
+            s.solve()
+            assert s.pipeline
+            for v in range(len(w.parent)):
+                if w.parent[v] >= 0:
+                    assert np.array_equal(s.labels(v), ref["u"][v].astype(np.float32)), (attempt, v)
 
 
 def test_autotuned_plan_is_bitexact():
