@@ -182,7 +182,8 @@ int hmf_get_flow_window(const hmf_ctx* ctx);
  * are cut at the flow plan's z chunks into per-slab graph nodes that wait
  * only for the slabs their stencil touches, so sweeps overlap flows and
  * consecutive iterations overlap.  Same arithmetic, bit-identical results.
- * hmf_get_pipeline returns 1 when the next solve runs pipelined. */
+ * On by default; hmf_get_pipeline returns 1 when the next solve runs
+ * pipelined. */
 int hmf_set_pipeline(hmf_ctx* ctx, int enabled);
 int hmf_get_pipeline(const hmf_ctx* ctx);
 

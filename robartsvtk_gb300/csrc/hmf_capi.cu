@@ -52,6 +52,7 @@ constexpr int kMaxDim = 1 << 30;
 
 constexpr int kTX = 32, kTY = 8;
 constexpr int kPipelineIterations = 8;  // iterations per replayed graph of a pipelined solve (even)
+constexpr int kTuneIterations = 8;      // iterations of each solve the autotuner times
 constexpr int kTreeThreads = 256;
 
 }  // namespace
@@ -699,9 +700,13 @@ int record_iteration(hmf_ctx* c, int parity, cudaStream_t s) {
 // kernel leaves HBM bandwidth unused, the sweep needs little besides it),
 // and the next iteration's first slabs start before this one's last.  The
 // arithmetic is unchanged: results are bit-identical.
+// A flow launch reads planes zs - 2 .. ze + 2 of its chunk [zs, ze), so the
+// dependencies above reach only the neighbouring slabs when every slab but
+// the last has at least 3 planes; with shorter chunks the pipeline is off.
 bool pipeline_active(const hmf_ctx* c) {
   return c->pipeline && c->vols.size() == 1 && !c->dag && c->use_tma && c->tree_kind == 0 && !c->gap_on &&
-         c->semantics == HMF_SEMANTICS_REF_CUDA && c->n_items > 0;
+         c->semantics == HMF_SEMANTICS_REF_CUDA && c->n_items > 0 && !c->h_fvol.empty() &&
+         c->h_fvol[0].zchunk >= 3;
 }
 
 // Per-slab sweep tables: the solver's table with every array pointer moved
@@ -1254,6 +1259,11 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
     V.pitch = (V.vx + 3) / 4 * 4;
     V.plane = (long long)V.pitch * V.vy;
     V.vol = V.plane * V.vz;
+    if (V.vol >= (1LL << 31)) {  // the flow kernel addresses a volume's elements with 32-bit offsets
+      g_create_error = "volumes of 2^31 or more elements (rows padded to 4 floats) are not supported";
+      delete c;
+      return HMF_ERR_INVALID_ARGUMENT;
+    }
     V.off = off;
     off += V.vol;  // a multiple of 4: every block starts 16-byte aligned
     c->vols.push_back(V);
@@ -1542,20 +1552,32 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   TunedPlan best{c->flow_warps, c->zchunk};
   double best_ms = 1e30;
   int rc = HMF_OK;
-  // candidates, for each window shape (32 x 32 and 32 x 64): the default
-  // plan's chunk, then 16, 24, 32, 48, 64, 96, ... up to the longest volume
+  DeviceGuard dg(c->device);
+  cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
+  // Each candidate is timed as the solve runs it (graph replay, the slab
+  // pipeline when on): a warm solve of kTuneIterations iterations captures
+  // the plan's graphs, a second one is timed with events on the caller's
+  // stream.  Candidates, for each window shape (32 x 32 and 32 x 64): the
+  // default plan's chunk, then 16, 24, 32, 48, 64, 96, ... up to the longest
+  // volume.
+  c->timing = false;
+  c->iterations = kTuneIterations;
   for (int w : {8, 16}) {
     c->flow_warps = w;
     const int z_default = default_zchunk(c);
     for (int i = -1; rc == HMF_OK; ++i) {
       const int z = i < 0 ? z_default : std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
+      drop_graphs(c);
       rc = plan_flow(c, z);
+      if (!rc) rc = hmf_solve(c, stream);
+      cudaError_t e = rc ? cudaSuccess : cudaEventRecord(c->ev_t0, user);
+      if (!rc && e == cudaSuccess) rc = hmf_solve(c, stream);
+      if (!rc && e == cudaSuccess) e = cudaEventRecord(c->ev_t1, user);
+      if (!rc && e == cudaSuccess) e = cudaEventSynchronize(c->ev_t1);
+      float ms = 1e30f;
+      if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1);
+      if (!rc && e != cudaSuccess) rc = cuda_fail(c, e, "autotune timing");
       if (rc) break;
-      c->iterations = 4;
-      c->timing = true;
-      rc = hmf_solve(c, stream);
-      if (rc) break;
-      const double ms = c->kind_count[0] ? c->kind_ms[0] / (double)c->kind_count[0] : 1e30;
       if (ms < best_ms) best_ms = ms, best = TunedPlan{w, z};
       if (i >= 0 && z >= maxz) break;
     }
@@ -1566,11 +1588,8 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   c->solved = false;
   c->flow_warps = best.warps;
   if (rc) return rc;
-  {
-    DeviceGuard dg(c->device);
-    drop_graphs(c);
-    rc = plan_flow(c, best.zchunk);
-  }
+  drop_graphs(c);
+  rc = plan_flow(c, best.zchunk);
   if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   const std::string key = tune_key(c);

@@ -88,7 +88,7 @@ struct hmf_ctx {
   cudaGraphExec_t graph_many = nullptr;  // pipelined solves: several iterations per replay
 
   // z-slab pipeline of the replayed iterations (hmf_set_pipeline)
-  bool pipeline = false;
+  bool pipeline = true;
   int n_slabs = 0, slab_tiles = 0;
   std::vector<hmf::Geometry> slab_geo;
   std::vector<hmf::TreeTable> h_tree_slabs;

@@ -107,7 +107,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   const bool xout = lane >= 2 && lane < 2 + ocols && x < G.vx;
   // per-row constants of this thread (rows warp*4 + r of the window)
   bool rin[4], ypos[4], ynl[4], rout[4];
-  long long rowoff[4];
+  int rowoff[4];  // element offsets within a plane (a volume holds fewer than 2^31 elements)
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int row = warp * 4 + r;
@@ -116,7 +116,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     ypos[r] = y > 0;
     ynl[r] = y != G.vy - 1;
     rout[r] = xout && row >= 2 && row < 2 + orows && y < G.vy;
-    rowoff[r] = (long long)y * G.pitch + x;
+    rowoff[r] = y * G.pitch + x;
   }
 
   // If a previous launch already timed out waiting for its copies, the whole
@@ -173,12 +173,6 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       *(volatile int*)&stop_cta = 1;
     }
   };
-  auto wait_main = [&](int p) {
-    wait_on(&mbars[(p - kstart) % kTmaMainSlots], (unsigned)(((p - kstart) / kTmaMainSlots) & 1));
-  };
-  auto wait_pz = [&](int p) {
-    wait_on(&zbars[(p - kstart) % kTmaPzSlots], (unsigned)(((p - kstart) / kTmaPzSlots) & 1));
-  };
 
   if (threadIdx.x == 0) {
     for (int p = kstart; p <= min(kstart + 1, kmain_end); ++p)
@@ -206,6 +200,10 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       gprev[r] = ppx[r] = ppy[r] = ppz[r] = mprev[r] = Px[r] = Py[r] = Pz[r] = Sprev[r] = pzn_c[r] = 0.f;
     }
     bool have_pz = false;  // pzn_c holds pz of plane k (loaded in step k-1)
+    // Ring positions of plane k, advanced step by step: slot and phase
+    // parity in the main ring (3 slots) and the pz ring (4 slots).
+    int rmi = 0, rzi = 0;
+    unsigned phm = 0, phz = 0;
 
     // returns false when the march stops (a copy wait ran out)
     auto zstep = [&](const int k, auto stag) -> bool {
@@ -219,15 +217,16 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       // ---- stage A: g(k) from the staged inputs (kern_CalcGradStep on the
       // divergence kern_Divergence left, recomputed from the stored flows)
       float g[4], rx[4], ry_[4], rz[4], Scur[4];
+      const int rz1 = rzi == kTmaPzSlots - 1 ? 0 : rzi + 1;  // pz slot of plane k + 1
       if (doA) {
-        wait_main(k);
+        wait_on(&mbars[rmi], phm);
         const bool has_next = ST || k + 1 < G.vz;
         const bool pz_held = ST || have_pz;
-        if (!pz_held) wait_pz(k);
-        if (has_next) wait_pz(k + 1);
-        const float* cur = mslot(k);
-        const float* zc = zslot(k);
-        const float* zn = has_next ? zslot(k + 1) : zc;
+        if (!pz_held) wait_on(&zbars[rzi], phz);
+        if (has_next) wait_on(&zbars[rz1], rz1 == 0 ? phz ^ 1u : phz);
+        const float* cur = mslots + rmi * (kTmaMainArrays * kPlane);
+        const float* zc = zslots + rzi * kPlane;
+        const float* zn = has_next ? zslots + rz1 * kPlane : zc;
         float pyv[5];
 #pragma unroll
         for (int r = 0; r < 4; ++r) pyv[r] = cur[kPlane + (warp * 4 + r) * kTmaBoxX + off + lane];
@@ -267,9 +266,19 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         return false;
       }
       // the copies two planes ahead, spread over the warps' first lanes
+      // (plane k + 2 takes main slot rmi - 1 mod 3, plane k + 3 pz slot rzi - 1 mod 4)
       if (lane == 0) {
-        if (warp < narr && k + 2 <= kmain_end) issue_main_array(k + 2, warp, warp_map);
-        if (warp == W - 1 && k + 3 <= kpz_end) issue_pz(k + 3);
+        if (warp < narr && k + 2 <= kmain_end) {
+          const int sl = rmi == 0 ? kTmaMainSlots - 1 : rmi - 1;
+          mbar_expect_tx(&mbars[sl], (unsigned)(kPlane * 4));
+          tma_load_plane(mslots + sl * (kTmaMainArrays * kPlane) + warp * kPlane, warp_map, xs, y0 - 2, k + 2,
+                         &mbars[sl]);
+        }
+        if (warp == W - 1 && k + 3 <= kpz_end) {
+          const int sl = rzi == 0 ? kTmaPzSlots - 1 : rzi - 1;
+          mbar_expect_tx(&zbars[sl], (unsigned)(kPlane * 4));
+          tma_load_plane(zslots + sl * kPlane, &V->flow_in[par][2], xs, y0 - 2, k + 3, &zbars[sl]);
+        }
       }
 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow)
@@ -314,13 +323,15 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         m[r] = 1.0f;
         Sprev[r] = Scur[r];
       }
-      if (__any_sync(FULL, slow[0] || slow[1] || slow[2] || slow[3])) {
+      // per row, one warp-uniform branch: the lanes that need the exact
+      // multiplier take its value; the others evaluate sqrt(1) and lim / 1
+      // (no special operands, so no slow path inside the division) and keep 1
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          if (slow[r]) {
-            const float Fs = sqrtf(h[r]);
-            if (Fs > lim[r]) m[r] = lim[r] / Fs;
-          }
+      for (int r = 0; r < 4; ++r) {
+        if (__any_sync(FULL, slow[r])) {
+          const float Fs = sqrtf(slow[r] ? h[r] : 1.0f);
+          const float q = lim[r] / Fs;
+          m[r] = (slow[r] && Fs > lim[r]) ? q : m[r];
         }
       }
       xm[warp * 32 + lane] = m[3];
@@ -344,7 +355,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       // ---- stage E: divergence of P(k-2) (kern_Divergence), store P(k-2) and div(k-2)
       const float Pdown = warp < W - 1 ? xP[((k & 1) * W + warp + 1) * 32 + lane] : 0.f;
       const bool zonl = ST || ko != G.vz - 1;
-      const long long zoff = (long long)ko * G.plane;
+      const int zoff = ko * (int)G.plane;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const float Pxr = __shfl_down_sync(FULL, Px[r], 1);
@@ -354,7 +365,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         if (INT || ynl[r]) dv = dv - Pyd;
         if (zonl) dv = dv - nPz[r];
         if (doE && rout[r]) {
-          const long long o = zoff + rowoff[r];
+          const int o = zoff + rowoff[r];
           out_x[o] = Px[r];
           out_y[o] = Py[r];
           out_z[o] = Pz[r];
@@ -372,6 +383,9 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         Py[r] = nPy[r];
         Pz[r] = nPz[r];
       }
+      if (++rmi == kTmaMainSlots) rmi = 0, phm ^= 1u;
+      rzi = rz1;
+      if (rzi == 0) phz ^= 1u;
       return true;
     };
 

@@ -108,6 +108,8 @@ def test_ref_cuda_bitexact_64_row_windows(dims, parent, smooth_nodes, iters, zch
     ((33, 61, 23), [-1, 0, 0, 0], (), 10, 5, 64),                # 5 slabs of 5 planes, the last of 3
     ((64, 16, 40), [-1, 0, 0, 1, 1, 2, 2], (1, 3, 5), 9, 0, 0),   # the default plan's chunks
     ((20, 12, 6), [-1, 0, 0], (), 4, 0, 0),                      # a single slab
+    ((27, 14, 11), [-1, 0, 0, 1, 1, 2, 2], (1, 5), 20, 3, 0),    # slabs of 3 planes, the last of 2
+    ((27, 14, 11), [-1, 0, 0, 1, 1, 2, 2], (1, 5), 20, 2, 0),    # 2-plane chunks: the pipeline stays off
 ])
 def test_ref_cuda_bitexact_slab_pipeline(dims, parent, smooth_nodes, iters, zchunk, window):
     w = random_tree_problem(28, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
