@@ -555,10 +555,12 @@ int tree_grid(hmf_ctx* c) {
 }
 
 // The convergence log's device view (the arena of hmf_set_convergence_log).
-hmf::GapLog gap_view(const hmf_ctx* c) {
+hmf::GapLog gap_view(const hmf_ctx* c, int t) {
   hmf::GapLog g{};
-  g.counter = reinterpret_cast<unsigned int*>(c->d_gap);
-  g.max_bits = g.counter + 2;
+  unsigned int* base = reinterpret_cast<unsigned int*>(c->d_gap);
+  g.base = base;
+  g.t = t;
+  g.max_bits = base + 2;
   g.sum = reinterpret_cast<double*>(c->d_gap + round_up(8 + 4 * (size_t)c->gap_cap, 8));
   g.capacity = c->gap_cap;
   g.vx = c->vols[0].vx;
@@ -570,14 +572,14 @@ size_t gap_bytes(int cap) { return round_up(8 + 4 * (size_t)cap, 8) + 8 * (size_
 
 // The sweep over the elements [0, G.vol) of `table`'s arrays.
 int launch_tree_bulk_geo(hmf_ctx* c, const hmf::TreeTable* table, const hmf::Geometry& G, cudaStream_t s,
-                         bool gap_log) {
+                         bool gap_log, int gap_t) {
   const int smem = hmf::tree_bulk_smem_bytes(c->n);
   const int vc = hmf::tree_bulk_chunk(c->n);
   const long long chunks = (G.vol + vc - 1) / vc;
   const int per_sm = std::max(1, (227 * 1024) / (smem + 4096));
   const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
   if (int rc = maybe_request_stall(c, HMF_STALL_SWEEP, s)) return rc;
-  const hmf::GapLog gap = gap_log ? gap_view(c) : hmf::GapLog{};
+  const hmf::GapLog gap = gap_log ? gap_view(c, gap_t) : hmf::GapLog{};
   switch (c->n) {
 #define HMF_TREE_N(N)                                                                        \
   case N:                                                                                    \
@@ -598,8 +600,8 @@ int launch_tree_bulk_geo(hmf_ctx* c, const hmf::TreeTable* table, const hmf::Geo
   return HMF_OK;
 }
 
-int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log) {
-  return launch_tree_bulk_geo(c, table, c->geo, s, gap_log);
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log, int gap_t) {
+  return launch_tree_bulk_geo(c, table, c->geo, s, gap_log, gap_t);
 }
 
 // Grid of the per-voxel DAG kernels: as many blocks as are resident at once.
@@ -661,7 +663,7 @@ int launch_dag_sweep(hmf_ctx* c, cudaStream_t s) {
 
 int launch_tree(hmf_ctx* c, cudaStream_t s) {
   if (c->dag) return launch_dag_sweep(c, s);
-  if (c->tree_kind == 0) return launch_tree_bulk_with(c, c->d_tree, s, c->gap_on);
+  if (c->tree_kind == 0) return launch_tree_bulk_with(c, c->d_tree, s, c->gap_on, c->gap_t);
   if (c->tree_kind == 1) {
     const size_t smem4 = 4 * (size_t)c->n * hmf::kTree4Threads * sizeof(float4);
     const long long quads = c->geo.vol / 4;
@@ -704,7 +706,7 @@ int record_iteration(hmf_ctx* c, int parity, cudaStream_t s) {
 // dependencies above reach only the neighbouring slabs when every slab but
 // the last has at least 3 planes; with shorter chunks the pipeline is off.
 bool pipeline_active(const hmf_ctx* c) {
-  return c->pipeline && c->vols.size() == 1 && !c->dag && c->use_tma && c->tree_kind == 0 && !c->gap_on &&
+  return c->pipeline && c->vols.size() == 1 && !c->dag && c->use_tma && c->tree_kind == 0 &&
          c->semantics == HMF_SEMANTICS_REF_CUDA && c->n_items > 0 && !c->h_fvol.empty() &&
          c->h_fvol[0].zchunk >= 3;
 }
@@ -784,11 +786,20 @@ int record_slab_iterations(hmf_ctx* c, int n_iter) {
       cudaStream_t st = c->slab_streams[k];
       for (int j = std::max(0, k - 1); j <= std::min(K - 1, k + 1); ++j)
         if (j != k) CK(cudaStreamWaitEvent(st, c->slab_ev_flow[j], 0), "cudaStreamWaitEvent(flow)");
-      if (int rc = launch_tree_bulk_geo(c, c->d_tree_slabs + k, c->slab_geo[k], st, false)) return rc;
+      if (int rc = launch_tree_bulk_geo(c, c->d_tree_slabs + k, c->slab_geo[k], st, c->gap_on, t)) return rc;
       CK(cudaEventRecord(c->slab_ev_sweep[k], st), "cudaEventRecord(sweep)");
     }
   }
   for (int k = 0; k < K; ++k) CK(cudaStreamWaitEvent(origin, c->slab_ev_sweep[k], 0), "cudaStreamWaitEvent(join)");
+  return HMF_OK;
+}
+
+// The convergence log's base advances by the graph's iterations after its
+// last sweep.
+int record_gap_advance(hmf_ctx* c, int n_iter) {
+  if (!c->gap_on) return HMF_OK;
+  hmf::gap_advance_kernel<<<1, 1, 0, c->stream>>>(reinterpret_cast<unsigned int*>(c->d_gap), n_iter);
+  CK(cudaGetLastError(), "gap_advance_kernel launch");
   return HMF_OK;
 }
 
@@ -802,7 +813,12 @@ int capture(hmf_ctx* c, int n_iter, cudaGraphExec_t* out) {
   int rc = HMF_OK;
   if (slabs) rc = record_slab_iterations(c, n_iter);
   else
-    for (int i = 0; i < n_iter && rc == HMF_OK; ++i) rc = record_iteration(c, i & 1, c->stream);
+    for (int i = 0; i < n_iter && rc == HMF_OK; ++i) {
+      c->gap_t = i;
+      rc = record_iteration(c, i & 1, c->stream);
+    }
+  c->gap_t = 0;
+  if (!rc) rc = record_gap_advance(c, n_iter);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->launches = before;
   if (rc) {
@@ -1497,9 +1513,11 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   } else if (c->timing || c->stall_kind >= 0) {
     for (int it = 0; it < c->iterations; ++it) {
       c->dag_last = c->dag && it == c->iterations - 1;
+      c->gap_t = it;  // the log's base stays 0 on this path
       rc = timed(c, 0, s, do_flow, it & 1);
       if (!rc) rc = timed(c, 1, s, do_tree, 0);
       c->dag_last = false;
+      c->gap_t = 0;
       if (rc) return rc;
     }
   } else {
@@ -1660,7 +1678,7 @@ int hmf_get_convergence(hmf_ctx* c, double* max_change, double* mean_change, int
   const int n = std::min(capacity, c->gap_logged);
   if (n == 0) return c->gap_logged;
   DeviceGuard dg(c->device);
-  const hmf::GapLog g = gap_view(c);
+  const hmf::GapLog g = gap_view(c, 0);
   std::vector<unsigned int> bits(n);
   std::vector<double> sums(n);
   CK(cudaMemcpyAsync(bits.data(), g.max_bits, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream),

@@ -105,6 +105,7 @@ struct hmf_ctx {
   char* d_gap = nullptr;  // counter[2], max bits[gap_cap], sums[gap_cap]
   int gap_cap = 0;
   int gap_logged = 0;     // iterations logged by the last solve
+  int gap_t = 0;          // iteration (within the graph being captured) of the sweep launched next
 
   bool timing = false;
   long long launches = 0;
@@ -195,7 +196,8 @@ int launch_tree(hmf_ctx* c, cudaStream_t s);
 int launch_flow_tma_with(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, cudaStream_t s);
 int launch_flow_tma_items(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parity, int first_item, int n_items,
                           cudaStream_t s);
-int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log = false);
+int launch_tree_bulk_with(hmf_ctx* c, const hmf::TreeTable* table, cudaStream_t s, bool gap_log = false,
+                          int gap_t = 0);
 // Tensor map of one pitched volume block; box = kTmaBoxX columns x `rows`
 // rows (0: the rows of the context's flow window).
 int encode_plane_map(hmf_ctx* c, CUtensorMap* m, const float* base, const hmf_ctx::Volume& V, int rows = 0);

@@ -323,15 +323,13 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         m[r] = 1.0f;
         Sprev[r] = Scur[r];
       }
-      // per row, one warp-uniform branch: the lanes that need the exact
-      // multiplier take its value; the others evaluate sqrt(1) and lim / 1
-      // (no special operands, so no slow path inside the division) and keep 1
+      if (__any_sync(FULL, slow[0] || slow[1] || slow[2] || slow[3])) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        if (__any_sync(FULL, slow[r])) {
-          const float Fs = sqrtf(slow[r] ? h[r] : 1.0f);
-          const float q = lim[r] / Fs;
-          m[r] = (slow[r] && Fs > lim[r]) ? q : m[r];
+        for (int r = 0; r < 4; ++r) {
+          if (slow[r]) {
+            const float Fs = sqrtf(h[r]);
+            if (Fs > lim[r]) m[r] = lim[r] / Fs;
+          }
         }
       }
       xm[warp * 32 + lane] = m[3];

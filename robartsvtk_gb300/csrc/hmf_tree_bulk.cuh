@@ -25,17 +25,24 @@ constexpr int kTreeBulkStages = 2;
 
 // Convergence log of a solve: per iteration, max and sum over non-root
 // vertices and voxels of |u_new - u_old|, reduced inside the label sweep
-// (warp shuffles, one pair of atomics per warp, the iteration advanced by
-// the CTA that finishes last).  Padding columns (x >= vx of each row of
-// `pitch` elements; pitch 0: none) are left out.
+// (warp shuffles, one pair of atomics per warp).  A sweep launch logs into
+// entry *base + t: `base` is the first iteration of the replayed graph it
+// belongs to (advanced by the graph's last node), `t` its iteration within
+// that graph -- so the sweeps of one iteration cut into slabs, and sweeps of
+// consecutive iterations running side by side, log where they belong.
+// Padding columns (x >= vx of each row of `pitch` elements; pitch 0: none)
+// are left out.
 struct GapLog {
   unsigned int* max_bits;  // [capacity] float bits (non-negative floats order as unsigned ints)
   double* sum;             // [capacity]
-  unsigned int* counter;   // [0] iteration of the next sweep, [1] CTAs finished with the current one
+  const unsigned int* base;
+  int t;
   int capacity;
   int vx, pitch;
-  int pad_;
 };
+
+// The graph's last node with the log on: the next replay's first iteration.
+__global__ void gap_advance_kernel(unsigned int* base, int n_iter) { *base += (unsigned)n_iter; }
 constexpr int kTreeBulkSmemBudget = 200 * 1024;
 
 // Chunk length (voxels) for a tree of n entries: the largest power of two
@@ -51,13 +58,11 @@ __host__ __device__ constexpr int tree_bulk_smem_bytes(int n) {
   return 128 + kTreeBulkStages * (3 * (n - 1) + 1) * tree_bulk_chunk(n) * 4;
 }
 
-// End of a sweep launch with the convergence log on (every thread of the
-// CTA): warp-shuffle max and sum, one pair of atomics per warp into this
-// iteration's entries, then the CTA's finish count; the CTA that finishes
-// last advances the iteration.  Every CTA reads the iteration before its own
-// finish count, so all CTAs of one launch log into the same entry.
+// End of a sweep launch with the convergence log on (every thread):
+// warp-shuffle max and sum, one pair of atomics per warp into the entry of
+// this launch's iteration.
 __device__ __forceinline__ void gap_log_commit(const GapLog& gap, float gmax, float gsum) {
-  const unsigned it = *(volatile unsigned*)&gap.counter[0];
+  const unsigned it = *gap.base + (unsigned)gap.t;
   for (int o = 16; o > 0; o >>= 1) {
     gmax = fmaxf(gmax, __shfl_down_sync(0xffffffffu, gmax, o));
     gsum += __shfl_down_sync(0xffffffffu, gsum, o);
@@ -65,15 +70,6 @@ __device__ __forceinline__ void gap_log_commit(const GapLog& gap, float gmax, fl
   if ((threadIdx.x & 31) == 0 && it < (unsigned)gap.capacity) {
     atomicMax(&gap.max_bits[it], __float_as_uint(gmax));
     atomicAdd(&gap.sum[it], (double)gsum);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(&gap.counter[1], 1u) == gridDim.x - 1) {
-      gap.counter[1] = 0;
-      __threadfence();
-      atomicAdd(&gap.counter[0], 1u);
-    }
   }
 }
 
