@@ -710,21 +710,30 @@ int record_iteration(hmf_ctx* c, int parity, cudaStream_t s) {
 // A flow launch reads planes zs - 2 .. ze + 2 of its chunk [zs, ze), so the
 // dependencies above reach only the neighbouring slabs when every slab but
 // the last has at least 3 planes; with shorter chunks the pipeline is off.
+//
+// A batch is cut into groups of consecutive volumes instead (about equal in
+// voxels): a group's flow items and its elements are contiguous, and groups
+// share nothing, so each group's launches depend only on the group's own
+// previous launch, and the groups' flows and sweeps overlap freely.
+constexpr int kBatchGroups = 6;
+
 bool pipeline_active(const hmf_ctx* c) {
-  return c->pipeline && c->vols.size() == 1 && !c->dag && c->use_tma && c->tree_kind == 0 &&
-         c->semantics == HMF_SEMANTICS_REF_CUDA && c->n_items > 0 && !c->h_fvol.empty() &&
-         c->h_fvol[0].zchunk >= 3;
+  if (!c->pipeline || c->dag || !c->use_tma || c->tree_kind != 0 || c->semantics != HMF_SEMANTICS_REF_CUDA ||
+      c->n_items <= 0 || c->h_fvol.empty())
+    return false;
+  if (c->vols.size() > 1) return true;
+  return c->h_fvol[0].zchunk >= 3;
 }
 
-// Per-slab sweep tables: the solver's table with every array pointer moved
-// to the slab's first plane (its inputs may move between solves, so they are
-// written before every pipelined solve, into the array the graphs point at).
+// Per-segment sweep tables: the solver's table with every array pointer
+// moved to the segment's first element (its inputs may move between solves,
+// so they are written before every pipelined solve, into the array the
+// graphs point at).
 int upload_slab_tables(hmf_ctx* c, cudaStream_t s) {
-  const auto& V = c->vols[0];
-  const int K = c->n_slabs, zc = c->h_fvol[0].zchunk;
+  const int K = c->n_slabs;
   c->h_tree_slabs.assign(K, c->h_tree);
   for (int k = 0; k < K; ++k) {
-    const long long base = (long long)k * zc * V.plane;
+    const long long base = c->seg_base[k];
     hmf::TreeTable& T = c->h_tree_slabs[k];
     for (int e = 0; e < T.n; ++e) {
       hmf::TreeEntry& E = T.e[e];
@@ -741,18 +750,56 @@ int upload_slab_tables(hmf_ctx* c, cudaStream_t s) {
   return HMF_OK;
 }
 
-// Slabs of the current plan (one per z chunk), their tables' device array,
-// streams and events (made when the graphs are captured).
+// Segments of the current plan (one per z chunk of a single volume, or
+// groups of a batch's volumes), their tables' device array, streams and
+// events (made when the graphs are captured).
 int prepare_slabs(hmf_ctx* c, cudaStream_t s) {
-  const auto& V = c->vols[0];
-  const int zc = c->h_fvol[0].zchunk;
-  const int K = (V.vz + zc - 1) / zc;
-  c->slab_tiles = c->n_items / K;
-  c->slab_geo.assign(K, c->geo);
-  for (int k = 0; k < K; ++k) {
-    const long long z0 = (long long)k * zc, z1 = std::min<long long>(V.vz, z0 + zc);
-    c->slab_geo[k].vol = (z1 - z0) * V.plane;
+  c->seg_first_item.clear();
+  c->seg_items.clear();
+  c->seg_base.clear();
+  c->slab_geo.clear();
+  if (c->vols.size() == 1) {
+    const auto& V = c->vols[0];
+    const int zc = c->h_fvol[0].zchunk;
+    const int K = (V.vz + zc - 1) / zc;
+    const int per = c->n_items / K;  // windows of one z chunk
+    for (int k = 0; k < K; ++k) {
+      const long long z0 = (long long)k * zc, z1 = std::min<long long>(V.vz, z0 + zc);
+      c->seg_first_item.push_back(k * per);
+      c->seg_items.push_back(per);
+      c->seg_base.push_back(z0 * V.plane);
+      c->slab_geo.push_back(c->geo);
+      c->slab_geo.back().vol = (z1 - z0) * V.plane;
+    }
+    c->seg_neighbours = 1;
+  } else {
+    // work items per volume (plan_flow enumerates them volume by volume)
+    std::vector<int> items(c->vols.size(), 0);
+    for (const auto& it : c->h_items) ++items[it.vol];
+    const int nv = (int)c->vols.size();
+    const int G = std::min(nv, kBatchGroups);
+    long long done = 0;
+    int b = 0, item = 0;
+    for (int g = 0; g < G && b < nv; ++g) {
+      const long long goal = (c->total * (g + 1)) / G;  // elements up to the end of this group
+      const int b0 = b, i0 = item;
+      const int later = G - 1 - g;  // groups after this one, one volume each at least
+      long long elems = 0;
+      do {
+        elems += c->vols[b].vol;
+        item += items[b];
+        ++b;
+      } while (b < nv - later && (g == G - 1 || done + elems < goal));
+      c->seg_first_item.push_back(i0);
+      c->seg_items.push_back(item - i0);
+      c->seg_base.push_back(c->vols[b0].off);
+      c->slab_geo.push_back(c->geo);
+      c->slab_geo.back().vol = elems;
+      done += elems;
+    }
+    c->seg_neighbours = 0;
   }
+  const int K = (int)c->seg_base.size();
   if (c->d_tree_slabs) cudaFree(c->d_tree_slabs);
   c->d_tree_slabs = nullptr;
   CK(cudaMalloc(&c->d_tree_slabs, sizeof(hmf::TreeTable) * K), "cudaMalloc(slab tables)");
@@ -782,14 +829,14 @@ int record_slab_iterations(hmf_ctx* c, int n_iter) {
     for (int k = 0; k < K; ++k) {
       cudaStream_t st = c->slab_streams[k];
       if (t > 0)  // sweep(t-1, k) precedes on this stream
-        for (int j = std::max(0, k - 1); j <= std::min(K - 1, k + 1); ++j)
+        for (int j = std::max(0, k - c->seg_neighbours); j <= std::min(K - 1, k + c->seg_neighbours); ++j)
           if (j != k) CK(cudaStreamWaitEvent(st, c->slab_ev_sweep[j], 0), "cudaStreamWaitEvent(sweep)");
-      if (int rc = launch_flow_tma_items(c, c->d_tma, t & 1, k * c->slab_tiles, c->slab_tiles, st)) return rc;
+      if (int rc = launch_flow_tma_items(c, c->d_tma, t & 1, c->seg_first_item[k], c->seg_items[k], st)) return rc;
       CK(cudaEventRecord(c->slab_ev_flow[k], st), "cudaEventRecord(flow)");
     }
     for (int k = 0; k < K; ++k) {
       cudaStream_t st = c->slab_streams[k];
-      for (int j = std::max(0, k - 1); j <= std::min(K - 1, k + 1); ++j)
+      for (int j = std::max(0, k - c->seg_neighbours); j <= std::min(K - 1, k + c->seg_neighbours); ++j)
         if (j != k) CK(cudaStreamWaitEvent(st, c->slab_ev_flow[j], 0), "cudaStreamWaitEvent(flow)");
       if (int rc = launch_tree_bulk_geo(c, c->d_tree_slabs + k, c->slab_geo[k], st, c->gap_on, t)) return rc;
       CK(cudaEventRecord(c->slab_ev_sweep[k], st), "cudaEventRecord(sweep)");

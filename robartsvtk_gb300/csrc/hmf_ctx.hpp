@@ -89,8 +89,11 @@ struct hmf_ctx {
 
   // z-slab pipeline of the replayed iterations (hmf_set_pipeline)
   bool pipeline = true;
-  int n_slabs = 0, slab_tiles = 0;
-  std::vector<hmf::Geometry> slab_geo;
+  int n_slabs = 0;         // segments: z slabs of a single volume, or groups of a batch's volumes
+  int seg_neighbours = 1;  // slabs wait for the neighbouring slabs (1), volume groups for none (0)
+  std::vector<int> seg_first_item, seg_items;  // flow work items of each segment
+  std::vector<long long> seg_base;             // first element of each segment
+  std::vector<hmf::Geometry> slab_geo;         // each segment's elements (vol = their count)
   std::vector<hmf::TreeTable> h_tree_slabs;
   hmf::TreeTable* d_tree_slabs = nullptr;
   std::vector<cudaStream_t> slab_streams;
