@@ -381,6 +381,8 @@ class HMFBatchSolver:
         check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
 
     # the flow plan's controls, shared with HMFSolver
+    set_pipeline = HMFSolver.set_pipeline
+    pipeline = HMFSolver.pipeline
     set_flow_window = HMFSolver.set_flow_window
     flow_window = HMFSolver.flow_window
     set_zchunk = HMFSolver.set_zchunk

@@ -21,10 +21,11 @@ def make_batch(seed, dims_list, parent=PARENT, iterations=15, smooth_nodes=(1, 3
     return ws
 
 
-def solve_batch(ws, semantics=REF_CUDA, autotune=False, device_inputs=False):
+def solve_batch(ws, semantics=REF_CUDA, autotune=False, device_inputs=False, pipeline=True):
     import torch
     keep = []
     with HMFBatchSolver([w.dims for w in ws], ws[0].parent, semantics) as b:
+        b.set_pipeline(pipeline)
         for i, w in enumerate(ws):
             for leaf, d in w.data.items():
                 if device_inputs:
@@ -68,10 +69,15 @@ def same(a, b, what):
 def test_batch_of_uneven_volumes_matches_oracle_per_volume():
     dims = [(37, 19, 23), (48, 48, 48), (5, 4, 3), (61, 30, 9), (1, 7, 11), (33, 65, 12)]
     ws = make_batch(100, dims)
-    res, stats = solve_batch(ws)
-    for i, w in enumerate(ws):
-        same(res[i], oracle(w), "volume %d %s" % (i, w.dims))
-    assert stats["launches"] == 1 + 2 * ws[0].iterations  # the whole batch: 2 launches per iteration
+    refs = [oracle(w) for w in ws]
+    # the whole batch in 2 launches per iteration, or (slab pipeline, the
+    # default) 2 per group of consecutive volumes, the groups as independent
+    # graph chains
+    for pipeline, per_iter in ((False, 2), (True, 2 * min(6, len(dims)))):
+        res, stats = solve_batch(ws, pipeline=pipeline)
+        for i, w in enumerate(ws):
+            same(res[i], refs[i], "volume %d %s pipeline %s" % (i, w.dims, pipeline))
+        assert stats["launches"] == 1 + per_iter * ws[0].iterations
 
 
 def test_batch_with_device_inputs_and_autotune():
