@@ -59,6 +59,8 @@ def parse():
                          "the command ncu wraps")
     ap.add_argument("--profile-dag", action="store_true",
                     help="one DAG solve (--dag-size, --dag-iterations): the command ncu wraps")
+    ap.add_argument("--profile-planes", type=int, default=0,
+                    help="--profile on the first N z planes of the workload (same x-y extent, a smaller capture)")
     ap.add_argument("--profile", action="store_true",
                     help="two solves (one warm, one profiled) and nothing else: the command ncu wraps")
     ap.add_argument("--large", action="store_true",
@@ -364,6 +366,60 @@ def run_ours(args):
     value = replicas.job_throughput(units_per_step, ms_rank, "cuda")
     ms = replicas.max_over_ranks(ms_rank, "cuda")
 
+    # ---- end to end through the public API with pinned host buffers -------
+    # (right after the device-resident steps, under its own clock record):
+    # every step stages the inputs from pinned host memory inside solve() and
+    # reads every leaf's labels back into pinned host memory; an event after
+    # solve() splits the step into the solve (with its input copies) and the
+    # copy-out (with its synchronisations)
+    h_data = {leaf: torch.from_numpy(d).pin_memory() for leaf, d in w.data.items()}
+    h_smooth_obj = {}
+    h_smooth = {}
+    for v, S in w.smooth.items():
+        if id(S) not in h_smooth_obj:
+            h_smooth_obj[id(S)] = torch.from_numpy(S).pin_memory()
+        h_smooth[v] = h_smooth_obj[id(S)]
+    h_out = {leaf: torch.empty(w.dims[::-1], dtype=torch.float32).pin_memory() for leaf in w.leaves}
+    h2d = sum(t.numel() * 4 for t in h_data.values()) + sum(t.numel() * 4 for t in h_smooth_obj.values())
+    d2h = sum(t.numel() * 4 for t in h_out.values())
+    split = []
+
+    def e2e_step(mark=None):
+        for leaf, t in h_data.items():
+            solver.set_data(leaf, t)
+        for v, t in h_smooth.items():
+            solver.set_smoothness(v, t)
+        solver.solve(stream)
+        if mark is not None:
+            mark.record(stream)
+        for leaf in w.leaves:
+            solver.labels(leaf, out=h_out[leaf], stream=stream)
+
+    e2e_step()
+    replicas.barrier()
+    e_steps = max(2, min(args.steps, 3))
+    marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(e_steps)]
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    e2e_clocks = ClockSampler(local)
+    e2e_clocks.start()
+    e2.record(stream)
+    for i in range(e_steps):
+        marks[i][0].record(stream)
+        e2e_step(marks[i][1])
+    e3.record(stream)
+    stream.synchronize()
+    e2e_clock_info = e2e_clocks.stop()
+    e2e_rank_ms = e2.elapsed_time(e3) / e_steps
+    e2e_value = replicas.job_throughput(units_per_step, e2e_rank_ms, "cuda")
+    e2e_ms = replicas.max_over_ranks(e2e_rank_ms, "cuda")
+    e2e_solve_ms = sum(a.elapsed_time(b) for a, b in marks) / e_steps
+    for leaf, t in d_data.items():  # device-resident inputs again for the legs below
+        solver.set_data(leaf, t)
+    for v, t in d_smooth.items():
+        solver.set_smoothness(v, t)
+
     # ---- per-kernel device times (events around every launch) -------------
     solver.set_timing(True)
     solver.solve(stream)
@@ -400,42 +456,6 @@ def run_ours(args):
     fp64["seconds"] = time.perf_counter() - t0
     fp64["what"] = ("max over leaves and voxels of |u_fp32 - u_fp64| after all %d iterations; argmax leaf "
                     "agreement between the two" % w.iterations)
-
-    # ---- end to end through the public API with pinned host buffers -------
-    h_data = {leaf: torch.from_numpy(d).pin_memory() for leaf, d in w.data.items()}
-    h_smooth_obj = {}
-    h_smooth = {}
-    for v, S in w.smooth.items():
-        if id(S) not in h_smooth_obj:
-            h_smooth_obj[id(S)] = torch.from_numpy(S).pin_memory()
-        h_smooth[v] = h_smooth_obj[id(S)]
-    h_out = {leaf: torch.empty(w.dims[::-1], dtype=torch.float32).pin_memory() for leaf in w.leaves}
-    h2d = sum(t.numel() * 4 for t in h_data.values()) + sum(t.numel() * 4 for t in h_smooth_obj.values())
-    d2h = sum(t.numel() * 4 for t in h_out.values())
-
-    def e2e_step():
-        for leaf, t in h_data.items():
-            solver.set_data(leaf, t)
-        for v, t in h_smooth.items():
-            solver.set_smoothness(v, t)
-        solver.solve(stream)
-        for leaf in w.leaves:
-            solver.labels(leaf, out=h_out[leaf], stream=stream)
-
-    e2e_step()
-    replicas.barrier()
-    e_steps = max(2, min(args.steps, 3))
-    e2 = torch.cuda.Event(enable_timing=True)
-    e3 = torch.cuda.Event(enable_timing=True)
-    stream.synchronize()
-    e2.record(stream)
-    for _ in range(e_steps):
-        e2e_step()
-    e3.record(stream)
-    stream.synchronize()
-    e2e_rank_ms = e2.elapsed_time(e3) / e_steps
-    e2e_value = replicas.job_throughput(units_per_step, e2e_rank_ms, "cuda")
-    e2e_ms = replicas.max_over_ranks(e2e_rank_ms, "cuda")
 
     # ---- roofline -----------------------------------------------------------
     peak, peak_kind = measured_peak_hbm()
@@ -478,7 +498,9 @@ def run_ours(args):
                          % (solver.device_bytes() / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms, "solve_with_input_copies_ms": e2e_solve_ms,
+                "copy_out_and_host_gaps_ms": e2e_rank_ms - e2e_solve_ms, "over_device_resident": e2e_rank_ms / ms_rank - 1.0,
+                "clocks": e2e_clock_info},
         "gpu_launches": launches,
         "clocks": clock_info,
         "roofline": roofline,
@@ -1030,11 +1052,18 @@ def bench_adjoint(args, device_stream):
 def run_profile(args):
     """Two solves of the benchmark workload with device-resident inputs;
     launches per solve: 1 init_kernel + iterations x (flow_kernel, tree_kernel)."""
+    import numpy as np
     import torch
 
     from robartsvtk_gb300 import HMFSolver
 
     w = make_workload(args, 0)
+    nz = args.profile_planes
+    if 0 < nz < w.dims[2]:  # the first nz planes ([z, y, x] arrays)
+        w.dims = (w.dims[0], w.dims[1], nz)
+        w.data = {leaf: np.ascontiguousarray(d[:nz]) for leaf, d in w.data.items()}
+        cut = {}
+        w.smooth = {v: cut.setdefault(id(S), np.ascontiguousarray(S[:nz])) for v, S in w.smooth.items()}
     solver = HMFSolver(w.dims, w.parent)
     keep = {}
     for leaf, d in w.data.items():

@@ -36,6 +36,11 @@ constexpr int kAfPlane = 1216;              // floats per staged plane (36 x 33 
 constexpr int kAfMainArrays = 10;           // px, py, s, c, u, Pbx, Pby, Pbz, dbp, S
 constexpr int kAfMainSlots = 3;
 constexpr int kAfPzSlots = 4;
+// Plane k + kAfMainLead (main ring) and pz of plane k + 1 + kAfPzLead are
+// issued in step k after its first CTA barrier; the leads may rise to
+// kAfMainSlots and kAfPzSlots - 1.
+constexpr int kAfMainLead = 2;
+constexpr int kAfPzLead = 2;
 constexpr int kAfR = 2;                     // rows per thread
 constexpr int kAfWarps = 32 / kAfR;
 constexpr int kAfThreads = 32 * kAfWarps;   // 512
@@ -188,9 +193,9 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     wait0(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1));
   };
   if (threadIdx.x == 0) {
-    for (int p = kstart; p <= min(kstart + 1, kA_end); ++p)
+    for (int p = kstart; p <= min(kstart + kAfMainLead - 1, kA_end); ++p)
       for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
-    for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
+    for (int p = kstart; p <= min(kstart + kAfPzLead, kpz_end); ++p) issue_pz(p);
     wait_main0(kstart);
     wait_pz0(kstart);
     if (kstart + 1 < G.vz) wait_pz0(kstart + 1);
@@ -281,8 +286,8 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
       XG_L[xw] = g[kAfR - 1];
       __syncthreads();  // (1)
       if (lane == 0) {
-        if (warp < narr && k + 2 <= kA_end) issue_main_array(k + 2, warp, warp_map);
-        if (warp == kAfWarps - 1 && k + 3 <= kpz_end) issue_pz(k + 3);
+        if (warp < narr && k + kAfMainLead <= kA_end) issue_main_array(k + kAfMainLead, warp, warp_map);
+        if (warp == kAfWarps - 1 && k + 1 + kAfPzLead <= kpz_end) issue_pz(k + 1 + kAfPzLead);
       }
 
       // ---- stage B: p'(k) (kern_DescentSpatialFlow) and the total adjoint t(k)
@@ -481,12 +486,13 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
     if (fp.error_flag) atomicOr(fp.error_flag, 2);
     // Copies still in flight into this CTA's shared memory must land before
     // it exits.  Up to step k_stop the main ring was filled to plane
-    // k_stop + 2 and the pz ring to k_stop + 3 (the initial issue: kstart + 1,
-    // kstart + 2), each slot holding at most one pending phase: wait for the
-    // last plane issued into each slot, with the default bound.
+    // k_stop + kAfMainLead and the pz ring to k_stop + 1 + kAfPzLead (the
+    // initial issue: kstart - 1 + kAfMainLead, kstart + kAfPzLead), each slot
+    // holding at most one pending phase: wait for the last plane issued into
+    // each slot, with the default bound.
     const int ks = k_stop >= 0 ? k_stop : kstart;
-    const int l_main = min(max(ks + 2, kstart + 1), kA_end);
-    const int l_pz = min(max(ks + 3, kstart + 2), kpz_end);
+    const int l_main = min(max(ks + kAfMainLead, kstart + kAfMainLead - 1), kA_end);
+    const int l_pz = min(max(ks + 1 + kAfPzLead, kstart + kAfPzLead), kpz_end);
     for (int p = max(kstart, l_main - kAfMainSlots + 1); p <= l_main; ++p)
       mbar_wait_bounded(&mbars[(p - kstart) % kAfMainSlots], (unsigned)(((p - kstart) / kAfMainSlots) & 1),
                         kTmaWaitLimitNs);

@@ -15,8 +15,8 @@
 //    registers from plane to plane.
 //  * The six or seven input planes a step needs (three flow components, sink,
 //    label, parent sink, smoothness) arrive by cp.async.bulk.tensor into
-//    shared-memory rings completed by mbarriers, two planes ahead of the one
-//    being computed.  Every mbarrier wait is bounded: on time-out the kernel
+//    shared-memory rings completed by mbarriers, issued two steps before
+//    their first use (kTmaMainLead, kTmaPzLead).  Every mbarrier wait is bounded: on time-out the kernel
 //    sets an error flag instead of hanging.
 //  * The stencil chain needs two halo columns/rows on the low side and up to
 //    two (columns) / three (rows) on the high side, so a window yields up to
@@ -175,9 +175,9 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   };
 
   if (threadIdx.x == 0) {
-    for (int p = kstart; p <= min(kstart + 1, kmain_end); ++p)
+    for (int p = kstart; p <= min(kstart + kTmaMainLead - 1, kmain_end); ++p)
       for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
-    for (int p = kstart; p <= min(kstart + 2, kpz_end); ++p) issue_pz(p);
+    for (int p = kstart; p <= min(kstart + kTmaPzLead, kpz_end); ++p) issue_pz(p);
     // the failure path on demand: a wait on a barrier that no copy completes
     if (stall_cta) wait_on(stall_bar, 0);
   }
@@ -265,19 +265,22 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
         k_stop = k;
         return false;
       }
-      // the copies two planes ahead, spread over the warps' first lanes
-      // (plane k + 2 takes main slot rmi - 1 mod 3, plane k + 3 pz slot rzi - 1 mod 4)
+      // the copies ahead, spread over the warps' first lanes: plane
+      // k + kTmaMainLead into the main slot that plane k + kTmaMainLead -
+      // kTmaMainSlots left (read in stage A at the latest), pz of plane
+      // k + 1 + kTmaPzLead into the pz slot of plane k + 1 + kTmaPzLead -
+      // kTmaPzSlots (read as zn in an earlier step, or as zc in this one)
       if (lane == 0) {
-        if (warp < narr && k + 2 <= kmain_end) {
-          const int sl = rmi == 0 ? kTmaMainSlots - 1 : rmi - 1;
+        if (warp < narr && k + kTmaMainLead <= kmain_end) {
+          const int sl = (rmi + kTmaMainLead) % kTmaMainSlots;
           mbar_expect_tx(&mbars[sl], (unsigned)(kPlane * 4));
-          tma_load_plane(mslots + sl * (kTmaMainArrays * kPlane) + warp * kPlane, warp_map, xs, y0 - 2, k + 2,
-                         &mbars[sl]);
+          tma_load_plane(mslots + sl * (kTmaMainArrays * kPlane) + warp * kPlane, warp_map, xs, y0 - 2,
+                         k + kTmaMainLead, &mbars[sl]);
         }
-        if (warp == W - 1 && k + 3 <= kpz_end) {
-          const int sl = rzi == 0 ? kTmaPzSlots - 1 : rzi - 1;
+        if (warp == W - 1 && k + 1 + kTmaPzLead <= kpz_end) {
+          const int sl = (rzi + 1 + kTmaPzLead) % kTmaPzSlots;
           mbar_expect_tx(&zbars[sl], (unsigned)(kPlane * 4));
-          tma_load_plane(zslots + sl * kPlane, &V->flow_in[par][2], xs, y0 - 2, k + 3, &zbars[sl]);
+          tma_load_plane(zslots + sl * kPlane, &V->flow_in[par][2], xs, y0 - 2, k + 1 + kTmaPzLead, &zbars[sl]);
         }
       }
 
@@ -399,12 +402,13 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   if (k_stop >= 0 && threadIdx.x == 0) {
     if (fp.error_flag) atomicOr(fp.error_flag, 2);
     // Copies still in flight into this CTA's shared memory must land before
-    // it exits.  Up to step k_stop the main ring was filled to plane
-    // k_stop + 1 and the pz ring to k_stop + 2 (the initial issue: kstart + 1,
-    // kstart + 2), each slot holding at most one pending phase: wait for the
-    // last plane issued into each slot, with the default bound.
-    const int l_main = min(max(k_stop + 1, kstart + 1), kmain_end);
-    const int l_pz = min(max(k_stop + 2, kstart + 2), kpz_end);
+    // it exits.  Steps before k_stop filled the main ring to plane
+    // k_stop - 1 + kTmaMainLead and the pz ring to k_stop + kTmaPzLead (the
+    // initial issue: kstart - 1 + kTmaMainLead, kstart + kTmaPzLead), each
+    // slot holding at most one pending phase: wait for the last plane issued
+    // into each slot, with the default bound.
+    const int l_main = min(max(k_stop, kstart) - 1 + kTmaMainLead, kmain_end);
+    const int l_pz = min(max(k_stop, kstart) + kTmaPzLead, kpz_end);
     for (int p = max(kstart, l_main - kTmaMainSlots + 1); p <= l_main; ++p)
       mbar_wait_bounded(&mbars[(p - kstart) % kTmaMainSlots],
                         (unsigned)(((p - kstart) / kTmaMainSlots) & 1), kTmaWaitLimitNs);

@@ -121,11 +121,20 @@ constexpr int kTmaRows = 32;   // window rows
 constexpr int kTmaPlane = kTmaBoxX * kTmaRows;        // floats per staged array plane
 // Two rings.  The z flow of plane k+1 is needed one step early (the divergence
 // of plane k), everything else only in its own step, so the main ring (px, py,
-// sink, label, parent sink, smoothness) has 3 slots and the pz ring 4: either
-// way two planes are in flight while one is computed.
+// sink, label, parent sink, smoothness) has 3 slots and the pz ring 4.  Plane
+// k + kTmaMainLead (main ring) and pz of plane k + 1 + kTmaPzLead are issued
+// in step k, after its first CTA barrier, kTmaMainLead / kTmaPzLead steps
+// before their first use.  The leads may rise to the slot counts (main) and
+// the slot count less one (pz); on a GB300 at 256^3 a lead of 3 on both rings
+// measured 0.9 % slower per iteration than 2, and 3 on either ring alone
+// within 0.2 %, so both stay at 2.
 constexpr int kTmaMainArrays = 6;
 constexpr int kTmaMainSlots = 3;
 constexpr int kTmaPzSlots = 4;
+constexpr int kTmaMainLead = 2;
+constexpr int kTmaPzLead = 2;
+static_assert(kTmaMainLead >= 1 && kTmaMainLead <= kTmaMainSlots, "main-ring lead");
+static_assert(kTmaPzLead >= 1 && kTmaPzLead <= kTmaPzSlots - 1, "pz-ring lead");
 constexpr int kTmaMaxOutX = 28;
 constexpr int kTmaMaxOutY = 27;
 constexpr int kTmaThreads = 256;
