@@ -104,6 +104,10 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the first sample: nvidia-smi has set up its session before the timed region starts
+            t0 = time.time()
+            while not self.lines and self.proc.poll() is None and time.time() - t0 < 3.0:
+                time.sleep(0.02)
         except OSError:
             self.proc = None
 
@@ -397,7 +401,7 @@ def run_ours(args):
 
     e2e_step()
     replicas.barrier()
-    e_steps = max(2, min(args.steps, 3))
+    e_steps = max(3, min(args.steps, 5))
     marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(e_steps)]
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)

@@ -1177,6 +1177,10 @@ bool valid_volume(const hmf_ctx* c, int b) { return c && b >= 0 && b < (int)c->v
 int check_error_flag(hmf_ctx* c) {
   int flag = 0;
   CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  return decode_error_flag(c, flag);
+}
+
+int decode_error_flag(hmf_ctx* c, int flag) {
   flag &= ~hmf::kStallRequest;  // a stall request no kernel took
   if (flag & 4) return fail(c, HMF_ERR_CUDA, "shared-memory staging area misaligned; results are invalid");
   if (flag & 2) return fail(c, HMF_ERR_CUDA, "an asynchronous-copy wait timed out; results are invalid");
@@ -1203,9 +1207,11 @@ int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* s
                          (size_t)V.vx * sizeof(float), (size_t)V.vy * V.vz, kind, s),
        "cudaMemcpy2DAsync(output)");
   }
-  if (where == HMF_HOST) {
+  if (where == HMF_HOST) {  // the error flag rides on the same stream: one synchronisation
+    if (!c->h_error) CK(cudaMallocHost(&c->h_error, sizeof(int)), "cudaMallocHost(error flag)");
+    CK(cudaMemcpyAsync(c->h_error, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(error flag)");
     CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(output)");
-    return check_error_flag(c);
+    return decode_error_flag(c, *c->h_error);
   }
   return HMF_OK;
 }
@@ -1465,6 +1471,7 @@ int hmf_destroy(hmf_ctx* c) {
   if (c->d_dag) cudaFree(c->d_dag);
   if (c->d_smooth_list) cudaFree(c->d_smooth_list);
   if (c->d_error) cudaFree(c->d_error);
+  if (c->h_error) cudaFreeHost(c->h_error);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_t0) cudaEventDestroy(c->ev_t0);
   if (c->ev_t1) cudaEventDestroy(c->ev_t1);

@@ -78,6 +78,7 @@ struct hmf_ctx {
   int tree_kind = 0;    // 0 tree_bulk_kernel, 1 tree4_kernel, 2 tree_kernel
   const float** d_smooth_list = nullptr;
   int* d_error = nullptr;
+  int* h_error = nullptr;  // pinned copy of *d_error read with host outputs (allocated at first use)
   int n_smooth_list = 0;
 
   cudaStream_t stream = nullptr;
@@ -212,6 +213,7 @@ int maybe_request_stall(hmf_ctx* c, int kind, cudaStream_t s);
 // Error flag set by the kernels (bit 0 negative input, 1 wait time-out,
 // 2 misaligned staging, 3 label index out of range), as a status.
 int check_error_flag(hmf_ctx* c);
+int decode_error_flag(hmf_ctx* c, int flag);
 
 // hmf_adjoint.cu
 void adjoint_free(hmf_ctx* c);
