@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--adjoint-size", type=int, default=128)
     ap.add_argument("--adjoint-iterations", type=int, default=300)
     ap.add_argument("--no-dag", action="store_true", help="skip the DAG solver measurement")
+    ap.add_argument("--no-paged", action="store_true", help="skip the out-of-core solve measurement")
+    ap.add_argument("--paged-planes", type=int, default=96,
+                    help="block planes the out-of-core leg's MaxGPUUsage budget is sized for")
     ap.add_argument("--no-dataterm", action="store_true", help="skip the data-term producer measurement")
     ap.add_argument("--dag-size", type=int, default=256)
     ap.add_argument("--dag-iterations", type=int, default=100)
@@ -514,6 +517,8 @@ def run_ours(args):
         "convergence_log": convergence,
         "post": post,
     }
+    if rank == 0 and not args.no_paged:
+        out["paged"] = bench_paged(args, w, solver, h_data, h_smooth, value, stream)
     if rank == 0 and not args.no_batched:
         out["batched"] = bench_batched(args, stream)
     if rank == 0 and not args.no_adjoint:
@@ -538,6 +543,57 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def bench_paged(args, w, in_core, h_data, h_smooth, in_core_value, device_stream):
+    """The same workload out of core (hmf_create_paged): a MaxGPUUsage budget
+    that holds two blocks of --paged-planes planes, the state in pinned host
+    memory, pinned host inputs; CUDA events around whole solves.  The labels
+    must equal the in-core solve's bit for bit."""
+    import numpy as np
+    import torch
+
+    from robartsvtk_gb300 import HMFSolver
+
+    total = torch.cuda.get_device_properties(torch.cuda.current_device()).total_memory
+    pitch = (w.dims[0] + 3) // 4 * 4
+    n_inputs = len(w.leaves) + len({id(S) for S in w.smooth.values()})
+    per_plane = (9 * (len(w.parent) - 1) + 1 + n_inputs) * pitch * w.dims[1] * 4
+    budget = 2 * (16 << 20) + 2 * args.paged_planes * per_plane
+    usage = budget / total
+    s = HMFSolver(w.dims, w.parent, max_gpu_usage=usage)
+    for leaf, t in h_data.items():
+        s.set_data(leaf, t)
+    for v, t in h_smooth.items():
+        s.set_smoothness(v, t)
+    for v, a in w.alpha.items():
+        s.set_smoothness_scalar(v, a)
+    s.set_params(w.iterations, w.step, w.cc)
+    s.solve(device_stream)  # warm: block contexts, pinned host state, graphs
+    device_stream.synchronize()
+    reps = 2
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(device_stream)
+    for _ in range(reps):
+        s.solve(device_stream)
+    e1.record(device_stream)
+    device_stream.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    plan = s.paged_plan()
+    same = all(np.array_equal(s.labels(leaf, stream=device_stream), in_core.labels(leaf, stream=device_stream))
+               for leaf in w.leaves)
+    units = w.nvox * len(w.leaves) * w.iterations
+    out = {
+        "workload": "the benchmark workload out of core: state in pinned host memory, pinned host inputs",
+        "max_gpu_usage": usage, "budget_bytes": budget, "device_bytes": s.device_bytes(),
+        "plan": plan, "ms_per_solve": ms, "value": units / (ms / 1000.0), "unit": UNIT,
+        "fraction_of_in_core": units / (ms / 1000.0) / in_core_value,
+        "link_gbs": plan["link_bytes"] / (ms / 1000.0) / 1e9,
+        "labels_identical_to_in_core": bool(same), "repetitions": reps,
+    }
+    s.close()
+    return out
 
 
 def bench_post(w, solver, device_stream):

@@ -143,6 +143,52 @@ size_t hmf_device_bytes(const hmf_ctx* ctx);
 int hmf_set_timing(hmf_ctx* ctx, int enabled);
 int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kind, int n_kinds);
 
+/* ---- Out-of-core solve (GPU memory budget) ---------------------------------
+ * Replaces the GPU buffer pager of vtkCudaHierarchicalMaxFlowSegmentation:
+ * MaxGPUUsage (vtkCudaHierarchicalMaxFlowSegmentation.h:52, a fraction of the
+ * device's memory, default 0.75), the buffer acquisition of
+ * CUDA_GetGPUBuffers (CUDA_hierarchicalmaxflow.cu:33-60) and the next-use
+ * paging of GetGPUBuffersV2 / SimulateIterationForBufferOrdering
+ * (vtkCudaHierarchicalMaxFlowSegmentation.cxx:884-1294), which move whole
+ * buffers across the host link before every pass once the state does not
+ * fit.
+ *
+ * hmf_create_paged makes a context whose solver state lives in pinned host
+ * memory (5 x (n_nodes - 1) + 1 arrays of VX*VY*VZ floats; 2 x (n_nodes - 1)
+ * + 1 when one round suffices) and whose device memory stays within
+ * max_gpu_usage x the device's memory (clamped to [0, 1]).  hmf_solve covers
+ * the volume with blocks of T z-planes (T from the budget: two block
+ * contexts of T planes fit) and iterates in rounds of k <= 8 iterations: each
+ * block is loaded, iterated k times with the in-core kernels, and stores back
+ * the planes at least 2k + 1 planes from its inner faces, which equal the
+ * in-core solve's.  Labels and sinks are therefore identical to hmf_create +
+ * hmf_solve's.  Volumes of 2^31 elements or more are allowed (each block is
+ * below that).  Works with hmf_set_data / hmf_set_smoothness (host inputs
+ * are copied once per solve into pinned memory unless already pinned; device
+ * inputs are read in place), hmf_set_smoothness_scalar, hmf_set_params,
+ * hmf_solve, hmf_get_labels, hmf_get_sink, hmf_leaf_order, hmf_device_bytes,
+ * hmf_set_timing / hmf_get_stats; every other call taking a context returns
+ * HMF_ERR_STATE.  Label trees, single volumes, both semantics (REF_CPU
+ * iterates per voxel: one round, no halo).
+ *  - hmf_set_paged_plan: block planes T and iterations per round k for later
+ *    solves (0: from the budget, k = min(8, (T - 4) / 8)); T >= 4 x (2k + 1)
+ *    unless one block covers the volume (then k > 0 splits the solve into
+ *    rounds of k iterations on that block).
+ *  - hmf_get_paged_plan: blocks, T, k and rounds of the last solve, and the
+ *    bytes it moved between host and device.
+ *  - hmf_paged_layout: host only (no device work): the blocks covering vz
+ *    planes with blocks of block_planes planes and halo_planes planes of
+ *    halo; writes up to `capacity` first planes (starts) and first owned
+ *    planes (owned: block j owns owned[j] .. owned[j+1]-1, the last block up
+ *    to vz-1) and returns the number of blocks, or HMF_ERR_INVALID_ARGUMENT
+ *    when the blocks are thinner than four halos. */
+int hmf_create_paged(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
+                     int device, double max_gpu_usage);
+int hmf_set_paged_plan(hmf_ctx* ctx, int block_planes, int round_iterations);
+int hmf_get_paged_plan(const hmf_ctx* ctx, int* blocks, int* block_planes, int* round_iterations, int* rounds,
+                       long long* link_bytes);
+int hmf_paged_layout(int vz, int block_planes, int halo_planes, int* starts, int* owned, int capacity);
+
 /* ---- Batches --------------------------------------------------------------
  * No counterpart in the reference, which solves one volume per filter
  * update: many volumes of different sizes that share one label tree, one set

@@ -95,6 +95,11 @@ SIGNATURES = [
     ("hmf_fp64_error", _I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _P]),
     ("hmf_fp64_loss", _I, [_P, _P, _I, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _P]),
     ("hmf_set_fp64_probe", _I, [_P, _I, _I, ctypes.c_longlong, ctypes.c_double]),
+    ("hmf_create_paged", _I, [ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_I), _I, _I, _I, ctypes.c_double]),
+    ("hmf_set_paged_plan", _I, [_P, _I, _I]),
+    ("hmf_get_paged_plan", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                ctypes.POINTER(ctypes.c_longlong)]),
+    ("hmf_paged_layout", _I, [_I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _I]),
     ("hmf_solve_noalloc", _I, [_I, _I, _I, ctypes.POINTER(_I), _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                ctypes.POINTER(ctypes.c_double), _I, ctypes.c_float, ctypes.c_float,
                                ctypes.POINTER(_P), _P]),

@@ -1,8 +1,8 @@
 """Builds libhmf_gb300.so in-tree (robartsvtk_gb300/_build/) for sm_103a.
 
-Seven translation units (the solver, its FP64 evaluation, its adjoint and
-its schedules, the vote and energy, the data-term producers, the C++
-facade), compiled
+Eight translation units (the solver, its out-of-core driver, its FP64
+evaluation, its adjoint and its schedules, the vote and energy, the
+data-term producers, the C++ facade), compiled
 in parallel with nvcc and linked into one shared library that exports the C
 ABI of include/hmf.h and the C++ facade of csrc/hmf_segmentation.hpp.  The
 kernel units are compiled with -fmad=false so the FP32 arithmetic follows the
@@ -31,6 +31,7 @@ UNITS = {
     "hmf_post.o": ("hmf_post.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]),
     "hmf_dataterm.o": ("hmf_dataterm.cu", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
                                            "-Xcompiler", "-ffp-contract=off"]),
+    "hmf_paged.o": ("hmf_paged.cu", []),
     "hmf_segmentation.o": ("hmf_segmentation.cpp", ["-x", "cu"]),
     "hmf_schedule.o": ("hmf_schedule.cpp", []),
 }

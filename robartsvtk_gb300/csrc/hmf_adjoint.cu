@@ -171,7 +171,7 @@ int plan(hmf_ctx* c, int T, int k_req) {
     S->arena = nullptr;
     S->bytes = 0;
     CK(cudaMalloc(&S->arena, need), "cudaMalloc(adjoint state)");
-    CK(cudaMemset(S->arena, 0, need), "cudaMemset(adjoint state)");
+    CK(cudaMemsetAsync(S->arena, 0, need, c->stream), "cudaMemsetAsync(adjoint state)");
     S->bytes = need;
   }
   S->iterations = T;
@@ -590,6 +590,7 @@ extern "C" {
 int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_every, double eps, double* loss,
                       void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_solve_adjoint")) return rc;
   if (c->vols.size() != 1) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the adjoint supports single-volume contexts");
   if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the adjoint is defined for trees (hmf_create), not graphs");
   if (c->semantics != HMF_SEMANTICS_REF_CUDA)

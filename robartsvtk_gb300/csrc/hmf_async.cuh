@@ -34,6 +34,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return done != 0;
 }
 
+// Tensor maps here live in global memory and are written by host copies
+// before a launch (one table per context, rewritten every solve).  The TMA
+// unit reads a map through the tensormap proxy, which may still hold the
+// 128-byte descriptor an earlier kernel used at the same address (a context
+// freed and another allocated in its place, or a table rewritten with other
+// arrays), so every thread that issues copies with a map first acquires it
+// for that proxy, at system scope because the writer is the host.
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
+
 __device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* map, int x, int y, int z,
                                                uint64_t* bar) {
   asm volatile(

@@ -233,7 +233,11 @@ int allocate_state(hmf_ctx* c) {
   const int nvol = (int)c->vols.size();
   c->arena_bytes = arr * (size_t)((c->dag ? 10 : 9) * nonroot + 1) + 4096;
   CK(cudaMalloc(&c->arena, c->arena_bytes), "cudaMalloc(state)");
-  CK(cudaMemset(c->arena, 0, c->arena_bytes), "cudaMemset(state)");
+  // Every write the solver's work depends on is queued on the context's own
+  // stream: the legacy stream's cudaMemset/cudaMemcpy are not ordered with
+  // non-blocking streams, so a zeroing queued there could land after a
+  // solve's first writes.
+  CK(cudaMemsetAsync(c->arena, 0, c->arena_bytes, c->stream), "cudaMemsetAsync(state)");
   char* p = c->arena;
   auto take = [&]() {
     float* r = reinterpret_cast<float*>(p);
@@ -269,7 +273,7 @@ int allocate_state(hmf_ctx* c) {
   if (c->dag) CK(cudaMalloc(&c->d_dag, sizeof(hmf::DagTable)), "cudaMalloc(graph table)");
   CK(cudaMalloc(&c->d_smooth_list, sizeof(float*) * hmf::kMaxVertices), "cudaMalloc(smooth list)");
   CK(cudaMalloc(&c->d_error, sizeof(int)), "cudaMalloc(error flag)");
-  CK(cudaMemset(c->d_error, 0, sizeof(int)), "cudaMemset(error flag)");
+  CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "cudaMemsetAsync(error flag)");
   return HMF_OK;
 }
 
@@ -307,10 +311,15 @@ int plan_flow(hmf_ctx* c, int zchunk) {
   if (c->d_items) cudaFree(c->d_items);
   c->d_items = nullptr;
   CK(cudaMalloc(&c->d_items, sizeof(hmf::FlowItem) * c->h_items.size()), "cudaMalloc(work items)");
-  CK(cudaMemcpy(c->d_items, c->h_items.data(), sizeof(hmf::FlowItem) * c->h_items.size(), cudaMemcpyHostToDevice),
-     "cudaMemcpy(work items)");
-  CK(cudaMemcpy(c->d_fvol, c->h_fvol.data(), sizeof(hmf::FlowVolume) * c->h_fvol.size(), cudaMemcpyHostToDevice),
-     "cudaMemcpy(volume table)");
+  // on the context's stream (ordered before its launches), completed before
+  // the host tables can change again
+  CK(cudaMemcpyAsync(c->d_items, c->h_items.data(), sizeof(hmf::FlowItem) * c->h_items.size(),
+                     cudaMemcpyHostToDevice, c->stream),
+     "cudaMemcpyAsync(work items)");
+  CK(cudaMemcpyAsync(c->d_fvol, c->h_fvol.data(), sizeof(hmf::FlowVolume) * c->h_fvol.size(), cudaMemcpyHostToDevice,
+                     c->stream),
+     "cudaMemcpyAsync(volume table)");
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize(work items)");
   return HMF_OK;
 }
 
@@ -442,7 +451,7 @@ int stage_inputs(hmf_ctx* c, cudaStream_t s, Staged& out) {
     c->staging = nullptr;
     c->staging_bytes = 0;
     CK(cudaMalloc(&c->staging, need), "cudaMalloc(input staging)");
-    CK(cudaMemset(c->staging, 0, need), "cudaMemset(input staging)");
+    CK(cudaMemsetAsync(c->staging, 0, need, s), "cudaMemsetAsync(input staging)");
     c->staging_bytes = need;
   }
   char* p = c->staging;
@@ -800,9 +809,14 @@ int prepare_slabs(hmf_ctx* c, cudaStream_t s) {
     c->seg_neighbours = 0;
   }
   const int K = (int)c->seg_base.size();
-  if (c->d_tree_slabs) cudaFree(c->d_tree_slabs);
-  c->d_tree_slabs = nullptr;
-  CK(cudaMalloc(&c->d_tree_slabs, sizeof(hmf::TreeTable) * K), "cudaMalloc(slab tables)");
+  // Every graph of one plan (captured one after another once the plan's
+  // graphs were dropped) points at the same table array, so it is
+  // reallocated only when the segment count changes.
+  if (!c->d_tree_slabs || c->n_slabs != K) {
+    if (c->d_tree_slabs) cudaFree(c->d_tree_slabs);
+    c->d_tree_slabs = nullptr;
+    CK(cudaMalloc(&c->d_tree_slabs, sizeof(hmf::TreeTable) * K), "cudaMalloc(slab tables)");
+  }
   c->n_slabs = K;
   if (int rc = upload_slab_tables(c, s)) return rc;
   while ((int)c->slab_streams.size() < K) {
@@ -1176,7 +1190,9 @@ bool valid_volume(const hmf_ctx* c, int b) { return c && b >= 0 && b < (int)c->v
 
 int check_error_flag(hmf_ctx* c) {
   int flag = 0;
-  CK(cudaMemcpy(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy(error flag)");
+  CK(cudaMemcpyAsync(&flag, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+     "cudaMemcpyAsync(error flag)");
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize(error flag)");
   return decode_error_flag(c, flag);
 }
 
@@ -1264,7 +1280,11 @@ void tune_file_append(const std::string& key, const TunedPlan& t) {
   std::fclose(f);
 }
 
-int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged) {
+int begin_solve_with(hmf_ctx* c, cudaStream_t user, Staged& staged, StateLoader load, void* arg);
+
+int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged) { return begin_solve_with(c, user, staged, nullptr, nullptr); }
+
+int begin_solve_with(hmf_ctx* c, cudaStream_t user, Staged& staged, StateLoader load, void* arg) {
   for (size_t b = 0; b < c->vols.size(); ++b)
     for (int l : c->leaves)
       if (!c->data[b][l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
@@ -1281,6 +1301,7 @@ int begin_solve(hmf_ctx* c, cudaStream_t user, Staged& staged) {
   if (rc) return rc;
   c->st_data = staged.data;
   c->st_smooth = staged.smooth;
+  if (load) return load(c, s, arg);  // a continued solve: the caller's state replaces the initialisation
   // flows of parity 0 start at zero
   const size_t bytes = (size_t)c->total * sizeof(float);
   for (int v = 0; v < c->n; ++v) {
@@ -1308,7 +1329,8 @@ namespace {
 // The common part of hmf_create_batch and hmf_create_dag: volumes, the graph
 // (`build`), device, stream, state, kernel attributes and the flow plan.
 template <class BuildGraph>
-int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics, int device, BuildGraph build) {
+int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics, int device, BuildGraph build,
+                   bool device_state = true) {
   g_create_error.clear();
   if (!out) return fail(nullptr, HMF_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
@@ -1333,7 +1355,7 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
     V.pitch = (V.vx + 3) / 4 * 4;
     V.plane = (long long)V.pitch * V.vy;
     V.vol = V.plane * V.vz;
-    if (V.vol >= (1LL << 31)) {  // the flow kernel addresses a volume's elements with 32-bit offsets
+    if (device_state && V.vol >= (1LL << 31)) {  // the flow kernel addresses a volume's elements with 32-bit offsets
       g_create_error = "volumes of 2^31 or more elements (rows padded to 4 floats) are not supported";
       delete c;
       return HMF_ERR_INVALID_ARGUMENT;
@@ -1395,6 +1417,10 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
       hmf_destroy(c);
       return HMF_ERR_CUDA;
     }
+    if (!device_state) {  // an out-of-core context: its blocks hold the device state
+      *out = c;
+      return HMF_OK;
+    }
     rc = allocate_state(c);
     if (!rc) rc = configure_kernels(c);
     if (!rc) {
@@ -1421,6 +1447,83 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
 }
 
 }  // namespace
+
+namespace hmfi {
+
+int solve_with(hmf_ctx* c, cudaStream_t user, StateLoader load, void* arg) {
+  DeviceGuard dg(c->device);
+  cudaStream_t s = c->stream;
+  Staged staged;
+  int rc = begin_solve_with(c, user, staged, load, arg);
+  if (rc) return rc;
+  c->gap_logged = 0;
+  if (c->gap_on && c->semantics == HMF_SEMANTICS_REF_CUDA) {
+    if (c->gap_cap < c->iterations) {  // a longer log: new arena, graphs re-captured with it
+      drop_graphs(c);
+      if (c->d_gap) cudaFree(c->d_gap);
+      c->d_gap = nullptr;
+      c->gap_cap = 0;
+      const int cap = std::max(c->iterations, 64);
+      CK(cudaMalloc(&c->d_gap, gap_bytes(cap)), "cudaMalloc(convergence log)");
+      c->gap_cap = cap;
+    }
+    CK(cudaMemsetAsync(c->d_gap, 0, gap_bytes(c->gap_cap), s), "cudaMemsetAsync(convergence log)");
+    c->gap_logged = c->iterations;
+  }
+  if (c->semantics == HMF_SEMANTICS_REF_CPU) {
+    rc = timed(c, 1, s, do_refcpu, 0);
+    if (rc) return rc;
+  } else if (c->timing || c->stall_kind >= 0) {
+    for (int it = 0; it < c->iterations; ++it) {
+      c->dag_last = c->dag && it == c->iterations - 1;
+      c->gap_t = it;  // the log's base stays 0 on this path
+      rc = timed(c, 0, s, do_flow, it & 1);
+      if (!rc) rc = timed(c, 1, s, do_tree, 0);
+      c->dag_last = false;
+      c->gap_t = 0;
+      if (rc) return rc;
+    }
+  } else {
+    if (!c->graph_pair) {
+      rc = capture(c, 2, &c->graph_pair);
+      if (!rc) rc = capture(c, 1, &c->graph_one);
+      // a pipelined solve replays several iterations per graph, so that the
+      // pipeline drains (at a graph's end) rarely
+      if (!rc && pipeline_active(c)) rc = capture(c, kPipelineIterations, &c->graph_many);
+      if (rc) return rc;
+    }
+    // a DAG's last iteration runs fewer tasks: launched on its own
+    const int graphed = c->dag ? std::max(0, c->iterations - 1) : c->iterations;
+    const long long per_iter = pipeline_active(c) ? 2LL * c->n_slabs : 2;
+    if (pipeline_active(c))
+      if (int rc2 = upload_slab_tables(c, s)) return rc2;
+    int it0 = 0;
+    if (c->graph_many)
+      for (; it0 + kPipelineIterations <= graphed; it0 += kPipelineIterations) {
+        CK(cudaGraphLaunch(c->graph_many, s), "cudaGraphLaunch");
+        c->launches += per_iter * kPipelineIterations;
+      }
+    for (int it = it0; it + 1 < graphed; it += 2) {
+      CK(cudaGraphLaunch(c->graph_pair, s), "cudaGraphLaunch");
+      c->launches += 2 * per_iter;
+    }
+    if ((graphed - it0) & 1) {
+      CK(cudaGraphLaunch(c->graph_one, s), "cudaGraphLaunch");
+      c->launches += per_iter;
+    }
+    if (c->dag && c->iterations > 0) {
+      rc = launch_flow(c, graphed & 1, s);
+      c->dag_last = true;
+      if (!rc) rc = launch_tree(c, s);
+      c->dag_last = false;
+      if (rc) return rc;
+    }
+  }
+  // final flows live in set (iterations & 1); nothing else depends on parity
+  return end_solve(c, user);
+}
+
+}  // namespace hmfi
 
 extern "C" {
 
@@ -1450,9 +1553,31 @@ int hmf_create(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_n
   return hmf_create_batch(out, 1, dims, parent, n_nodes, semantics, device);
 }
 
+int hmf_create_paged(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
+                     int device, double max_gpu_usage) {
+  const int dims[3] = {vx, vy, vz};
+  hmf_ctx* c = nullptr;
+  int rc = create_context(&c, 1, dims, semantics, device, [&](hmf_ctx* k) { return build_tree(k, parent, n_nodes); },
+                          false);
+  if (rc) {
+    if (out) *out = nullptr;
+    return rc;
+  }
+  rc = paged_setup(c, max_gpu_usage);
+  if (rc) {
+    g_create_error = c->err;
+    hmf_destroy(c);
+    *out = nullptr;
+    return rc;
+  }
+  *out = c;
+  return HMF_OK;
+}
+
 int hmf_destroy(hmf_ctx* c) {
   if (!c) return HMF_OK;
   DeviceGuard dg(c->device);
+  paged_free(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph_pair) cudaGraphExecDestroy(c->graph_pair);
   if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
@@ -1548,79 +1673,13 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
   DeviceGuard dg(c->device);
   cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
-  cudaStream_t s = c->stream;
-  Staged staged;
-  int rc = begin_solve(c, user, staged);
-  if (rc) return rc;
-  c->gap_logged = 0;
-  if (c->gap_on && c->semantics == HMF_SEMANTICS_REF_CUDA) {
-    if (c->gap_cap < c->iterations) {  // a longer log: new arena, graphs re-captured with it
-      drop_graphs(c);
-      if (c->d_gap) cudaFree(c->d_gap);
-      c->d_gap = nullptr;
-      c->gap_cap = 0;
-      const int cap = std::max(c->iterations, 64);
-      CK(cudaMalloc(&c->d_gap, gap_bytes(cap)), "cudaMalloc(convergence log)");
-      c->gap_cap = cap;
-    }
-    CK(cudaMemsetAsync(c->d_gap, 0, gap_bytes(c->gap_cap), s), "cudaMemsetAsync(convergence log)");
-    c->gap_logged = c->iterations;
-  }
-  if (c->semantics == HMF_SEMANTICS_REF_CPU) {
-    rc = timed(c, 1, s, do_refcpu, 0);
-    if (rc) return rc;
-  } else if (c->timing || c->stall_kind >= 0) {
-    for (int it = 0; it < c->iterations; ++it) {
-      c->dag_last = c->dag && it == c->iterations - 1;
-      c->gap_t = it;  // the log's base stays 0 on this path
-      rc = timed(c, 0, s, do_flow, it & 1);
-      if (!rc) rc = timed(c, 1, s, do_tree, 0);
-      c->dag_last = false;
-      c->gap_t = 0;
-      if (rc) return rc;
-    }
-  } else {
-    if (!c->graph_pair) {
-      rc = capture(c, 2, &c->graph_pair);
-      if (!rc) rc = capture(c, 1, &c->graph_one);
-      // a pipelined solve replays several iterations per graph, so that the
-      // pipeline drains (at a graph's end) rarely
-      if (!rc && pipeline_active(c)) rc = capture(c, kPipelineIterations, &c->graph_many);
-      if (rc) return rc;
-    }
-    // a DAG's last iteration runs fewer tasks: launched on its own
-    const int graphed = c->dag ? std::max(0, c->iterations - 1) : c->iterations;
-    const long long per_iter = pipeline_active(c) ? 2LL * c->n_slabs : 2;
-    if (pipeline_active(c))
-      if (int rc2 = upload_slab_tables(c, s)) return rc2;
-    int it0 = 0;
-    if (c->graph_many)
-      for (; it0 + kPipelineIterations <= graphed; it0 += kPipelineIterations) {
-        CK(cudaGraphLaunch(c->graph_many, s), "cudaGraphLaunch");
-        c->launches += per_iter * kPipelineIterations;
-      }
-    for (int it = it0; it + 1 < graphed; it += 2) {
-      CK(cudaGraphLaunch(c->graph_pair, s), "cudaGraphLaunch");
-      c->launches += 2 * per_iter;
-    }
-    if ((graphed - it0) & 1) {
-      CK(cudaGraphLaunch(c->graph_one, s), "cudaGraphLaunch");
-      c->launches += per_iter;
-    }
-    if (c->dag && c->iterations > 0) {
-      rc = launch_flow(c, graphed & 1, s);
-      c->dag_last = true;
-      if (!rc) rc = launch_tree(c, s);
-      c->dag_last = false;
-      if (rc) return rc;
-    }
-  }
-  // final flows live in set (iterations & 1); nothing else depends on parity
-  return end_solve(c, user);
+  if (c->pg) return paged_solve(c, user);
+  return solve_with(c, user, nullptr, nullptr);
 }
 
 int hmf_autotune(hmf_ctx* c, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_autotune")) return rc;
   if (!c->use_tma || c->semantics != HMF_SEMANTICS_REF_CUDA) return HMF_OK;
   const int saved_iters = c->iterations;
   const bool saved_timing = c->timing;
@@ -1677,6 +1736,7 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
 
 int hmf_set_pipeline(hmf_ctx* c, int enabled) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_set_pipeline")) return rc;
   if ((enabled != 0) == c->pipeline) return HMF_OK;
   DeviceGuard dg(c->device);
   drop_graphs(c);
@@ -1688,6 +1748,7 @@ int hmf_get_pipeline(const hmf_ctx* c) { return c ? (pipeline_active(c) ? 1 : 0)
 
 int hmf_set_flow_window(hmf_ctx* c, int rows) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_set_flow_window")) return rc;
   if (rows != 0 && rows != 32 && rows != 64)
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "flow window rows must be 32 or 64 (0: default)");
   DeviceGuard dg(c->device);
@@ -1700,6 +1761,7 @@ int hmf_get_flow_window(const hmf_ctx* c) { return c ? 4 * c->flow_warps : HMF_E
 
 int hmf_set_zchunk(hmf_ctx* c, int z) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_set_zchunk")) return rc;
   if (z < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the z chunk must be >= 0 (0: default plan)");
   DeviceGuard dg(c->device);
   drop_graphs(c);
@@ -1712,6 +1774,7 @@ int hmf_get_zchunk(const hmf_ctx* c) { return c ? c->zchunk : HMF_ERR_INVALID_AR
 
 int hmf_set_convergence_log(hmf_ctx* c, int enabled) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_set_convergence_log")) return rc;
   if (enabled) {
     if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the convergence log is for label trees (hmf_create)");
     if (c->semantics != HMF_SEMANTICS_REF_CUDA)
@@ -1733,6 +1796,7 @@ int hmf_set_convergence_log(hmf_ctx* c, int enabled) {
 
 int hmf_get_convergence(hmf_ctx* c, double* max_change, double* mean_change, int capacity) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_get_convergence")) return rc;
   if (capacity < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "capacity must be >= 0");
   const int n = std::min(capacity, c->gap_logged);
   if (n == 0) return c->gap_logged;
@@ -1759,6 +1823,7 @@ int hmf_get_convergence(hmf_ctx* c, double* max_change, double* mean_change, int
 
 int hmf_set_wait_limit(hmf_ctx* c, long long limit_ns) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_set_wait_limit")) return rc;
   if (limit_ns < 0) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the wait limit must be >= 0 (0: default)");
   const unsigned long long v = limit_ns ? (unsigned long long)limit_ns : hmf::kTmaWaitLimitNs;
   if (v == c->wait_limit_ns) return HMF_OK;
@@ -1770,6 +1835,7 @@ int hmf_set_wait_limit(hmf_ctx* c, long long limit_ns) {
 
 int hmf_inject_wait_stall(hmf_ctx* c, int kernel) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_inject_wait_stall")) return rc;
   if (kernel < -1 || kernel > HMF_STALL_REVERSE_SWEEP) return fail(c, HMF_ERR_INVALID_ARGUMENT, "unknown kernel");
   c->stall_kind = kernel;
   return HMF_OK;
@@ -1781,6 +1847,7 @@ int hmf_batch_get_labels(hmf_ctx* c, int volume, int node, float* out, int where
   if (!valid_vertex(c, node) || node == c->root)
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "labels exist for non-root vertices only");
   if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
+  if (c->pg) return paged_copy_out(c, true, node, out, where, stream);
   return copy_out(c, volume, c->label[node], out, where, stream);
 }
 
@@ -1793,6 +1860,7 @@ int hmf_batch_get_sink(hmf_ctx* c, int volume, int node, float* out, int where, 
   if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
   if (!valid_vertex(c, node)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "vertex id out of range");
   if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");
+  if (c->pg) return paged_copy_out(c, false, node, out, where, stream);
   return copy_out(c, volume, c->sink[node], out, where, stream);
 }
 
@@ -1811,6 +1879,7 @@ int hmf_leaf_order(const hmf_ctx* c, int* out, int cap) {
 
 size_t hmf_device_bytes(const hmf_ctx* c) {
   if (!c) return 0;
+  if (c->pg) return paged_bytes(c);
   return c->arena_bytes + c->staging_bytes + adjoint_bytes(c) + fp64_bytes(c) + sizeof(hmf::FlowVertex) * hmf::kMaxVertices * 2 +
          sizeof(hmf::FlowVertexTMA) * c->vols.size() * (c->n - 1) + sizeof(hmf::TreeTable) +
          sizeof(hmf::FlowItem) * c->h_items.size();

@@ -137,6 +137,10 @@ struct hmf_ctx {
   struct AdjointState* adj = nullptr;
   // FP64 evaluation of the same iteration (hmf_fp64.cu), created on demand
   struct Fp64State* f64 = nullptr;
+  // out-of-core solve (hmf_create_paged, hmf_paged.cu): the state lives in
+  // pinned host memory and blocks of planes are iterated on the device; such
+  // a context holds no device state of its own (arena == nullptr)
+  struct PagedState* pg = nullptr;
 
   long long adj_max_bytes = 0;  // hmf_set_adjoint_memory (0: 85% of the free device memory)
   int adj_max_slots = 0;        // (0: no cap)
@@ -214,6 +218,26 @@ int maybe_request_stall(hmf_ctx* c, int kind, cudaStream_t s);
 // 2 misaligned staging, 3 label index out of range), as a status.
 int check_error_flag(hmf_ctx* c);
 int decode_error_flag(hmf_ctx* c, int flag);
+
+// hmf_solve's body: stage the inputs, write the tables, then either
+// initialise (load == nullptr) or call load(c, c->stream, arg), which must
+// fill every array the iterations read (sinks, labels, divergences and the
+// parity-0 flows), and run c->iterations iterations.
+using StateLoader = int (*)(hmf_ctx* c, cudaStream_t s, void* arg);
+int solve_with(hmf_ctx* c, cudaStream_t user, StateLoader load, void* arg);
+// Calls that need the device state of an in-core context refuse
+// out-of-core contexts.
+inline int refuse_paged(hmf_ctx* c, const char* what) {
+  if (!c || !c->pg) return HMF_OK;
+  return fail(c, HMF_ERR_STATE, std::string(what) + " is not available on an out-of-core context (hmf_create_paged)");
+}
+
+// hmf_paged.cu
+int paged_setup(hmf_ctx* c, double max_gpu_usage);
+int paged_solve(hmf_ctx* c, cudaStream_t user);
+int paged_copy_out(hmf_ctx* c, bool labels, int node, float* out, int where, void* stream);
+void paged_free(hmf_ctx* c);
+size_t paged_bytes(const hmf_ctx* c);
 
 // hmf_adjoint.cu
 void adjoint_free(hmf_ctx* c);

@@ -174,6 +174,14 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     }
   };
 
+  // every thread that issues copies acquires the maps it uses
+  if (threadIdx.x == 0) {
+    for (int a = 0; a < narr; ++a) tensormap_acquire(main_map(a));
+    tensormap_acquire(&V->flow_in[par][2]);
+  } else if (lane == 0) {
+    if (warp < narr) tensormap_acquire(warp_map);
+    if (warp == W - 1) tensormap_acquire(&V->flow_in[par][2]);
+  }
   if (threadIdx.x == 0) {
     for (int p = kstart; p <= min(kstart + kTmaMainLead - 1, kmain_end); ++p)
       for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));

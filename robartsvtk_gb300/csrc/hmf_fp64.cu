@@ -378,6 +378,7 @@ constexpr int kF64Threads = 256;
 
 int fp64_usable(hmf_ctx* c) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "the FP64 solve")) return rc;
   if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the FP64 solve is for label trees (hmf_create)");
   if (c->vols.size() != 1) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the FP64 solve is for single-volume contexts");
   if (c->semantics != HMF_SEMANTICS_REF_CUDA)

@@ -1,0 +1,542 @@
+// hmf_paged.cu -- out-of-core solve (hmf_create_paged): the solver state of
+// the whole volume lives in pinned host memory and the device iterates it
+// block by block.
+//
+// The reference pages whole-volume buffers between host and device when they
+// do not all fit in MaxGPUUsage of the GPU's memory: it acquires what fits
+// (CUDA_GetGPUBuffers, CUDA_hierarchicalmaxflow.cu:33-60), simulates one
+// iteration to learn each buffer's next use
+// (vtkCudaHierarchicalMaxFlowSegmentation.cxx:884-1038) and, before every
+// pass, moves the buffers the pass needs onto the GPU, evicting the one used
+// furthest in the future (GetGPUBuffersV2, :1088-1294).  Every iteration then
+// crosses the host link once per paged buffer.
+//
+// Here the unit of residency is a block of z-planes of every array, and the
+// link is crossed once per k iterations (temporal blocking): one iteration's
+// new state at plane z reads the old state at planes z-2 .. z+2 only, so a
+// block of T planes iterated k times on its own (its faces taking the
+// volume-face rules) is exact on every plane at least 2k planes from a face
+// that lies inside the volume -- 2k + 1 on the high-z side, whose first step
+// forms the old divergence of the top plane without the z-flow of the plane
+// beyond it.  The volume is covered by overlapping blocks,
+// each owning the planes it computes exactly; a round loads every block's
+// planes from the host state, runs k iterations with the in-core kernels
+// (same arithmetic: results identical to the in-core solve) and stores the
+// owned planes back.  Two block contexts alternate on two streams, so one
+// block's copies run while the other computes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "hmf_ctx.hpp"
+
+struct PagedState {
+  double usage = 0.75;      // fraction of the device's memory (MaxGPUUsage)
+  int forced_planes = 0;    // hmf_set_paged_plan (0: from the budget)
+  int forced_iterations = 0;
+
+  // plan of the last solve
+  int block_planes = 0, round_iterations = 0, halo = 0;
+  std::vector<int> starts, owned;  // per block: first plane, first owned plane
+  int rounds = 0;
+  long long link_bytes = 0;  // bytes between host and device in the last solve
+
+  hmf_ctx* blk[2] = {nullptr, nullptr};
+  int blk_planes = 0;  // planes the block contexts were created for
+  cudaStream_t st[2] = {nullptr, nullptr};
+  cudaEvent_t ev_loaded[2] = {nullptr, nullptr};
+  cudaEvent_t ev_end[2] = {nullptr, nullptr};
+
+  // host state: per vertex sink; per non-root vertex label and three flows;
+  // dense VX*VY*VZ floats each (pinned).  The divergence is not kept: the
+  // flow step forms the old divergence from the flows and writes the new one
+  // before the sweep reads it.
+  char* host = nullptr;
+  size_t host_bytes = 0;
+  std::vector<float*> sink, label, fx, fy, fz;
+  // pinned copies of pageable host inputs
+  char* inputs = nullptr;
+  size_t input_bytes = 0;
+  // error flag of every block solve of the last solve (pinned)
+  int* flags = nullptr;
+  int flag_cap = 0, n_flags = 0;
+};
+
+namespace hmfi {
+
+namespace {
+
+// Iterations per round: a round moves each plane of ~6 arrays per vertex
+// across the host link and back, and an iteration moves ~12 per vertex
+// through HBM; at the link's ~0.05 of HBM bandwidth about 8 iterations
+// per round balance the two.
+constexpr int kMaxRoundIterations = 8;
+constexpr size_t kBlockFixedBytes = 16u << 20;  // tables, graphs and alignment of one block context
+
+struct BlockLoad {
+  PagedState* P;
+  int slot, first;  // block context slot, first plane of the block
+  long long plane;  // elements per dense plane
+  long long* bytes;
+};
+
+// Copies `planes` planes between a pitched array of a block context and a
+// dense host array.
+int copy_planes(hmf_ctx* c, float* dst, size_t dpitch, const float* src, size_t spitch, int vx, int vy,
+                int planes, cudaMemcpyKind kind, cudaStream_t s) {
+  const size_t row = (size_t)vx * sizeof(float);
+  if (dpitch == row && spitch == row) {
+    CK(cudaMemcpyAsync(dst, src, row * vy * planes, kind, s), "cudaMemcpyAsync(paged state)");
+  } else {
+    CK(cudaMemcpy2DAsync(dst, dpitch, src, spitch, row, (size_t)vy * planes, kind, s),
+       "cudaMemcpy2DAsync(paged state)");
+  }
+  return HMF_OK;
+}
+
+// StateLoader of a continued block solve: the block's planes of the host
+// state into its sinks, labels and parity-0 flows.
+int load_block(hmf_ctx* b, cudaStream_t s, void* arg) {
+  hmf_ctx* c = b;
+  const BlockLoad& L = *static_cast<const BlockLoad*>(arg);
+  PagedState& P = *L.P;
+  const auto& V = b->vols[0];
+  const size_t dp = (size_t)V.pitch * sizeof(float), sp = (size_t)V.vx * sizeof(float);
+  const long long off = (long long)L.first * L.plane;
+  long long n = 0;
+  for (int v = 0; v < b->n; ++v) {
+    if (int rc = copy_planes(c, b->sink[v], dp, P.sink[v] + off, sp, V.vx, V.vy, V.vz, cudaMemcpyHostToDevice, s))
+      return rc;
+    ++n;
+    if (v == b->root) continue;
+    const float* src[4] = {P.label[v], P.fx[v], P.fy[v], P.fz[v]};
+    float* dst[4] = {b->label[v], b->fx[0][v], b->fy[0][v], b->fz[0][v]};
+    for (int a = 0; a < 4; ++a)
+      if (int rc = copy_planes(c, dst[a], dp, src[a] + off, sp, V.vx, V.vy, V.vz, cudaMemcpyHostToDevice, s))
+        return rc;
+    n += 4;
+  }
+  *L.bytes += n * (long long)V.vz * L.plane * (long long)sizeof(float);
+  CK(cudaEventRecord(P.ev_loaded[L.slot], s), "cudaEventRecord(block loaded)");
+  return HMF_OK;
+}
+
+// The owned planes [z0, z1) of a solved block back into the host state: all
+// of it between rounds, the sinks and labels after the last round.
+int store_block(hmf_ctx* c, PagedState& P, hmf_ctx* b, int first, int z0, int z1, int parity, bool final_round,
+                long long plane, cudaStream_t s) {
+  const auto& V = b->vols[0];
+  const size_t dp = (size_t)V.vx * sizeof(float), sp = (size_t)V.pitch * sizeof(float);
+  const int planes = z1 - z0;
+  if (planes <= 0) return HMF_OK;
+  const long long hoff = (long long)z0 * plane, boff = (long long)(z0 - first) * V.plane;
+  long long n = 0;
+  for (int v = 0; v < b->n; ++v) {
+    if (int rc = copy_planes(c, P.sink[v] + hoff, dp, b->sink[v] + boff, sp, V.vx, V.vy, planes,
+                             cudaMemcpyDeviceToHost, s))
+      return rc;
+    ++n;
+    if (v == b->root) continue;
+    if (int rc = copy_planes(c, P.label[v] + hoff, dp, b->label[v] + boff, sp, V.vx, V.vy, planes,
+                             cudaMemcpyDeviceToHost, s))
+      return rc;
+    ++n;
+    if (final_round) continue;
+    const float* src[3] = {b->fx[parity][v], b->fy[parity][v], b->fz[parity][v]};
+    float* dst[3] = {P.fx[v], P.fy[v], P.fz[v]};
+    for (int a = 0; a < 3; ++a)
+      if (int rc = copy_planes(c, dst[a] + hoff, dp, src[a] + boff, sp, V.vx, V.vy, planes, cudaMemcpyDeviceToHost, s))
+        return rc;
+    n += 3;
+  }
+  P.link_bytes += n * (long long)planes * plane * (long long)sizeof(float);
+  return HMF_OK;
+}
+
+void free_blocks(PagedState& P) {
+  for (auto& b : P.blk)
+    if (b) {
+      hmf_destroy(b);
+      b = nullptr;
+    }
+  P.blk_planes = 0;
+}
+
+// Device bytes one block context of `planes` planes holds: 9 arrays per
+// non-root vertex and the root's (hmf_create's state), plus the staged
+// inputs.
+size_t block_bytes(const hmf_ctx* c, int planes, int staged_inputs) {
+  const auto& V = c->vols[0];
+  const size_t arr = round_up((size_t)V.pitch * V.vy * planes * sizeof(float), 256);
+  return arr * (size_t)(9 * (c->n - 1) + 1 + staged_inputs) + kBlockFixedBytes;
+}
+
+}  // namespace
+
+int paged_setup(hmf_ctx* c, double max_gpu_usage) {
+  if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "out-of-core solves are for label trees");
+  if (!(max_gpu_usage >= 0.0)) max_gpu_usage = 0.0;
+  auto* P = new PagedState();
+  c->pg = P;
+  P->usage = std::min(1.0, max_gpu_usage);
+  for (int i = 0; i < 2; ++i) {
+    CK(cudaStreamCreateWithFlags(&P->st[i], cudaStreamNonBlocking), "cudaStreamCreate(paged)");
+    CK(cudaEventCreateWithFlags(&P->ev_loaded[i], cudaEventDisableTiming), "cudaEventCreate(paged)");
+    CK(cudaEventCreateWithFlags(&P->ev_end[i], cudaEventDisableTiming), "cudaEventCreate(paged)");
+  }
+  return HMF_OK;
+}
+
+void paged_free(hmf_ctx* c) {
+  PagedState* P = c->pg;
+  if (!P) return;
+  for (auto s : P->st)
+    if (s) cudaStreamSynchronize(s);
+  free_blocks(*P);
+  for (int i = 0; i < 2; ++i) {
+    if (P->st[i]) cudaStreamDestroy(P->st[i]);
+    if (P->ev_loaded[i]) cudaEventDestroy(P->ev_loaded[i]);
+    if (P->ev_end[i]) cudaEventDestroy(P->ev_end[i]);
+  }
+  if (P->host) cudaFreeHost(P->host);
+  if (P->inputs) cudaFreeHost(P->inputs);
+  if (P->flags) cudaFreeHost(P->flags);
+  delete P;
+  c->pg = nullptr;
+}
+
+size_t paged_bytes(const hmf_ctx* c) {
+  size_t n = 0;
+  for (auto b : c->pg->blk)
+    if (b) n += hmf_device_bytes(b);
+  return n;
+}
+
+int paged_solve(hmf_ctx* c, cudaStream_t user) {
+  PagedState& P = *c->pg;
+  const auto& V = c->vols[0];
+  for (int l : c->leaves)
+    if (!c->data[0][l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
+  c->solved = false;
+  const long long plane = (long long)V.vx * V.vy;
+  const size_t arr = (size_t)plane * V.vz * sizeof(float);
+
+  // ---- inputs: device inputs are read in place, host inputs from pinned memory
+  std::vector<const float*> in_data(c->n, nullptr), in_smooth(c->n, nullptr);
+  std::vector<int> w_data(c->n, HMF_HOST), w_smooth(c->n, HMF_HOST);
+  std::vector<const float*> pinned_src;
+  std::vector<float*> pinned_dst;
+  auto resolve = [&](const hmf_ctx::Input& in, const float** ptr, int* where) -> int {
+    *ptr = in.ptr;
+    *where = in.where;
+    if (!in.ptr || in.where == HMF_DEVICE) return HMF_OK;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, in.ptr) == cudaSuccess && a.type == cudaMemoryTypeHost) return HMF_OK;
+    cudaGetLastError();
+    for (size_t i = 0; i < pinned_src.size(); ++i)
+      if (pinned_src[i] == in.ptr) {
+        *ptr = pinned_dst[i];
+        return HMF_OK;
+      }
+    pinned_src.push_back(in.ptr);
+    pinned_dst.push_back(nullptr);
+    *ptr = nullptr;  // filled below
+    return HMF_OK;
+  };
+  for (int l : c->leaves) resolve(c->data[0][l], &in_data[l], &w_data[l]);
+  for (int v = 0; v < c->n; ++v)
+    if (v != c->root) resolve(c->smooth[0][v], &in_smooth[v], &w_smooth[v]);
+  if (!pinned_src.empty()) {
+    const size_t need = arr * pinned_src.size();
+    if (need > P.input_bytes) {
+      if (P.inputs) cudaFreeHost(P.inputs);
+      P.inputs = nullptr;
+      P.input_bytes = 0;
+      CK(cudaMallocHost(&P.inputs, need), "cudaMallocHost(paged inputs)");
+      P.input_bytes = need;
+    }
+    for (size_t i = 0; i < pinned_src.size(); ++i) {
+      pinned_dst[i] = reinterpret_cast<float*>(P.inputs + i * arr);
+      std::memcpy(pinned_dst[i], pinned_src[i], arr);
+    }
+    auto fix = [&](const hmf_ctx::Input& in, const float** ptr) {
+      if (*ptr || !in.ptr) return;
+      for (size_t i = 0; i < pinned_src.size(); ++i)
+        if (pinned_src[i] == in.ptr) *ptr = pinned_dst[i];
+    };
+    for (int l : c->leaves) fix(c->data[0][l], &in_data[l]);
+    for (int v = 0; v < c->n; ++v)
+      if (v != c->root) fix(c->smooth[0][v], &in_smooth[v]);
+  }
+  // inputs each block stages (all of them, at most) and those that cross the host link
+  int staged_inputs = (int)c->leaves.size(), host_inputs = 0;
+  for (int l : c->leaves) host_inputs += w_data[l] == HMF_HOST;
+  {
+    std::vector<const float*> distinct;
+    for (int v = 0; v < c->n; ++v)
+      if (in_smooth[v] && std::find(distinct.begin(), distinct.end(), in_smooth[v]) == distinct.end()) {
+        distinct.push_back(in_smooth[v]);
+        host_inputs += w_smooth[v] == HMF_HOST;
+      }
+    staged_inputs += (int)distinct.size();
+  }
+
+  // ---- plan: block thickness T from the budget, k iterations per round
+  const bool cpu = c->semantics == HMF_SEMANTICS_REF_CPU;
+  int T = P.forced_planes;
+  if (T <= 0) {
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    const size_t budget = (size_t)(P.usage * (double)total_b);
+    const size_t per_plane = block_bytes(c, 1, staged_inputs) - kBlockFixedBytes;
+    if (budget <= 2 * kBlockFixedBytes + 2 * per_plane)
+      return fail(c, HMF_ERR_OUT_OF_MEMORY, "MaxGPUUsage leaves no room for two blocks of planes");
+    T = (int)std::min<size_t>((size_t)V.vz, (budget - 2 * kBlockFixedBytes) / (2 * per_plane));
+  }
+  T = std::min(T, V.vz);
+  int k;
+  if (cpu) {
+    k = c->iterations;  // per-voxel iterations (REF_CPU): no halo, one round
+  } else if (T >= V.vz) {
+    // one block, no halo: one round unless the plan asks for several
+    k = P.forced_iterations > 0 ? std::min(P.forced_iterations, c->iterations) : c->iterations;
+  } else {
+    k = P.forced_iterations > 0 ? P.forced_iterations : std::min(kMaxRoundIterations, (T - 4) / 8);
+    k = std::min(k, c->iterations);
+    if (k < 1 && c->iterations > 0)
+      return fail(c, HMF_ERR_OUT_OF_MEMORY, "MaxGPUUsage holds fewer than 12 planes per block");
+  }
+  // the flow step recomputes the old divergence from the stored flows, which
+  // at a block's top plane lacks the z-flow above it: one more halo plane
+  const int halo = (T >= V.vz || cpu || k == 0) ? 0 : 2 * k + 1;
+  const int nb = hmf_paged_layout(V.vz, T, halo, nullptr, nullptr, 0);
+  if (nb < 0)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT,
+                "block planes must be at least four times the halo (2 x iterations per round + 1)");
+  P.starts.assign(nb, 0);
+  P.owned.assign(nb, 0);
+  hmf_paged_layout(V.vz, T, halo, P.starts.data(), P.owned.data(), nb);
+  std::vector<int> round_iters;
+  if (c->iterations == 0 || k == 0) round_iters.push_back(0);
+  for (int left = c->iterations; k > 0 && left > 0; left -= k) round_iters.push_back(std::min(k, left));
+  P.block_planes = T;
+  P.round_iterations = k;
+  P.halo = halo;
+  P.rounds = (int)round_iters.size();
+  P.link_bytes = 0;
+
+  // ---- memory: two block contexts, the host state, the error flags
+  if (P.blk_planes != T) {
+    free_blocks(P);
+    for (int i = 0; i < 2 && i < nb; ++i) {
+      int rc = hmf_create(&P.blk[i], V.vx, V.vy, T, c->parent.data(), c->n, c->semantics, c->device);
+      if (rc) {
+        free_blocks(P);
+        return fail(c, rc, std::string("block context: ") + hmf_last_error(nullptr));
+      }
+    }
+    P.blk_planes = T;
+  }
+  const bool need_state = P.rounds > 1;
+  const size_t n_arrays = need_state ? (size_t)5 * (c->n - 1) + 1 : (size_t)2 * (c->n - 1) + 1;
+  if (P.host_bytes < n_arrays * arr) {
+    if (P.host) cudaFreeHost(P.host);
+    P.host = nullptr;
+    P.host_bytes = 0;
+    CK(cudaMallocHost(&P.host, n_arrays * arr), "cudaMallocHost(paged state)");
+    P.host_bytes = n_arrays * arr;
+  }
+  {
+    char* p = P.host;
+    auto take = [&]() {
+      float* r = reinterpret_cast<float*>(p);
+      p += arr;
+      return r;
+    };
+    P.sink.assign(c->n, nullptr);
+    P.label.assign(c->n, nullptr);
+    P.fx.assign(c->n, nullptr);
+    P.fy.assign(c->n, nullptr);
+    P.fz.assign(c->n, nullptr);
+    for (int v = 0; v < c->n; ++v) {
+      P.sink[v] = take();
+      if (v == c->root) continue;
+      P.label[v] = take();
+      if (!need_state) continue;
+      P.fx[v] = take();
+      P.fy[v] = take();
+      P.fz[v] = take();
+    }
+  }
+  const int n_flags = P.rounds * nb;
+  if (P.flag_cap < n_flags) {
+    if (P.flags) cudaFreeHost(P.flags);
+    P.flags = nullptr;
+    P.flag_cap = 0;
+    CK(cudaMallocHost(&P.flags, sizeof(int) * n_flags), "cudaMallocHost(paged flags)");
+    P.flag_cap = n_flags;
+  }
+  for (int i = 0; i < n_flags; ++i) P.flags[i] = 0;
+  P.n_flags = n_flags;
+
+  // ---- block contexts: parameters and inputs
+  for (int i = 0; i < 2 && i < nb; ++i) {
+    hmf_ctx* b = P.blk[i];
+    for (int v = 0; v < c->n; ++v)
+      if (v != c->root) hmf_set_smoothness_scalar(b, v, c->alpha[v]);
+    b->timing = c->timing;
+  }
+
+  // ---- rounds
+  CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
+  for (int i = 0; i < 2; ++i) CK(cudaStreamWaitEvent(P.st[i], c->ev_join, 0), "cudaStreamWaitEvent(join)");
+  long long launches = 0;
+  double kind_ms[3] = {0, 0, 0};
+  long long kind_count[3] = {0, 0, 0};
+  int flag_i = 0;
+  for (int r = 0; r < P.rounds; ++r) {
+    const int kr = round_iters[r];
+    const bool last = r + 1 == P.rounds;
+    auto store = [&](int j) -> int {
+      const int slot = j & 1;
+      const int z1 = j + 1 < nb ? P.owned[j + 1] : V.vz;
+      return store_block(c, P, P.blk[slot], P.starts[j], P.owned[j], z1, kr & 1, last, plane, P.st[slot]);
+    };
+    for (int j = 0; j < nb; ++j) {
+      const int slot = j & 1;
+      hmf_ctx* b = P.blk[slot];
+      const long long off = (long long)P.starts[j] * plane;
+      for (int l : c->leaves) {
+        int rc = hmf_set_data(b, l, in_data[l] + off, w_data[l]);
+        if (rc) return fail(c, rc, std::string("block input: ") + b->err);
+      }
+      for (int v = 0; v < c->n; ++v) {
+        if (v == c->root) continue;
+        int rc = hmf_set_smoothness(b, v, in_smooth[v] ? in_smooth[v] + off : nullptr, w_smooth[v]);
+        if (rc) return fail(c, rc, std::string("block input: ") + b->err);
+      }
+      hmf_set_params(b, kr, c->step, c->cc);
+      int rc;
+      if (r == 0) {
+        rc = solve_with(b, P.st[slot], nullptr, nullptr);
+      } else {
+        BlockLoad L{&P, slot, P.starts[j], plane, &P.link_bytes};
+        rc = solve_with(b, P.st[slot], load_block, &L);
+      }
+      if (rc) return fail(c, rc, std::string("block solve: ") + b->err);
+      CK(cudaMemcpyAsync(&P.flags[flag_i++], b->d_error, sizeof(int), cudaMemcpyDeviceToHost, P.st[slot]),
+         "cudaMemcpyAsync(block error flag)");
+      for (int q = 0; q < 3; ++q) {
+        kind_ms[q] += b->kind_ms[q] * b->kind_count[q];
+        kind_count[q] += b->kind_count[q];
+      }
+      launches += b->launches;
+      // the previous block's owned planes go back once this block has read
+      // its halo planes from them
+      if (j > 0) {
+        if (r > 0) CK(cudaStreamWaitEvent(P.st[(j - 1) & 1], P.ev_loaded[slot], 0), "cudaStreamWaitEvent(loaded)");
+        if (int rc2 = store(j - 1)) return rc2;
+      }
+    }
+    if (int rc = store(nb - 1)) return rc;
+    // the next round reads what every block of this one stored
+    for (int i = 0; i < 2; ++i) CK(cudaEventRecord(P.ev_end[i], P.st[i]), "cudaEventRecord(round)");
+    CK(cudaStreamWaitEvent(P.st[0], P.ev_end[1], 0), "cudaStreamWaitEvent(round)");
+    CK(cudaStreamWaitEvent(P.st[1], P.ev_end[0], 0), "cudaStreamWaitEvent(round)");
+  }
+  for (int i = 0; i < 2; ++i) {
+    CK(cudaEventRecord(P.ev_end[i], P.st[i]), "cudaEventRecord(done)");
+    CK(cudaStreamWaitEvent(user, P.ev_end[i], 0), "cudaStreamWaitEvent(done)");
+  }
+  // host inputs cross the link once per block per round
+  P.link_bytes += (long long)host_inputs * nb * (long long)T * plane * (long long)sizeof(float) * P.rounds;
+  c->launches = launches;
+  for (int q = 0; q < 3; ++q) {
+    c->kind_count[q] = kind_count[q];
+    c->kind_ms[q] = kind_count[q] ? kind_ms[q] / kind_count[q] : 0.0;
+  }
+  c->solved = true;
+  return HMF_OK;
+}
+
+int paged_copy_out(hmf_ctx* c, bool labels, int node, float* out, int where, void* stream) {
+  PagedState& P = *c->pg;
+  if (!out) return fail(c, HMF_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+  if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
+  if (where == HMF_DEVICE)
+    if (int rc = check_device_pointer(c, out, "output")) return rc;
+  const auto& V = c->vols[0];
+  const size_t bytes = (size_t)V.vx * V.vy * V.vz * sizeof(float);
+  const float* src = labels ? P.label[node] : P.sink[node];
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (where == HMF_DEVICE) {
+    CK(cudaMemcpyAsync(out, src, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(paged output)");
+    return HMF_OK;
+  }
+  CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(paged output)");
+  int flag = 0;
+  for (int i = 0; i < P.n_flags; ++i) flag |= P.flags[i];
+  if (int rc = decode_error_flag(c, flag)) return rc;
+  std::memcpy(out, src, bytes);
+  return HMF_OK;
+}
+
+}  // namespace hmfi
+
+using namespace hmfi;
+
+extern "C" {
+
+int hmf_set_paged_plan(hmf_ctx* c, int block_planes, int round_iterations) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (!c->pg) return fail(c, HMF_ERR_STATE, "hmf_set_paged_plan needs an out-of-core context (hmf_create_paged)");
+  if (block_planes < 0 || round_iterations < 0)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "block planes and iterations per round must be >= 0");
+  c->pg->forced_planes = block_planes;
+  c->pg->forced_iterations = round_iterations;
+  return HMF_OK;
+}
+
+int hmf_get_paged_plan(const hmf_ctx* c, int* blocks, int* block_planes, int* round_iterations, int* rounds,
+                       long long* link_bytes) {
+  if (!c || !c->pg) return HMF_ERR_INVALID_ARGUMENT;
+  const PagedState& P = *c->pg;
+  if (blocks) *blocks = (int)P.starts.size();
+  if (block_planes) *block_planes = P.block_planes;
+  if (round_iterations) *round_iterations = P.round_iterations;
+  if (rounds) *rounds = P.rounds;
+  if (link_bytes) *link_bytes = P.link_bytes;
+  return HMF_OK;
+}
+
+int hmf_paged_layout(int vz, int block_planes, int halo_planes, int* starts, int* owned, int capacity) {
+  if (vz < 1 || block_planes < 1 || halo_planes < 0) return HMF_ERR_INVALID_ARGUMENT;
+  const int T = std::min(block_planes, vz), H = halo_planes;
+  int nb = 1;
+  if (T < vz) {
+    // every block but the first and last owns T - 2H planes at most, and
+    // with T >= 4H a block's owned planes are read only by its neighbours
+    if (T < 4 * H || T - 2 * H < 1) return HMF_ERR_INVALID_ARGUMENT;
+    nb = 1 + (int)(((long long)vz - T + (T - 2 * H) - 1) / (T - 2 * H));
+  }
+  std::vector<int> b(nb), a(nb);
+  for (int j = 0; j < nb; ++j) {
+    b[j] = nb == 1 ? 0 : (int)((long long)j * (vz - T) / (nb - 1));
+    a[j] = j == 0 ? 0 : b[j] + H;
+  }
+  for (int j = 1; j < nb; ++j) {
+    // block j-1 is exact up to b[j-1] + T - H; block j+1 starts at or after
+    // what block j owns
+    if (a[j] > b[j - 1] + T - H || a[j] <= a[j - 1]) return HMF_ERR_INVALID_ARGUMENT;
+    if (j + 1 < nb && b[j + 1] < a[j]) return HMF_ERR_INVALID_ARGUMENT;
+  }
+  for (int j = 0; j < nb && j < capacity; ++j) {
+    if (starts) starts[j] = b[j];
+    if (owned) owned[j] = a[j];
+  }
+  return nb;
+}
+
+}  // extern "C"

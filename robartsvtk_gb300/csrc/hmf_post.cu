@@ -268,6 +268,7 @@ int hmf_decomposition_energy(int vx, int vy, int vz, const int* parent, int n_no
 
 int hmf_batch_get_vote(hmf_ctx* c, int volume, int* out, int where, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_get_vote")) return rc;
   if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
   if (!out) return fail(c, HMF_ERR_INVALID_ARGUMENT, "output pointer is NULL");
   if (where != HMF_HOST && where != HMF_DEVICE) return fail(c, HMF_ERR_INVALID_ARGUMENT, "bad `where`");
@@ -312,6 +313,7 @@ int hmf_get_vote(hmf_ctx* c, int* out, int where, void* stream) { return hmf_bat
 
 int hmf_batch_get_energy(hmf_ctx* c, int volume, double* f0, double* f, int n) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_get_energy")) return rc;
   if (!valid_volume(c, volume)) return fail(c, HMF_ERR_INVALID_ARGUMENT, "volume index out of range");
   if (c->dag) return fail(c, HMF_ERR_INVALID_ARGUMENT, "the energy decomposition is defined for trees, not graphs");
   if (!c->solved) return fail(c, HMF_ERR_STATE, "hmf_solve has not run");

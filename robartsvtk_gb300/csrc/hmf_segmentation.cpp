@@ -95,12 +95,15 @@ int HierarchicalMaxFlowSegmentation::Update(void* stream) {
   if (dims[0] <= 0) return Fail("Missing data prior for leaf node.");
 
   const bool rebuild = !ctx_ || ctx_parent_ != parent_ || ctx_semantics_ != semantics_ ||
-                       ctx_device_ != device_ || dims[0] != ctx_dims_[0] || dims[1] != ctx_dims_[1] ||
-                       dims[2] != ctx_dims_[2];
+                       ctx_device_ != device_ || ctx_usage_ != max_gpu_usage_ || dims[0] != ctx_dims_[0] ||
+                       dims[1] != ctx_dims_[1] || dims[2] != ctx_dims_[2];
   if (rebuild) {
     if (ctx_) hmf_destroy(ctx_);
     ctx_ = nullptr;
-    int rc = hmf_create(&ctx_, dims[0], dims[1], dims[2], parent_.data(), n, semantics_, device_);
+    int rc = max_gpu_usage_ < 0.0
+                 ? hmf_create(&ctx_, dims[0], dims[1], dims[2], parent_.data(), n, semantics_, device_)
+                 : hmf_create_paged(&ctx_, dims[0], dims[1], dims[2], parent_.data(), n, semantics_, device_,
+                                    max_gpu_usage_);
     if (rc != HMF_OK) {
       ctx_ = nullptr;
       return Fail(hmf_last_error(nullptr));
@@ -108,6 +111,7 @@ int HierarchicalMaxFlowSegmentation::Update(void* stream) {
     ctx_parent_ = parent_;
     ctx_semantics_ = semantics_;
     ctx_device_ = device_;
+    ctx_usage_ = max_gpu_usage_;
     for (int k = 0; k < 3; ++k) ctx_dims_[k] = dims[k];
     int nl = hmf_leaf_order(ctx_, nullptr, 0);
     leaves_.assign(nl, -1);

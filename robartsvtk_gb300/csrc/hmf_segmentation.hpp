@@ -55,6 +55,14 @@ class HierarchicalMaxFlowSegmentation {
   // CudaObject::SetDevice (Common/vtkCudaCommon/CudaObject.h:44)
   void SetDevice(int device) { device_ = device; }
   int GetDevice() const { return device_; }
+  // vtkCudaHierarchicalMaxFlowSegmentation's MaxGPUUsage (.h:52): the
+  // fraction of the device's memory the solve may hold, clamped to [0, 1]
+  // as vtkCudaHierarchicalMaxFlowSegmentation2's setter does (.h:74-75).  A
+  // negative value (the default) solves in core; otherwise the solve runs
+  // out of core (hmf_create_paged) within that budget, with the same
+  // results.
+  void SetMaxGPUUsage(double usage) { max_gpu_usage_ = usage < 0.0 ? -1.0 : (usage > 1.0 ? 1.0 : usage); }
+  double GetMaxGPUUsage() const { return max_gpu_usage_; }
   // HMF_SEMANTICS_REF_CUDA (default) or HMF_SEMANTICS_REF_CPU
   void SetSemantics(int semantics) { semantics_ = semantics; }
   int GetSemantics() const { return semantics_; }
@@ -82,11 +90,13 @@ class HierarchicalMaxFlowSegmentation {
   float step_ = 0.1f;
   int device_ = 0;
   int semantics_ = HMF_SEMANTICS_REF_CUDA;
+  double max_gpu_usage_ = -1.0;
 
   hmf_ctx* ctx_ = nullptr;
   int ctx_dims_[3] = {0, 0, 0};
   std::vector<int> ctx_parent_;
   int ctx_semantics_ = -1, ctx_device_ = -1;
+  double ctx_usage_ = -1.0;
 
   std::vector<int> leaves_;
   std::map<int, std::vector<float>> outputs_;

@@ -74,15 +74,23 @@ class HMFSolver:
     """One solver context: a volume size (vx, vy, vz), a label tree given as a
     parent array, and a semantics (REF_CUDA or REF_CPU)."""
 
-    def __init__(self, dims, parent, semantics: int = REF_CUDA, device: int = 0):
+    def __init__(self, dims, parent, semantics: int = REF_CUDA, device: int = 0, max_gpu_usage=None):
+        """max_gpu_usage: None solves in core; a fraction of the device's
+        memory (the reference's MaxGPUUsage) makes an out-of-core context
+        (hmf_create_paged) whose state lives in pinned host memory."""
         self._lib = _capi.load()
         self.dims = tuple(int(d) for d in dims)
         self.parent = [int(p) for p in parent]
         self.nvox = self.dims[0] * self.dims[1] * self.dims[2]
         par = (ctypes.c_int * len(self.parent))(*self.parent)
         ctx = ctypes.c_void_p()
-        check(self._lib.hmf_create(ctypes.byref(ctx), *self.dims, par, len(self.parent), int(semantics),
-                                   int(device)))
+        self.max_gpu_usage = max_gpu_usage
+        if max_gpu_usage is None:
+            check(self._lib.hmf_create(ctypes.byref(ctx), *self.dims, par, len(self.parent), int(semantics),
+                                       int(device)))
+        else:
+            check(self._lib.hmf_create_paged(ctypes.byref(ctx), *self.dims, par, len(self.parent), int(semantics),
+                                             int(device), float(max_gpu_usage)))
         self._ctx = ctx
         self._keep: dict = {}
         n = self._lib.hmf_leaf_order(self._ctx, None, 0)
@@ -307,6 +315,21 @@ class HMFSolver:
 
     def device_bytes(self) -> int:
         return int(self._lib.hmf_device_bytes(self._ctx))
+
+    def set_paged_plan(self, block_planes: int = 0, round_iterations: int = 0) -> None:
+        """Out-of-core contexts: planes per block and iterations per round of
+        later solves (0: from the budget)."""
+        check(self._lib.hmf_set_paged_plan(self._ctx, int(block_planes), int(round_iterations)), self._ctx)
+
+    def paged_plan(self) -> dict:
+        """Out-of-core contexts: the plan of the last solve and the bytes it
+        moved between host and device."""
+        vals = [ctypes.c_int() for _ in range(4)]
+        link = ctypes.c_longlong()
+        check(self._lib.hmf_get_paged_plan(self._ctx, *[ctypes.byref(v) for v in vals], ctypes.byref(link)),
+              self._ctx)
+        return {"blocks": vals[0].value, "block_planes": vals[1].value, "round_iterations": vals[2].value,
+                "rounds": vals[3].value, "link_bytes": link.value}
 
     def close(self) -> None:
         if getattr(self, "_ctx", None):
@@ -612,6 +635,7 @@ class HierarchicalMaxFlowSegmentation:
         self.CC = 0.25
         self.StepSize = 0.1
         self.Device = 0
+        self.MaxGPUUsage = None
         self.Semantics = semantics
         self._data: dict[int, object] = {}
         self._smooth: dict[int, object] = {}
@@ -656,6 +680,16 @@ class HierarchicalMaxFlowSegmentation:
 
     def SetDevice(self, d: int):
         self.Device = int(d)
+
+    # vtkCudaHierarchicalMaxFlowSegmentation::MaxGPUUsage (.h:52), clamped as
+    # vtkCudaHierarchicalMaxFlowSegmentation2's vtkSetClampMacro (.h:74-75);
+    # None (the default) solves in core, a fraction solves out of core within
+    # that share of the device's memory (same results)
+    def SetMaxGPUUsage(self, usage):
+        self.MaxGPUUsage = None if usage is None else min(1.0, max(0.0, float(usage)))
+
+    def GetMaxGPUUsage(self):
+        return self.MaxGPUUsage
 
     def GetDevice(self) -> int:
         return self.Device
@@ -714,10 +748,11 @@ class HierarchicalMaxFlowSegmentation:
         dims = (shape[2], shape[1], shape[0])
         try:
             if (self._solver is None or self._solver.dims != dims or self._solver.parent != self.Structure
-                    or getattr(self._solver, "_semantics", None) != self.Semantics):
+                    or getattr(self._solver, "_semantics", None) != self.Semantics
+                    or self._solver.max_gpu_usage != self.MaxGPUUsage):
                 if self._solver is not None:
                     self._solver.close()
-                self._solver = HMFSolver(dims, self.Structure, self.Semantics, self.Device)
+                self._solver = HMFSolver(dims, self.Structure, self.Semantics, self.Device, self.MaxGPUUsage)
                 self._solver._semantics = self.Semantics
             sol = self._solver
             for leaf in sol.leaves:
