@@ -547,9 +547,10 @@ def run_ours(args):
 
 def bench_paged(args, w, in_core, h_data, h_smooth, in_core_value, device_stream):
     """The same workload out of core (hmf_create_paged): a MaxGPUUsage budget
-    that holds two blocks of --paged-planes planes, the state in pinned host
-    memory, pinned host inputs; CUDA events around whole solves.  The labels
-    must equal the in-core solve's bit for bit."""
+    that holds three blocks of --paged-planes planes and the inputs (which
+    then stay on the device), the state in pinned host memory, pinned host
+    inputs; CUDA events around whole solves.  The labels must equal the
+    in-core solve's bit for bit."""
     import numpy as np
     import torch
 
@@ -559,7 +560,8 @@ def bench_paged(args, w, in_core, h_data, h_smooth, in_core_value, device_stream
     pitch = (w.dims[0] + 3) // 4 * 4
     n_inputs = len(w.leaves) + len({id(S) for S in w.smooth.values()})
     per_plane = (9 * (len(w.parent) - 1) + 1 + n_inputs) * pitch * w.dims[1] * 4
-    budget = 2 * (16 << 20) + 2 * args.paged_planes * per_plane
+    inputs = n_inputs * w.nvox * 4
+    budget = 3 * (16 << 20) + inputs + 3 * args.paged_planes * per_plane
     usage = budget / total
     s = HMFSolver(w.dims, w.parent, max_gpu_usage=usage)
     for leaf, t in h_data.items():

@@ -154,11 +154,11 @@ int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kin
  * fit.
  *
  * hmf_create_paged makes a context whose solver state lives in pinned host
- * memory (5 x (n_nodes - 1) + 1 arrays of VX*VY*VZ floats; 2 x (n_nodes - 1)
- * + 1 when one round suffices) and whose device memory stays within
+ * memory (two copies of 5 x (n_nodes - 1) + 1 arrays of VX*VY*VZ floats;
+ * one copy of 2 x (n_nodes - 1) + 1 when one round suffices) and whose device memory stays within
  * max_gpu_usage x the device's memory (clamped to [0, 1]).  hmf_solve covers
- * the volume with blocks of T z-planes (T from the budget: two block
- * contexts of T planes fit) and iterates in rounds of k <= 8 iterations: each
+ * the volume with blocks of T z-planes (T from the budget: three block
+ * contexts of T planes fit) and iterates in rounds of k <= 12 iterations: each
  * block is loaded, iterated k times with the in-core kernels, and stores back
  * the planes at least 2k + 1 planes from its inner faces, which equal the
  * in-core solve's.  Labels and sinks are therefore identical to hmf_create +
@@ -171,9 +171,14 @@ int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kin
  * HMF_ERR_STATE.  Label trees, single volumes, both semantics (REF_CPU
  * iterates per voxel: one round, no halo).
  *  - hmf_set_paged_plan: block planes T and iterations per round k for later
- *    solves (0: from the budget, k = min(8, (T - 4) / 8)); T >= 4 x (2k + 1)
+ *    solves (0: from the budget, k = min(12, (T - 4) / 8)); T >= 4 x (2k + 1)
  *    unless one block covers the volume (then k > 0 splits the solve into
- *    rounds of k iterations on that block).
+ *    rounds of k iterations on that block); and where host inputs are read
+ *    from: HMF_PAGED_INPUTS_AUTO (on the device for the whole solve when
+ *    they take at most a quarter of the budget, else from host memory every
+ *    round), HMF_PAGED_INPUTS_HOST, HMF_PAGED_INPUTS_DEVICE.  Three block
+ *    contexts of T planes are in flight (one loading, one iterating, one
+ *    storing), and the host state is double-buffered between rounds.
  *  - hmf_get_paged_plan: blocks, T, k and rounds of the last solve, and the
  *    bytes it moved between host and device.
  *  - hmf_paged_layout: host only (no device work): the blocks covering vz
@@ -184,7 +189,10 @@ int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kin
  *    when the blocks are thinner than four halos. */
 int hmf_create_paged(hmf_ctx** out, int vx, int vy, int vz, const int* parent, int n_nodes, int semantics,
                      int device, double max_gpu_usage);
-int hmf_set_paged_plan(hmf_ctx* ctx, int block_planes, int round_iterations);
+#define HMF_PAGED_INPUTS_AUTO 0
+#define HMF_PAGED_INPUTS_HOST 1
+#define HMF_PAGED_INPUTS_DEVICE 2
+int hmf_set_paged_plan(hmf_ctx* ctx, int block_planes, int round_iterations, int inputs);
 int hmf_get_paged_plan(const hmf_ctx* ctx, int* blocks, int* block_planes, int* round_iterations, int* rounds,
                        long long* link_bytes);
 int hmf_paged_layout(int vz, int block_planes, int halo_planes, int* starts, int* owned, int capacity);

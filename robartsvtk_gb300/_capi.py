@@ -23,6 +23,9 @@ HMF_STALL_REVERSE_SWEEP = 3
 HMF_FP64_PROBE_NONE = 0
 HMF_FP64_PROBE_DATA = 1
 HMF_FP64_PROBE_ALPHA = 2
+HMF_PAGED_INPUTS_AUTO = 0
+HMF_PAGED_INPUTS_HOST = 1
+HMF_PAGED_INPUTS_DEVICE = 2
 
 ERRORS = {
     -1: "HMF_ERR_INVALID_ARGUMENT",
@@ -96,7 +99,7 @@ SIGNATURES = [
     ("hmf_fp64_loss", _I, [_P, _P, _I, ctypes.c_double, ctypes.POINTER(ctypes.c_double), _P]),
     ("hmf_set_fp64_probe", _I, [_P, _I, _I, ctypes.c_longlong, ctypes.c_double]),
     ("hmf_create_paged", _I, [ctypes.POINTER(_P), _I, _I, _I, ctypes.POINTER(_I), _I, _I, _I, ctypes.c_double]),
-    ("hmf_set_paged_plan", _I, [_P, _I, _I]),
+    ("hmf_set_paged_plan", _I, [_P, _I, _I, _I]),
     ("hmf_get_paged_plan", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                 ctypes.POINTER(ctypes.c_longlong)]),
     ("hmf_paged_layout", _I, [_I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _I]),

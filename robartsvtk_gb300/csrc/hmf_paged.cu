@@ -18,12 +18,19 @@
 // volume-face rules) is exact on every plane at least 2k planes from a face
 // that lies inside the volume -- 2k + 1 on the high-z side, whose first step
 // forms the old divergence of the top plane without the z-flow of the plane
-// beyond it.  The volume is covered by overlapping blocks,
-// each owning the planes it computes exactly; a round loads every block's
-// planes from the host state, runs k iterations with the in-core kernels
-// (same arithmetic: results identical to the in-core solve) and stores the
-// owned planes back.  Two block contexts alternate on two streams, so one
-// block's copies run while the other computes.
+// beyond it.  The volume is covered by overlapping blocks, each owning the
+// planes it computes exactly; a round loads every block's planes from the
+// host state, runs k iterations with the in-core kernels (same arithmetic:
+// results identical to the in-core solve) and stores the owned planes back.
+//
+// Pipelining: three block contexts take the blocks in turn, each on its own
+// stream, so that one block's planes come in over the link while another
+// iterates and a third's go out (the two copy directions run concurrently).
+// The host state is double-buffered -- round r reads copy (r-1)&1 and writes
+// copy r&1 -- so a block's store never waits for a neighbour's load of the
+// same round; across rounds a block's load waits only for the stores of the
+// three blocks whose owned planes it covers, and a store for the loads of the
+// previous round that read what it overwrites.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,33 +39,50 @@
 
 #include "hmf_ctx.hpp"
 
+namespace {
+
+constexpr int kBlockContexts = 3;  // blocks in flight: loading, iterating, storing
+
+// One copy of the host state: per vertex the sink; per non-root vertex the
+// label and the three flows; dense VX*VY*VZ floats each (pinned).  The
+// divergence is not kept: the flow step forms the old divergence from the
+// flows and writes the new one before the sweep reads it.
+struct HostState {
+  char* mem = nullptr;
+  size_t bytes = 0;
+  std::vector<float*> sink, label, fx, fy, fz;
+};
+
+}  // namespace
+
 struct PagedState {
   double usage = 0.75;      // fraction of the device's memory (MaxGPUUsage)
   int forced_planes = 0;    // hmf_set_paged_plan (0: from the budget)
   int forced_iterations = 0;
+  int inputs_mode = HMF_PAGED_INPUTS_AUTO;
 
   // plan of the last solve
   int block_planes = 0, round_iterations = 0, halo = 0;
   std::vector<int> starts, owned;  // per block: first plane, first owned plane
   int rounds = 0;
+  bool inputs_on_device = false;
   long long link_bytes = 0;  // bytes between host and device in the last solve
+  int final_copy = 0;        // host state copy holding the final sinks and labels
 
-  hmf_ctx* blk[2] = {nullptr, nullptr};
+  hmf_ctx* blk[kBlockContexts] = {};
+  int n_blk = 0;
   int blk_planes = 0;  // planes the block contexts were created for
-  cudaStream_t st[2] = {nullptr, nullptr};
-  cudaEvent_t ev_loaded[2] = {nullptr, nullptr};
-  cudaEvent_t ev_end[2] = {nullptr, nullptr};
+  cudaStream_t st[kBlockContexts] = {};
+  std::vector<cudaEvent_t> ev_loaded[2], ev_stored[2];  // [round parity][block]
+  cudaEvent_t ev_end[kBlockContexts] = {};
 
-  // host state: per vertex sink; per non-root vertex label and three flows;
-  // dense VX*VY*VZ floats each (pinned).  The divergence is not kept: the
-  // flow step forms the old divergence from the flows and writes the new one
-  // before the sweep reads it.
-  char* host = nullptr;
-  size_t host_bytes = 0;
-  std::vector<float*> sink, label, fx, fy, fz;
+  HostState host[2];
   // pinned copies of pageable host inputs
   char* inputs = nullptr;
   size_t input_bytes = 0;
+  // device copies of the inputs when they stay resident (HMF_PAGED_INPUTS_DEVICE)
+  char* d_inputs = nullptr;
+  size_t d_input_bytes = 0;
   // error flag of every block solve of the last solve (pinned)
   int* flags = nullptr;
   int flag_cap = 0, n_flags = 0;
@@ -68,16 +92,19 @@ namespace hmfi {
 
 namespace {
 
-// Iterations per round: a round moves each plane of ~6 arrays per vertex
-// across the host link and back, and an iteration moves ~12 per vertex
-// through HBM; at the link's ~0.05 of HBM bandwidth about 8 iterations
-// per round balance the two.
-constexpr int kMaxRoundIterations = 8;
+// Iterations per round, at most: a round moves each plane of ~5 arrays per
+// vertex across the host link and back, an iteration ~12 per vertex through
+// HBM, and the link runs at ~0.03 of HBM bandwidth, so longer rounds pay off
+// until the halo (2k + 1 planes a side) eats the block: with k = (T - 4) / 8
+// the halo takes about half of T.  Measured at 256^3 tree4 with 96-plane
+// blocks: 8 iterations per round 290 ms per 96 iterations, 11 272 ms.
+constexpr int kMaxRoundIterations = 12;
 constexpr size_t kBlockFixedBytes = 16u << 20;  // tables, graphs and alignment of one block context
 
 struct BlockLoad {
-  PagedState* P;
-  int slot, first;  // block context slot, first plane of the block
+  const HostState* H;
+  cudaEvent_t loaded;
+  int first;        // first plane of the block
   long long plane;  // elements per dense plane
   long long* bytes;
 };
@@ -101,17 +128,17 @@ int copy_planes(hmf_ctx* c, float* dst, size_t dpitch, const float* src, size_t 
 int load_block(hmf_ctx* b, cudaStream_t s, void* arg) {
   hmf_ctx* c = b;
   const BlockLoad& L = *static_cast<const BlockLoad*>(arg);
-  PagedState& P = *L.P;
+  const HostState& H = *L.H;
   const auto& V = b->vols[0];
   const size_t dp = (size_t)V.pitch * sizeof(float), sp = (size_t)V.vx * sizeof(float);
   const long long off = (long long)L.first * L.plane;
   long long n = 0;
   for (int v = 0; v < b->n; ++v) {
-    if (int rc = copy_planes(c, b->sink[v], dp, P.sink[v] + off, sp, V.vx, V.vy, V.vz, cudaMemcpyHostToDevice, s))
+    if (int rc = copy_planes(c, b->sink[v], dp, H.sink[v] + off, sp, V.vx, V.vy, V.vz, cudaMemcpyHostToDevice, s))
       return rc;
     ++n;
     if (v == b->root) continue;
-    const float* src[4] = {P.label[v], P.fx[v], P.fy[v], P.fz[v]};
+    const float* src[4] = {H.label[v], H.fx[v], H.fy[v], H.fz[v]};
     float* dst[4] = {b->label[v], b->fx[0][v], b->fy[0][v], b->fz[0][v]};
     for (int a = 0; a < 4; ++a)
       if (int rc = copy_planes(c, dst[a], dp, src[a] + off, sp, V.vx, V.vy, V.vz, cudaMemcpyHostToDevice, s))
@@ -119,14 +146,14 @@ int load_block(hmf_ctx* b, cudaStream_t s, void* arg) {
     n += 4;
   }
   *L.bytes += n * (long long)V.vz * L.plane * (long long)sizeof(float);
-  CK(cudaEventRecord(P.ev_loaded[L.slot], s), "cudaEventRecord(block loaded)");
+  CK(cudaEventRecord(L.loaded, s), "cudaEventRecord(block loaded)");
   return HMF_OK;
 }
 
-// The owned planes [z0, z1) of a solved block back into the host state: all
-// of it between rounds, the sinks and labels after the last round.
-int store_block(hmf_ctx* c, PagedState& P, hmf_ctx* b, int first, int z0, int z1, int parity, bool final_round,
-                long long plane, cudaStream_t s) {
+// The owned planes [z0, z1) of a solved block into a host state copy: all of
+// it between rounds, the sinks and labels after the last round.
+int store_block(hmf_ctx* c, PagedState& P, HostState& H, hmf_ctx* b, int first, int z0, int z1, int parity,
+                bool final_round, long long plane, cudaStream_t s) {
   const auto& V = b->vols[0];
   const size_t dp = (size_t)V.vx * sizeof(float), sp = (size_t)V.pitch * sizeof(float);
   const int planes = z1 - z0;
@@ -134,18 +161,18 @@ int store_block(hmf_ctx* c, PagedState& P, hmf_ctx* b, int first, int z0, int z1
   const long long hoff = (long long)z0 * plane, boff = (long long)(z0 - first) * V.plane;
   long long n = 0;
   for (int v = 0; v < b->n; ++v) {
-    if (int rc = copy_planes(c, P.sink[v] + hoff, dp, b->sink[v] + boff, sp, V.vx, V.vy, planes,
+    if (int rc = copy_planes(c, H.sink[v] + hoff, dp, b->sink[v] + boff, sp, V.vx, V.vy, planes,
                              cudaMemcpyDeviceToHost, s))
       return rc;
     ++n;
     if (v == b->root) continue;
-    if (int rc = copy_planes(c, P.label[v] + hoff, dp, b->label[v] + boff, sp, V.vx, V.vy, planes,
+    if (int rc = copy_planes(c, H.label[v] + hoff, dp, b->label[v] + boff, sp, V.vx, V.vy, planes,
                              cudaMemcpyDeviceToHost, s))
       return rc;
     ++n;
     if (final_round) continue;
     const float* src[3] = {b->fx[parity][v], b->fy[parity][v], b->fz[parity][v]};
-    float* dst[3] = {P.fx[v], P.fy[v], P.fz[v]};
+    float* dst[3] = {H.fx[v], H.fy[v], H.fz[v]};
     for (int a = 0; a < 3; ++a)
       if (int rc = copy_planes(c, dst[a] + hoff, dp, src[a] + boff, sp, V.vx, V.vy, planes, cudaMemcpyDeviceToHost, s))
         return rc;
@@ -161,16 +188,57 @@ void free_blocks(PagedState& P) {
       hmf_destroy(b);
       b = nullptr;
     }
+  P.n_blk = 0;
   P.blk_planes = 0;
 }
 
-// Device bytes one block context of `planes` planes holds: 9 arrays per
-// non-root vertex and the root's (hmf_create's state), plus the staged
-// inputs.
-size_t block_bytes(const hmf_ctx* c, int planes, int staged_inputs) {
+// Device bytes of one plane of a block context: 9 arrays per non-root vertex
+// and the root's (hmf_create's state) plus the inputs it stages.
+size_t plane_bytes(const hmf_ctx* c, int staged_inputs) {
   const auto& V = c->vols[0];
-  const size_t arr = round_up((size_t)V.pitch * V.vy * planes * sizeof(float), 256);
-  return arr * (size_t)(9 * (c->n - 1) + 1 + staged_inputs) + kBlockFixedBytes;
+  return (size_t)V.pitch * V.vy * sizeof(float) * (size_t)(9 * (c->n - 1) + 1 + staged_inputs);
+}
+
+// The host state copy `H`: sinks and labels, and the flows when `flows`.
+int host_state(hmf_ctx* c, HostState& H, size_t arr, bool flows) {
+  const size_t n_arrays = flows ? (size_t)5 * (c->n - 1) + 1 : (size_t)2 * (c->n - 1) + 1;
+  if (H.bytes < n_arrays * arr) {
+    if (H.mem) cudaFreeHost(H.mem);
+    H.mem = nullptr;
+    H.bytes = 0;
+    CK(cudaMallocHost(&H.mem, n_arrays * arr), "cudaMallocHost(paged state)");
+    H.bytes = n_arrays * arr;
+  }
+  char* p = H.mem;
+  auto take = [&]() {
+    float* r = reinterpret_cast<float*>(p);
+    p += arr;
+    return r;
+  };
+  H.sink.assign(c->n, nullptr);
+  H.label.assign(c->n, nullptr);
+  H.fx.assign(c->n, nullptr);
+  H.fy.assign(c->n, nullptr);
+  H.fz.assign(c->n, nullptr);
+  for (int v = 0; v < c->n; ++v) {
+    H.sink[v] = take();
+    if (v == c->root) continue;
+    H.label[v] = take();
+    if (!flows) continue;
+    H.fx[v] = take();
+    H.fy[v] = take();
+    H.fz[v] = take();
+  }
+  return HMF_OK;
+}
+
+int ensure_events(hmf_ctx* c, std::vector<cudaEvent_t>& evs, int n) {
+  while ((int)evs.size() < n) {
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate(paged)");
+    evs.push_back(e);
+  }
+  return HMF_OK;
 }
 
 }  // namespace
@@ -181,9 +249,8 @@ int paged_setup(hmf_ctx* c, double max_gpu_usage) {
   auto* P = new PagedState();
   c->pg = P;
   P->usage = std::min(1.0, max_gpu_usage);
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kBlockContexts; ++i) {
     CK(cudaStreamCreateWithFlags(&P->st[i], cudaStreamNonBlocking), "cudaStreamCreate(paged)");
-    CK(cudaEventCreateWithFlags(&P->ev_loaded[i], cudaEventDisableTiming), "cudaEventCreate(paged)");
     CK(cudaEventCreateWithFlags(&P->ev_end[i], cudaEventDisableTiming), "cudaEventCreate(paged)");
   }
   return HMF_OK;
@@ -195,20 +262,24 @@ void paged_free(hmf_ctx* c) {
   for (auto s : P->st)
     if (s) cudaStreamSynchronize(s);
   free_blocks(*P);
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kBlockContexts; ++i) {
     if (P->st[i]) cudaStreamDestroy(P->st[i]);
-    if (P->ev_loaded[i]) cudaEventDestroy(P->ev_loaded[i]);
     if (P->ev_end[i]) cudaEventDestroy(P->ev_end[i]);
   }
-  if (P->host) cudaFreeHost(P->host);
+  for (int q = 0; q < 2; ++q) {
+    for (auto e : P->ev_loaded[q]) cudaEventDestroy(e);
+    for (auto e : P->ev_stored[q]) cudaEventDestroy(e);
+    if (P->host[q].mem) cudaFreeHost(P->host[q].mem);
+  }
   if (P->inputs) cudaFreeHost(P->inputs);
+  if (P->d_inputs) cudaFree(P->d_inputs);
   if (P->flags) cudaFreeHost(P->flags);
   delete P;
   c->pg = nullptr;
 }
 
 size_t paged_bytes(const hmf_ctx* c) {
-  size_t n = 0;
+  size_t n = c->pg->inputs_on_device ? c->pg->d_input_bytes : 0;
   for (auto b : c->pg->blk)
     if (b) n += hmf_device_bytes(b);
   return n;
@@ -223,77 +294,46 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   const long long plane = (long long)V.vx * V.vy;
   const size_t arr = (size_t)plane * V.vz * sizeof(float);
 
-  // ---- inputs: device inputs are read in place, host inputs from pinned memory
+  // ---- inputs: the distinct input arrays, where they are, where blocks read them
   std::vector<const float*> in_data(c->n, nullptr), in_smooth(c->n, nullptr);
   std::vector<int> w_data(c->n, HMF_HOST), w_smooth(c->n, HMF_HOST);
-  std::vector<const float*> pinned_src;
-  std::vector<float*> pinned_dst;
-  auto resolve = [&](const hmf_ctx::Input& in, const float** ptr, int* where) -> int {
-    *ptr = in.ptr;
-    *where = in.where;
-    if (!in.ptr || in.where == HMF_DEVICE) return HMF_OK;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, in.ptr) == cudaSuccess && a.type == cudaMemoryTypeHost) return HMF_OK;
-    cudaGetLastError();
-    for (size_t i = 0; i < pinned_src.size(); ++i)
-      if (pinned_src[i] == in.ptr) {
-        *ptr = pinned_dst[i];
-        return HMF_OK;
-      }
-    pinned_src.push_back(in.ptr);
-    pinned_dst.push_back(nullptr);
-    *ptr = nullptr;  // filled below
-    return HMF_OK;
-  };
-  for (int l : c->leaves) resolve(c->data[0][l], &in_data[l], &w_data[l]);
+  for (int l : c->leaves) in_data[l] = c->data[0][l].ptr, w_data[l] = c->data[0][l].where;
   for (int v = 0; v < c->n; ++v)
-    if (v != c->root) resolve(c->smooth[0][v], &in_smooth[v], &w_smooth[v]);
-  if (!pinned_src.empty()) {
-    const size_t need = arr * pinned_src.size();
-    if (need > P.input_bytes) {
-      if (P.inputs) cudaFreeHost(P.inputs);
-      P.inputs = nullptr;
-      P.input_bytes = 0;
-      CK(cudaMallocHost(&P.inputs, need), "cudaMallocHost(paged inputs)");
-      P.input_bytes = need;
-    }
-    for (size_t i = 0; i < pinned_src.size(); ++i) {
-      pinned_dst[i] = reinterpret_cast<float*>(P.inputs + i * arr);
-      std::memcpy(pinned_dst[i], pinned_src[i], arr);
-    }
-    auto fix = [&](const hmf_ctx::Input& in, const float** ptr) {
-      if (*ptr || !in.ptr) return;
-      for (size_t i = 0; i < pinned_src.size(); ++i)
-        if (pinned_src[i] == in.ptr) *ptr = pinned_dst[i];
-    };
-    for (int l : c->leaves) fix(c->data[0][l], &in_data[l]);
-    for (int v = 0; v < c->n; ++v)
-      if (v != c->root) fix(c->smooth[0][v], &in_smooth[v]);
-  }
-  // inputs each block stages (all of them, at most) and those that cross the host link
-  int staged_inputs = (int)c->leaves.size(), host_inputs = 0;
-  for (int l : c->leaves) host_inputs += w_data[l] == HMF_HOST;
+    if (v != c->root && c->smooth[0][v].ptr) in_smooth[v] = c->smooth[0][v].ptr, w_smooth[v] = c->smooth[0][v].where;
+  std::vector<const float*> host_src;  // distinct host inputs
+  auto note_host = [&](const float* p, int w) {
+    if (p && w == HMF_HOST && std::find(host_src.begin(), host_src.end(), p) == host_src.end()) host_src.push_back(p);
+  };
+  for (int l : c->leaves) note_host(in_data[l], w_data[l]);
+  for (int v = 0; v < c->n; ++v) note_host(in_smooth[v], w_smooth[v]);
+  int staged_inputs = (int)c->leaves.size();
   {
     std::vector<const float*> distinct;
     for (int v = 0; v < c->n; ++v)
-      if (in_smooth[v] && std::find(distinct.begin(), distinct.end(), in_smooth[v]) == distinct.end()) {
+      if (in_smooth[v] && std::find(distinct.begin(), distinct.end(), in_smooth[v]) == distinct.end())
         distinct.push_back(in_smooth[v]);
-        host_inputs += w_smooth[v] == HMF_HOST;
-      }
     staged_inputs += (int)distinct.size();
   }
 
   // ---- plan: block thickness T from the budget, k iterations per round
   const bool cpu = c->semantics == HMF_SEMANTICS_REF_CPU;
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  const size_t budget = (size_t)(P.usage * (double)total_b);
+  const size_t host_in_bytes = arr * host_src.size();
+  // host inputs stay on the device for the whole solve when they take at most
+  // a quarter of the budget (or when asked): the blocks then read them in
+  // place instead of over the link every round
+  const bool dev_inputs = !host_src.empty() &&
+                          (P.inputs_mode == HMF_PAGED_INPUTS_DEVICE ||
+                           (P.inputs_mode == HMF_PAGED_INPUTS_AUTO && 4 * host_in_bytes <= budget));
   int T = P.forced_planes;
   if (T <= 0) {
-    size_t free_b = 0, total_b = 0;
-    CK(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-    const size_t budget = (size_t)(P.usage * (double)total_b);
-    const size_t per_plane = block_bytes(c, 1, staged_inputs) - kBlockFixedBytes;
-    if (budget <= 2 * kBlockFixedBytes + 2 * per_plane)
-      return fail(c, HMF_ERR_OUT_OF_MEMORY, "MaxGPUUsage leaves no room for two blocks of planes");
-    T = (int)std::min<size_t>((size_t)V.vz, (budget - 2 * kBlockFixedBytes) / (2 * per_plane));
+    const size_t per_plane = plane_bytes(c, staged_inputs);
+    const size_t fixed = kBlockContexts * kBlockFixedBytes + (dev_inputs ? host_in_bytes : 0);
+    if (budget <= fixed + kBlockContexts * per_plane)
+      return fail(c, HMF_ERR_OUT_OF_MEMORY, "MaxGPUUsage leaves no room for three blocks of planes");
+    T = (int)std::min<size_t>((size_t)V.vz, (budget - fixed) / (kBlockContexts * per_plane));
   }
   T = std::min(T, V.vz);
   int k;
@@ -326,52 +366,95 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   P.halo = halo;
   P.rounds = (int)round_iters.size();
   P.link_bytes = 0;
+  P.final_copy = (P.rounds - 1) & 1;
 
-  // ---- memory: two block contexts, the host state, the error flags
-  if (P.blk_planes != T) {
+  // ---- memory: block contexts, the inputs, the host state, the error flags
+  const int nc = std::min(kBlockContexts, nb);
+  if (P.blk_planes != T || P.n_blk < nc) {
     free_blocks(P);
-    for (int i = 0; i < 2 && i < nb; ++i) {
+    for (int i = 0; i < nc; ++i) {
       int rc = hmf_create(&P.blk[i], V.vx, V.vy, T, c->parent.data(), c->n, c->semantics, c->device);
       if (rc) {
         free_blocks(P);
         return fail(c, rc, std::string("block context: ") + hmf_last_error(nullptr));
       }
     }
+    P.n_blk = nc;
     P.blk_planes = T;
   }
-  const bool need_state = P.rounds > 1;
-  const size_t n_arrays = need_state ? (size_t)5 * (c->n - 1) + 1 : (size_t)2 * (c->n - 1) + 1;
-  if (P.host_bytes < n_arrays * arr) {
-    if (P.host) cudaFreeHost(P.host);
-    P.host = nullptr;
-    P.host_bytes = 0;
-    CK(cudaMallocHost(&P.host, n_arrays * arr), "cudaMallocHost(paged state)");
-    P.host_bytes = n_arrays * arr;
-  }
-  {
-    char* p = P.host;
-    auto take = [&]() {
-      float* r = reinterpret_cast<float*>(p);
-      p += arr;
-      return r;
-    };
-    P.sink.assign(c->n, nullptr);
-    P.label.assign(c->n, nullptr);
-    P.fx.assign(c->n, nullptr);
-    P.fy.assign(c->n, nullptr);
-    P.fz.assign(c->n, nullptr);
-    for (int v = 0; v < c->n; ++v) {
-      P.sink[v] = take();
-      if (v == c->root) continue;
-      P.label[v] = take();
-      if (!need_state) continue;
-      P.fx[v] = take();
-      P.fy[v] = take();
-      P.fz[v] = take();
+  CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
+  for (int i = 0; i < kBlockContexts; ++i)
+    CK(cudaStreamWaitEvent(P.st[i], c->ev_join, 0), "cudaStreamWaitEvent(join)");
+  // Host inputs: on the device for the whole solve, or from pinned memory
+  // (the caller's, when already pinned, else a pinned copy) every round.
+  std::vector<const float*> host_dst(host_src.size(), nullptr);
+  if (dev_inputs) {
+    if (host_in_bytes > P.d_input_bytes) {
+      for (auto s : P.st) CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(paged inputs)");
+      if (P.d_inputs) cudaFree(P.d_inputs);
+      P.d_inputs = nullptr;
+      P.d_input_bytes = 0;
+      CK(cudaMalloc(&P.d_inputs, host_in_bytes), "cudaMalloc(paged inputs)");
+      P.d_input_bytes = host_in_bytes;
     }
+    for (size_t i = 0; i < host_src.size(); ++i) {
+      host_dst[i] = reinterpret_cast<const float*>(P.d_inputs + i * arr);
+      CK(cudaMemcpyAsync(const_cast<float*>(host_dst[i]), host_src[i], arr, cudaMemcpyHostToDevice, P.st[0]),
+         "cudaMemcpyAsync(paged inputs)");
+    }
+    P.link_bytes += (long long)host_in_bytes;
+    CK(cudaEventRecord(P.ev_end[0], P.st[0]), "cudaEventRecord(inputs)");
+    for (int i = 1; i < kBlockContexts; ++i)
+      CK(cudaStreamWaitEvent(P.st[i], P.ev_end[0], 0), "cudaStreamWaitEvent(inputs)");
+  } else if (!host_src.empty()) {
+    std::vector<size_t> copy;  // pageable inputs: copied into pinned memory
+    for (size_t i = 0; i < host_src.size(); ++i) {
+      cudaPointerAttributes a;
+      if (cudaPointerGetAttributes(&a, host_src[i]) == cudaSuccess && a.type == cudaMemoryTypeHost)
+        host_dst[i] = host_src[i];
+      else
+        copy.push_back(i);
+      cudaGetLastError();
+    }
+    if (!copy.empty()) {
+      // the previous solve's copies read the pinned buffer, which the host
+      // rewrites here: they are done once its streams are
+      for (auto s : P.st) CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(paged inputs)");
+      if (arr * copy.size() > P.input_bytes) {
+        if (P.inputs) cudaFreeHost(P.inputs);
+        P.inputs = nullptr;
+        P.input_bytes = 0;
+        CK(cudaMallocHost(&P.inputs, arr * copy.size()), "cudaMallocHost(paged inputs)");
+        P.input_bytes = arr * copy.size();
+      }
+      for (size_t q = 0; q < copy.size(); ++q) {
+        host_dst[copy[q]] = reinterpret_cast<const float*>(P.inputs + q * arr);
+        std::memcpy(const_cast<float*>(host_dst[copy[q]]), host_src[copy[q]], arr);
+      }
+    }
+  }
+  P.inputs_on_device = dev_inputs;
+  auto route = [&](const float* p, int w, int* where) -> const float* {
+    *where = w;
+    if (!p || w != HMF_HOST) return p;
+    const size_t i = std::find(host_src.begin(), host_src.end(), p) - host_src.begin();
+    if (dev_inputs) *where = HMF_DEVICE;
+    return host_dst[i];
+  };
+  for (int l : c->leaves) in_data[l] = route(in_data[l], w_data[l], &w_data[l]);
+  for (int v = 0; v < c->n; ++v) in_smooth[v] = route(in_smooth[v], w_smooth[v], &w_smooth[v]);
+  const int link_inputs = dev_inputs ? 0 : (int)host_src.size();  // inputs the blocks read over the link
+
+  const bool need_state = P.rounds > 1;
+  for (int q = 0; q < (need_state ? 2 : 1); ++q)
+    if (int rc = host_state(c, P.host[q], arr, need_state)) return rc;
+  for (int q = 0; q < 2; ++q) {
+    if (int rc = ensure_events(c, P.ev_loaded[q], nb)) return rc;
+    if (int rc = ensure_events(c, P.ev_stored[q], nb)) return rc;
   }
   const int n_flags = P.rounds * nb;
   if (P.flag_cap < n_flags) {
+    for (auto s : P.st) CK(cudaStreamSynchronize(s), "cudaStreamSynchronize(paged flags)");
     if (P.flags) cudaFreeHost(P.flags);
     P.flags = nullptr;
     P.flag_cap = 0;
@@ -380,18 +463,14 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   }
   for (int i = 0; i < n_flags; ++i) P.flags[i] = 0;
   P.n_flags = n_flags;
-
-  // ---- block contexts: parameters and inputs
-  for (int i = 0; i < 2 && i < nb; ++i) {
+  for (int i = 0; i < nc; ++i) {
     hmf_ctx* b = P.blk[i];
     for (int v = 0; v < c->n; ++v)
       if (v != c->root) hmf_set_smoothness_scalar(b, v, c->alpha[v]);
     b->timing = c->timing;
   }
 
-  // ---- rounds
-  CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
-  for (int i = 0; i < 2; ++i) CK(cudaStreamWaitEvent(P.st[i], c->ev_join, 0), "cudaStreamWaitEvent(join)");
+  // ---- rounds: round r reads host copy (r-1)&1 and writes copy r&1
   long long launches = 0;
   double kind_ms[3] = {0, 0, 0};
   long long kind_count[3] = {0, 0, 0};
@@ -399,14 +478,12 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   for (int r = 0; r < P.rounds; ++r) {
     const int kr = round_iters[r];
     const bool last = r + 1 == P.rounds;
-    auto store = [&](int j) -> int {
-      const int slot = j & 1;
-      const int z1 = j + 1 < nb ? P.owned[j + 1] : V.vz;
-      return store_block(c, P, P.blk[slot], P.starts[j], P.owned[j], z1, kr & 1, last, plane, P.st[slot]);
-    };
+    HostState& out = P.host[r & 1];
+    const HostState& in = P.host[(r + 1) & 1];  // copy (r-1)&1
     for (int j = 0; j < nb; ++j) {
-      const int slot = j & 1;
+      const int slot = j % nc;
       hmf_ctx* b = P.blk[slot];
+      cudaStream_t s = P.st[slot];
       const long long off = (long long)P.starts[j] * plane;
       for (int l : c->leaves) {
         int rc = hmf_set_data(b, l, in_data[l] + off, w_data[l]);
@@ -418,40 +495,43 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
         if (rc) return fail(c, rc, std::string("block input: ") + b->err);
       }
       hmf_set_params(b, kr, c->step, c->cc);
+      // a block's planes hold the owned planes of its neighbours and itself:
+      // its load follows their stores of the previous round
+      const int lo = std::max(0, j - 1), hi = std::min(nb - 1, j + 1);
+      if (r > 0)
+        for (int m = lo; m <= hi; ++m)
+          CK(cudaStreamWaitEvent(s, P.ev_stored[(r + 1) & 1][m], 0), "cudaStreamWaitEvent(stored)");
       int rc;
       if (r == 0) {
-        rc = solve_with(b, P.st[slot], nullptr, nullptr);
+        rc = solve_with(b, s, nullptr, nullptr);
       } else {
-        BlockLoad L{&P, slot, P.starts[j], plane, &P.link_bytes};
-        rc = solve_with(b, P.st[slot], load_block, &L);
+        BlockLoad L{&in, P.ev_loaded[r & 1][j], P.starts[j], plane, &P.link_bytes};
+        rc = solve_with(b, s, load_block, &L);
       }
       if (rc) return fail(c, rc, std::string("block solve: ") + b->err);
-      CK(cudaMemcpyAsync(&P.flags[flag_i++], b->d_error, sizeof(int), cudaMemcpyDeviceToHost, P.st[slot]),
+      CK(cudaMemcpyAsync(&P.flags[flag_i++], b->d_error, sizeof(int), cudaMemcpyDeviceToHost, s),
          "cudaMemcpyAsync(block error flag)");
       for (int q = 0; q < 3; ++q) {
         kind_ms[q] += b->kind_ms[q] * b->kind_count[q];
         kind_count[q] += b->kind_count[q];
       }
       launches += b->launches;
-      // the previous block's owned planes go back once this block has read
-      // its halo planes from them
-      if (j > 0) {
-        if (r > 0) CK(cudaStreamWaitEvent(P.st[(j - 1) & 1], P.ev_loaded[slot], 0), "cudaStreamWaitEvent(loaded)");
-        if (int rc2 = store(j - 1)) return rc2;
-      }
+      // the store overwrites planes of copy r&1 that the previous round's
+      // loads of this block and its neighbours read
+      if (r > 1)
+        for (int m = lo; m <= hi; ++m)
+          CK(cudaStreamWaitEvent(s, P.ev_loaded[(r + 1) & 1][m], 0), "cudaStreamWaitEvent(loaded)");
+      const int z1 = j + 1 < nb ? P.owned[j + 1] : V.vz;
+      if (int rc2 = store_block(c, P, out, b, P.starts[j], P.owned[j], z1, kr & 1, last, plane, s)) return rc2;
+      CK(cudaEventRecord(P.ev_stored[r & 1][j], s), "cudaEventRecord(stored)");
     }
-    if (int rc = store(nb - 1)) return rc;
-    // the next round reads what every block of this one stored
-    for (int i = 0; i < 2; ++i) CK(cudaEventRecord(P.ev_end[i], P.st[i]), "cudaEventRecord(round)");
-    CK(cudaStreamWaitEvent(P.st[0], P.ev_end[1], 0), "cudaStreamWaitEvent(round)");
-    CK(cudaStreamWaitEvent(P.st[1], P.ev_end[0], 0), "cudaStreamWaitEvent(round)");
   }
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kBlockContexts; ++i) {
     CK(cudaEventRecord(P.ev_end[i], P.st[i]), "cudaEventRecord(done)");
     CK(cudaStreamWaitEvent(user, P.ev_end[i], 0), "cudaStreamWaitEvent(done)");
   }
-  // host inputs cross the link once per block per round
-  P.link_bytes += (long long)host_inputs * nb * (long long)T * plane * (long long)sizeof(float) * P.rounds;
+  // inputs read from host memory cross the link once per block per round
+  P.link_bytes += (long long)link_inputs * nb * (long long)T * plane * (long long)sizeof(float) * P.rounds;
   c->launches = launches;
   for (int q = 0; q < 3; ++q) {
     c->kind_count[q] = kind_count[q];
@@ -469,7 +549,8 @@ int paged_copy_out(hmf_ctx* c, bool labels, int node, float* out, int where, voi
     if (int rc = check_device_pointer(c, out, "output")) return rc;
   const auto& V = c->vols[0];
   const size_t bytes = (size_t)V.vx * V.vy * V.vz * sizeof(float);
-  const float* src = labels ? P.label[node] : P.sink[node];
+  const HostState& H = P.host[P.final_copy];
+  const float* src = labels ? H.label[node] : H.sink[node];
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (where == HMF_DEVICE) {
     CK(cudaMemcpyAsync(out, src, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(paged output)");
@@ -489,13 +570,16 @@ using namespace hmfi;
 
 extern "C" {
 
-int hmf_set_paged_plan(hmf_ctx* c, int block_planes, int round_iterations) {
+int hmf_set_paged_plan(hmf_ctx* c, int block_planes, int round_iterations, int inputs) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
   if (!c->pg) return fail(c, HMF_ERR_STATE, "hmf_set_paged_plan needs an out-of-core context (hmf_create_paged)");
   if (block_planes < 0 || round_iterations < 0)
     return fail(c, HMF_ERR_INVALID_ARGUMENT, "block planes and iterations per round must be >= 0");
+  if (inputs != HMF_PAGED_INPUTS_AUTO && inputs != HMF_PAGED_INPUTS_HOST && inputs != HMF_PAGED_INPUTS_DEVICE)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "unknown input placement");
   c->pg->forced_planes = block_planes;
   c->pg->forced_iterations = round_iterations;
+  c->pg->inputs_mode = inputs;
   return HMF_OK;
 }
 

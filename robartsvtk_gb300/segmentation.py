@@ -316,10 +316,14 @@ class HMFSolver:
     def device_bytes(self) -> int:
         return int(self._lib.hmf_device_bytes(self._ctx))
 
-    def set_paged_plan(self, block_planes: int = 0, round_iterations: int = 0) -> None:
+    def set_paged_plan(self, block_planes: int = 0, round_iterations: int = 0, inputs: str = "auto") -> None:
         """Out-of-core contexts: planes per block and iterations per round of
-        later solves (0: from the budget)."""
-        check(self._lib.hmf_set_paged_plan(self._ctx, int(block_planes), int(round_iterations)), self._ctx)
+        later solves (0: from the budget), and where host inputs are read from
+        ("auto", "host": over the link every round, "device": copied to the
+        device once per solve)."""
+        mode = {"auto": _capi.HMF_PAGED_INPUTS_AUTO, "host": _capi.HMF_PAGED_INPUTS_HOST,
+                "device": _capi.HMF_PAGED_INPUTS_DEVICE}[inputs]
+        check(self._lib.hmf_set_paged_plan(self._ctx, int(block_planes), int(round_iterations), mode), self._ctx)
 
     def paged_plan(self) -> dict:
         """Out-of-core contexts: the plan of the last solve and the bytes it

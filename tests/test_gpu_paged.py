@@ -65,9 +65,9 @@ def _in_core(w, semantics=REF_CUDA, **kw):
         return out
 
 
-def _paged(w, semantics=REF_CUDA, plan=(0, 0), usage=0.75, **kw):
+def _paged(w, semantics=REF_CUDA, plan=(0, 0), usage=0.75, inputs="auto", **kw):
     with HMFSolver(w.dims, w.parent, semantics, max_gpu_usage=usage) as s:
-        s.set_paged_plan(*plan)
+        s.set_paged_plan(*plan, inputs=inputs)
         keep = _fill(s, w, **kw)
         s.solve()
         out = _outputs(s, w)
@@ -82,18 +82,20 @@ def _assert_same(a, b):
             assert np.array_equal(a[part][v], b[part][v]), (part, v)
 
 
+@pytest.mark.parametrize("inputs", ["host", "device"])
 @pytest.mark.parametrize("dims,plan,iterations,blocks", [
     ((37, 19, 45), (20, 2), 13, 4),   # rounds 2,2,2,2,2,2,1
     ((37, 19, 50), (20, 2), 13, 4),   # every block owns planes exactly 2k+1 from its top face
     ((40, 24, 61), (28, 3), 10, 4),   # rounds 3,3,3,1
     ((33, 17, 29), (12, 1), 4, 4),    # the thinnest blocks for one iteration per round
+    ((44, 20, 96), (20, 2), 9, 9),    # nine blocks: each block context takes three
     ((32, 16, 20), (64, 0), 12, 1),   # one block covers the volume: one round
     ((37, 19, 45), (64, 3), 13, 1),   # one block, rounds of 3: the state crosses the host link
 ])
-def test_paged_plans_equal_the_in_core_solve(dims, plan, iterations, blocks):
+def test_paged_plans_equal_the_in_core_solve(dims, plan, iterations, blocks, inputs):
     w = random_tree_problem(21, dims, PARENT, iterations=iterations, smooth_nodes=(1, 4))
     ref = _in_core(w)
-    got, info = _paged(w, plan=plan)
+    got, info = _paged(w, plan=plan, inputs=inputs)
     assert info["blocks"] == blocks
     _assert_same(got, ref)
     assert info["link_bytes"] > 0
@@ -107,15 +109,39 @@ def test_paged_device_inputs_and_shared_smoothness():
     _assert_same(got, ref)
 
 
+def test_paged_pinned_host_inputs_read_over_the_link():
+    """Inputs in pinned host memory (torch pin_memory) are read in place by
+    every block of every round."""
+    import torch
+    w = random_tree_problem(30, (36, 20, 48), PARENT, iterations=7, smooth_nodes=(2,))
+    ref = _in_core(w)
+    pinned = {k: torch.from_numpy(v).pin_memory() for k, v in w.data.items()}
+    spinned = {k: torch.from_numpy(v).pin_memory() for k, v in w.smooth.items()}
+    with HMFSolver(w.dims, w.parent, REF_CUDA, max_gpu_usage=0.75) as s:
+        s.set_paged_plan(20, 2, inputs="host")
+        for leaf, t in pinned.items():
+            s.set_data(leaf, t)
+        for v, t in spinned.items():
+            s.set_smoothness(v, t)
+        for v, a in w.alpha.items():
+            s.set_smoothness_scalar(v, a)
+        s.set_params(w.iterations, w.step, w.cc)
+        s.solve()
+        got = _outputs(s, w)
+    _assert_same(got, ref)
+
+
 def test_paged_plan_from_a_memory_budget():
-    """A MaxGPUUsage budget that holds two blocks of ~20 planes: the plan
-    comes from the budget, and the device memory stays within it."""
+    """A MaxGPUUsage budget that holds three blocks of ~20 planes and the
+    inputs: the plan comes from the budget, and the device memory stays
+    within it."""
     import torch
     w = random_tree_problem(23, (64, 48, 80), [-1, 0, 0, 1, 1, 2, 2], iterations=9, smooth_nodes=(1,))
     total = torch.cuda.get_device_properties(0).total_memory
     pitch = 64
     per_plane = (9 * 6 + 1 + 4 + 1) * pitch * 48 * 4
-    budget = 2 * (16 << 20) + 2 * 20 * per_plane
+    inputs = 5 * 64 * 48 * 80 * 4
+    budget = 3 * (16 << 20) + inputs + 3 * 20 * per_plane
     usage = budget / total
     ref = _in_core(w)
     with HMFSolver(w.dims, w.parent, REF_CUDA, max_gpu_usage=usage) as s:
