@@ -192,18 +192,19 @@ adj_flow_tma_kernel(const AdjFlowVertex* __restrict__ vertices, const AdjFlowPar
   auto wait_pz0 = [&](int p) {
     wait0(&zbars[(p - kstart) % kAfPzSlots], (unsigned)(((p - kstart) / kAfPzSlots) & 1));
   };
-  // every thread that issues copies acquires the maps it uses
-  if (threadIdx.x == 0) {
-    for (int a = 0; a < narr; ++a) tensormap_acquire(main_map(a));
-    tensormap_acquire(&V->pz);
-  } else if (lane == 0) {
-    if (warp < narr) tensormap_acquire(warp_map);
-    if (warp == kAfWarps - 1) tensormap_acquire(&V->pz);
+  // Lane 0 of warp a issues every copy of main-ring array a, lane 0 of the
+  // last warp every z-flow copy; each first acquires the one map it uses.
+  if (lane == 0) {
+    if (warp < narr) {
+      tensormap_acquire(warp_map);
+      for (int p = kstart; p <= min(kstart + kAfMainLead - 1, kA_end); ++p) issue_main_array(p, warp, warp_map);
+    }
+    if (warp == kAfWarps - 1) {
+      tensormap_acquire(&V->pz);
+      for (int p = kstart; p <= min(kstart + kAfPzLead, kpz_end); ++p) issue_pz(p);
+    }
   }
   if (threadIdx.x == 0) {
-    for (int p = kstart; p <= min(kstart + kAfMainLead - 1, kA_end); ++p)
-      for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
-    for (int p = kstart; p <= min(kstart + kAfPzLead, kpz_end); ++p) issue_pz(p);
     wait_main0(kstart);
     wait_pz0(kstart);
     if (kstart + 1 < G.vz) wait_pz0(kstart + 1);

@@ -174,21 +174,21 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     }
   };
 
-  // every thread that issues copies acquires the maps it uses
-  if (threadIdx.x == 0) {
-    for (int a = 0; a < narr; ++a) tensormap_acquire(main_map(a));
-    tensormap_acquire(&V->flow_in[par][2]);
-  } else if (lane == 0) {
-    if (warp < narr) tensormap_acquire(warp_map);
-    if (warp == W - 1) tensormap_acquire(&V->flow_in[par][2]);
+  // Lane 0 of warp a issues every copy of main-ring array a, lane 0 of the
+  // last warp every z-flow copy; each first acquires the one map it uses
+  // (the acquires run side by side in their warps).
+  if (lane == 0) {
+    if (warp < narr) {
+      tensormap_acquire(warp_map);
+      for (int p = kstart; p <= min(kstart + kTmaMainLead - 1, kmain_end); ++p) issue_main_array(p, warp, warp_map);
+    }
+    if (warp == W - 1) {
+      tensormap_acquire(&V->flow_in[par][2]);
+      for (int p = kstart; p <= min(kstart + kTmaPzLead, kpz_end); ++p) issue_pz(p);
+    }
   }
-  if (threadIdx.x == 0) {
-    for (int p = kstart; p <= min(kstart + kTmaMainLead - 1, kmain_end); ++p)
-      for (int a = 0; a < narr; ++a) issue_main_array(p, a, main_map(a));
-    for (int p = kstart; p <= min(kstart + kTmaPzLead, kpz_end); ++p) issue_pz(p);
-    // the failure path on demand: a wait on a barrier that no copy completes
-    if (stall_cta) wait_on(stall_bar, 0);
-  }
+  // the failure path on demand: a wait on a barrier that no copy completes
+  if (threadIdx.x == 0 && stall_cta) wait_on(stall_bar, 0);
 
   // A window whose 32 x 32 columns/rows all lie strictly inside the volume
   // (not on its first or last column/row) needs none of the x / y boundary
