@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--adjoint-iterations", type=int, default=300)
     ap.add_argument("--no-dag", action="store_true", help="skip the DAG solver measurement")
     ap.add_argument("--no-paged", action="store_true", help="skip the out-of-core solve measurement")
+    ap.add_argument("--no-large-forward", action="store_true",
+                    help="skip the forward solve of the 512x512x384 tree8 workload")
     ap.add_argument("--paged-planes", type=int, default=96,
                     help="block planes the out-of-core leg's MaxGPUUsage budget is sized for")
     ap.add_argument("--no-dataterm", action="store_true", help="skip the data-term producer measurement")
@@ -404,6 +406,7 @@ def run_ours(args):
 
     e2e_step()
     replicas.barrier()
+    link = host_link_bandwidth(h_data[w.leaves[0]], stream)
     e_steps = max(3, min(args.steps, 5))
     marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(e_steps)]
     e2 = torch.cuda.Event(enable_timing=True)
@@ -507,7 +510,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms, "solve_with_input_copies_ms": e2e_solve_ms,
                 "copy_out_and_host_gaps_ms": e2e_rank_ms - e2e_solve_ms, "over_device_resident": e2e_rank_ms / ms_rank - 1.0,
-                "clocks": e2e_clock_info},
+                "host_link": link, "clocks": e2e_clock_info},
         "gpu_launches": launches,
         "clocks": clock_info,
         "roofline": roofline,
@@ -527,6 +530,8 @@ def run_ours(args):
         out["dataterm"] = bench_dataterm(args, stream)
     if rank == 0 and not args.no_dag:
         out["dag"] = bench_dag(args, stream, None if args.no_cpu_baseline else host_threads())
+    if rank == 0 and not args.no_large_forward:
+        out["large_forward"] = bench_large_forward(args)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
         cb = cpu_ref_cuda_sample(w, args.cpu_seconds, host_threads())
@@ -543,6 +548,29 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def host_link_bandwidth(pinned, stream, reps=4):
+    """Host <-> device copy rate of this machine right before the end-to-end leg:
+    `reps` copies of one pinned input volume each way, CUDA events (the
+    end-to-end time depends on it, and it varies between boxes)."""
+    import torch
+
+    dev = torch.empty_like(pinned, device="cuda")
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with torch.cuda.stream(stream):
+        dev.copy_(pinned, non_blocking=True)
+        e[0].record(stream)
+        for _ in range(reps):
+            dev.copy_(pinned, non_blocking=True)
+        e[1].record(stream)
+        for _ in range(reps):
+            pinned.copy_(dev, non_blocking=True)
+        e[2].record(stream)
+    stream.synchronize()
+    nbytes = reps * pinned.numel() * 4
+    return {"h2d_gbs": nbytes / e[0].elapsed_time(e[1]) / 1e6, "d2h_gbs": nbytes / e[1].elapsed_time(e[2]) / 1e6,
+            "bytes_per_copy": pinned.numel() * 4}
 
 
 def bench_paged(args, w, in_core, h_data, h_smooth, in_core_value, device_stream):
@@ -817,14 +845,13 @@ def backward_bytes_per_step(w):
     return 4.0 * w.nvox * (sweep + flow)
 
 
-def run_large(args):
-    """512x512x384 CT-like phantom, tree root -> 2 -> 4 -> 8 (14 non-root
+def large_forward(args):
+    """The 512x512x384 CT-like phantom, tree root -> 2 -> 4 -> 8 (14 non-root
     vertices, 8 leaves), one shared per-voxel smoothness image, 400
-    iterations: one forward solve, then hmf_solve_adjoint with the automatic
-    plan (every state kept if it fits, else the fewest-forward-iterations
-    schedule over the state slots that fit in 85% of the free HBM).  Inputs
-    are resident on the device; times are CUDA events on one stream."""
-    import numpy as np
+    iterations, solved forward once after a 5-iteration warm-up (inputs
+    resident on the device, CUDA events on one stream), with per-kernel
+    averages of a 10-iteration solve timed launch by launch.  Returns the
+    workload, the solver (still holding the state) and the forward record."""
     import torch
 
     from robartsvtk_gb300 import HMFSolver, synthetic
@@ -838,15 +865,75 @@ def run_large(args):
     d = {leaf: torch.from_numpy(a).cuda() for leaf, a in w.data.items()}
     S = torch.from_numpy(next(iter(w.smooth.values()))).cuda()
     s = HMFSolver(w.dims, w.parent)
-    # phantom class k is leaf 7 + k; the adjoint's truth indexes s.leaves
-    order = np.array([s.leaves.index(leaf) for leaf in sorted(w.data)], dtype=np.int32)
-    truth = torch.from_numpy(order[w.truth]).cuda()
+    s._bench_inputs = (d, S)  # keep the device inputs alive with the solver
     for leaf, t in d.items():
         s.set_data(leaf, t)
     for v in w.smooth:
         s.set_smoothness(v, S)
     for v, a in w.alpha.items():
         s.set_smoothness_scalar(v, a)
+    s.set_params(5, w.step, w.cc)
+    s.solve(stream)  # warm-up (tables, first launches)
+    s.set_params(w.iterations, w.step, w.cc)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.solve(stream)
+    e1.record(stream)
+    stream.synchronize()
+    t_fwd = e0.elapsed_time(e1)
+    T = w.iterations
+    s.set_params(min(T, 10), w.step, w.cc)
+    s.set_timing(True)
+    s.solve(stream)
+    kstats = s.stats()
+    s.set_timing(False)
+    s.set_params(T, w.step, w.cc)
+    vli = w.nvox * len(w.leaves) * T
+    b_iter = compulsory_bytes_per_iteration(w)
+    fwd = {"workload": "ellipsoids%dx%dx%d_tree8" % tuple(w.dims), "volume": list(w.dims), "vertices": len(w.parent),
+           "leaves": len(w.leaves), "iterations": T, "data": "synthetic (seeded phantom)", "generate_s": gen_s,
+           "ms": t_fwd, "value": vli / (t_fwd / 1000.0), "unit": "voxel*label*iter/s",
+           "bytes_per_iteration": b_iter, "achieved_gbs": b_iter * T / (t_fwd / 1000.0) / 1e9,
+           "frac": b_iter * T / (t_fwd / 1000.0) / 1e9 / peak, "peak_gbs": peak, "peak_source": peak_kind,
+           "flow_kernel_ms": kstats["flow_ms"], "tree_kernel_ms": kstats["tree_ms"],
+           "device_bytes": s.device_bytes()}
+    return w, s, stream, fwd
+
+
+def bench_large_forward(args):
+    """The large forward solve of `large_forward` inside the default run, with
+    the agreement of its label vote with the phantom's classes."""
+    import numpy as np
+    import torch
+
+    w, s, stream, fwd = large_forward(args)
+    vote = torch.empty(w.dims[::-1], dtype=torch.int32, device="cuda")
+    s.vote(out=vote, stream=stream)
+    stream.synchronize()
+    leaf_of_class = torch.tensor(sorted(w.data), dtype=torch.int32, device="cuda")
+    truth = leaf_of_class[torch.from_numpy(w.truth.astype(np.int64)).cuda()]
+    fwd["vote_agrees_with_phantom"] = float((vote == truth).float().mean().item())
+    s.close()
+    del vote, truth
+    torch.cuda.empty_cache()
+    return fwd
+
+
+def run_large(args):
+    """The large forward solve (large_forward), then hmf_solve_adjoint with
+    the automatic plan (every state kept if it fits, else the
+    fewest-forward-iterations schedule over the state slots that fit in the
+    free HBM less a margin).  Times are CUDA events on one stream."""
+    import numpy as np
+    import torch
+
+    w, s, stream, fwd = large_forward(args)
+    peak, peak_kind = measured_peak_hbm()
+    # phantom class k is leaf 7 + k; the adjoint's truth indexes s.leaves
+    order = np.array([s.leaves.index(leaf) for leaf in sorted(w.data)], dtype=np.int32)
+    truth = torch.from_numpy(order[w.truth]).cuda()
 
     def timed(fn):
         stream.synchronize()
@@ -858,20 +945,9 @@ def run_large(args):
         stream.synchronize()
         return e0.elapsed_time(e1), r
 
-    s.set_params(5, w.step, w.cc)
-    s.solve(stream)  # warm-up (tables, first launches)
-    s.set_params(w.iterations, w.step, w.cc)
-    t_fwd, _ = timed(lambda: s.solve(stream))
     T = w.iterations
-    # per-kernel averages of a short solve with per-launch events
-    s.set_params(min(T, 10), w.step, w.cc)
-    s.set_timing(True)
-    s.solve(stream)
-    kstats = s.stats()
-    s.set_timing(False)
-    s.set_params(T, w.step, w.cc)
+    t_fwd = fwd["ms"]
     vli = w.nvox * len(w.leaves) * T
-    b_iter = compulsory_bytes_per_iteration(w)
     # the adjoint may use the free device memory but a margin (the library's
     # default budget is 85% of it): every state slot saves forward passes
     free_b, _ = torch.cuda.mem_get_info()
@@ -882,12 +958,7 @@ def run_large(args):
     t_bwd = t_adj - plan["forward_iterations"] * t_it
     b_bwd = backward_bytes_per_step(w)
     out = {
-        "workload": "ellipsoids%dx%dx%d_tree8" % tuple(w.dims), "volume": list(w.dims), "vertices": len(w.parent),
-        "leaves": len(w.leaves), "iterations": T, "data": "synthetic (seeded phantom)", "generate_s": gen_s,
-        "forward": {"ms": t_fwd, "value": vli / (t_fwd / 1000.0), "unit": "voxel*label*iter/s",
-                    "bytes_per_iteration": b_iter, "achieved_gbs": b_iter * T / (t_fwd / 1000.0) / 1e9,
-                    "frac": b_iter * T / (t_fwd / 1000.0) / 1e9 / peak,
-                    "flow_kernel_ms": kstats["flow_ms"], "tree_kernel_ms": kstats["tree_ms"]},
+        "workload": fwd["workload"], "forward": fwd,
         "adjoint": {"ms": t_adj, "ratio_to_forward": t_adj / t_fwd, "loss": loss, **plan,
                     "device_bytes": s.device_bytes(),
                     "backward_ms": t_bwd,
