@@ -12,6 +12,7 @@
 //   n_alpha  (node alpha) x n_alpha
 //   n_data   (node file)  x n_data
 //   n_smooth (node file)  x n_smooth
+//   [max_gpu_usage]       (optional: SetMaxGPUUsage, an out-of-core solve)
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -80,6 +81,8 @@ int main(int argc, char** argv) {
     inputs[-1 - node] = read_raw(dir + "/" + file, nvox);
     filter.SetSmoothnessInputDataObject(node, inputs[-1 - node].data(), dims);
   }
+  double usage;
+  if (spec >> usage) filter.SetMaxGPUUsage(usage);
 
   const int rc = filter.Update();
   std::ofstream status(dir + "/status.txt");

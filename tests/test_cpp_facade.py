@@ -4,8 +4,8 @@ libhmf_gb300.so, as a VTK-free C++ application would use it.
 
 CPU: the program compiles and links against the header and the library.
 GPU: Update() on a seeded problem equals the oracle bit for bit, REF_CUDA
-and REF_CPU semantics; a missing leaf input fails with the reference's
-message and Update's -1.
+and REF_CPU semantics, in core and with SetMaxGPUUsage (out of core); a
+missing leaf input fails with the reference's message and Update's -1.
 """
 import os
 import subprocess
@@ -30,7 +30,7 @@ def _compile(out_dir) -> str:
     return exe
 
 
-def _write_spec(d, w, semantics, leaves_with_data=None):
+def _write_spec(d, w, semantics, leaves_with_data=None, max_gpu_usage=None):
     lines = ["%d %d %d" % w.dims, " ".join([str(len(w.parent))] + [str(p) for p in w.parent]),
              "%d %r %r %d" % (w.iterations, float(w.step), float(w.cc), semantics)]
     lines.append(" ".join([str(len(w.alpha))] + ["%d %r" % (v, float(a)) for v, a in w.alpha.items()]))
@@ -41,6 +41,8 @@ def _write_spec(d, w, semantics, leaves_with_data=None):
     for v, S in w.smooth.items():
         S.astype(np.float32).tofile(os.path.join(d, "s%d.raw" % v))
     lines.append(" ".join([str(len(w.smooth))] + ["%d s%d.raw" % (v, v) for v in w.smooth]))
+    if max_gpu_usage is not None:
+        lines.append("%r" % float(max_gpu_usage))
     with open(os.path.join(d, "spec.txt"), "w") as f:
         f.write("\n".join(lines) + "\n")
 
@@ -50,12 +52,13 @@ def test_facade_compiles_and_links(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("semantics", [0, 1])
-def test_facade_update_matches_the_oracle(tmp_path, semantics):
+@pytest.mark.parametrize("semantics,max_gpu_usage", [(0, None), (1, None), (0, 0.5), (1, 0.5)])
+def test_facade_update_matches_the_oracle(tmp_path, semantics, max_gpu_usage):
+    """Update() in core and, with SetMaxGPUUsage, out of core."""
     from oracle import oracle as O
     exe = _compile(tmp_path)
     w = random_tree_problem(61, (27, 14, 11), [-1, 0, 0, 1, 1, 2, 2], iterations=20, smooth_nodes=(1, 5))
-    _write_spec(str(tmp_path), w, semantics)
+    _write_spec(str(tmp_path), w, semantics, max_gpu_usage=max_gpu_usage)
     subprocess.run([exe, str(tmp_path)], check=True)
     status = open(os.path.join(tmp_path, "status.txt")).read().split("\n")
     assert status[0] == "1", status

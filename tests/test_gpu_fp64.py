@@ -14,7 +14,7 @@ import pytest
 from oracle import oracle as O
 from robartsvtk_gb300 import REF_CPU, HMFBatchSolver, HMFError, HMFSolver
 from robartsvtk_gb300._capi import HMF_FP64_PROBE_ALPHA, HMF_FP64_PROBE_DATA, check
-from robartsvtk_gb300.synthetic import ellipsoids_tree4, random_tree_problem
+from robartsvtk_gb300.synthetic import ellipsoids_tree4, ellipsoids_tree8, random_tree_problem
 from tests.golden.cases import CASES, problem
 
 pytestmark = pytest.mark.gpu
@@ -157,3 +157,24 @@ def test_ellipsoids256_tree4_full_length_parity():
           % (err, identical, agree, e64["max_abs_err"], e64["argmax_agreement"]))
     assert err <= LABEL_TOL and agree >= 0.999
     assert e64["argmax_agreement"] >= 0.999
+
+
+def test_ellipsoids_tree8_three_level_tree_parity():
+    """The three-level tree of the 512x512x384 workload (root -> 2 -> 4 -> 8,
+    14 flows, 15-entry sweep) on a 256x256x192 crop of its phantom
+    generator, 40 iterations: the GPU's FP32 labels bit-identical to the
+    FP32 oracle, and the FP64 GPU solve's distance stated."""
+    w = ellipsoids_tree8(seed=5, dims=(256, 256, 192), iterations=40)
+    with HMFSolver(w.dims, w.parent) as s:
+        _configure(s, w)
+        s.solve()
+        u32 = np.stack([s.labels(l) for l in w.leaves])
+        s.solve_fp64()
+        e64 = s.fp64_error()
+    ref = O.solve(w.dims, w.parent, w.data, w.smooth, w.alpha, w.iterations, w.step, w.cc)["u"][w.leaves]
+    identical = bool(np.array_equal(u32, ref.astype(np.float32)))
+    print("ellipsoids256x256x192_tree8 40 it: bit-identical to the oracle: %s; max|u_gpu - u_fp64| %.3g, argmax "
+          "agreement with FP64 %.6f" % (identical, e64["max_abs_err"], e64["argmax_agreement"]))
+    assert identical
+    assert e64["argmax_agreement"] >= 0.999
+
