@@ -336,6 +336,9 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
     T = (int)std::min<size_t>((size_t)V.vz, (budget - fixed) / (kBlockContexts * per_plane));
   }
   T = std::min(T, V.vz);
+  // a block context addresses its elements with 32-bit offsets
+  T = (int)std::min<long long>(T, ((1LL << 31) - 1) / ((long long)V.pitch * V.vy));
+  if (T < 1) return fail(c, HMF_ERR_INVALID_ARGUMENT, "one plane of the volume holds 2^31 elements or more");
   int k;
   if (cpu) {
     k = c->iterations;  // per-voxel iterations (REF_CPU): no halo, one round

@@ -224,3 +224,20 @@ def test_filter_facade_with_max_gpu_usage():
         outs.append({leaf: f.GetOutputDataObject(leaf).copy() for leaf in w.leaves})
     for leaf in w.leaves:
         assert np.array_equal(outs[0][leaf], outs[1][leaf])
+
+
+def test_paged_zero_iterations_and_a_budget_too_small():
+    """Zero iterations: every block initialises only, equal to the in-core
+    initialisation.  A budget below three blocks of planes is refused before
+    any device work."""
+    w = random_tree_problem(32, (30, 16, 40), PARENT, iterations=0, smooth_nodes=(1,))
+    ref = _in_core(w)
+    got, info = _paged(w, plan=(12, 0))
+    assert info["rounds"] == 1 and info["round_iterations"] == 0
+    _assert_same(got, ref)
+    with HMFSolver(w.dims, w.parent, REF_CUDA, max_gpu_usage=1e-9) as s:
+        keep = _fill(s, w)
+        with pytest.raises(HMFError, match="MaxGPUUsage"):
+            s.solve()
+        del keep
+
