@@ -532,8 +532,12 @@ def run_ours(args):
         out["dag"] = bench_dag(args, stream, None if args.no_cpu_baseline else host_threads())
     if rank == 0 and not args.no_large_forward:
         out["large_forward"] = bench_large_forward(args)
+    if rank == 0:
+        out["ref_cpu_semantics_gpu"] = bench_ref_cpu_semantics(w, d_data, d_smooth, stream)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(w, args.cpu_seconds, host_threads())
+        out["ref_cpu_semantics_gpu"]["ratio_to_cpu_baseline"] = (out["ref_cpu_semantics_gpu"]["value"]
+                                                                 / out["cpu_baseline"]["value"])
         cb = cpu_ref_cuda_sample(w, args.cpu_seconds, host_threads())
         cb["ratio"] = value / cb["value"]
         out["cpu_baseline_ref_cuda"] = cb
@@ -548,6 +552,38 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def bench_ref_cpu_semantics(w, d_data, d_smooth, device_stream, reps=3):
+    """The computation the reference arm times -- the reference CPU class as
+    written (REF_CPU semantics) -- on the GPU, same workload and inputs:
+    the like-for-like counterpart of cpu_baseline (CUDA events, 3 solves
+    after a warm one)."""
+    import torch
+
+    from robartsvtk_gb300 import REF_CPU, HMFSolver
+
+    s = HMFSolver(w.dims, w.parent, REF_CPU)
+    for leaf, t in d_data.items():
+        s.set_data(leaf, t)
+    for v, t in d_smooth.items():
+        s.set_smoothness(v, t)
+    for v, a in w.alpha.items():
+        s.set_smoothness_scalar(v, a)
+    s.set_params(w.iterations, w.step, w.cc)
+    s.solve(device_stream)
+    device_stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(device_stream)
+    for _ in range(reps):
+        s.solve(device_stream)
+    e1.record(device_stream)
+    device_stream.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    s.close()
+    return {"what": "REF_CPU semantics (the reference CPU class's computation) on the GPU, device-resident inputs",
+            "ms_per_solve": ms, "value": w.nvox * len(w.leaves) * w.iterations / (ms / 1000.0), "unit": UNIT}
 
 
 def host_link_bandwidth(pinned, stream, reps=4):
