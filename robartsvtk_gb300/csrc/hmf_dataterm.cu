@@ -23,6 +23,8 @@
 #include <cstdint>
 #include <cstring>
 #include <initializer_list>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -254,15 +256,48 @@ __global__ void ll_out_kernel(const LLParams P, const Hist H, const float* __res
 }
 
 // Device copies of host inputs for one call.
+// Scratch of one call, drawn from a memory pool of the library's own (one
+// per device, keeping up to 256 MB between calls) and returned to it in
+// stream order: no cudaMalloc / cudaFree per call, whose implicit device
+// synchronisation would also stall the caller's other streams.
+cudaMemPool_t scratch_pool() {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props;
+  std::memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    cudaGetLastError();
+    pool = nullptr;  // plain cudaMalloc then
+  } else {
+    unsigned long long keep = 256ull << 20;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  pools[dev] = pool;
+  return pool;
+}
+
 struct Scratch {
+  explicit Scratch(cudaStream_t s) : stream(s), pool(scratch_pool()) {}
+  cudaStream_t stream;
+  cudaMemPool_t pool;
   std::vector<void*> bufs;
   ~Scratch() {
-    for (void* p : bufs) cudaFree(p);
+    for (void* p : bufs) pool ? cudaFreeAsync(p, stream) : cudaFree(p);
   }
   template <class T>
   cudaError_t alloc(T** out, size_t count) {
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, count * sizeof(T), pool, stream)
+                         : cudaMalloc(&p, count * sizeof(T));
     if (e == cudaSuccess) bufs.push_back(p);
     *out = static_cast<T*>(p);
     return e;
@@ -319,7 +354,7 @@ int hmf_data_term(int op, int entropy, int normalize, double k1, double c1, doub
     P.c1 = lg ? -std::log(c1) : c1;
     P.c2 = lg ? -std::log(c2) : c2;
   }
-  Scratch sc;
+  Scratch sc(s);
   const float* d1 = nullptr;
   const float* d2 = nullptr;
   float* dout = out;
@@ -415,7 +450,7 @@ int hmf_log_likelihood(const float* image, int components, const int* const* lab
   P.label_id = label_id;
   P.resolution = resolution;
   LLMaps M{};
-  Scratch sc;
+  Scratch sc(s);
   const float* img = nullptr;
   float* dout = out;
   cudaError_t e = sc.bring(image, (size_t)n_voxels * components, where, &img, s);
@@ -512,10 +547,9 @@ int hmf_log_likelihood(const float* image, int components, const int* const* lab
     ll_out_kernel<<<grid_for(n_voxels), kThreads, 0, s>>>(P, H, img, cost, (int)bins, n_voxels, dout);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess && where == HMF_HOST) {
+  if (e == cudaSuccess && where == HMF_HOST)
     e = cudaMemcpyAsync(out, dout, sizeof(float) * (size_t)n_voxels, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the call is synchronous
   if (e != cudaSuccess) return cuda_fail(c, e, "log-likelihood kernels");
   return HMF_OK;
 }
