@@ -938,9 +938,13 @@ def large_forward(args):
     return w, s, stream, fwd
 
 
-def bench_large_forward(args):
+def bench_large_forward(args, adjoint_iterations=40):
     """The large forward solve of `large_forward` inside the default run, with
-    the agreement of its label vote with the phantom's classes."""
+    the agreement of its label vote with the phantom's classes; then the
+    adjoint w.r.t. the data terms on the same volume and tree over
+    `adjoint_iterations` iterations (400 take ~100 s: bench.py --large), its
+    automatic plan in the free HBM less a margin, to state the backward
+    step's throughput and HBM fraction at this shape."""
     import numpy as np
     import torch
 
@@ -949,10 +953,40 @@ def bench_large_forward(args):
     s.vote(out=vote, stream=stream)
     stream.synchronize()
     leaf_of_class = torch.tensor(sorted(w.data), dtype=torch.int32, device="cuda")
-    truth = leaf_of_class[torch.from_numpy(w.truth.astype(np.int64)).cuda()]
-    fwd["vote_agrees_with_phantom"] = float((vote == truth).float().mean().item())
+    truth_leaf = leaf_of_class[torch.from_numpy(w.truth.astype(np.int64)).cuda()]
+    fwd["vote_agrees_with_phantom"] = float((vote == truth_leaf).float().mean().item())
+    del vote, truth_leaf
+    if adjoint_iterations > 0:
+        peak, _ = measured_peak_hbm()
+        order = np.array([s.leaves.index(leaf) for leaf in sorted(w.data)], dtype=np.int32)
+        truth = torch.from_numpy(order[w.truth]).cuda()
+        T = adjoint_iterations
+        s.set_params(T, w.step, w.cc)
+        free_b, _ = torch.cuda.mem_get_info()
+        s.set_adjoint_memory(max_bytes=max(0, free_b - (6 << 30)))
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.solve_adjoint(truth, stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        t_adj = e0.elapsed_time(e1)
+        plan = s.adjoint_plan()
+        t_it = fwd["ms"] / fwd["iterations"]
+        t_bwd = t_adj - plan["forward_iterations"] * t_it
+        b_bwd = backward_bytes_per_step(w)
+        vli = w.nvox * len(w.leaves) * T
+        fwd["adjoint"] = {"iterations": T, "ms": t_adj, **plan, "device_bytes": s.device_bytes(),
+                          "backward_ms": t_bwd, "backward_ms_per_step": t_bwd / T,
+                          "backward_note": "adjoint time minus the schedule's forward iterations at the forward "
+                                           "solve's per-iteration time",
+                          "backward_value": vli / (t_bwd / 1000.0), "unit": UNIT,
+                          "backward_bytes_per_step": b_bwd,
+                          "backward_achieved_gbs": b_bwd * T / (t_bwd / 1000.0) / 1e9,
+                          "backward_frac": b_bwd * T / (t_bwd / 1000.0) / 1e9 / peak}
+        del truth
     s.close()
-    del vote, truth
     torch.cuda.empty_cache()
     return fwd
 
