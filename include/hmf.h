@@ -214,7 +214,8 @@ int hmf_batch_get_sink(hmf_ctx* ctx, int volume, int node, float* out, int where
 
 /* Autotuner (no counterpart in the reference): times a few iterations of the
  * flow kernel for each window shape (hmf_set_flow_window) and candidate
- * z-chunk length (planes per CTA column) on the context's current inputs,
+ * z-chunk length (planes per CTA column), then the best of those with 2 and
+ * 4 units per CTA (hmf_set_flow_units), on the context's current inputs,
  * keeps the fastest for this context and caches it for contexts of the same
  * shape created later (key: SM count, semantics, tree shape, volume sizes
  * rounded up to multiples of 16).  The cache lives for the process; with the
@@ -231,6 +232,14 @@ int hmf_get_zchunk(const hmf_ctx* ctx);
  * z chunk returns to its default plan for the shape. */
 int hmf_set_flow_window(hmf_ctx* ctx, int rows);
 int hmf_get_flow_window(const hmf_ctx* ctx);
+/* Units of flow-kernel work per CTA: a unit is one vertex's z-march over one
+ * window and z chunk; a CTA marches `units` of them one after another (the
+ * vertices of a window first, so that their shared parent sinks and
+ * smoothness planes come from L2), in 1..64 (0 restores 1).  Fewer, longer
+ * CTAs save per-CTA set-up on small volumes and batches; hmf_autotune times
+ * 1, 2 and 4 with its best window and chunk.  Results do not depend on it. */
+int hmf_set_flow_units(hmf_ctx* ctx, int units);
+int hmf_get_flow_units(const hmf_ctx* ctx);
 /* Slab pipeline of the replayed iterations (single volumes of label trees,
  * REF_CUDA, convergence log off): each iteration's flow and sweep launches
  * are cut at the flow plan's z chunks into per-slab graph nodes that wait

@@ -78,6 +78,8 @@ SIGNATURES = [
     ("hmf_get_pipeline", _I, [_P]),
     ("hmf_set_flow_window", _I, [_P, _I]),
     ("hmf_get_flow_window", _I, [_P]),
+    ("hmf_set_flow_units", _I, [_P, _I]),
+    ("hmf_get_flow_units", _I, [_P]),
     ("hmf_get_adjoint_schedule", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_longlong),
                                       ctypes.POINTER(ctypes.c_longlong)]),
     ("hmf_adjoint_schedule", ctypes.c_longlong, [_I, _I, _I, ctypes.POINTER(_I), ctypes.c_longlong]),

@@ -53,6 +53,7 @@ constexpr int kMaxDim = 1 << 30;
 constexpr int kTX = 32, kTY = 8;
 constexpr int kPipelineIterations = 32;  // iterations per replayed graph of a pipelined solve (even)
 constexpr int kTuneIterations = 8;      // iterations of each solve the autotuner times
+constexpr int kMaxFlowUnits = 64;       // units (window-vertex marches) one flow CTA may take
 constexpr int kTreeThreads = 256;
 
 }  // namespace
@@ -522,16 +523,29 @@ int launch_flow_tma_items(hmf_ctx* c, const hmf::FlowVertexTMA* table, int parit
   fp.icc = 1.0f / c->cc;
   fp.parity = parity;
   fp.n_vertices = c->n - 1;
+  fp.n_items = n_items;
+  fp.units_per_cta = c->flow_units;
   fp.vols = c->d_fvol;
   fp.items = c->d_items + first_item;
   fp.error_flag = c->d_error;
   fp.wait_limit_ns = c->wait_limit_ns;
   if (int rc = maybe_request_stall(c, HMF_STALL_FLOW, s)) return rc;
-  const dim3 grid((unsigned)n_items * (unsigned)(c->n - 1), 1, 1);
-  if (c->flow_warps == 16)
-    hmf::flow_tma_kernel<16><<<grid, hmf::FlowTmaShape<16>::kThreads, hmf::FlowTmaShape<16>::kSmemBytes, s>>>(table, fp);
-  else
-    hmf::flow_tma_kernel<8><<<grid, hmf::FlowTmaShape<8>::kThreads, hmf::FlowTmaShape<8>::kSmemBytes, s>>>(table, fp);
+  const long long units = (long long)n_items * (c->n - 1);
+  const dim3 grid((unsigned)((units + c->flow_units - 1) / c->flow_units), 1, 1);
+  const bool multi = c->flow_units > 1;
+  if (c->flow_warps == 16) {
+    if (multi)
+      hmf::flow_tma_kernel<16, true>
+          <<<grid, hmf::FlowTmaShape<16>::kThreads, hmf::FlowTmaShape<16>::kSmemBytes, s>>>(table, fp);
+    else
+      hmf::flow_tma_kernel<16, false>
+          <<<grid, hmf::FlowTmaShape<16>::kThreads, hmf::FlowTmaShape<16>::kSmemBytes, s>>>(table, fp);
+  } else {
+    if (multi)
+      hmf::flow_tma_kernel<8, true><<<grid, hmf::FlowTmaShape<8>::kThreads, hmf::FlowTmaShape<8>::kSmemBytes, s>>>(table, fp);
+    else
+      hmf::flow_tma_kernel<8, false><<<grid, hmf::FlowTmaShape<8>::kThreads, hmf::FlowTmaShape<8>::kSmemBytes, s>>>(table, fp);
+  }
   CK(cudaGetLastError(), "flow_tma_kernel launch");
   ++c->launches;
   return HMF_OK;
@@ -1143,10 +1157,16 @@ int configure_kernels(hmf_ctx* c) {
   CK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
      "cudaFuncSetAttribute(init_kernel)");
-  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::FlowTmaShape<8>::kSmemBytes),
      "cudaFuncSetAttribute(flow_tma_kernel)");
-  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          hmf::FlowTmaShape<16>::kSmemBytes),
+     "cudaFuncSetAttribute(flow_tma_kernel)");
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          hmf::FlowTmaShape<8>::kSmemBytes),
+     "cudaFuncSetAttribute(flow_tma_kernel)");
+  CK(cudaFuncSetAttribute(hmf::flow_tma_kernel<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           hmf::FlowTmaShape<16>::kSmemBytes),
      "cudaFuncSetAttribute(flow_tma_kernel)");
   CK(cudaFuncSetAttribute(hmf::tree4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1240,7 +1260,7 @@ int copy_out(hmf_ctx* c, int b, const float* src, float* out, int where, void* s
 // to a file path it is also read from and appended to that file (one
 // "key warps zchunk" line per tuned shape), so later processes reuse it.
 struct TunedPlan {
-  int warps, zchunk;
+  int warps, zchunk, units;
 };
 std::mutex g_tune_mutex;
 std::map<std::string, TunedPlan> g_tune_cache;
@@ -1263,10 +1283,13 @@ void tune_file_read() {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  char key[4096];
-  int w, z;
-  while (std::fscanf(f, "%4095s %d %d", key, &w, &z) == 3)
-    if ((w == 8 || w == 16) && z >= 1) g_tune_cache[key] = TunedPlan{w, z};
+  char line[4200], key[4096];
+  while (std::fgets(line, sizeof(line), f)) {
+    int w = 0, z = 0, u = 1;  // lines written before the units field read as one unit per CTA
+    if (std::sscanf(line, "%4095s %d %d %d", key, &w, &z, &u) >= 3 && (w == 8 || w == 16) && z >= 1 && u >= 1 &&
+        u <= kMaxFlowUnits)
+      g_tune_cache[key] = TunedPlan{w, z, u};
+  }
   std::fclose(f);
 }
 
@@ -1276,7 +1299,7 @@ void tune_file_append(const std::string& key, const TunedPlan& t) {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "%s %d %d\n", key.c_str(), t.warps, t.zchunk);
+  std::fprintf(f, "%s %d %d %d\n", key.c_str(), t.warps, t.zchunk, t.units);
   std::fclose(f);
 }
 
@@ -1431,6 +1454,7 @@ int create_context(hmf_ctx** out, int n_volumes, const int* dims, int semantics,
         auto it = g_tune_cache.find(tune_key(c));
         if (it != g_tune_cache.end()) {
           c->flow_warps = it->second.warps;
+          c->flow_units = it->second.units;
           z = it->second.zchunk;
         }
       }
@@ -1685,7 +1709,7 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   const bool saved_timing = c->timing;
   int maxz = 1;
   for (const auto& V : c->vols) maxz = std::max(maxz, V.vz);
-  TunedPlan best{c->flow_warps, c->zchunk};
+  TunedPlan best{c->flow_warps, c->zchunk, c->flow_units};
   double best_ms = 1e30;
   int rc = HMF_OK;
   DeviceGuard dg(c->device);
@@ -1695,34 +1719,49 @@ int hmf_autotune(hmf_ctx* c, void* stream) {
   // the plan's graphs, a second one is timed with events on the caller's
   // stream.  Candidates, for each window shape (32 x 32 and 32 x 64): the
   // default plan's chunk, then 16, 24, 32, 48, 64, 96, ... up to the longest
-  // volume.
+  // volume, one unit per CTA; then the best of those with 2 and 4 units
+  // (window-vertex marches) per CTA.
   c->timing = false;
   c->iterations = kTuneIterations;
+  auto time_plan = [&](int w, int z, int u, float* ms) -> int {
+    c->flow_warps = w;
+    c->flow_units = u;
+    drop_graphs(c);
+    int r = plan_flow(c, z);
+    if (!r) r = hmf_solve(c, stream);
+    cudaError_t e = r ? cudaSuccess : cudaEventRecord(c->ev_t0, user);
+    if (!r && e == cudaSuccess) r = hmf_solve(c, stream);
+    if (!r && e == cudaSuccess) e = cudaEventRecord(c->ev_t1, user);
+    if (!r && e == cudaSuccess) e = cudaEventSynchronize(c->ev_t1);
+    *ms = 1e30f;
+    if (!r && e == cudaSuccess) e = cudaEventElapsedTime(ms, c->ev_t0, c->ev_t1);
+    if (!r && e != cudaSuccess) r = cuda_fail(c, e, "autotune timing");
+    return r;
+  };
   for (int w : {8, 16}) {
     c->flow_warps = w;
     const int z_default = default_zchunk(c);
     for (int i = -1; rc == HMF_OK; ++i) {
       const int z = i < 0 ? z_default : std::min((i & 1 ? 24 : 16) << (i >> 1), maxz);
-      drop_graphs(c);
-      rc = plan_flow(c, z);
-      if (!rc) rc = hmf_solve(c, stream);
-      cudaError_t e = rc ? cudaSuccess : cudaEventRecord(c->ev_t0, user);
-      if (!rc && e == cudaSuccess) rc = hmf_solve(c, stream);
-      if (!rc && e == cudaSuccess) e = cudaEventRecord(c->ev_t1, user);
-      if (!rc && e == cudaSuccess) e = cudaEventSynchronize(c->ev_t1);
-      float ms = 1e30f;
-      if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1);
-      if (!rc && e != cudaSuccess) rc = cuda_fail(c, e, "autotune timing");
+      float ms = 0;
+      rc = time_plan(w, z, 1, &ms);
       if (rc) break;
-      if (ms < best_ms) best_ms = ms, best = TunedPlan{w, z};
+      if (ms < best_ms) best_ms = ms, best = TunedPlan{w, z, 1};
       if (i >= 0 && z >= maxz) break;
     }
     if (rc) break;
+  }
+  for (int u : {2, 4}) {
+    if (rc) break;
+    float ms = 0;
+    rc = time_plan(best.warps, best.zchunk, u, &ms);
+    if (!rc && ms < best_ms) best_ms = ms, best.units = u;
   }
   c->iterations = saved_iters;
   c->timing = saved_timing;
   c->solved = false;
   c->flow_warps = best.warps;
+  c->flow_units = best.units;
   if (rc) return rc;
   drop_graphs(c);
   rc = plan_flow(c, best.zchunk);
@@ -1758,6 +1797,19 @@ int hmf_set_flow_window(hmf_ctx* c, int rows) {
 }
 
 int hmf_get_flow_window(const hmf_ctx* c) { return c ? 4 * c->flow_warps : HMF_ERR_INVALID_ARGUMENT; }
+
+int hmf_set_flow_units(hmf_ctx* c, int units) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_set_flow_units")) return rc;
+  if (units < 0 || units > kMaxFlowUnits)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "units per flow CTA must lie in [0, 64]");
+  DeviceGuard dg(c->device);
+  drop_graphs(c);  // the captured launches carry the grid
+  c->flow_units = units ? units : 1;
+  return HMF_OK;
+}
+
+int hmf_get_flow_units(const hmf_ctx* c) { return c ? c->flow_units : HMF_ERR_INVALID_ARGUMENT; }
 
 int hmf_set_zchunk(hmf_ctx* c, int z) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;

@@ -69,6 +69,7 @@ struct hmf_ctx {
   int n_items = 0;
   int zchunk = 0;  // planes per window column (0: not planned yet)
   int flow_warps = 8;  // flow_tma_kernel<W>: windows of 32 x 4W (hmf_set_flow_window)
+  int flow_units = 1;  // flow_tma_kernel: (window, vertex) units marched by one CTA (hmf_set_flow_units)
   hmf::TreeTable* d_tree = nullptr;
   hmf::DagTable* d_dag = nullptr;
   bool dag_last = false;  // the next sweep is the last iteration's

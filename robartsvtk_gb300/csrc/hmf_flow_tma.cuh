@@ -46,10 +46,14 @@ __device__ __forceinline__ float projection_multiplier(float h, float lim) {
   return (F > lim) ? lim / F : 1.0f;
 }
 
+// One unit of work: the z-march of one vertex over one work item (a window
+// and z chunk of a volume); false when the CTA must stop (an earlier launch
+// or this march timed out, or the shared window is misaligned).
 // W warps per CTA: the window is 32 columns x 4W rows (FlowTmaShape<W>).
-template <int W>
-__global__ void __launch_bounds__(FlowTmaShape<W>::kThreads, FlowTmaShape<W>::kCtasPerSm)
-flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams fp) {
+template <int W, bool MULTI>
+__device__ __forceinline__ bool flow_tma_unit(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams& fp,
+                                              const int unit_arg, const bool reinit) {
+  const int unit = MULTI ? unit_arg : (int)blockIdx.x;
   constexpr int kPlane = FlowTmaShape<W>::kPlane;  // floats per staged array plane
   constexpr int kRows = FlowTmaShape<W>::kRows;
   // Pointers into the shared window are formed by pointer arithmetic only,
@@ -67,14 +71,14 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
   __shared__ int abort_cta;
   __shared__ int stop_cta;  // a copy wait ran out: the CTA stops issuing, drains its copies and leaves
 
-  // blockIdx.x = vertex + n_vertices * item: the vertices of one window run
-  // side by side, so a parent sink and a shared smoothness image read by
-  // several of them come from L2.
+  // unit = vertex + n_vertices * item: the vertices of one window run side
+  // by side (or one after another in a CTA), so a parent sink and a shared
+  // smoothness image read by several of them come from L2.
   const int nv = fp.n_vertices;
-  const FlowItem item = fp.items[blockIdx.x / nv];
+  const FlowItem item = fp.items[unit / nv];
   const FlowVolume FV = fp.vols[item.vol];
   const Geometry G = FV.G;
-  const FlowVertexTMA* V = vertices + (size_t)item.vol * nv + (blockIdx.x % nv);
+  const FlowVertexTMA* V = vertices + (size_t)item.vol * nv + (unit % nv);
   const int tile = item.tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
@@ -132,6 +136,14 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
       abort_cta = 1;
       if (fp.error_flag) atomicOr(fp.error_flag, 4);
     }
+    // a later unit of the CTA: the previous march's barriers (every phase
+    // complete, every copy landed) are invalidated before they are set up
+    // again
+    if (MULTI && reinit) {
+      for (int s = 0; s < kTmaMainSlots; ++s) mbar_inval(&mbars[s]);
+      for (int s = 0; s < kTmaPzSlots; ++s) mbar_inval(&zbars[s]);
+      mbar_inval(stall_bar);
+    }
     // one arrival per main-ring array: each array's copy is issued (with its
     // own expect_tx) by the lane 0 of its own warp
     for (int s = 0; s < kTmaMainSlots; ++s) mbar_init(&mbars[s], (unsigned)narr);
@@ -142,7 +154,7 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  if (abort_cta) return;
+  if (abort_cta) return false;
 
   auto mslot = [&](int p) { return mslots + ((p - kstart) % kTmaMainSlots) * (kTmaMainArrays * kPlane); };
   auto zslot = [&](int p) { return zslots + ((p - kstart) % kTmaPzSlots) * kPlane; };
@@ -423,6 +435,35 @@ flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const FlowTmaParams 
     for (int p = max(kstart, l_pz - kTmaPzSlots + 1); p <= l_pz; ++p)
       mbar_wait_bounded(&zbars[(p - kstart) % kTmaPzSlots], (unsigned)(((p - kstart) / kTmaPzSlots) & 1),
                         kTmaWaitLimitNs);
+  }
+  return k_stop < 0;
+}
+
+// One unit per CTA (MULTI false, the default plan), or fp.units_per_cta
+// consecutive units (the vertices of one window first), one march after
+// another: every copy of a march is waited for before it ends, so after a
+// CTA barrier the next unit re-initialises the rings' mbarriers and reuses
+// the shared memory.  Two instantiations, so that the loop's live values
+// cost the single-unit kernel no registers.
+template <int W, bool MULTI>
+__global__ void __launch_bounds__(FlowTmaShape<W>::kThreads, FlowTmaShape<W>::kCtasPerSm)
+flow_tma_kernel(const FlowVertexTMA* __restrict__ vertices, const __grid_constant__ FlowTmaParams fp) {
+  // (a grid constant: the march's lambdas refer to fp in place, no local copy)
+  if (!MULTI) {
+    flow_tma_unit<W, false>(vertices, fp, 0, false);
+    return;
+  }
+  const int total = fp.n_items * fp.n_vertices;
+  const int u0 = blockIdx.x * fp.units_per_cta;
+  const int u1 = min(u0 + fp.units_per_cta, total);
+  for (int unit = u0; unit < u1; ++unit) {
+    if (unit > u0) {
+      // the rings' generic reads of the last march before the next march's
+      // copies (async proxy) write the same shared memory
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+    }
+    if (!flow_tma_unit<W, true>(vertices, fp, unit, unit > u0)) break;
   }
 }
 

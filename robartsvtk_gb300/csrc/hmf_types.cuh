@@ -189,7 +189,9 @@ struct FlowTmaParams {
   float step;
   float icc;
   int parity;
-  int n_vertices;  // non-root vertices (grid.x = n_vertices * items)
+  int n_vertices;     // non-root vertices: units = n_vertices * n_items
+  int n_items;        // work items of this launch (from `items`)
+  int units_per_cta;  // grid.x = ceil(units / units_per_cta)
   const FlowVolume* vols;
   const FlowItem* items;
   int* error_flag;

@@ -148,6 +148,14 @@ class HMFSolver:
     def flow_window(self) -> int:
         return check(self._lib.hmf_get_flow_window(self._ctx), self._ctx)
 
+    def set_flow_units(self, units: int) -> None:
+        """Window-vertex marches per flow-kernel CTA, 1..64 (0: 1)."""
+        check(self._lib.hmf_set_flow_units(self._ctx, int(units)), self._ctx)
+
+    @property
+    def flow_units(self) -> int:
+        return check(self._lib.hmf_get_flow_units(self._ctx), self._ctx)
+
     def autotune(self, stream=None) -> None:
         """Time the flow kernel for each candidate z chunk on the current
         inputs and keep the fastest (hmf_autotune)."""
@@ -400,6 +408,10 @@ class HMFBatchSolver:
 
     def set_timing(self, enabled: bool) -> None:
         check(self._lib.hmf_set_timing(self._ctx, 1 if enabled else 0), self._ctx)
+
+    def set_flow_units(self, units: int) -> None:
+        """Window-vertex marches per flow-kernel CTA, 1..64 (0: 1)."""
+        check(self._lib.hmf_set_flow_units(self._ctx, int(units)), self._ctx)
 
     def autotune(self, stream=None) -> None:
         check(self._lib.hmf_autotune(self._ctx, _stream_handle(stream)), self._ctx)

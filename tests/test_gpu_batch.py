@@ -21,11 +21,13 @@ def make_batch(seed, dims_list, parent=PARENT, iterations=15, smooth_nodes=(1, 3
     return ws
 
 
-def solve_batch(ws, semantics=REF_CUDA, autotune=False, device_inputs=False, pipeline=True):
+def solve_batch(ws, semantics=REF_CUDA, autotune=False, device_inputs=False, pipeline=True, units=0):
     import torch
     keep = []
     with HMFBatchSolver([w.dims for w in ws], ws[0].parent, semantics) as b:
         b.set_pipeline(pipeline)
+        if units:
+            b.set_flow_units(units)
         for i, w in enumerate(ws):
             for leaf, d in w.data.items():
                 if device_inputs:
@@ -78,6 +80,19 @@ def test_batch_of_uneven_volumes_matches_oracle_per_volume():
         for i, w in enumerate(ws):
             same(res[i], refs[i], "volume %d %s pipeline %s" % (i, w.dims, pipeline))
         assert stats["launches"] == 1 + per_iter * ws[0].iterations
+
+
+@pytest.mark.parametrize("units", [2, 5])
+def test_batch_with_several_marches_per_cta(units):
+    """Flow CTAs that march several (window, vertex) units, crossing from one
+    volume's units to the next, with and without the volume-group pipeline."""
+    dims = [(37, 19, 23), (5, 4, 3), (61, 30, 9), (33, 65, 12)]
+    ws = make_batch(150, dims)
+    refs = [oracle(w) for w in ws]
+    for pipeline in (False, True):
+        res, _ = solve_batch(ws, pipeline=pipeline, units=units)
+        for i, w in enumerate(ws):
+            same(res[i], refs[i], "volume %d units %d pipeline %s" % (i, units, pipeline))
 
 
 def test_batch_with_device_inputs_and_autotune():

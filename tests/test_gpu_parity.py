@@ -20,11 +20,14 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 LABEL_TOL = 1e-4  # per-voxel max |u_gpu - u_oracle| accepted for end-to-end workloads
 
 
-def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None, window=0, zchunk=0, pipeline=False):
+def run_gpu(w, semantics=REF_CUDA, device_inputs=False, iterations=None, window=0, zchunk=0, pipeline=False,
+            units=0):
     import torch
     with HMFSolver(w.dims, w.parent, semantics) as s:
         if window:
             s.set_flow_window(window)
+        if units:
+            s.set_flow_units(units)
         if zchunk:
             s.set_zchunk(zchunk)
         if pipeline:
@@ -114,6 +117,19 @@ def test_ref_cuda_bitexact_64_row_windows(dims, parent, smooth_nodes, iters, zch
 def test_ref_cuda_bitexact_slab_pipeline(dims, parent, smooth_nodes, iters, zchunk, window):
     w = random_tree_problem(28, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
     assert_same(run_gpu(w, window=window, zchunk=zchunk, pipeline=True), oracle(w), "pipelined " + str(dims))
+
+
+@pytest.mark.parametrize("dims,parent,smooth_nodes,iters,zchunk,window,pipeline,units", [
+    ((40, 30, 50), [-1, 0, 0, 1, 1, 2, 2], (1, 2), 9, 7, 0, True, 2),     # pipelined slabs, 2 marches per CTA
+    ((64, 16, 40), [-1, 0, 0, 1, 1, 2, 2], (1, 3, 5), 7, 0, 0, False, 3),  # 3 marches: CTAs span windows
+    ((33, 61, 12), [-1, 0, 0, 0, 0], (), 6, 0, 64, False, 4),             # 64-row windows
+    ((70, 19, 23), [-1, 0, 1, 2, 2, 1, 0], (3, 4), 8, 4, 0, True, 64),    # one CTA per slab launch or fewer
+])
+def test_ref_cuda_bitexact_units_per_cta(dims, parent, smooth_nodes, iters, zchunk, window, pipeline, units):
+    """Several (window, vertex) marches per flow-kernel CTA, one after another."""
+    w = random_tree_problem(31, dims, parent, iterations=iters, smooth_nodes=smooth_nodes)
+    assert_same(run_gpu(w, window=window, zchunk=zchunk, pipeline=pipeline, units=units), oracle(w),
+                "units %d %s" % (units, dims))
 
 
 def test_slab_pipeline_with_device_inputs_that_move():
