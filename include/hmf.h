@@ -119,6 +119,20 @@ int hmf_set_params(hmf_ctx* ctx, int iterations, float step_size, float cc);
  * (.cxx:478-716). */
 int hmf_solve(hmf_ctx* ctx, void* stream);
 
+/* Run NumberOfIterations more iterations from the state the last hmf_solve
+ * or hmf_solve_continue ended in, without the initialisation: a solve of
+ * k1 iterations continued by k2 gives bit-identically the solve of k1 + k2
+ * (same inputs and parameters).  No counterpart in the reference, which
+ * always starts from the initialisation (.cxx:478-716); with the convergence
+ * log it lets a caller iterate in rounds and stop when the label change is
+ * small.  Label-tree contexts (batches included), both semantics; refused
+ * with HMF_ERR_INVALID_ARGUMENT for graphs (hmf_create_dag), and with
+ * HMF_ERR_STATE on out-of-core contexts and when the last call that wrote
+ * the state was not a solve (hmf_solve_adjoint, hmf_autotune) or failed.  The inputs
+ * are staged again, so data terms and smoothness may change between calls;
+ * the FP64 evaluation and the adjoint always start from the initialisation. */
+int hmf_solve_continue(hmf_ctx* ctx, void* stream);
+
 /* Copy the labelling of a non-root vertex (the leaves are the reference's
  * outputs, GetOutputDataObject(idx), vtkHierarchicalMaxFlowSegmentation.cxx:337-346;
  * branch labellings are also available) to `out` (VX*VY*VZ floats). */

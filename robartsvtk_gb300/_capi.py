@@ -47,6 +47,7 @@ SIGNATURES = [
     ("hmf_set_smoothness_scalar", _I, [_P, _I, ctypes.c_double]),
     ("hmf_set_params", _I, [_P, _I, ctypes.c_float, ctypes.c_float]),
     ("hmf_solve", _I, [_P, _P]),
+    ("hmf_solve_continue", _I, [_P, _P]),
     ("hmf_get_labels", _I, [_P, _I, _P, _I, _P]),
     ("hmf_get_sink", _I, [_P, _I, _P, _I, _P]),
     ("hmf_leaf_order", _I, [_P, ctypes.POINTER(_I), _I]),

@@ -1316,6 +1316,7 @@ int begin_solve_with(hmf_ctx* c, cudaStream_t user, Staged& staged, StateLoader 
   c->launches = 0;
   for (int k = 0; k < 3; ++k) c->kind_ms[k] = 0, c->kind_count[k] = 0;
   c->solved = false;
+  c->continuable = false;
   // order after the caller's queued work
   CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
   CK(cudaStreamWaitEvent(s, c->ev_join, 0), "cudaStreamWaitEvent(join)");
@@ -1545,6 +1546,9 @@ int solve_with(hmf_ctx* c, cudaStream_t user, StateLoader load, void* arg) {
     }
   }
   // final flows live in set (iterations & 1); nothing else depends on parity
+  // (REF_CPU leaves the flows at zero in set 0)
+  c->flow_parity = c->semantics == HMF_SEMANTICS_REF_CUDA ? (c->iterations & 1) : 0;
+  c->continuable = true;
   return end_solve(c, user);
 }
 
@@ -1700,6 +1704,37 @@ int hmf_solve(hmf_ctx* c, void* stream) {
   cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
   if (c->pg) return paged_solve(c, user);
   return solve_with(c, user, nullptr, nullptr);
+}
+
+namespace {
+// StateLoader of hmf_solve_continue: the state is the last run's, in place;
+// the replayed iterations start from flow set 0, so flows left in set 1 by
+// an odd iteration count move there first (device copies, exact).
+int continue_state(hmf_ctx* c, cudaStream_t s, void*) {
+  if (c->flow_parity == 0) return HMF_OK;
+  const size_t bytes = (size_t)c->total * sizeof(float);
+  for (int v = 0; v < c->n; ++v) {
+    if (v == c->root) continue;
+    CK(cudaMemcpyAsync(c->fx[0][v], c->fx[1][v], bytes, cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync(flows)");
+    CK(cudaMemcpyAsync(c->fy[0][v], c->fy[1][v], bytes, cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync(flows)");
+    CK(cudaMemcpyAsync(c->fz[0][v], c->fz[1][v], bytes, cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync(flows)");
+  }
+  c->flow_parity = 0;
+  return HMF_OK;
+}
+}  // namespace
+
+int hmf_solve_continue(hmf_ctx* c, void* stream) {
+  if (!c) return HMF_ERR_INVALID_ARGUMENT;
+  if (int rc = refuse_paged(c, "hmf_solve_continue")) return rc;
+  if (c->dag)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT,
+                "graphs (hmf_create_dag) cannot continue: their last iteration runs fewer tasks");
+  // the adjoint and the autotuner leave other state in the solver's arrays
+  if (!c->solved || !c->continuable)
+    return fail(c, HMF_ERR_STATE, "hmf_solve_continue follows hmf_solve or hmf_solve_continue");
+  DeviceGuard dg(c->device);
+  return solve_with(c, reinterpret_cast<cudaStream_t>(stream), continue_state, nullptr);
 }
 
 int hmf_autotune(hmf_ctx* c, void* stream) {

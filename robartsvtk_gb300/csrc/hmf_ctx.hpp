@@ -117,6 +117,8 @@ struct hmf_ctx {
   double kind_ms[3] = {0, 0, 0};
   long long kind_count[3] = {0, 0, 0};
   bool solved = false;
+  int flow_parity = 0;       // the flow set holding the current flows (after the last solve or continuation)
+  bool continuable = false;  // the arrays hold the state the last solve ended in
 
   // host copies of the device tables (kept per context: pageable-memory
   // cudaMemcpyAsync stages them before returning)

@@ -165,6 +165,12 @@ class HMFSolver:
     def solve(self, stream=None) -> None:
         check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
 
+    def solve_continue(self, stream=None) -> None:
+        """`iterations` more iterations from the state the last solve ended in,
+        without re-initialising (hmf_solve_continue): solve(k1) then
+        solve_continue(k2) equals solve(k1 + k2) bit for bit."""
+        check(self._lib.hmf_solve_continue(self._ctx, _stream_handle(stream)), self._ctx)
+
     def _fetch(self, fn, node, out, stream):
         if out is None:
             out = np.empty((self.dims[2], self.dims[1], self.dims[0]), dtype=np.float32)
@@ -418,6 +424,8 @@ class HMFBatchSolver:
 
     def solve(self, stream=None) -> None:
         check(self._lib.hmf_solve(self._ctx, _stream_handle(stream)), self._ctx)
+
+    solve_continue = HMFSolver.solve_continue
 
     # the flow plan's controls, shared with HMFSolver
     set_pipeline = HMFSolver.set_pipeline
