@@ -483,9 +483,10 @@ const char* hmf_last_error(const hmf_ctx* ctx);
  *    + leaves + distinct smoothness images) plus about 24 KiB of tables, with
  *    VX' = VX rounded up to a multiple of 4; a larger problem is rejected with
  *    HMF_ERR_INVALID_ARGUMENT before anything is queued.
- *  - The first call on a device looks up the array's device address and sets
- *    the kernels' attributes for that device; make that first call before any
- *    stream capture.
+ *  - Every call looks up the array's device address in the current context
+ *    and sets the kernels' attributes (neither allocates).  The call cannot
+ *    be recorded into a graph: inside a stream capture it returns
+ *    HMF_ERR_INVALID_ARGUMENT before anything is queued.
  *  - Work is queued on `stream`; the call returns after it has finished
  *    (it synchronises `stream` to report negative inputs).
  *  - Every call shares the one array: calls whose work overlaps on the GPU

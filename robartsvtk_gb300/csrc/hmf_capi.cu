@@ -2021,11 +2021,12 @@ constexpr int kNoAllocMaxDevices = 64;
 // Held on every GPU that loads this library, until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// Device address of g_noalloc_scratch per device ordinal.  In host code the
-// symbol itself is only a stand-in, so the address is looked up once per
-// device, with that device current, and handed to the kernels.
+// Device address of g_noalloc_scratch in the current context.  In host code
+// the symbol itself is only a stand-in, so the address is looked up on every
+// call (no allocation), with the device current, and handed to the kernels:
+// a cached address would outlive a cudaDeviceReset, after which the module
+// (and the array) are loaded again elsewhere.
 std::mutex g_noalloc_mutex;
-unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
 int noalloc_fail(int code, const char* msg) {
   g_create_error = msg;
@@ -2047,21 +2048,18 @@ int noalloc_setup(int device, unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (device < 0 || device >= kNoAllocMaxDevices)
     return noalloc_fail(HMF_ERR_CUDA, "device ordinal beyond the supported range");
-  if (!g_noalloc_addr[device]) {
-    void* p = nullptr;
-    NCK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
-    NCK(cudaFuncSetAttribute(hmf::flow_kernel<kTX, kTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             hmf::FlowTile<kTX, kTY>::SMEM_BYTES),
-        "cudaFuncSetAttribute(flow_kernel)");
-    NCK(cudaFuncSetAttribute(hmf::tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             3 * hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
-        "cudaFuncSetAttribute(tree_kernel)");
-    NCK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
-        "cudaFuncSetAttribute(init_kernel)");
-    g_noalloc_addr[device] = static_cast<unsigned char*>(p);
-  }
-  *out = g_noalloc_addr[device];
+  void* p = nullptr;
+  NCK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+  NCK(cudaFuncSetAttribute(hmf::flow_kernel<kTX, kTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           hmf::FlowTile<kTX, kTY>::SMEM_BYTES),
+      "cudaFuncSetAttribute(flow_kernel)");
+  NCK(cudaFuncSetAttribute(hmf::tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           3 * hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
+      "cudaFuncSetAttribute(tree_kernel)");
+  NCK(cudaFuncSetAttribute(hmf::init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           hmf::kMaxVertices * kTreeThreads * (int)sizeof(float)),
+      "cudaFuncSetAttribute(init_kernel)");
+  *out = static_cast<unsigned char*>(p);
   return HMF_OK;
 }
 
@@ -2203,12 +2201,18 @@ extern "C" int hmf_solve_noalloc(int vx, int vy, int vz, const int* parent, int 
 
   int device = 0;
   NCK(cudaGetDevice(&device), "cudaGetDevice");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  // the call stages its tables from this frame and waits for its stream:
+  // nothing of it can be recorded into a graph
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  NCK(cudaStreamIsCapturing(s, &capturing), "cudaStreamIsCapturing");
+  if (capturing != cudaStreamCaptureStatusNone)
+    return noalloc_fail(HMF_ERR_INVALID_ARGUMENT, "hmf_solve_noalloc cannot run inside a stream capture");
   unsigned char* base = nullptr;
   rc = noalloc_setup(device, &base);
   if (rc) return rc;
   int sm_count = 0;
   NCK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
   unsigned char* p = base;
   auto* d_flow = reinterpret_cast<hmf::FlowVertex*>(p);

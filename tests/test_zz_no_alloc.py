@@ -31,7 +31,9 @@ def _context_labels(w, semantics=0):
         return {v: s.labels(v) for v in range(len(w.parent)) if w.parent[v] >= 0}
 
 
-def _noalloc_labels(w, semantics=0, stream=None):
+def _noalloc_labels(w, semantics=0, stream=None, capture=False):
+    """Labels of a hmf_solve_noalloc call; with `capture`, the return code of
+    the call made inside a CUDA graph capture of `stream` instead."""
     import torch
     lib = _capi.load()
     n = len(w.parent)
@@ -54,6 +56,12 @@ def _noalloc_labels(w, semantics=0, stream=None):
     par = (ctypes.c_int * n)(*w.parent)
     torch.cuda.synchronize()
     handle = stream.cuda_stream if stream is not None else None
+    if capture:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            rc = lib.hmf_solve_noalloc(*w.dims, par, n, semantics, data, smooth, alpha, w.iterations, w.step,
+                                       w.cc, labels, handle)
+        return rc
     rc = lib.hmf_solve_noalloc(*w.dims, par, n, semantics, data, smooth, alpha, w.iterations, w.step, w.cc,
                                labels, handle)
     assert rc == 0, lib.hmf_last_error(None)
@@ -110,6 +118,22 @@ def test_noalloc_reports_negative_input():
     with pytest.raises(AssertionError):
         _noalloc_labels(w_bad)
     assert b"non-negative" in lib.hmf_last_error(None)
+    ref = _context_labels(w)
+    got = _noalloc_labels(w)
+    for v in ref:
+        assert np.array_equal(got[v], ref[v]), v
+
+
+def test_noalloc_refuses_a_stream_capture():
+    """Inside a CUDA graph capture the call returns HMF_ERR_INVALID_ARGUMENT
+    before queuing anything (it stages its tables from its own stack frame and
+    waits for its stream), and the next call outside the capture succeeds."""
+    import torch
+    lib = _capi.load()
+    w = random_tree_problem(45, (12, 9, 7), [-1, 0, 0], iterations=3)
+    rc = _noalloc_labels(w, stream=torch.cuda.Stream(), capture=True)
+    assert rc == -1
+    assert b"capture" in lib.hmf_last_error(None)
     ref = _context_labels(w)
     got = _noalloc_labels(w)
     for v in ref:
