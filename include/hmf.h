@@ -125,9 +125,9 @@ int hmf_solve(hmf_ctx* ctx, void* stream);
  * (same inputs and parameters).  No counterpart in the reference, which
  * always starts from the initialisation (.cxx:478-716); with the convergence
  * log it lets a caller iterate in rounds and stop when the label change is
- * small.  Label-tree contexts (batches included), both semantics; refused
- * with HMF_ERR_INVALID_ARGUMENT for graphs (hmf_create_dag), and with
- * HMF_ERR_STATE on out-of-core contexts and when the last call that wrote
+ * small.  Label-tree contexts (batches and out-of-core contexts included),
+ * both semantics; refused with HMF_ERR_INVALID_ARGUMENT for graphs
+ * (hmf_create_dag), and with HMF_ERR_STATE when the last call that wrote
  * the state was not a solve (hmf_solve_adjoint, hmf_autotune) or failed.  The inputs
  * are staged again, so data terms and smoothness may change between calls;
  * the FP64 evaluation and the adjoint always start from the initialisation. */
@@ -169,7 +169,7 @@ int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kin
  *
  * hmf_create_paged makes a context whose solver state lives in pinned host
  * memory (two copies of 5 x (n_nodes - 1) + 1 arrays of VX*VY*VZ floats;
- * one copy of 2 x (n_nodes - 1) + 1 when one round suffices) and whose device memory stays within
+ * one copy when one round suffices) and whose device memory stays within
  * max_gpu_usage x the device's memory (clamped to [0, 1]).  hmf_solve covers
  * the volume with blocks of T z-planes (T from the budget: three block
  * contexts of T planes fit) and iterates in rounds of k <= 12 iterations: each
@@ -180,7 +180,8 @@ int hmf_get_stats(const hmf_ctx* ctx, long long* launches, double* avg_ms_by_kin
  * below that).  Works with hmf_set_data / hmf_set_smoothness (host inputs
  * are copied once per solve into pinned memory unless already pinned; device
  * inputs are read in place), hmf_set_smoothness_scalar, hmf_set_params,
- * hmf_solve, hmf_get_labels, hmf_get_sink, hmf_leaf_order, hmf_device_bytes,
+ * hmf_solve, hmf_solve_continue (from the host copy the last solve ended
+ * in), hmf_get_labels, hmf_get_sink, hmf_leaf_order, hmf_device_bytes,
  * hmf_set_timing / hmf_get_stats; every other call taking a context returns
  * HMF_ERR_STATE.  Label trees, single volumes, both semantics (REF_CPU
  * iterates per voxel: one round, no halo).

@@ -1726,14 +1726,16 @@ int continue_state(hmf_ctx* c, cudaStream_t s, void*) {
 
 int hmf_solve_continue(hmf_ctx* c, void* stream) {
   if (!c) return HMF_ERR_INVALID_ARGUMENT;
-  if (int rc = refuse_paged(c, "hmf_solve_continue")) return rc;
   if (c->dag)
     return fail(c, HMF_ERR_INVALID_ARGUMENT,
                 "graphs (hmf_create_dag) cannot continue: their last iteration runs fewer tasks");
   // the adjoint and the autotuner leave other state in the solver's arrays
+  // (neither runs on an out-of-core context)
   if (!c->solved || !c->continuable)
     return fail(c, HMF_ERR_STATE, "hmf_solve_continue follows hmf_solve or hmf_solve_continue");
   DeviceGuard dg(c->device);
+  // out of core: the state is the host copy the last solve ended in
+  if (c->pg) return paged_solve(c, reinterpret_cast<cudaStream_t>(stream), true);
   return solve_with(c, reinterpret_cast<cudaStream_t>(stream), continue_state, nullptr);
 }
 

@@ -237,7 +237,7 @@ inline int refuse_paged(hmf_ctx* c, const char* what) {
 
 // hmf_paged.cu
 int paged_setup(hmf_ctx* c, double max_gpu_usage);
-int paged_solve(hmf_ctx* c, cudaStream_t user);
+int paged_solve(hmf_ctx* c, cudaStream_t user, bool cont = false);
 int paged_copy_out(hmf_ctx* c, bool labels, int node, float* out, int where, void* stream);
 void paged_free(hmf_ctx* c);
 size_t paged_bytes(const hmf_ctx* c);

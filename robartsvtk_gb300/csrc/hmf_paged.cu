@@ -67,13 +67,13 @@ struct PagedState {
   int rounds = 0;
   bool inputs_on_device = false;
   long long link_bytes = 0;  // bytes between host and device in the last solve
-  int final_copy = 0;        // host state copy holding the final sinks and labels
+  int final_copy = 0;        // host state copy holding the final state
 
   hmf_ctx* blk[kBlockContexts] = {};
   int n_blk = 0;
   int blk_planes = 0;  // planes the block contexts were created for
   cudaStream_t st[kBlockContexts] = {};
-  std::vector<cudaEvent_t> ev_loaded[2], ev_stored[2];  // [round parity][block]
+  std::vector<cudaEvent_t> ev_loaded[2], ev_stored[2];  // [host copy loaded from / stored into][block]
   cudaEvent_t ev_end[kBlockContexts] = {};
 
   HostState host[2];
@@ -150,10 +150,11 @@ int load_block(hmf_ctx* b, cudaStream_t s, void* arg) {
   return HMF_OK;
 }
 
-// The owned planes [z0, z1) of a solved block into a host state copy: all of
-// it between rounds, the sinks and labels after the last round.
+// The owned planes [z0, z1) of a solved block into a host state copy: sinks,
+// labels and the flows of set `parity` (after the last round too, so that a
+// continued solve starts from them).
 int store_block(hmf_ctx* c, PagedState& P, HostState& H, hmf_ctx* b, int first, int z0, int z1, int parity,
-                bool final_round, long long plane, cudaStream_t s) {
+                long long plane, cudaStream_t s) {
   const auto& V = b->vols[0];
   const size_t dp = (size_t)V.vx * sizeof(float), sp = (size_t)V.pitch * sizeof(float);
   const int planes = z1 - z0;
@@ -170,7 +171,6 @@ int store_block(hmf_ctx* c, PagedState& P, HostState& H, hmf_ctx* b, int first, 
                              cudaMemcpyDeviceToHost, s))
       return rc;
     ++n;
-    if (final_round) continue;
     const float* src[3] = {b->fx[parity][v], b->fy[parity][v], b->fz[parity][v]};
     float* dst[3] = {H.fx[v], H.fy[v], H.fz[v]};
     for (int a = 0; a < 3; ++a)
@@ -199,9 +199,10 @@ size_t plane_bytes(const hmf_ctx* c, int staged_inputs) {
   return (size_t)V.pitch * V.vy * sizeof(float) * (size_t)(9 * (c->n - 1) + 1 + staged_inputs);
 }
 
-// The host state copy `H`: sinks and labels, and the flows when `flows`.
-int host_state(hmf_ctx* c, HostState& H, size_t arr, bool flows) {
-  const size_t n_arrays = flows ? (size_t)5 * (c->n - 1) + 1 : (size_t)2 * (c->n - 1) + 1;
+// The host state copy `H`: sinks, labels and flows (the same layout in every
+// solve, so that a continued solve reads the last one's).
+int host_state(hmf_ctx* c, HostState& H, size_t arr) {
+  const size_t n_arrays = (size_t)5 * (c->n - 1) + 1;
   if (H.bytes < n_arrays * arr) {
     if (H.mem) cudaFreeHost(H.mem);
     H.mem = nullptr;
@@ -224,7 +225,6 @@ int host_state(hmf_ctx* c, HostState& H, size_t arr, bool flows) {
     H.sink[v] = take();
     if (v == c->root) continue;
     H.label[v] = take();
-    if (!flows) continue;
     H.fx[v] = take();
     H.fy[v] = take();
     H.fz[v] = take();
@@ -285,12 +285,17 @@ size_t paged_bytes(const hmf_ctx* c) {
   return n;
 }
 
-int paged_solve(hmf_ctx* c, cudaStream_t user) {
+int paged_solve(hmf_ctx* c, cudaStream_t user, bool cont) {
   PagedState& P = *c->pg;
   const auto& V = c->vols[0];
   for (int l : c->leaves)
     if (!c->data[0][l].ptr) return fail(c, HMF_ERR_MISSING_INPUT, "Missing data prior for leaf node.");
   c->solved = false;
+  c->continuable = false;
+  // Host copy q of round r: rounds write copy (r + o) & 1 and read the other
+  // one; a continued solve's first round reads the copy the last solve
+  // ended in (o = that copy ^ 1) instead of initialising its blocks.
+  const int o = cont ? (P.final_copy ^ 1) : 0;
   const long long plane = (long long)V.vx * V.vy;
   const size_t arr = (size_t)plane * V.vz * sizeof(float);
 
@@ -369,7 +374,7 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   P.halo = halo;
   P.rounds = (int)round_iters.size();
   P.link_bytes = 0;
-  P.final_copy = (P.rounds - 1) & 1;
+  P.final_copy = (P.rounds - 1 + o) & 1;
 
   // ---- memory: block contexts, the inputs, the host state, the error flags
   const int nc = std::min(kBlockContexts, nb);
@@ -388,6 +393,12 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   CK(cudaEventRecord(c->ev_join, user), "cudaEventRecord(join)");
   for (int i = 0; i < kBlockContexts; ++i)
     CK(cudaStreamWaitEvent(P.st[i], c->ev_join, 0), "cudaStreamWaitEvent(join)");
+  // a continued solve reads the host copy the last solve's blocks stored on
+  // every stream, whatever its layout was: each stream waits for all of it
+  if (cont)
+    for (int i = 0; i < kBlockContexts; ++i)
+      for (int q = 0; q < kBlockContexts; ++q)
+        CK(cudaStreamWaitEvent(P.st[i], P.ev_end[q], 0), "cudaStreamWaitEvent(last solve)");
   // Host inputs: on the device for the whole solve, or from pinned memory
   // (the caller's, when already pinned, else a pinned copy) every round.
   std::vector<const float*> host_dst(host_src.size(), nullptr);
@@ -448,9 +459,9 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
   for (int v = 0; v < c->n; ++v) in_smooth[v] = route(in_smooth[v], w_smooth[v], &w_smooth[v]);
   const int link_inputs = dev_inputs ? 0 : (int)host_src.size();  // inputs the blocks read over the link
 
-  const bool need_state = P.rounds > 1;
-  for (int q = 0; q < (need_state ? 2 : 1); ++q)
-    if (int rc = host_state(c, P.host[q], arr, need_state)) return rc;
+  // one round of a fresh solve writes copy 0 only
+  for (int q = 0; q < (P.rounds > 1 || cont ? 2 : 1); ++q)
+    if (int rc = host_state(c, P.host[q], arr)) return rc;
   for (int q = 0; q < 2; ++q) {
     if (int rc = ensure_events(c, P.ev_loaded[q], nb)) return rc;
     if (int rc = ensure_events(c, P.ev_stored[q], nb)) return rc;
@@ -473,16 +484,17 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
     b->timing = c->timing;
   }
 
-  // ---- rounds: round r reads host copy (r-1)&1 and writes copy r&1
+  // ---- rounds: round r reads host copy (r + 1 + o) & 1 and writes copy (r + o) & 1
   long long launches = 0;
   double kind_ms[3] = {0, 0, 0};
   long long kind_count[3] = {0, 0, 0};
   int flag_i = 0;
   for (int r = 0; r < P.rounds; ++r) {
     const int kr = round_iters[r];
-    const bool last = r + 1 == P.rounds;
-    HostState& out = P.host[r & 1];
-    const HostState& in = P.host[(r + 1) & 1];  // copy (r-1)&1
+    const int out_q = (r + o) & 1, in_q = (r + 1 + o) & 1;
+    HostState& out = P.host[out_q];
+    const HostState& in = P.host[in_q];
+    const bool loads = r > 0 || cont;
     for (int j = 0; j < nb; ++j) {
       const int slot = j % nc;
       hmf_ctx* b = P.blk[slot];
@@ -499,16 +511,17 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
       }
       hmf_set_params(b, kr, c->step, c->cc);
       // a block's planes hold the owned planes of its neighbours and itself:
-      // its load follows their stores of the previous round
+      // its load follows their stores of the previous round (a continued
+      // solve's first round follows all of the last solve: joined above)
       const int lo = std::max(0, j - 1), hi = std::min(nb - 1, j + 1);
       if (r > 0)
         for (int m = lo; m <= hi; ++m)
-          CK(cudaStreamWaitEvent(s, P.ev_stored[(r + 1) & 1][m], 0), "cudaStreamWaitEvent(stored)");
+          CK(cudaStreamWaitEvent(s, P.ev_stored[in_q][m], 0), "cudaStreamWaitEvent(stored)");
       int rc;
-      if (r == 0) {
+      if (!loads) {
         rc = solve_with(b, s, nullptr, nullptr);
       } else {
-        BlockLoad L{&in, P.ev_loaded[r & 1][j], P.starts[j], plane, &P.link_bytes};
+        BlockLoad L{&in, P.ev_loaded[in_q][j], P.starts[j], plane, &P.link_bytes};
         rc = solve_with(b, s, load_block, &L);
       }
       if (rc) return fail(c, rc, std::string("block solve: ") + b->err);
@@ -519,14 +532,14 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
         kind_count[q] += b->kind_count[q];
       }
       launches += b->launches;
-      // the store overwrites planes of copy r&1 that the previous round's
+      // the store overwrites planes of copy out_q that the previous round's
       // loads of this block and its neighbours read
-      if (r > 1)
+      if (r >= 2 || (cont && r >= 1))
         for (int m = lo; m <= hi; ++m)
-          CK(cudaStreamWaitEvent(s, P.ev_loaded[(r + 1) & 1][m], 0), "cudaStreamWaitEvent(loaded)");
+          CK(cudaStreamWaitEvent(s, P.ev_loaded[out_q][m], 0), "cudaStreamWaitEvent(loaded)");
       const int z1 = j + 1 < nb ? P.owned[j + 1] : V.vz;
-      if (int rc2 = store_block(c, P, out, b, P.starts[j], P.owned[j], z1, kr & 1, last, plane, s)) return rc2;
-      CK(cudaEventRecord(P.ev_stored[r & 1][j], s), "cudaEventRecord(stored)");
+      if (int rc2 = store_block(c, P, out, b, P.starts[j], P.owned[j], z1, kr & 1, plane, s)) return rc2;
+      CK(cudaEventRecord(P.ev_stored[out_q][j], s), "cudaEventRecord(stored)");
     }
   }
   for (int i = 0; i < kBlockContexts; ++i) {
@@ -541,6 +554,7 @@ int paged_solve(hmf_ctx* c, cudaStream_t user) {
     c->kind_ms[q] = kind_count[q] ? kind_ms[q] / kind_count[q] : 0.0;
   }
   c->solved = true;
+  c->continuable = true;
   return HMF_OK;
 }
 

@@ -1,8 +1,8 @@
 """Continued solves (hmf_solve_continue): k2 more iterations from the state a
 solve of k1 ended in must equal, bit for bit, one solve of k1 + k2 -- and the
 oracle's.  Covers odd k1 (flows left in the second set), the slab pipeline,
-the launch-by-launch path, batches, REF_CPU, the convergence log per call and
-the refusals.  GPU only."""
+the launch-by-launch path, batches, REF_CPU, out-of-core contexts, the
+convergence log per call and the refusals.  GPU only."""
 import numpy as np
 import pytest
 
@@ -156,6 +156,31 @@ def test_refusals():
             d.solve_continue()
         assert e.value.code == HMF_ERR_INVALID_ARGUMENT
     with HMFSolver(w.dims, w.parent, max_gpu_usage=0.5) as p:
+        _configure(p, w, 3)
         with pytest.raises(HMFError) as e:
             p.solve_continue()
         assert e.value.code == HMF_ERR_STATE
+
+
+@pytest.mark.parametrize("semantics,dims,plans,rounds", [
+    (REF_CUDA, (37, 19, 45), ((20, 2), (20, 2)), (5, 6)),        # 4 blocks; odd rounds: flows of set 1 stored
+    (REF_CUDA, (37, 19, 45), ((20, 2), (28, 3)), (4, 7)),        # another layout for the continuation
+    (REF_CUDA, (32, 16, 20), ((64, 0), (64, 0), (64, 0)), (3, 1, 4)),  # one block: single rounds
+    (REF_CUDA, (37, 19, 45), ((20, 2), (20, 2)), (6, 0)),        # a continuation of no iterations
+    (REF_CPU, (29, 13, 17), ((0, 0), (0, 0)), (4, 7)),
+])
+def test_continue_out_of_core(semantics, dims, plans, rounds):
+    """Out-of-core contexts continue from the host copy their last solve
+    ended in: equal to one in-core solve of all the rounds' iterations."""
+    w = random_tree_problem(67, dims, [-1, 0, 0, 1, 1, 2, 2], iterations=sum(rounds), smooth_nodes=(1, 4))
+    ref = _in_rounds(w, (sum(rounds),), semantics=semantics)
+    with HMFSolver(w.dims, w.parent, semantics, max_gpu_usage=0.75) as p:
+        _configure(p, w, rounds[0])
+        p.set_paged_plan(*plans[0])
+        p.solve()
+        for plan, k in zip(plans[1:], rounds[1:]):
+            p.set_paged_plan(*plan)
+            p.set_params(k, w.step, w.cc)
+            p.solve_continue()
+        got = _state(p, w)
+    _same(got, ref, "out of core %s %s" % (plans, rounds))
