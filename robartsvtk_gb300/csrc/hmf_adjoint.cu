@@ -473,14 +473,19 @@ int backward_step(hmf_ctx* c, const Staged& staged, int slotA, int slotB, int cu
     const int grid = (int)std::min<long long>(chunks, (long long)c->sm_count * per_sm);
     bool pre = true;  // vertex ids in pre-order: the sink pass runs in id order
     for (int k = 0; k < n; ++k) pre = pre && c->preorder[k] == k;
+    bool flat = c->root == 0;  // every other vertex a leaf of root 0: parents known at compile time
+    for (int v = 1; v < n; ++v) flat = flat && c->parent[v] == 0;
     if (int rc = maybe_request_stall(c, HMF_STALL_REVERSE_SWEEP, s)) return rc;
-    switch (n * 2 + (pre ? 1 : 0)) {
+    switch (n * 4 + (flat ? 2 : pre ? 1 : 0)) {
 #define HMF_SWEEP_CASE(N)                                                                                  \
-  case 2 * N:                                                                                              \
-    hmf::adj_sweep_kernel<N, false><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);           \
+  case 4 * N:                                                                                              \
+    hmf::adj_sweep_kernel<N, false, false><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);    \
     break;                                                                                                 \
-  case 2 * N + 1:                                                                                          \
-    hmf::adj_sweep_kernel<N, true><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);            \
+  case 4 * N + 1:                                                                                          \
+    hmf::adj_sweep_kernel<N, true, false><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);     \
+    break;                                                                                                 \
+  case 4 * N + 2:                                                                                          \
+    hmf::adj_sweep_kernel<N, true, true><<<grid, hmf::kSwVc, smem, s>>>(S->d_tree, G, W, c->d_error);      \
     break;
       HMF_SWEEP_CASE(2) HMF_SWEEP_CASE(3) HMF_SWEEP_CASE(4) HMF_SWEEP_CASE(5)
       HMF_SWEEP_CASE(6) HMF_SWEEP_CASE(7) HMF_SWEEP_CASE(8)
@@ -618,10 +623,13 @@ int hmf_solve_adjoint(hmf_ctx* c, const int* truth, int where, int checkpoint_ev
      "cudaFuncSetAttribute(adj_flow_tma_kernel)");
 
 #define HMF_SWEEP_ATTR(N)                                                                                  \
-  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                           hmf::adj_sweep_smem_bytes(N)),                                                     \
      "cudaFuncSetAttribute(adj_sweep_kernel)");                                                              \
-  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                          hmf::adj_sweep_smem_bytes(N)),                                                     \
+     "cudaFuncSetAttribute(adj_sweep_kernel)");                                                              \
+  CK(cudaFuncSetAttribute(hmf::adj_sweep_kernel<N, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                           hmf::adj_sweep_smem_bytes(N)),                                                     \
      "cudaFuncSetAttribute(adj_sweep_kernel)");
   HMF_SWEEP_ATTR(2) HMF_SWEEP_ATTR(3) HMF_SWEEP_ATTR(4) HMF_SWEEP_ATTR(5)

@@ -18,6 +18,9 @@
 // registers.  When the vertex ids are in pre-order (PRE), the sink pass runs
 // in compile-time vertex order; otherwise runtime vertices (parents,
 // children, pre-order positions) are reached through predicated selects.
+// FLAT trees (root 0, every other vertex a leaf under it) also have their
+// parents at compile time, so no select or parent test is left; the
+// operations and their order are the same.
 #pragma once
 
 #include "hmf_adjoint.cuh"
@@ -49,7 +52,7 @@ __device__ __forceinline__ void sw_add(float (&a)[N], int v, float x) {
     if (w == v) a[w] = a[w] + x;
 }
 
-template <int N, bool PRE>
+template <int N, bool PRE, bool FLAT>
 __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restrict__ table, const Geometry G,
                                                           const AdjSweep S, int* __restrict__ error_flag) {
   __shared__ AdjTree T;
@@ -78,7 +81,10 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
   __syncthreads();
   if (abort_cta) return;
 
-  const int root = T.root;
+  static_assert(!FLAT || PRE, "a flat tree with root 0 has its ids in pre-order");
+  const int root = FLAT ? 0 : T.root;
+  auto par = [&](int v) { return FLAT ? (v == 0 ? -1 : 0) : T.parent[v]; };
+  auto is_leaf = [&](int v) { return FLAT ? v != 0 : T.n_kids[v] == 0; };
   const float cc = T.cc, icc = T.icc, step = T.step, step_icc = T.step * T.icc;
   const long long arr = S.arr;
   const long long nchunks = (G.vol + kSwVc - 1) / kSwVc;
@@ -91,7 +97,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
     uint64_t* bar = &bars[s];
     float* dst = stage0 + (size_t)s * kStage;
     {
-      const bool nr = v != root, leaf = T.n_kids[v] == 0;
+      const bool nr = v != root, leaf = is_leaf(v);
       mbar_expect_tx(bar, len * 4 * (3 + (nr ? 4 : 0)) + (leaf ? len * 8 : 0));
     }
     auto ld = [&](int kind, int v, const float* src) {
@@ -99,7 +105,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
     };
     {
       const long long b = T.sbase[v];
-      const bool nr = v != root, leaf = T.n_kids[v] == 0;
+      const bool nr = v != root, leaf = is_leaf(v);
       ld(kSwSBN, v, S.sbn + v * arr);
       ld(kSwBS, v, S.stB + b * arr);
       if (leaf) ld(kSwD, v, T.data[v]);
@@ -143,7 +149,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
       auto at = [&](int kind, int v) { return st[(kind * N + v) * kSwVc + q]; };
 #pragma unroll
       for (int v = 0; v < N; ++v) {
-        const bool nr = v != root, leaf = T.n_kids[v] == 0;
+        const bool nr = v != root, leaf = is_leaf(v);
         SBN[v] = at(kSwSBN, v);
         BS[v] = at(kSwBS, v);
         AS[v] = leaf ? 0.f : at(kSwAS, v);
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
           if (v == root) continue;
           const float d = step * GB[v];
           if (v == w) a = a + d;
-          else if (T.parent[v] == w) a = a - d;
+          else if (par(v) == w) a = a - d;
         }
         SBN[w] = a;
         UB[w] = UB[w] - step_icc * GB[w];
@@ -189,7 +195,7 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
 #pragma unroll
       for (int v = 0; v < N; ++v) {
         if (v == root) continue;
-        const int p = T.parent[v];
+        const int p = par(v);
         const float zv = AU[v] + cc * ((sw_sel(BS, p) - BD[v]) - BS[v]);
         const float zb = (zv > 0.0f && zv < 1.0f) ? UB[v] : 0.0f;
         UBO[v] = UBO[v] + zb;
@@ -202,8 +208,8 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
       for (int k = 0; k < N; ++k) {
         if (PRE) {
           const int v = k;  // ids are in pre-order
-          if (T.n_kids[v] == 0) {
-            const int p = T.parent[v];
+          if (is_leaf(v)) {
+            const int p = par(v);
             const float yv = (sw_sel(AS, p) - BD[v]) + AU[v] * icc;
             if (yv < 0.0f) continue;
             if (yv > D[v]) {
@@ -218,14 +224,14 @@ __global__ void __launch_bounds__(kSwVc) adj_sweep_kernel(const AdjTree* __restr
           } else {
             const float Wb = SBN[v] * T.inv_kids[v];
             if (v != root) {
-              sw_add(SBO, T.parent[v], Wb);
+              sw_add(SBO, par(v), Wb);
               DBP[v] = DBP[v] - Wb;
               UBO[v] = UBO[v] + icc * Wb;
             }
             const float iW = icc * Wb;
 #pragma unroll
             for (int w = v + 1; w < N; ++w)  // children follow their parent in pre-order
-              if (T.parent[w] == v) {
+              if (par(w) == v) {
                 SBN[w] = SBN[w] + Wb;
                 DBP[w] = DBP[w] + Wb;
                 UBO[w] = UBO[w] - iW;
