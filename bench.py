@@ -406,7 +406,7 @@ def run_ours(args):
 
     e2e_step()
     replicas.barrier()
-    link = host_link_bandwidth(h_data[w.leaves[0]], stream)
+    link = host_link_bandwidth(list(h_data.values()) + list(h_smooth_obj.values()), list(h_out.values()), stream)
     e_steps = max(3, min(args.steps, 5))
     marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(e_steps)]
     e2 = torch.cuda.Event(enable_timing=True)
@@ -586,27 +586,34 @@ def bench_ref_cpu_semantics(w, d_data, d_smooth, device_stream, reps=3):
             "ms_per_solve": ms, "value": w.nvox * len(w.leaves) * w.iterations / (ms / 1000.0), "unit": UNIT}
 
 
-def host_link_bandwidth(pinned, stream, reps=4):
-    """Host <-> device copy rate of this machine right before the end-to-end leg:
-    `reps` copies of one pinned input volume each way, CUDA events (the
-    end-to-end time depends on it, and it varies between boxes)."""
+def host_link_bandwidth(inputs, outputs, stream, reps=2):
+    """Host <-> device copy rate of this machine right before the end-to-end leg,
+    over the end-to-end step's own pinned buffers: every input copied to the
+    device and every output buffer filled from it, `reps` times, CUDA events
+    (the end-to-end time depends on it, and it varies between boxes and
+    buffers)."""
     import torch
 
-    dev = torch.empty_like(pinned, device="cuda")
+    dev = torch.empty_like(inputs[0], device="cuda")
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     with torch.cuda.stream(stream):
-        dev.copy_(pinned, non_blocking=True)
+        for t in inputs:
+            dev.copy_(t, non_blocking=True)
         e[0].record(stream)
         for _ in range(reps):
-            dev.copy_(pinned, non_blocking=True)
+            for t in inputs:
+                dev.copy_(t, non_blocking=True)
         e[1].record(stream)
         for _ in range(reps):
-            pinned.copy_(dev, non_blocking=True)
+            for t in outputs:
+                t.copy_(dev, non_blocking=True)
         e[2].record(stream)
     stream.synchronize()
-    nbytes = reps * pinned.numel() * 4
-    return {"h2d_gbs": nbytes / e[0].elapsed_time(e[1]) / 1e6, "d2h_gbs": nbytes / e[1].elapsed_time(e[2]) / 1e6,
-            "bytes_per_copy": pinned.numel() * 4}
+    h2d = reps * sum(t.numel() * 4 for t in inputs)
+    d2h = reps * sum(t.numel() * 4 for t in outputs)
+    return {"h2d_gbs": h2d / e[0].elapsed_time(e[1]) / 1e6, "d2h_gbs": d2h / e[1].elapsed_time(e[2]) / 1e6,
+            "h2d_ms_per_step": e[0].elapsed_time(e[1]) / reps, "d2h_ms_per_step": e[1].elapsed_time(e[2]) / reps,
+            "buffers": "the end-to-end step's %d pinned inputs and %d pinned outputs" % (len(inputs), len(outputs))}
 
 
 def bench_paged(args, w, in_core, h_data, h_smooth, in_core_value, device_stream):
