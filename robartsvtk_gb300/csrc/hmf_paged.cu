@@ -538,7 +538,9 @@ int paged_solve(hmf_ctx* c, cudaStream_t user, bool cont) {
         for (int m = lo; m <= hi; ++m)
           CK(cudaStreamWaitEvent(s, P.ev_loaded[out_q][m], 0), "cudaStreamWaitEvent(loaded)");
       const int z1 = j + 1 < nb ? P.owned[j + 1] : V.vz;
-      if (int rc2 = store_block(c, P, out, b, P.starts[j], P.owned[j], z1, kr & 1, plane, s)) return rc2;
+      // (REF_CPU never moves the flows: they stay the zeros of set 0)
+      const int flow_set = cpu ? 0 : (kr & 1);
+      if (int rc2 = store_block(c, P, out, b, P.starts[j], P.owned[j], z1, flow_set, plane, s)) return rc2;
       CK(cudaEventRecord(P.ev_stored[out_q][j], s), "cudaEventRecord(stored)");
     }
   }
