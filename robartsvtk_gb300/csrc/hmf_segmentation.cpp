@@ -75,7 +75,11 @@ const float* HierarchicalMaxFlowSegmentation::GetOutputDataObject(int node) cons
 // RequestData (vtkHierarchicalMaxFlowSegmentation.cxx:555-933) with
 // CheckInputConsistancy (:363-505): validate, then initialise and iterate on
 // the device, then fetch the leaf labellings.
-int HierarchicalMaxFlowSegmentation::Update(void* stream) {
+int HierarchicalMaxFlowSegmentation::Update(void* stream) { return Run(stream, false); }
+
+int HierarchicalMaxFlowSegmentation::ContinueUpdate(void* stream) { return Run(stream, true); }
+
+int HierarchicalMaxFlowSegmentation::Run(void* stream, bool continued) {
   error_.clear();
   if (parent_.empty()) return Fail("Hierarchy must be provided.");
   const int n = (int)parent_.size();
@@ -97,6 +101,9 @@ int HierarchicalMaxFlowSegmentation::Update(void* stream) {
   const bool rebuild = !ctx_ || ctx_parent_ != parent_ || ctx_semantics_ != semantics_ ||
                        ctx_device_ != device_ || ctx_usage_ != max_gpu_usage_ || dims[0] != ctx_dims_[0] ||
                        dims[1] != ctx_dims_[1] || dims[2] != ctx_dims_[2];
+  if (continued && rebuild)
+    return Fail("ContinueUpdate follows an Update with the same hierarchy, extent, semantics, device and "
+                "MaxGPUUsage.");
   if (rebuild) {
     if (ctx_) hmf_destroy(ctx_);
     ctx_ = nullptr;
@@ -131,7 +138,8 @@ int HierarchicalMaxFlowSegmentation::Update(void* stream) {
     if (hmf_set_data(ctx_, l, it->second.ptr, it->second.where) != HMF_OK) return Fail(hmf_last_error(ctx_));
   }
   hmf_set_params(ctx_, iterations_, step_, cc_);
-  if (hmf_solve(ctx_, stream) != HMF_OK) return Fail(hmf_last_error(ctx_));
+  if ((continued ? hmf_solve_continue(ctx_, stream) : hmf_solve(ctx_, stream)) != HMF_OK)
+    return Fail(hmf_last_error(ctx_));
   const size_t V = (size_t)dims[0] * dims[1] * dims[2];
   outputs_.clear();
   for (int l : leaves_) {

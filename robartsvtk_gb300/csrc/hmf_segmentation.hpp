@@ -68,6 +68,12 @@ class HierarchicalMaxFlowSegmentation {
   int GetSemantics() const { return semantics_; }
 
   int Update(void* stream = nullptr);
+  // NumberOfIterations more iterations from the state the last Update or
+  // ContinueUpdate ended in (hmf_solve_continue; no counterpart in the
+  // reference): the inputs and parameters as set now, the hierarchy,
+  // extent, semantics, device and MaxGPUUsage unchanged since that Update.
+  // Update(k1) then ContinueUpdate(k2) gives Update(k1 + k2)'s outputs.
+  int ContinueUpdate(void* stream = nullptr);
 
   const float* GetOutputDataObject(int node) const;
   int GetNumberOfOutputPorts() const { return (int)leaves_.size(); }
@@ -81,6 +87,7 @@ class HierarchicalMaxFlowSegmentation {
     int where = HMF_HOST;
   };
   int Fail(const std::string& msg);
+  int Run(void* stream, bool continued);
 
   std::vector<int> parent_;
   std::map<int, double> scalars_;

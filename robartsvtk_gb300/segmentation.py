@@ -755,6 +755,18 @@ class HierarchicalMaxFlowSegmentation:
 
     # RequestData (.cxx:555-933) with CheckInputConsistancy (:363-505)
     def Update(self, stream=None) -> int:
+        return self._run(stream, continued=False)
+
+    def ContinueUpdate(self, stream=None) -> int:
+        """NumberOfIterations more iterations from the state the last Update
+        or ContinueUpdate ended in (hmf_solve_continue; no counterpart in the
+        reference), with the inputs and parameters as set now: Update with k1
+        iterations then ContinueUpdate with k2 gives Update(k1 + k2)'s
+        outputs.  The hierarchy, extent, semantics, device and MaxGPUUsage must
+        be those of that Update."""
+        return self._run(stream, continued=True)
+
+    def _run(self, stream, continued: bool) -> int:
         self._error = ""
         if not self.Structure:
             return self._report("Hierarchy must be provided.")
@@ -774,6 +786,9 @@ class HierarchicalMaxFlowSegmentation:
             if (self._solver is None or self._solver.dims != dims or self._solver.parent != self.Structure
                     or getattr(self._solver, "_semantics", None) != self.Semantics
                     or self._solver.max_gpu_usage != self.MaxGPUUsage):
+                if continued:
+                    return self._report("ContinueUpdate follows an Update with the same hierarchy, extent, "
+                                        "semantics, device and MaxGPUUsage.")
                 if self._solver is not None:
                     self._solver.close()
                 self._solver = HMFSolver(dims, self.Structure, self.Semantics, self.Device, self.MaxGPUUsage)
@@ -789,7 +804,10 @@ class HierarchicalMaxFlowSegmentation:
                 sol.set_smoothness_scalar(v, self.SmoothnessScalars.get(v, 1.0))
                 sol.set_smoothness(v, self._smooth.get(v))
             sol.set_params(self.NumberOfIterations, self.StepSize, self.CC)
-            sol.solve(stream)
+            if continued:
+                sol.solve_continue(stream)
+            else:
+                sol.solve(stream)
             self._outputs = {leaf: sol.labels(leaf, stream=stream) for leaf in sol.leaves}
         except HMFError as e:
             return self._report(str(e))
@@ -817,6 +835,11 @@ class DirectedAcyclicGraphMaxFlowSegmentation(HierarchicalMaxFlowSegmentation):
         self._error = msg
         print("ERROR: DirectedAcyclicGraphMaxFlowSegmentation: " + msg, file=sys.stderr)
         return -1
+
+    def ContinueUpdate(self, stream=None) -> int:
+        """Refused: a graph's last iteration runs fewer tasks than the others,
+        so a solve cannot be continued (hmf_solve_continue refuses graphs)."""
+        return self._report("ContinueUpdate is for label trees, not graphs.")
 
     # RequestData / CheckInputConsistancy (vtkDirectedAcyclicGraphMaxFlowSegmentation.cxx:387-527, :574-1032)
     def Update(self, stream=None) -> int:

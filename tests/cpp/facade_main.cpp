@@ -12,7 +12,8 @@
 //   n_alpha  (node alpha) x n_alpha
 //   n_data   (node file)  x n_data
 //   n_smooth (node file)  x n_smooth
-//   [max_gpu_usage]       (optional: SetMaxGPUUsage, an out-of-core solve)
+//   [max_gpu_usage [k2]]  (optional: SetMaxGPUUsage, an out-of-core solve when
+//                          >= 0; then ContinueUpdate with k2 iterations)
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -82,9 +83,17 @@ int main(int argc, char** argv) {
     filter.SetSmoothnessInputDataObject(node, inputs[-1 - node].data(), dims);
   }
   double usage;
-  if (spec >> usage) filter.SetMaxGPUUsage(usage);
+  int k2 = -1;
+  if (spec >> usage) {
+    filter.SetMaxGPUUsage(usage);
+    if (!(spec >> k2)) k2 = -1;
+  }
 
-  const int rc = filter.Update();
+  int rc = filter.Update();
+  if (rc == 1 && k2 >= 0) {
+    filter.SetNumberOfIterations(k2);
+    rc = filter.ContinueUpdate();
+  }
   std::ofstream status(dir + "/status.txt");
   status << rc << "\n" << filter.GetNumberOfOutputPorts() << "\n" << filter.GetLastError() << "\n";
   if (rc != 1) return 0;

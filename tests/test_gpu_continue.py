@@ -7,8 +7,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from robartsvtk_gb300 import REF_CPU, REF_CUDA, HMFBatchSolver, HMFError, HMFSolver
-from robartsvtk_gb300.segmentation import DAGSolver
+from robartsvtk_gb300 import REF_CPU, REF_CUDA, HierarchicalMaxFlowSegmentation, HMFBatchSolver, HMFError, HMFSolver
+from robartsvtk_gb300.segmentation import DAGSolver, DirectedAcyclicGraphMaxFlowSegmentation
 from robartsvtk_gb300.synthetic import random_tree_problem
 
 pytestmark = pytest.mark.gpu
@@ -184,3 +184,33 @@ def test_continue_out_of_core(semantics, dims, plans, rounds):
             p.solve_continue()
         got = _state(p, w)
     _same(got, ref, "out of core %s %s" % (plans, rounds))
+
+
+def test_filter_continue_update():
+    """The filter facade: Update() with 8 iterations, ContinueUpdate() with 5
+    equals the oracle's 13; changing the extent in between is refused, and so
+    is ContinueUpdate on the graph filter."""
+    w = random_tree_problem(68, (21, 17, 9), [-1, 0, 0, 1, 1], iterations=13, smooth_nodes=(2,))
+    f = HierarchicalMaxFlowSegmentation()
+    f.SetHierarchy(w.parent)
+    for leaf, d in w.data.items():
+        f.SetDataInputDataObject(leaf, d)
+    for v, S in w.smooth.items():
+        f.SetSmoothnessInputDataObject(v, S)
+    for v, a in w.alpha.items():
+        f.AddSmoothnessScalar(v, a)
+    f.SetNumberOfIterations(8)
+    assert f.Update() == 1, f.GetLastError()
+    f.SetNumberOfIterations(5)
+    assert f.ContinueUpdate() == 1, f.GetLastError()
+    ref = _oracle(w, 13)
+    for leaf in w.leaves:
+        assert np.array_equal(f.GetOutputDataObject(leaf), ref["u"][leaf].astype(np.float32)), leaf
+    small = random_tree_problem(69, (7, 6, 5), [-1, 0, 0, 1, 1], iterations=2)
+    for leaf, d in small.data.items():
+        f.SetDataInputDataObject(leaf, d)
+    f.SetSmoothnessInputDataObject(2, None)
+    assert f.ContinueUpdate() == -1
+    assert "ContinueUpdate follows an Update" in f.GetLastError()
+    g = DirectedAcyclicGraphMaxFlowSegmentation()
+    assert g.ContinueUpdate() == -1
