@@ -92,6 +92,26 @@ def test_facade_reports_missing_hierarchy():
     assert "extent" in f.GetLastError()
 
 
+def test_facade_continue_update_needs_an_update():
+    """ContinueUpdate without an Update on the same hierarchy and extent is
+    refused before any device work; the graph filter refuses it always."""
+    from robartsvtk_gb300 import DirectedAcyclicGraphMaxFlowSegmentation, HierarchicalMaxFlowSegmentation
+    f = HierarchicalMaxFlowSegmentation()
+    f.SetStructure([-1, 0, 0])
+    f.SetDataInputDataObject(1, np.zeros((2, 2, 2), np.float32))
+    f.SetDataInputDataObject(2, np.zeros((2, 2, 2), np.float32))
+    assert f.ContinueUpdate() == -1
+    assert "ContinueUpdate follows an Update" in f.GetLastError()
+    g = DirectedAcyclicGraphMaxFlowSegmentation()
+    g.SetStructure(3, [(0, 1), (0, 2)])
+    assert g.ContinueUpdate() == -1
+    assert "label trees" in g.GetLastError()
+
+
+def test_continue_without_context_is_rejected(hmf_lib):
+    assert hmf_lib.hmf_solve_continue(None, None) == -1
+
+
 def test_facade_clamps_like_vtk():
     from robartsvtk_gb300 import HierarchicalMaxFlowSegmentation
     f = HierarchicalMaxFlowSegmentation()
