@@ -363,9 +363,24 @@ int paged_solve(hmf_ctx* c, cudaStream_t user, bool cont) {
   if (nb < 0)
     return fail(c, HMF_ERR_INVALID_ARGUMENT,
                 "block planes must be at least four times the halo (2 x iterations per round + 1)");
+  // A block from the budget is as thick as the budget allows; the same
+  // number of blocks also covers the volume with thinner ones, which iterate
+  // fewer planes twice (the halos): take the thinnest (the block count does
+  // not grow as T does).
+  if (P.forced_planes <= 0 && halo > 0 && nb > 1) {
+    int lo = 4 * halo, hi = T;
+    while (lo < hi) {
+      const int mid = lo + (hi - lo) / 2;
+      const int n_mid = hmf_paged_layout(V.vz, mid, halo, nullptr, nullptr, 0);
+      if (n_mid > 0 && n_mid <= nb) hi = mid;
+      else lo = mid + 1;
+    }
+    T = lo;
+  }
   P.starts.assign(nb, 0);
   P.owned.assign(nb, 0);
-  hmf_paged_layout(V.vz, T, halo, P.starts.data(), P.owned.data(), nb);
+  if (hmf_paged_layout(V.vz, T, halo, P.starts.data(), P.owned.data(), nb) != nb)
+    return fail(c, HMF_ERR_INVALID_ARGUMENT, "block layout");
   std::vector<int> round_iters;
   if (c->iterations == 0 || k == 0) round_iters.push_back(0);
   for (int left = c->iterations; k > 0 && left > 0; left -= k) round_iters.push_back(std::min(k, left));
