@@ -61,6 +61,17 @@ def test_layout_covers_the_volume_with_exact_owned_planes(hmf_lib, vz, T, H):
         assert nb == 1 + -(-(vz - Tb) // (Tb - 2 * H))
 
 
+def test_block_count_never_grows_with_thicker_blocks(hmf_lib):
+    """The out-of-core plan shrinks a budget-derived block to the thinnest
+    one with the same block count, found by bisection: that needs the count
+    to be non-increasing in the block thickness (from 4 x halo up)."""
+    for vz in (45, 96, 256, 384, 1000):
+        for H in (3, 5, 19, 23, 25):
+            counts = [hmf_lib.hmf_paged_layout(vz, T, H, None, None, 0) for T in range(4 * H, vz + 2)]
+            assert all(c > 0 for c in counts)
+            assert all(a >= b for a, b in zip(counts, counts[1:])), (vz, H)
+
+
 def test_layout_rejects_blocks_thinner_than_four_halos(hmf_lib):
     assert hmf_lib.hmf_paged_layout(100, 15, 4, None, None, 0) == -1
     assert hmf_lib.hmf_paged_layout(100, 16, 4, None, None, 0) > 0
